@@ -1,0 +1,435 @@
+#!/usr/bin/env python
+"""Benchmark of the bifurcation / LLE / basins engine on one GB300 (or N
+replicas, one per GPU, under torchrun).
+
+Default workload: the 2-D LLE map of the Rossler flow (classic RK4, h=0.01),
+a in [0.1, 0.4] x c in [2, 10] on a 1024 x 1024 grid, b = 0.2, x0 = (1,1,1),
+5,000 transient steps, then 5,002 Benettin blocks of 10 steps of the orbit
+and of its twin (offset 1e-8 along x): 105,040 trajectory-steps per grid
+point, 1.101e11 per map. One bench step = one full map. The engine arm runs
+the FP32 kernel (exact-difference twin, FP64 log-stretch sum); the line also
+carries the plain FP64 kernel's rate and the FP32 map's error against FP64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+                  [--workload lle|bif1d|basins] [--precision fp32|fp64]
+
+--impl reference times the CPU path of the reference algorithm (the oracle's
+C++ restatement, OpenMP over all host cores) on a bounded sample of the same
+workload; the reference itself has no CPU implementation and its GPU code
+cannot be built or run on the benchmark machine.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "steps/s on 1 GB300, batched FP32 vs plain FP64 at stated LLE error; p99 latency"
+UNIT = "trajectory-steps/s"
+
+# ---- workloads -----------------------------------------------------------------
+LLE = dict(system="rossler", sysid=1, flops=63, tMax=500.0, NT=0.1, nPts=1024, h=0.01, eps=1e-8,
+           initialConditions=[1.0, 1.0, 1.0], ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2],
+           transientTime=50.0, values=[0.2, 0.2, 5.7])
+BIF1D = dict(system="lorenz", sysid=0, flops=71, tMax=100.0, nPts=1000, h=0.01, initialConditions=[0.1, 0.1, 0.1],
+             ranges=[20.0, 200.0], indicesOfMutVars=[1], writableVar=0, maxValue=1e4, transientTime=100.0,
+             values=[10.0, 28.0, 8.0 / 3.0])
+BASINS = dict(system="lorenz", sysid=0, flops=71, tMax=50.0, nPts=2048, h=0.01, initialConditions=[0.0, 0.0, 27.0],
+              ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8,
+              transientTime=200.0, values=[10.0, 24.0, 8.0 / 3.0], eps=0.05)
+
+
+def lle_steps_per_point(w) -> int:
+    ntp = int(w["NT"] / w["h"])
+    calc = int(w["tMax"] / w["h"]) // ntp + 1
+    return int(w["transientTime"] / w["h"]) + 2 * ntp * (calc + 1)
+
+
+def sweep_steps_per_point(w) -> int:
+    return int(w["transientTime"] / w["h"]) + int(w["tMax"] / w["h"])
+
+
+def kw_of(w, drop=("system", "sysid", "flops")):
+    return {k: v for k, v in w.items() if k not in drop}
+
+
+# ---- distributed / clocks -----------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpus):
+        self.gpus = gpus
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            time.sleep(0.2)
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = [r.split(", ") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        rows = [r for r in rows if len(r) >= 9 and r[0].strip().isdigit() and int(r[0]) in self.gpus]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(r[1]) for r in rows]
+        smax = max(float(r[2]) for r in rows)
+        load = [s for s, r in zip(sm, rows) if float(r[3]) > 200.0] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[5 + j].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows)}
+
+
+# ---- CPU leg (the oracle restatement of the reference algorithm) --------------------------
+def cpu_sample_lle(w, target_s=10.0):
+    from oracle import oracle as O
+
+    nthreads = os.cpu_count() or 1
+    n_all = w["nPts"] * w["nPts"]
+    args = (w["sysid"], w["tMax"], w["NT"], w["nPts"], w["h"], w["eps"], w["initialConditions"], w["ranges"],
+            w["indicesOfMutVars"], w["transientTime"], w["values"])
+    probe = 2 * nthreads
+    t = time.perf_counter()
+    O.lle2d(*args, p_begin=n_all // 2, p_end=n_all // 2 + probe, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    n = int(min(n_all, max(probe, probe * target_s / max(dt, 1e-3))))
+    begin = n_all // 2 - n // 2
+    t = time.perf_counter()
+    O.lle2d(*args, p_begin=begin, p_end=begin + n, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    steps = n * lle_steps_per_point(w)
+    return {"value": steps / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n} contiguous grid points from the middle of the 1024x1024 map, full 105,040 steps each, "
+                      f"FP64, {dt:.1f} s"}
+
+
+def cpu_sample_sweep(w, kind, target_s=10.0):
+    from oracle import oracle as O
+
+    nthreads = os.cpu_count() or 1
+    dim = 1 if kind == "bif1d" else 2
+    n_all = w["nPts"] ** dim
+    probe = 2 * nthreads
+    def run(b, e):
+        if kind == "bif1d":
+            O.bifurcation(w["sysid"], 1, w["tMax"], w["nPts"], w["h"], w["initialConditions"], w["ranges"],
+                          w["indicesOfMutVars"], w["writableVar"], w["maxValue"], w["transientTime"], w["values"],
+                          cap=64, p_begin=b, p_end=e, nthreads=nthreads)
+        else:
+            O.basins_features(w["sysid"], w["tMax"], w["nPts"], w["h"], w["initialConditions"], w["ranges"],
+                              w["indicesOfMutVars"], w["writableVar"], w["maxValue"], w["transientTime"], w["values"],
+                              p_begin=b, p_end=e, nthreads=nthreads)
+    t = time.perf_counter()
+    run(0, probe)
+    dt = time.perf_counter() - t
+    n = int(min(n_all, max(probe, probe * target_s / max(dt, 1e-3))))
+    b = n_all // 2 - n // 2 if n < n_all else 0
+    t = time.perf_counter()
+    run(b, b + n)
+    dt = time.perf_counter() - t
+    return {"value": n * sweep_steps_per_point(w) / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n} of {n_all} grid points, full horizon, FP64, {dt:.1f} s"}
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS}[args.workload]
+    fn = (lambda: cpu_sample_lle(w, args.cpu_seconds)) if args.workload == "lle" else \
+        (lambda: cpu_sample_sweep(w, args.workload, args.cpu_seconds))
+    vals, last = [], None
+    for _ in range(args.steps):
+        last = fn()
+        vals.append(last["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(args), "cpu_baseline": {**last, "value": v},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args):
+    if args.workload == "lle":
+        return {"workload": "LLE map, Rossler RK4 h=0.01, a in [0.1,0.4] x c in [2,10], 1024x1024, b=0.2, "
+                            "x0=(1,1,1), 5000 transient + 5002 blocks x 10 steps x 2 trajectories",
+                "grid_points": 1048576, "steps_per_point": lle_steps_per_point(LLE), "eps": 1e-8,
+                "precision": args.precision, "l2": "256 MB buffer written between timed steps; the map's state "
+                                                  "lives in registers (inputs: 88 B of parameters)"}
+    if args.workload == "bif1d":
+        return {"workload": "1-D bifurcation, Lorenz RK4 h=0.01, rho in [20,200] x 1000, 10000 transient + "
+                            "10000 recorded steps, peaks of x", "grid_points": 1000,
+                "steps_per_point": sweep_steps_per_point(BIF1D), "precision": args.precision,
+                "l2": "256 MB buffer written between timed steps"}
+    return {"workload": "basins, Lorenz rho=24 RK4 h=0.01, 2048x2048 ICs x,y in [-30,30], z=27, 20000 transient + "
+                        "5000 recorded steps, features + reference clustering eps=0.05",
+            "grid_points": 2048 * 2048, "steps_per_point": sweep_steps_per_point(BASINS),
+            "precision": args.precision, "l2": "256 MB buffer written between timed steps"}
+
+
+def traffic_from_profiles(kernel_tag: str):
+    """dram bytes per launch recorded in profiles/<kernel_tag>.md (a line
+    'dram_bytes_per_launch: N'), or None."""
+    p = ROOT / "profiles" / f"{kernel_tag}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ---- engine arm ----------------------------------------------------------------------------
+def engine_arm(args, ws, rank, local):
+    import torch
+
+    import chaoslibrary_gb300 as C
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    prec = C.FP32 if args.precision == "fp32" else C.FP64
+    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS}[args.workload]
+    n_points = w["nPts"] ** (1 if args.workload == "bif1d" else 2)
+    if args.workload == "lle":
+        steps_pp = lle_steps_per_point(w)
+        out = torch.empty(n_points, dtype=torch.float64, device=dev)
+        kw = kw_of(w)
+
+        def step(o=None):
+            return C.lle2d(w["system"], precision=prec, out=out if o is None else o, **kw)
+
+        def step_host():
+            return C.lle2d(w["system"], precision=prec, **kw)
+        d2h = n_points * 8
+        launches_per_step = 1
+        tag = f"lle_{args.precision}_rossler_1024"
+    elif args.workload == "bif1d":
+        steps_pp = sweep_steps_per_point(w)
+        cap = 64
+        outs = dict(counts=torch.empty(n_points, dtype=torch.int32, device=dev),
+                    flags=torch.empty(n_points, dtype=torch.int32, device=dev),
+                    first=torch.empty(n_points, dtype=torch.float64, device=dev),
+                    peaks=torch.empty(n_points * cap, dtype=torch.float64, device=dev),
+                    intervals=torch.empty(n_points * cap, dtype=torch.float64, device=dev))
+        kw = kw_of(w)
+
+        def step(o=None):
+            return C.bifurcation1d(w["system"], precision=prec, peakCapacity=cap, out=outs, **kw)
+
+        def step_host():
+            return C.bifurcation1d(w["system"], precision=prec, peakCapacity=cap, **kw)
+        d2h = n_points * (4 + 4 + 8 + 16 * cap)
+        launches_per_step = 1
+        tag = f"bif1d_{args.precision}_lorenz_1000"
+    else:
+        steps_pp = sweep_steps_per_point(w)
+        outs = dict(labels=torch.empty(n_points, dtype=torch.int32, device=dev),
+                    avg_peaks=torch.empty(n_points, dtype=torch.float64, device=dev),
+                    avg_intervals=torch.empty(n_points, dtype=torch.float64, device=dev),
+                    flags=torch.empty(n_points, dtype=torch.int32, device=dev))
+        kw = kw_of(w)
+
+        def step(o=None):
+            return C.basins(w["system"], precision=prec, out=outs, **kw)
+
+        def step_host():
+            return C.basins(w["system"], precision=prec, **kw)
+        d2h = n_points * (4 + 8 + 8 + 4)
+        launches_per_step = None
+        tag = f"basins_{args.precision}_lorenz_2048"
+    steps_per_call = n_points * steps_pp
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stream = torch.cuda.current_stream(dev)
+    with Clocks([local] if ws == 1 else list(range(ws))) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+        wall = time.perf_counter() - wall0
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = max_over_ranks(ws, sum(ms) / 1e3)
+    value = ws * steps_per_call * args.steps / t_total
+    clocks = clk.summary()
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == C.FP32 else "f64",
+            "data": "synthetic (deterministic parameter / initial-condition grids)",
+            "config": config_of(args), "clocks": clocks, "wall_s_timed_region": wall}
+    if launches_per_step:
+        line["gpu_launches"] = launches_per_step * args.steps
+
+    # roofline: FP32 (or FP64) FMA pipe, algorithmic flops of the integration
+    if rank == 0:
+        mean_s = statistics.mean(ms) / 1e3
+        algo = w["flops"] * steps_per_call
+        achieved = algo / mean_s / 1e12
+        peak = C.fma_probe() / 1e12 if prec == C.FP32 else None
+        line["roofline"] = {"bound": "fp32_fma" if prec == C.FP32 else "fp64_fma", "achieved": achieved,
+                            "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
+                            "traffic": traffic_from_profiles(tag),
+                            "algorithmic": f"{w['flops']} flops per RK4 step x {steps_per_call:.4g} steps per launch",
+                            "peak_source": "measured in this run: FP32 fmaf-chain probe (chaos_fma_probe), "
+                                           "2048 threads/SM; MEASURED_PEAKS.json has only HBM and bf16 tensor peaks"}
+
+    # e2e through the public API with host buffers (copies inside the timed region)
+    t_e2e = []
+    for _ in range(max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_host()
+        t_e2e.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(ws, statistics.median(t_e2e))
+    line["e2e"] = {"value": ws * steps_per_call / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 88,
+                   "d2h_bytes_per_step": d2h}
+
+    if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras:
+        line.update(lle_precision_report(C, prec, dev))
+    if rank == 0 and ws == 1 and not args.no_extras:
+        try:
+            if args.workload == "lle":
+                line["cpu_baseline"] = cpu_sample_lle(w, args.cpu_seconds)
+            else:
+                line["cpu_baseline"] = cpu_sample_sweep(w, args.workload, args.cpu_seconds)
+        except Exception as e:  # the checker is optional at run time
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def lle_precision_report(C, prec, dev):
+    """Plain FP64 kernel rate and the FP32 map's error against it, on the
+    512x512 map over the same parameter ranges (262,144 points)."""
+    import torch
+
+    w = dict(LLE)
+    w["nPts"] = 512
+    kw = kw_of(w)
+    n = 512 * 512
+    o64 = torch.empty(n, dtype=torch.float64, device=dev)
+    o32 = torch.empty(n, dtype=torch.float64, device=dev)
+    C.lle2d("rossler", precision=C.FP64, out=o64, **dict(kw, nPts=64))  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    C.lle2d("rossler", precision=C.FP64, out=o64, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3
+    e0.record()
+    C.lle2d("rossler", precision=C.FP32, out=o32, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    t32 = e0.elapsed_time(e1) / 1e3
+    a, b = o64.cpu().numpy(), o32.cpu().numpy()
+    fin = np.isfinite(a) & np.isfinite(b)
+    d = np.abs(a[fin] - b[fin])
+    reg = a[fin] < 0.005
+    steps = n * lle_steps_per_point(w)
+    return {"fp64_plain": {"value": steps / t64, "unit": UNIT, "map": "512x512 (same ranges)",
+                           "fp32_same_map": steps / t32, "speedup_fp32_vs_fp64": t64 / t32},
+            "lle_error_vs_fp64": {"points": int(fin.sum()), "p50": float(np.median(d)),
+                                  "p90": float(np.percentile(d, 90)), "p99": float(np.percentile(d, 99)),
+                                  "max": float(d.max()), "frac_le_1e-3": float(np.mean(d <= 1e-3)),
+                                  "regular_points": int(reg.sum()),
+                                  "regular_max": float(d[reg].max()) if reg.any() else None,
+                                  "chaotic_class_agreement": float(np.mean((a[fin] > 0.01) == (b[fin] > 0.01))),
+                                  "nonfinite_mismatch": int(np.sum(np.isfinite(a) != np.isfinite(b)))}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "basins"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the CPU baseline")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, ws, rank)
+    else:
+        engine_arm(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,48 @@
+"""GB300 (sm_103a) engine for ChaosLibrary's bifurcation / LLE / basins hot path.
+
+Python front end over the C ABI in include/chaos_gb300.h (libchaos_gb300.so,
+built by ``chaoslibrary_gb300.build``). Two layers:
+
+* the reference's four entry points with their exact argument lists
+  (``bifurcation1D``, ``bifurcation2D``, ``LLE2D``, ``basinsOfAttraction_2``),
+  which write the reference's CSV files;
+* array functions (``bifurcation1d``, ``lle2d``, ``basins``, ``dbscan`` ...)
+  that return numpy arrays, or write into CUDA tensors when given ``out=``.
+
+There is no CPU implementation here: without the built library every call
+raises.
+"""
+from __future__ import annotations
+
+from ._native import (  # noqa: F401
+    FP32,
+    FP64,
+    SYSTEMS,
+    ChaosError,
+    LLE2D,
+    Basins,
+    Bifurcation,
+    LLE,
+    basins,
+    basins_features,
+    basinsOfAttraction_2,
+    bifurcation1D,
+    bifurcation1d,
+    bifurcation2D,
+    bifurcation2d,
+    dbscan,
+    dbscan_compat,
+    lib,
+    lib_path,
+    lle2d,
+    peak_finder,
+    point_dbscan,
+    set_system,
+    system_info,
+)
+
+__all__ = [
+    "FP32", "FP64", "SYSTEMS", "ChaosError", "bifurcation1D", "bifurcation2D", "LLE2D", "basinsOfAttraction_2",
+    "Bifurcation", "LLE", "Basins", "bifurcation1d", "bifurcation2d", "lle2d", "basins", "basins_features",
+    "dbscan", "dbscan_compat", "peak_finder", "point_dbscan", "lib", "lib_path", "set_system", "system_info",
+]

@@ -1,0 +1,345 @@
+"""ctypes bindings of libchaos_gb300.so (see include/chaos_gb300.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+from types import SimpleNamespace
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+FP64, FP32 = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+SYSTEMS = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "rossler_cd": 4, "sin3": 5, "sin2": 6,
+           "memristor": 7}
+STATUS = {0: "CHAOS_OK", -1: "CHAOS_E_ARGS", -2: "CHAOS_E_NOMEM", -3: "CHAOS_E_CUDA", -4: "CHAOS_E_IO",
+          -5: "CHAOS_E_TIMEOUT", -6: "CHAOS_E_UNSUPPORTED", -7: "CHAOS_E_BUSY", -8: "CHAOS_E_NODEV"}
+
+
+class ChaosError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Exec(C.Structure):
+    _fields_ = [("precision", C.c_int), ("memory", C.c_int), ("stream", C.c_void_p), ("device", C.c_int)]
+
+
+def lib_path() -> Path:
+    return Path(os.environ.get("CHAOS_GB300_LIB", _PKG / "lib" / "libchaos_gb300.so"))
+
+
+_lib = None
+_P = C.c_void_p
+_D = C.c_double
+_I = C.c_int
+_L = C.c_longlong
+
+_SIGS = {
+    "chaos_abi_version": ([], _I),
+    "chaos_last_error": ([], C.c_char_p),
+    "chaos_system_info": ([_I, _P, _P], _I),
+    "chaos_synchronize": ([_P], _I),
+    "chaos_bifurcation1d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _P], _I),
+    "chaos_bifurcation2d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P], _I),
+    "chaos_lle2d": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, _P], _I),
+    "chaos_basins_features": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _P, _P, _P, _P], _I),
+    "chaos_basins": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P, _P, _P], _I),
+    "chaos_dbscan_compat": ([_P, _P, _P, _P, _L, _D, _P], _I),
+    "chaos_dbscan": ([_P, _P, _L, _I, _D, _I, _P, _P], _I),
+    "chaos_peak_finder": ([_P, _P, _L, _I, _D, _I, _P, _P, _P], _I),
+    "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
+    "chaos_fma_probe": ([_P, _L, _P, _P], _I),
+    "chaos_compat_set_system": ([_I], _I),
+    "chaos_compat_set_precision": ([_I], _I),
+    "chaos_compat_get_system": ([], _I),
+    "chaos_compat_bifurcation1D": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, C.c_char_p], _I),
+    "chaos_compat_bifurcation2D": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, C.c_char_p], _I),
+    "chaos_compat_LLE2D": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
+    "chaos_compat_basinsOfAttraction_2": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, C.c_char_p], _I),
+}
+
+
+def lib() -> C.CDLL:
+    """The loaded engine library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not path.exists():
+            raise ChaosError(-8, f"{path} is missing: build it with chaoslibrary_gb300.build.build() "
+                                 "(the engine has no CPU fallback)")
+        L = C.CDLL(str(path))
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise ChaosError(rc, lib().chaos_last_error().decode(errors="replace"))
+
+
+def _sys(system) -> int:
+    return SYSTEMS[system] if isinstance(system, str) else int(system)
+
+
+def _prec(precision) -> int:
+    if isinstance(precision, str):
+        return FP32 if precision.lower() in ("fp32", "f32", "float32") else FP64
+    return int(precision)
+
+
+def system_info(system) -> tuple[int, int]:
+    nx, na = C.c_int(), C.c_int()
+    _check(lib().chaos_system_info(_sys(system), C.byref(nx), C.byref(na)))
+    return nx.value, na.value
+
+
+class _Args:
+    """Keeps the ctypes views of numpy inputs alive for one call."""
+
+    def __init__(self):
+        self.keep = []
+
+    def d(self, x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        self.keep.append(a)
+        return a.ctypes.data
+
+    def i(self, x):
+        a = np.ascontiguousarray(x, dtype=np.int32)
+        self.keep.append(a)
+        return a.ctypes.data
+
+
+def _out_ptr(arr):
+    if arr is None:
+        return None
+    if hasattr(arr, "data_ptr"):
+        return arr.data_ptr()
+    return arr.ctypes.data
+
+
+def _exec(precision, outs: dict, stream=None, device=None) -> Exec:
+    """Host-memory call unless the outputs are CUDA tensors (device call on
+    torch's current stream of that device, asynchronous)."""
+    tensors = [v for v in outs.values() if v is not None and hasattr(v, "data_ptr")]
+    if tensors:
+        import torch
+
+        dev = tensors[0].device
+        st = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        return Exec(_prec(precision), MEM_DEVICE, C.c_void_p(st), dev.index if dev.index is not None else -1)
+    return Exec(_prec(precision), MEM_HOST, None, -1 if device is None else int(device))
+
+
+def fma_probe(iters: int = 200000, device=None) -> float:
+    """Measured FP32 FMA throughput of the device, in flop/s."""
+    ex = Exec(FP64, MEM_HOST, None, -1 if device is None else int(device))
+    sec, fl = C.c_double(), C.c_double()
+    _check(lib().chaos_fma_probe(C.byref(ex), iters, C.byref(sec), C.byref(fl)))
+    return fl.value / sec.value
+
+
+def set_system(system) -> None:
+    """System used by the reference-signature wrappers (bifurcation1D, ...)."""
+    _check(lib().chaos_compat_set_system(_sys(system)))
+
+
+def set_precision(precision) -> None:
+    _check(lib().chaos_compat_set_precision(_prec(precision)))
+
+
+# ---- array API ---------------------------------------------------------------
+
+def bifurcation1d(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                  transientTime, values, preScaller=1, peakCapacity=None, precision=FP64, out=None, stream=None):
+    """1-D sweep; returns counts, flags, first, peaks[nPts, cap], intervals[nPts, cap]."""
+    A = _Args()
+    B = int(tMax / h / preScaller) if h > 0 and preScaller > 0 else 1
+    cap = int(peakCapacity or max(B // 2, 1))
+    if out is None:
+        out = dict(counts=np.zeros(nPts, np.int32), flags=np.zeros(nPts, np.int32), first=np.zeros(nPts),
+                   peaks=np.zeros((nPts, cap)), intervals=np.zeros((nPts, cap)))
+    ex = _exec(precision, out, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_bifurcation1d(C.byref(ex), _sys(system), tMax, nPts, h, ic.size, A.d(ic), A.d(ranges),
+                                     A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals),
+                                     vals.size, preScaller, cap, _out_ptr(out["counts"]), _out_ptr(out["flags"]),
+                                     _out_ptr(out.get("first")), _out_ptr(out.get("peaks")),
+                                     _out_ptr(out.get("intervals"))))
+    return out
+
+
+def bifurcation2d(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                  transientTime, values, preScaller=1, eps=0.001, precision=FP64, out=None, stream=None):
+    A = _Args()
+    n = nPts * nPts
+    if out is None:
+        out = dict(labels=np.zeros(n, np.int32), counts=np.zeros(n, np.int32))
+    ex = _exec(precision, out, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_bifurcation2d(C.byref(ex), _sys(system), tMax, nPts, h, ic.size, A.d(ic), A.d(ranges),
+                                     A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals),
+                                     vals.size, preScaller, eps, _out_ptr(out["labels"]),
+                                     _out_ptr(out.get("counts"))))
+    return out
+
+
+def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime, values,
+          writableVar=0, maxValue=0.0, precision=FP64, out=None, stream=None):
+    """LLE map; result[j*nPts + i] (row = second parameter), as the reference CSV."""
+    A = _Args()
+    if out is None:
+        out = np.zeros(nPts * nPts)
+    ex = _exec(precision, {"lle": out}, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_lle2d(C.byref(ex), _sys(system), tMax, NT, nPts, h, eps, A.d(ic), ic.size, A.d(ranges),
+                             A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size,
+                             _out_ptr(out)))
+    return out
+
+
+def basins_features(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                    transientTime, values, preScaller=1, precision=FP64, out=None, stream=None):
+    A = _Args()
+    n = nPts * nPts
+    if out is None:
+        out = dict(flags=np.zeros(n, np.int32), avg_peaks=np.zeros(n), avg_intervals=np.zeros(n),
+                   counts=np.zeros(n, np.int32))
+    ex = _exec(precision, out, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_basins_features(C.byref(ex), _sys(system), tMax, nPts, h, ic.size, A.d(ic), A.d(ranges),
+                                       A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals),
+                                       vals.size, preScaller, _out_ptr(out["flags"]), _out_ptr(out["avg_peaks"]),
+                                       _out_ptr(out["avg_intervals"]), _out_ptr(out.get("counts"))))
+    return out
+
+
+def basins(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+           transientTime, values, preScaller=1, eps=0.05, precision=FP64, out=None, stream=None):
+    A = _Args()
+    n = nPts * nPts
+    if out is None:
+        out = dict(labels=np.zeros(n, np.int32), avg_peaks=np.zeros(n), avg_intervals=np.zeros(n),
+                   flags=np.zeros(n, np.int32))
+    ex = _exec(precision, out, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_basins(C.byref(ex), _sys(system), tMax, nPts, h, ic.size, A.d(ic), A.d(ranges),
+                              A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size,
+                              preScaller, eps, _out_ptr(out["labels"]), _out_ptr(out.get("avg_peaks")),
+                              _out_ptr(out.get("avg_intervals")), _out_ptr(out.get("flags"))))
+    return out
+
+
+def dbscan_compat(avg_peaks, avg_intervals, flags, eps, out=None, stream=None):
+    A = _Args()
+    n = len(avg_peaks)
+    if out is None:
+        out = np.zeros(n, np.int32)
+    if hasattr(out, "data_ptr"):
+        ex = _exec(FP64, {"labels": out}, stream)
+        ptrs = (avg_peaks.data_ptr(), avg_intervals.data_ptr(), flags.data_ptr())
+    else:
+        ex = _exec(FP64, {}, stream)
+        ptrs = (A.d(avg_peaks), A.d(avg_intervals), A.i(flags))
+    _check(lib().chaos_dbscan_compat(C.byref(ex), *ptrs, n, eps, _out_ptr(out)))
+    return out
+
+
+def dbscan(features, eps, min_pts, mask=None, out=None, stream=None):
+    A = _Args()
+    if hasattr(features, "data_ptr"):
+        n, d = features.shape
+        if out is None:
+            import torch
+
+            out = torch.empty(n, dtype=torch.int32, device=features.device)
+        ex = _exec(FP64, {"labels": out}, stream)
+        _check(lib().chaos_dbscan(C.byref(ex), features.data_ptr(), n, d, eps, min_pts,
+                                  None if mask is None else mask.data_ptr(), out.data_ptr()))
+        return out
+    f = np.ascontiguousarray(np.atleast_2d(features), np.float64)
+    n, d = f.shape
+    if out is None:
+        out = np.zeros(n, np.int32)
+    ex = _exec(FP64, {}, stream)
+    _check(lib().chaos_dbscan(C.byref(ex), A.d(f), n, d, eps, min_pts, None if mask is None else A.i(mask),
+                              _out_ptr(out)))
+    return out
+
+
+def peak_finder(data, h, peakCapacity=None, stream=None):
+    A = _Args()
+    d = np.ascontiguousarray(np.atleast_2d(data), np.float64)
+    n, ln = d.shape
+    cap = int(peakCapacity or max(ln // 2, 1))
+    out = dict(counts=np.zeros(n, np.int32), peaks=np.zeros((n, cap)), intervals=np.zeros((n, cap)))
+    ex = _exec(FP64, {}, stream)
+    _check(lib().chaos_peak_finder(C.byref(ex), A.d(d), n, ln, h, cap, _out_ptr(out["counts"]),
+                                   _out_ptr(out["peaks"]), _out_ptr(out["intervals"])))
+    return out
+
+
+def point_dbscan(intervals, counts, eps, stream=None):
+    A = _Args()
+    iv = np.ascontiguousarray(np.atleast_2d(intervals), np.float64)
+    n, stride = iv.shape
+    out = np.zeros(n, np.int32)
+    ex = _exec(FP64, {}, stream)
+    _check(lib().chaos_point_dbscan(C.byref(ex), A.d(iv), A.i(counts), n, stride, eps, _out_ptr(out)))
+    return out
+
+
+# ---- the reference's entry points (CSV files) -----------------------------------
+
+def bifurcation1D(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
+                  writableVar, maxValue, transientTime, values, amountOfValues, preScaller, OUT_FILE_PATH):
+    A = _Args()
+    _check(lib().chaos_compat_bifurcation1D(tMax, nPts, h, amountOfInitialConditions, A.d(initialConditions),
+                                            A.d(ranges), A.i(indicesOfMutVars), writableVar, maxValue,
+                                            transientTime, A.d(values), amountOfValues, preScaller,
+                                            str(OUT_FILE_PATH).encode()))
+
+
+def bifurcation2D(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
+                  writableVar, maxValue, transientTime, values, amountOfValues, preScaller, eps, OUT_FILE_PATH):
+    A = _Args()
+    _check(lib().chaos_compat_bifurcation2D(tMax, nPts, h, amountOfInitialConditions, A.d(initialConditions),
+                                            A.d(ranges), A.i(indicesOfMutVars), writableVar, maxValue,
+                                            transientTime, A.d(values), amountOfValues, preScaller, eps,
+                                            str(OUT_FILE_PATH).encode()))
+
+
+def LLE2D(tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges, indicesOfMutVars,
+          writableVar, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH):
+    A = _Args()
+    _check(lib().chaos_compat_LLE2D(tMax, NT, nPts, h, eps, A.d(initialConditions), amountOfInitialConditions,
+                                    A.d(ranges), A.i(indicesOfMutVars), writableVar, maxValue, transientTime,
+                                    A.d(values), amountOfValues, str(OUT_FILE_PATH).encode()))
+
+
+def basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
+                         writableVar, maxValue, transientTime, values, amountOfValues, preScaller, eps,
+                         OUT_FILE_PATH):
+    A = _Args()
+    _check(lib().chaos_compat_basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, A.d(initialConditions),
+                                                   A.d(ranges), A.i(indicesOfMutVars), writableVar, maxValue,
+                                                   transientTime, A.d(values), amountOfValues, preScaller, eps,
+                                                   str(OUT_FILE_PATH).encode()))
+
+
+# namespaces as in the reference (Bifurcation::bifurcation1D, LLE::LLE2D, Basins::basinsOfAttraction_2)
+Bifurcation = SimpleNamespace(bifurcation1D=bifurcation1D, bifurcation2D=bifurcation2D)
+LLE = SimpleNamespace(LLE2D=LLE2D)
+Basins = SimpleNamespace(basinsOfAttraction_2=basinsOfAttraction_2)

@@ -1,0 +1,85 @@
+"""Builds libchaos_gb300.so (all CUDA kernels + the C ABI + the compat wrappers)
+for sm_103a with nvcc, in-tree, translation units compiled in parallel."""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIBDIR = PKG / "lib"
+LIB = LIBDIR / "libchaos_gb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
+
+# (source, extra flags). The FP64 and clustering units keep every rounding
+# the source writes (no multiply-add contraction).
+SOURCES = [
+    ("kern_f64.cu", ["--fmad=false"]),
+    ("kern_f32.cu", []),
+    ("dbscan.cu", ["--fmad=false", "--extended-lambda"]),
+    ("capi.cu", []),
+    ("probe.cu", []),
+    ("compat.cpp", []),
+]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise FileNotFoundError("nvcc not found")
+
+
+def _deps() -> list[Path]:
+    return sorted(CSRC.glob("*")) + sorted((PKG.parent / "include").glob("*.h*")) + [Path(__file__)]
+
+
+def up_to_date() -> bool:
+    if not LIB.exists():
+        return False
+    t = LIB.stat().st_mtime
+    return all(d.stat().st_mtime <= t for d in _deps())
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    if not force and up_to_date():
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    cc = nvcc()
+    procs = []
+    objs = []
+    for src, extra in SOURCES:
+        obj = BUILD / (src + ".o")
+        objs.append(obj)
+        cmd = [cc, *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+        if src.endswith(".cpp"):
+            cmd = [cc, *COMMON, "-x", "c++", "-c", str(CSRC / src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    failed = []
+    for src, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            failed.append(f"--- {src}\n{out}")
+        elif verbose and out.strip():
+            print(out)
+    if failed:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(failed))
+    tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+    link = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    if verbose:
+        print(" ".join(link), flush=True)
+    subprocess.run(link, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,507 @@
+// C-ABI layer: argument checks, device buffers from a stream-ordered pool,
+// host<->device copies and kernel launches. Declared in include/chaos_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/chaos_gb300.h"
+#include "capi_internal.h"
+#include "dbscan.h"
+#include "launch.h"
+#include "systems.h"
+
+namespace chaos {
+
+namespace {
+thread_local std::string g_err;
+
+struct DeviceCtx {
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+};
+std::mutex g_mu;
+std::vector<DeviceCtx> g_dev;
+}  // namespace
+
+int set_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) return set_error(CHAOS_E_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return set_error(CHAOS_E_NODEV, "%s: %s", what, cudaGetErrorString(e));
+    return set_error(CHAOS_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Per-device stream and memory pool, created on first use. The pool keeps
+// freed blocks (release threshold = max) so repeated calls do not go back to
+// the driver.
+static int device_ctx(int dev, DeviceCtx** out) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count <= 0) return cuda_error(e == cudaSuccess ? cudaErrorNoDevice : e, "device count");
+    if (dev < 0 || dev >= count) return set_error(CHAOS_E_ARGS, "device %d out of range (%d devices)", dev, count);
+    if ((int)g_dev.size() < count) g_dev.resize(count);
+    DeviceCtx& c = g_dev[dev];
+    if (!c.ready) {
+        if ((e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_error(e, "stream create");
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        if ((e = cudaMemPoolCreate(&c.pool, &props)) != cudaSuccess) return cuda_error(e, "pool create");
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(c.pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        c.ready = true;
+    }
+    *out = &c;
+    return CHAOS_OK;
+}
+
+int Call::begin(const chaos_exec* e) {
+    ex = e ? *e : chaos_exec{CHAOS_FP64, CHAOS_MEM_HOST, nullptr, -1};
+    if (ex.precision != CHAOS_FP64 && ex.precision != CHAOS_FP32)
+        return set_error(CHAOS_E_ARGS, "precision must be CHAOS_FP64 or CHAOS_FP32");
+    if (ex.memory != CHAOS_MEM_HOST && ex.memory != CHAOS_MEM_DEVICE)
+        return set_error(CHAOS_E_ARGS, "memory must be CHAOS_MEM_HOST or CHAOS_MEM_DEVICE");
+    cudaError_t err = cudaGetDevice(&prevDevice);
+    if (err != cudaSuccess) return cuda_error(err, "get device");
+    device = ex.device >= 0 ? ex.device : prevDevice;
+    if (device != prevDevice && (err = cudaSetDevice(device)) != cudaSuccess) return cuda_error(err, "set device");
+    DeviceCtx* c = nullptr;
+    int rc = device_ctx(device, &c);
+    if (rc) return rc;
+    pool = c->pool;
+    stream = ex.stream ? (cudaStream_t)ex.stream : c->stream;
+    return CHAOS_OK;
+}
+
+void* Call::alloc(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    void* p = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, stream);
+    if (e != cudaSuccess) {
+        cuda_error(e, "device allocation");
+        failed = true;
+        return nullptr;
+    }
+    owned.push_back(p);
+    return p;
+}
+
+int Call::finish(int rc) {
+    for (void* p : owned) cudaFreeAsync(p, stream);
+    owned.clear();
+    if (rc == CHAOS_OK) {
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess && ex.memory == CHAOS_MEM_HOST) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) rc = cuda_error(e, "execution");
+    }
+    if (device != prevDevice) cudaSetDevice(prevDevice);
+    return rc;
+}
+
+int Call::to_host(void* host, const void* dev, size_t bytes) {
+    if (ex.memory != CHAOS_MEM_HOST || !host || bytes == 0) return CHAOS_OK;
+    cudaError_t e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, stream);
+    return e == cudaSuccess ? CHAOS_OK : cuda_error(e, "copy to host");
+}
+
+const void* Call::input(const void* user, size_t bytes) {
+    if (!user) return nullptr;
+    if (ex.memory == CHAOS_MEM_DEVICE) return user;
+    void* d = alloc(bytes);
+    if (!d) return nullptr;
+    cudaError_t e = cudaMemcpyAsync(d, user, bytes, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) {
+        cuda_error(e, "copy to device");
+        failed = true;
+        return nullptr;
+    }
+    return d;
+}
+
+void* Call::output(void* user, size_t bytes) {
+    if (!user) return nullptr;
+    if (ex.memory == CHAOS_MEM_DEVICE) return user;
+    return alloc(bytes);
+}
+
+// ---------------------------------------------------------------------------
+// argument checks shared by the sweeps
+
+static int check_system(int system, int nIC, int nValues) {
+    if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
+    if (nIC != system_nx(system))
+        return set_error(CHAOS_E_ARGS, "amountOfInitialConditions %d != SIZE_X %d of system %d", nIC,
+                         system_nx(system), system);
+    if (nValues != system_na(system))
+        return set_error(CHAOS_E_ARGS, "amountOfValues %d != SIZE_A %d of system %d", nValues, system_na(system),
+                         system);
+    return CHAOS_OK;
+}
+
+int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, double h, int nIC, const double* ic,
+               const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
+               const double* values, int nValues, int preScaller, bool basins) {
+    int rc = check_system(system, nIC, nValues);
+    if (rc) return rc;
+    if (!ic || !ranges || !mut || !values) return set_error(CHAOS_E_ARGS, "null parameter array");
+    if (!(h > 0) || !(tMax > 0) || !(transientTime >= 0)) return set_error(CHAOS_E_ARGS, "need h > 0, tMax > 0, transientTime >= 0");
+    if (nPts < 2) return set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+    if (preScaller < 1) return set_error(CHAOS_E_ARGS, "preScaller must be >= 1");
+    if (wv < 0 || wv >= nIC) return set_error(CHAOS_E_ARGS, "writableVar %d out of range", wv);
+    const int lim = basins ? nIC : nValues;
+    for (int d = 0; d < dim; ++d)
+        if (mut[d] < 0 || mut[d] >= lim) return set_error(CHAOS_E_ARGS, "indicesOfMutVars[%d] = %d out of range", d, mut[d]);
+    const double Bd = tMax / h / preScaller, Sd = transientTime / h;
+    if (!(Bd >= 1) || Bd > 2.0e9 || Sd > 2.0e9) return set_error(CHAOS_E_ARGS, "tMax/h/preScaller must be in [1, 2e9]");
+    memset(&P, 0, sizeof P);
+    P.system = system;
+    P.dim = dim;
+    P.B = (int)Bd;
+    P.S = (int)Sd;
+    P.preScaller = basins ? preScaller : 1;
+    P.wv = wv;
+    P.checkMax = maxValue != 0;
+    P.mutateState = basins ? 1 : 0;
+    P.h = h;
+    P.hInterval = h * (double)preScaller;
+    P.maxValue = maxValue;
+    for (int i = 0; i < nIC; ++i) P.ic[i] = ic[i];
+    for (int i = 0; i < nValues; ++i) P.values[i] = values[i];
+    P.mut[0] = mut[0];
+    P.mut[1] = dim > 1 ? mut[1] : -1;
+    P.grid.nPts = nPts;
+    for (int d = 0; d < dim; ++d) {
+        P.grid.start[d] = ranges[2 * d];
+        P.grid.scale[d] = (ranges[2 * d + 1] - ranges[2 * d]) / (double)(nPts - 1);
+    }
+    P.pBegin = 0;
+    P.nPoints = dim == 1 ? (long long)nPts : (long long)nPts * nPts;
+    return CHAOS_OK;
+}
+
+size_t scratch_budget_bytes() {
+    const char* s = getenv("CHAOS_SCRATCH_BUDGET_MB");
+    size_t mb = s ? (size_t)strtoull(s, nullptr, 10) : 8192;
+    return std::max<size_t>(mb, 1) << 20;
+}
+
+}  // namespace chaos
+
+using namespace chaos;
+
+extern "C" {
+
+int chaos_abi_version(void) { return CHAOS_ABI_VERSION; }
+const char* chaos_last_error(void) { return g_err.c_str(); }
+
+int chaos_system_info(int system, int* sizeX, int* sizeA) {
+    if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
+    if (sizeX) *sizeX = system_nx(system);
+    if (sizeA) *sizeA = system_na(system);
+    return CHAOS_OK;
+}
+
+int chaos_synchronize(const chaos_exec* ex) {
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    rc = e == cudaSuccess ? CHAOS_OK : cuda_error(e, "synchronize");
+    return c.finish(rc);
+}
+
+int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, int peakCapacity, int* counts,
+                        int* flags, double* firstSample, double* peaks, double* intervals) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 1, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        false);
+    if (rc) return rc;
+    if (!counts || !flags) return set_error(CHAOS_E_ARGS, "counts and flags are required");
+    if (peakCapacity < 0 || ((peaks || intervals) && peakCapacity == 0))
+        return set_error(CHAOS_E_ARGS, "peakCapacity must be > 0 when peaks or intervals are requested");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const long long n = P.nPoints;
+    const size_t rowBytes = (size_t)n * peakCapacity * sizeof(double);
+    BifOut O;
+    O.cap = peakCapacity;
+    O.counts = (int*)c.output(counts, n * sizeof(int));
+    O.flags = (int*)c.output(flags, n * sizeof(int));
+    O.first = (double*)c.output(firstSample, n * sizeof(double));
+    O.peaks = (double*)c.output(peaks, rowBytes);
+    O.intervals = (double*)c.output(intervals, rowBytes);
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_bif_f32(P, O, c.stream) : launch_bif_f64(P, O, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation kernel"));
+    rc = c.to_host(counts, O.counts, n * sizeof(int));
+    if (!rc) rc = c.to_host(flags, O.flags, n * sizeof(int));
+    if (!rc) rc = c.to_host(firstSample, O.first, n * sizeof(double));
+    if (!rc) rc = c.to_host(peaks, O.peaks, rowBytes);
+    if (!rc) rc = c.to_host(intervals, O.intervals, rowBytes);
+    return c.finish(rc);
+}
+
+int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, double eps, int* labels,
+                        int* counts) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 2, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        false);
+    if (rc) return rc;
+    if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const long long n = P.nPoints;
+    // every detected peak sits at least two samples after the previous one,
+    // so B/2 rows hold all kept intervals of a point
+    const int cap = std::max(P.B / 2, 1);
+    const size_t perPoint = (size_t)cap * (sizeof(double) + 2 * sizeof(int));
+    long long chunk = (long long)std::max<size_t>(scratch_budget_bytes() / perPoint, 1);
+    chunk = std::min(chunk, n);
+    int* dLabels = (int*)c.output(labels, n * sizeof(int));
+    int* dCounts = counts ? (int*)c.output(counts, n * sizeof(int)) : (int*)c.alloc(n * sizeof(int));
+    int* dFlags = (int*)c.alloc(chunk * sizeof(int));
+    double* dIv = (double*)c.alloc((size_t)chunk * cap * sizeof(double));
+    int* dLab = (int*)c.alloc((size_t)chunk * cap * sizeof(int));
+    int* dSlot = (int*)c.alloc((size_t)chunk * cap * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    for (long long b = 0; b < n; b += chunk) {
+        SweepParams Q = P;
+        Q.pBegin = b;
+        Q.nPoints = std::min(chunk, n - b);
+        BifOut O{dCounts + b, dFlags, nullptr, nullptr, dIv, cap};
+        cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_bif_f32(Q, O, c.stream) : launch_bif_f64(Q, O, c.stream);
+        if (e == cudaSuccess)
+            e = launch_point_dbscan(dIv, dCounts + b, Q.nPoints, cap, eps, dLab, dSlot, dLabels + b, c.stream);
+        if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation 2-D kernels"));
+    }
+    rc = c.to_host(labels, dLabels, n * sizeof(int));
+    if (!rc && counts) rc = c.to_host(counts, dCounts, n * sizeof(int));
+    return c.finish(rc);
+}
+
+int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nPts, double h, double eps,
+                const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+                const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                const double* values, int amountOfValues, double* lle) {
+    (void)writableVar;
+    (void)maxValue;
+    int rc = check_system(system, amountOfInitialConditions, amountOfValues);
+    if (rc) return rc;
+    if (!initialConditions || !ranges || !indicesOfMutVars || !values || !lle)
+        return set_error(CHAOS_E_ARGS, "null argument");
+    if (nPts < 1) return set_error(CHAOS_E_ARGS, "nPts must be >= 1");
+    if (!(h > 0) || !(tMax > 0) || !(NT > 0) || !(transientTime >= 0) || !(eps > 0))
+        return set_error(CHAOS_E_ARGS, "need h, tMax, NT, eps > 0 and transientTime >= 0");
+    for (int d = 0; d < 2; ++d)
+        if (indicesOfMutVars[d] < 0 || indicesOfMutVars[d] >= amountOfValues)
+            return set_error(CHAOS_E_ARGS, "indicesOfMutVars[%d] out of range", d);
+    if (NT / h > 2.0e9 || tMax / h > 2.0e9 || transientTime / h > 2.0e9)
+        return set_error(CHAOS_E_ARGS, "step counts must fit in int");
+    LleParams L;
+    memset(&L, 0, sizeof L);
+    L.system = system;
+    L.nPts = nPts;
+    L.ntp = static_cast<int>(NT / h);
+    L.trans = static_cast<int>(transientTime / h);
+    const int all = static_cast<int>(tMax / h);
+    if (L.ntp < 1) return set_error(CHAOS_E_ARGS, "NT / h must be >= 1");
+    L.calcBlocks = all / L.ntp + 1;
+    L.h = h;
+    L.eps = eps;
+    L.tMax = tMax;
+    for (int i = 0; i < amountOfInitialConditions; ++i) L.ic[i] = initialConditions[i];
+    for (int i = 0; i < amountOfValues; ++i) L.values[i] = values[i];
+    L.mut[0] = indicesOfMutVars[0];
+    L.mut[1] = indicesOfMutVars[1];
+    L.rangeA[0] = ranges[0];
+    L.rangeA[1] = ranges[1];
+    L.rangeB[0] = ranges[2];
+    L.rangeB[1] = ranges[3];
+    L.stepA = nPts > 1 ? (ranges[1] - ranges[0]) / (nPts - 1) : 0.0;
+    L.stepB = nPts > 1 ? (ranges[3] - ranges[2]) / (nPts - 1) : 0.0;
+    L.pBegin = 0;
+    L.nPoints = (long long)nPts * nPts;
+    if (ex && ex->precision == CHAOS_FP32 && !system_has_difference_form(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_lle_f32(L, dOut, c.stream) : launch_lle_f64(L, dOut, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "LLE kernel"));
+    rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_basins_features(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                          int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                          const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                          const double* values, int amountOfValues, int preScaller, int* flags, double* avgPeaks,
+                          double* avgIntervals, int* counts) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 2, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        true);
+    if (rc) return rc;
+    if (!flags || !avgPeaks || !avgIntervals) return set_error(CHAOS_E_ARGS, "flags, avgPeaks and avgIntervals are required");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const long long n = P.nPoints;
+    BasinsOut O;
+    O.flags = (int*)c.output(flags, n * sizeof(int));
+    O.avgPeaks = (double*)c.output(avgPeaks, n * sizeof(double));
+    O.avgIntervals = (double*)c.output(avgIntervals, n * sizeof(double));
+    O.counts = (int*)c.output(counts, n * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "basins kernel"));
+    rc = c.to_host(flags, O.flags, n * sizeof(int));
+    if (!rc) rc = c.to_host(avgPeaks, O.avgPeaks, n * sizeof(double));
+    if (!rc) rc = c.to_host(avgIntervals, O.avgIntervals, n * sizeof(double));
+    if (!rc) rc = c.to_host(counts, O.counts, n * sizeof(int));
+    return c.finish(rc);
+}
+
+int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double h, int amountOfInitialConditions,
+                 const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                 int writableVar, double maxValue, double transientTime, const double* values, int amountOfValues,
+                 int preScaller, double eps, int* labels, double* avgPeaks, double* avgIntervals, int* flags) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 2, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        true);
+    if (rc) return rc;
+    if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
+    if (!(eps >= 0)) return set_error(CHAOS_E_ARGS, "eps must be >= 0");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const long long n = P.nPoints;
+    BasinsOut O;
+    O.flags = flags ? (int*)c.output(flags, n * sizeof(int)) : (int*)c.alloc(n * sizeof(int));
+    O.avgPeaks = avgPeaks ? (double*)c.output(avgPeaks, n * sizeof(double)) : (double*)c.alloc(n * sizeof(double));
+    O.avgIntervals = avgIntervals ? (double*)c.output(avgIntervals, n * sizeof(double)) : (double*)c.alloc(n * sizeof(double));
+    O.counts = nullptr;
+    int* dLabels = (int*)c.output(labels, n * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "basins kernel"));
+    rc = dbscan_compat_device(c, O.avgPeaks, O.avgIntervals, O.flags, n, eps, dLabels);
+    if (!rc) rc = c.to_host(labels, dLabels, n * sizeof(int));
+    if (!rc && flags) rc = c.to_host(flags, O.flags, n * sizeof(int));
+    if (!rc && avgPeaks) rc = c.to_host(avgPeaks, O.avgPeaks, n * sizeof(double));
+    if (!rc && avgIntervals) rc = c.to_host(avgIntervals, O.avgIntervals, n * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_dbscan_compat(const chaos_exec* ex, const double* avgPeaks, const double* avgIntervals, const int* flags,
+                        long long n, double eps, int* labels) {
+    if (n < 0 || (n > 0 && (!avgPeaks || !avgIntervals || !flags || !labels)))
+        return set_error(CHAOS_E_ARGS, "null array or negative n");
+    if (!(eps >= 0)) return set_error(CHAOS_E_ARGS, "eps must be >= 0");
+    if (n > 0x7fffffffLL) return set_error(CHAOS_E_ARGS, "n must be < 2^31");
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    if (n == 0) return c.finish(CHAOS_OK);
+    const double* dP = (const double*)c.input(avgPeaks, n * sizeof(double));
+    const double* dI = (const double*)c.input(avgIntervals, n * sizeof(double));
+    const int* dF = (const int*)c.input(flags, n * sizeof(int));
+    int* dL = (int*)c.output(labels, n * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    rc = dbscan_compat_device(c, dP, dI, dF, n, eps, dL);
+    if (!rc) rc = c.to_host(labels, dL, n * sizeof(int));
+    return c.finish(rc);
+}
+
+int chaos_dbscan(const chaos_exec* ex, const double* features, long long n, int dims, double eps, int minPts,
+                 const int* mask, int* labels) {
+    if (n < 0 || (n > 0 && (!features || !labels))) return set_error(CHAOS_E_ARGS, "null array or negative n");
+    if (dims < 1 || dims > 3) return set_error(CHAOS_E_ARGS, "dims must be 1..3");
+    if (!(eps > 0) || minPts < 1) return set_error(CHAOS_E_ARGS, "need eps > 0 and minPts >= 1");
+    if (n > 0x7fffffffLL) return set_error(CHAOS_E_ARGS, "n must be < 2^31");
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    if (n == 0) return c.finish(CHAOS_OK);
+    const double* dF = (const double*)c.input(features, (size_t)n * dims * sizeof(double));
+    const int* dM = (const int*)c.input(mask, n * sizeof(int));
+    int* dL = (int*)c.output(labels, n * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    rc = dbscan_device(c, dF, n, dims, eps, minPts, dM, dL);
+    if (!rc) rc = c.to_host(labels, dL, n * sizeof(int));
+    return c.finish(rc);
+}
+
+int chaos_peak_finder(const chaos_exec* ex, const double* data, long long nSeries, int len, double h,
+                      int peakCapacity, int* counts, double* peaks, double* intervals) {
+    if (nSeries < 0 || len < 0 || peakCapacity < 1 || (nSeries > 0 && (!data || !counts || !peaks || !intervals)))
+        return set_error(CHAOS_E_ARGS, "bad peak finder arguments");
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    if (nSeries == 0) return c.finish(CHAOS_OK);
+    const size_t rows = (size_t)nSeries * peakCapacity * sizeof(double);
+    const double* dD = (const double*)c.input(data, (size_t)nSeries * len * sizeof(double));
+    int* dC = (int*)c.output(counts, nSeries * sizeof(int));
+    double* dP = (double*)c.output(peaks, rows);
+    double* dI = (double*)c.output(intervals, rows);
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = launch_peak_finder(dD, nSeries, len, h, peakCapacity, dC, dP, dI, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "peak finder kernel"));
+    rc = c.to_host(counts, dC, nSeries * sizeof(int));
+    if (!rc) rc = c.to_host(peaks, dP, rows);
+    if (!rc) rc = c.to_host(intervals, dI, rows);
+    return c.finish(rc);
+}
+
+int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int* counts, long long n, int stride,
+                       double eps, int* labels) {
+    if (n < 0 || stride < 1 || (n > 0 && (!intervals || !counts || !labels)))
+        return set_error(CHAOS_E_ARGS, "bad point dbscan arguments");
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    if (n == 0) return c.finish(CHAOS_OK);
+    const double* dI = (const double*)c.input(intervals, (size_t)n * stride * sizeof(double));
+    const int* dC = (const int*)c.input(counts, n * sizeof(int));
+    int* dL = (int*)c.output(labels, n * sizeof(int));
+    int* lab = (int*)c.alloc((size_t)n * stride * sizeof(int));
+    int* slot = (int*)c.alloc((size_t)n * stride * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = launch_point_dbscan(dI, dC, n, stride, eps, lab, slot, dL, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "point dbscan kernel"));
+    rc = c.to_host(labels, dL, n * sizeof(int));
+    return c.finish(rc);
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+// The reference's host entry points (Bifurcation::bifurcation1D/2D,
+// LLE::LLE2D, Basins::basinsOfAttraction_2) on top of the C ABI, writing the
+// reference's CSV files byte for byte: same headers, same stream precisions
+// (default for headers and LLE values, 12 for bifurcation rows, 15 for every
+// basins file), same ", " separators with the reference's line-break rule
+// (a row break is written as ", " then "\n"), NaN LLE values printed as 0.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <string>
+#include <vector>
+
+#include "../../include/chaos_compat.hpp"
+#include "../../include/chaos_gb300.h"
+#include "capi_internal.h"
+
+namespace {
+
+int g_system = -1;
+int g_precision = -1;
+
+int parse_system(const char* s) {
+    static const char* names[] = {"lorenz", "rossler", "chen", "chameleon", "rossler_cd", "sin3", "sin2", "memristor"};
+    for (int i = 0; i < 8; ++i)
+        if (strcmp(s, names[i]) == 0) return i;
+    char* end = nullptr;
+    long v = strtol(s, &end, 10);
+    return (end && *end == 0) ? (int)v : CHAOS_SYS_CHAMELEON;
+}
+
+int active_system() {
+    if (g_system >= 0) return g_system;
+    const char* s = getenv("CHAOS_SYSTEM");
+    return s ? parse_system(s) : CHAOS_SYS_CHAMELEON;
+}
+
+chaos_exec active_exec() {
+    int prec = g_precision;
+    if (prec < 0) {
+        const char* s = getenv("CHAOS_PRECISION");
+        prec = (s && (strcmp(s, "fp32") == 0 || strcmp(s, "1") == 0)) ? CHAOS_FP32 : CHAOS_FP64;
+    }
+    return chaos_exec{prec, CHAOS_MEM_HOST, nullptr, -1};
+}
+
+// getValueByIdx as the reference's host code evaluates it for the CSV
+// (Bifurcation/src/bifurcationCUDA.cu:400-419): start + n*scale.
+double host_grid_value(long long idx, int nPts, double start, double finish) {
+    const long long n = idx % nPts;
+    const double scale = (finish - start) / (nPts - 1);
+    return start + n * scale;
+}
+
+// Writes n values with the reference's matrix rule: ", " before every value
+// but the first, "\n" (after the ", ") whenever nPts values are on the line.
+template <class T, class F> void write_matrix(std::ofstream& o, const T* v, long long n, int nPts, F fmt) {
+    int counter = 0;
+    for (long long i = 0; i < n; ++i) {
+        if (counter != 0) o << ", ";
+        if (counter == nPts) {
+            o << "\n";
+            counter = 0;
+        }
+        fmt(o, v[i]);
+        ++counter;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int chaos_compat_set_system(int system) {
+    if (system < 0 || system > CHAOS_SYS_MEMRISTOR) return chaos::set_error(CHAOS_E_ARGS, "unknown system %d", system);
+    g_system = system;
+    return CHAOS_OK;
+}
+
+int chaos_compat_set_precision(int precision) {
+    if (precision != CHAOS_FP64 && precision != CHAOS_FP32) return chaos::set_error(CHAOS_E_ARGS, "bad precision");
+    g_precision = precision;
+    return CHAOS_OK;
+}
+
+int chaos_compat_get_system(void) { return active_system(); }
+
+int chaos_compat_bifurcation1D(double tMax, int nPts, double h, int amountOfInitialConditions,
+                               const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                               int writableVar, double maxValue, double transientTime, const double* values,
+                               int amountOfValues, int preScaller, const char* OUT_FILE_PATH) {
+    if (nPts < 2 || !(h > 0) || preScaller < 1) return chaos::set_error(CHAOS_E_ARGS, "bad sweep arguments");
+    const int B = (int)(tMax / h / preScaller);
+    const int cap = B / 2 > 0 ? B / 2 : 1;
+    std::vector<int> counts(nPts), flags(nPts);
+    std::vector<double> first(nPts), peaks((size_t)nPts * cap), intervals((size_t)nPts * cap);
+    chaos_exec ex = active_exec();
+    int rc = chaos_bifurcation1d(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions,
+                                 ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                 amountOfValues, preScaller, cap, counts.data(), flags.data(), first.data(),
+                                 peaks.data(), intervals.data());
+    if (rc) return rc;
+    std::ofstream o(OUT_FILE_PATH);
+    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+    o << ranges[0] << " " << ranges[1] << "\n";
+    o << std::setprecision(12);
+    for (int k = 0; k < nPts; ++k) {
+        const double p = host_grid_value(k, nPts, ranges[0], ranges[1]);
+        if (counts[k] == -1) {
+            o << p << ", " << first[k] << ", " << 0 << '\n';
+        } else {
+            for (int j = 0; j < counts[k]; ++j)
+                o << p << ", " << peaks[(size_t)k * cap + j] << ", " << intervals[(size_t)k * cap + j] << '\n';
+        }
+    }
+    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+}
+
+int chaos_compat_bifurcation2D(double tMax, int nPts, double h, int amountOfInitialConditions,
+                               const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                               int writableVar, double maxValue, double transientTime, const double* values,
+                               int amountOfValues, int preScaller, double eps, const char* OUT_FILE_PATH) {
+    if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+    const long long n = (long long)nPts * nPts;
+    std::vector<int> labels(n);
+    chaos_exec ex = active_exec();
+    int rc = chaos_bifurcation2d(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions,
+                                 ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                 amountOfValues, preScaller, eps, labels.data(), nullptr);
+    if (rc) return rc;
+    std::ofstream o(OUT_FILE_PATH);
+    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+    o << ranges[0] << " " << ranges[1] << "\n";
+    o << ranges[2] << " " << ranges[3] << "\n";
+    o << std::setprecision(12);
+    write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+}
+
+int chaos_compat_LLE2D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                       int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                       int writableVar, double maxValue, double transientTime, const double* values,
+                       int amountOfValues, const char* OUT_FILE_PATH) {
+    if (nPts < 1) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 1");
+    const long long n = (long long)nPts * nPts;
+    std::vector<double> lle(n);
+    chaos_exec ex = active_exec();
+    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHEN_RK4) ex.precision = CHAOS_FP64;
+    std::ofstream o(OUT_FILE_PATH);
+    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+    o << ranges[0] << " " << ranges[1] << "\n";
+    o << ranges[2] << " " << ranges[3] << "\n";
+    int rc = chaos_lle2d(&ex, active_system(), tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
+                         ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
+                         lle.data());
+    if (rc) return rc;
+    write_matrix(o, lle.data(), n, nPts, [](std::ofstream& s, double v) { s << (std::isnan(v) ? 0 : v); });
+    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+}
+
+int chaos_compat_basinsOfAttraction_2(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                      const double* initialConditions, const double* ranges,
+                                      const int* indicesOfMutVars, int writableVar, double maxValue,
+                                      double transientTime, const double* values, int amountOfValues,
+                                      int preScaller, double eps, const char* OUT_FILE_PATH) {
+    if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+    const long long n = (long long)nPts * nPts;
+    std::vector<int> labels(n), flags(n);
+    std::vector<double> ap(n), ai(n);
+    chaos_exec ex = active_exec();
+    int rc = chaos_basins(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                          indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                          eps, labels.data(), ap.data(), ai.data(), flags.data());
+    if (rc) return rc;
+    const std::string base(OUT_FILE_PATH);
+    const std::string paths[4] = {base, base + "_1.csv", base + "_2.csv", base + "_3.csv"};
+    for (int f = 0; f < 4; ++f) {
+        std::ofstream o(paths[f]);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", paths[f].c_str());
+        o << std::setprecision(15);
+        o << ranges[0] << " " << ranges[1] << "\n";
+        o << ranges[2] << " " << ranges[3] << "\n";
+        if (f == 0) write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+        if (f == 1) write_matrix(o, ap.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
+        if (f == 2) write_matrix(o, ai.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
+        if (f == 3) write_matrix(o, flags.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+        if (!o.good()) return chaos::set_error(CHAOS_E_IO, "write failed: %s", paths[f].c_str());
+    }
+    return CHAOS_OK;
+}
+
+}  // extern "C"
+
+namespace Bifurcation {
+int bifurcation1D(const double tMax, const int nPts, const double h, const int amountOfInitialConditions,
+                  const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                  const int writableVar, const double maxValue, const double transientTime, const double* values,
+                  const int amountOfValues, const int preScaller, std::string OUT_FILE_PATH) {
+    return chaos_compat_bifurcation1D(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                                      indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
+                                      preScaller, OUT_FILE_PATH.c_str());
+}
+int bifurcation2D(const double tMax, const int nPts, const double h, const int amountOfInitialConditions,
+                  const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                  const int writableVar, const double maxValue, const double transientTime, const double* values,
+                  const int amountOfValues, const int preScaller, const double eps, std::string OUT_FILE_PATH) {
+    return chaos_compat_bifurcation2D(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                                      indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
+                                      preScaller, eps, OUT_FILE_PATH.c_str());
+}
+}  // namespace Bifurcation
+
+namespace LLE {
+int LLE2D(const double tMax, const double NT, const int nPts, const double h, const double eps,
+          const double* initialConditions, const int amountOfInitialConditions, const double* ranges,
+          const int* indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,
+          const double* values, const int amountOfValues, std::string OUT_FILE_PATH) {
+    return chaos_compat_LLE2D(tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                              indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
+                              OUT_FILE_PATH.c_str());
+}
+}  // namespace LLE
+
+namespace Basins {
+int basinsOfAttraction_2(const double tMax, const int nPts, const double h, const int amountOfInitialConditions,
+                         const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                         const int writableVar, const double maxValue, const double transientTime,
+                         const double* values, const int amountOfValues, const int preScaller, const double eps,
+                         std::string OUT_FILE_PATH) {
+    return chaos_compat_basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                                             indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                             amountOfValues, preScaller, eps, OUT_FILE_PATH.c_str());
+}
+}  // namespace Basins

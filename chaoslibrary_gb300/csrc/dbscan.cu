@@ -1,0 +1,720 @@
+// Grid clustering on the device.
+//
+// Both clusterings share one pipeline over points in a D-dimensional feature
+// space (D = 1..3), all integer/FP64 and bound by memory traffic:
+//   1. cell of every point: floor(f / side) per dimension, side = eps/sqrt(D)
+//      shrunk by 1e-9, so two points of one cell are always within eps and a
+//      neighbour within eps is at most R = 2 cells away per dimension;
+//   2. an open-addressing hash table of the occupied cells (64-bit packed
+//      coordinates), their dense numbering and a counting sort of the points
+//      by cell, with the features gathered into cell order (coalesced reads
+//      for everything that follows);
+//   3. per cell: bounding box and the list of occupied neighbour cells;
+//   4. (DBSCAN) core flags: a cell holding >= minPts points makes all of them
+//      core; otherwise neighbours are counted exactly, with early exit;
+//   5. union-find over points (parent[v] <= v, lock-free hooking with
+//      atomicCAS): every cell's core points are linked to its smallest one,
+//      then one warp per neighbouring cell pair looks for a core pair within
+//      eps (lanes stride over the second cell, per-point box pruning, early
+//      exit), so the root of a component is its smallest core index;
+//   6. numbering by prefix sums over the root indices.
+// Distances are sqrt(sum of squared differences) <= eps in FP64, in dimension
+// order, each operation rounded on its own (this file is compiled with
+// --fmad=false), as the reference computes them (Basins/src/basinsCUDA.cu:918).
+// Cells whose coordinates had to be clamped (|f| / side >= 2^19) or that hold
+// a NaN feature lose the one-cell-is-connected shortcut and are resolved by
+// exact pair tests.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "dbscan.h"
+
+namespace chaos {
+
+namespace {
+
+constexpr int kTPB = 256;
+constexpr unsigned long long kEmpty = ~0ull;
+constexpr long long kLim = 1LL << 19;  // clamp of cell coordinates (21-bit packing for D = 3)
+constexpr int kR = 2;                  // neighbour reach in cells
+
+struct Feat {
+    const double* f[3];
+    int D;
+};
+
+__device__ __forceinline__ unsigned long long pack(const long long* c, int D) {
+    if (D <= 2) {
+        const unsigned long long a = (unsigned long long)(c[0] + 2147483648LL);
+        const unsigned long long b = (unsigned long long)((D == 2 ? c[1] : 0) + 2147483648LL);
+        return (a << 32) | (b & 0xffffffffull);
+    }
+    return (((unsigned long long)c[0] & 0x1FFFFFull) << 42) | (((unsigned long long)c[1] & 0x1FFFFFull) << 21) |
+           ((unsigned long long)c[2] & 0x1FFFFFull);
+}
+
+__device__ __forceinline__ void unpack(unsigned long long k, int D, long long* c) {
+    if (D <= 2) {
+        c[0] = (long long)(k >> 32) - 2147483648LL;
+        c[1] = (long long)(k & 0xffffffffull) - 2147483648LL;
+        c[2] = 0;
+        return;
+    }
+    for (int d = 0; d < 3; ++d) {
+        long long v = (long long)((k >> (42 - 21 * d)) & 0x1FFFFFull);
+        if (v & 0x100000) v -= 0x200000;
+        c[d] = v;
+    }
+}
+
+__device__ __forceinline__ unsigned long long mix(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+__device__ __forceinline__ double dist2(const double* a, const double* b, int D) {
+    double s = 0.0;
+    for (int d = 0; d < D; ++d) {
+        const double df = a[d] - b[d];
+        s = s + df * df;
+    }
+    return s;
+}
+
+// ---- prefix sum ------------------------------------------------------------
+constexpr int kScanItems = 4096;  // 1024 threads x 4
+
+__global__ void __launch_bounds__(1024) scan_block_kernel(const int* in, int* out, int* blockSums, long long n) {
+    __shared__ int warpSums[32];
+    const long long base = (long long)blockIdx.x * kScanItems + threadIdx.x * 4;
+    int v[4], s = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[j] = base + j < n ? in[base + j] : 0;
+        s += v[j];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int ws = warpSums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        warpSums[lane] = ws;
+    }
+    __syncthreads();
+    int prefix = (w > 0 ? warpSums[w - 1] : 0) + x - s;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (base + j < n) out[base + j] = prefix;
+        prefix += v[j];
+    }
+    if (threadIdx.x == 1023) blockSums[blockIdx.x] = warpSums[31];
+}
+
+__global__ void add_offsets_kernel(int* out, const int* offsets, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += offsets[i / kScanItems];
+}
+
+inline unsigned blocks(long long n, int tpb = kTPB) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// ---- grid construction -----------------------------------------------------
+__global__ void cell_key_kernel(Feat F, const int* include, long long n, double side, unsigned long long* key,
+                                unsigned char* unsafe) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!include[i]) { key[i] = kEmpty; unsafe[i] = 0; return; }
+    long long c[3] = {0, 0, 0};
+    bool bad = false;
+    for (int d = 0; d < F.D; ++d) {
+        const double q = F.f[d][i] / side;
+        if (q != q) { c[0] = kLim + 5; c[1] = kLim + 5; c[2] = kLim + 5; bad = true; break; }
+        long long v;
+        if (q >= (double)kLim) { v = kLim; bad = true; }
+        else if (q < -(double)kLim) { v = -kLim; bad = true; }
+        else v = (long long)floor(q);
+        c[d] = v;
+    }
+    key[i] = pack(c, F.D);
+    unsafe[i] = bad ? 1 : 0;
+}
+
+__global__ void hash_insert_kernel(const unsigned long long* key, long long n, unsigned long long* tab,
+                                   unsigned long long mask, long long* slot) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = key[i];
+    if (k == kEmpty) { slot[i] = -1; return; }
+    unsigned long long h = mix(k) & mask;
+    for (unsigned long long probe = 0; probe <= mask; ++probe) {
+        const unsigned long long prev = atomicCAS(&tab[h], kEmpty, k);
+        if (prev == kEmpty || prev == k) { slot[i] = (long long)h; return; }
+        h = (h + 1) & mask;
+    }
+    slot[i] = -1;  // unreachable: the table has twice as many slots as points
+}
+
+__global__ void occupied_kernel(const unsigned long long* tab, long long cap, int* occ) {
+    const long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < cap) occ[h] = tab[h] != kEmpty;
+}
+
+__global__ void cell_ids_kernel(const unsigned long long* tab, long long cap, const int* occScan, int* slotCell,
+                                unsigned long long* cellKey) {
+    const long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cap) return;
+    if (tab[h] != kEmpty) {
+        slotCell[h] = occScan[h];
+        cellKey[occScan[h]] = tab[h];
+    } else {
+        slotCell[h] = -1;
+    }
+}
+
+__global__ void point_cell_kernel(const long long* slot, long long n, const int* slotCell, int* cellOf, int* cnt) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (slot[i] < 0) { cellOf[i] = -1; return; }
+    const int c = slotCell[slot[i]];
+    cellOf[i] = c;
+    atomicAdd(&cnt[c], 1);
+}
+
+__global__ void scatter_kernel(Feat F, long long n, const int* cellOf, const int* start, int* cursor, int* order,
+                               double* s0, double* s1, double* s2) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cellOf[i];
+    if (c < 0) return;
+    const int pos = start[c] + atomicAdd(&cursor[c], 1);
+    order[pos] = (int)i;
+    s0[pos] = F.f[0][i];
+    if (F.D > 1) s1[pos] = F.f[1][i];
+    if (F.D > 2) s2[pos] = F.f[2][i];
+}
+
+struct Sorted {
+    const double* s[3];
+    const int* order;
+    const int* start;  // C + 1 entries
+    int D;
+    __device__ __forceinline__ void load(int pos, double* v) const {
+        for (int d = 0; d < D; ++d) v[d] = s[d][pos];
+    }
+};
+
+// warp per cell: bounding box and the unsafe flag
+__global__ void cell_box_kernel(Sorted S, int C, const unsigned char* unsafePt, double* boxLo, double* boxHi,
+                                unsigned char* unsafeCell) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= C) return;
+    const int b = S.start[w], e = S.start[w + 1];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    int bad = 0;
+    for (int p = b + lane; p < e; p += 32) {
+        for (int d = 0; d < S.D; ++d) {
+            const double v = S.s[d][p];
+            lo[d] = fmin(lo[d], v);
+            hi[d] = fmax(hi[d], v);
+        }
+        bad |= unsafePt[S.order[p]];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) {
+        for (int d = 0; d < 3; ++d) {
+            boxLo[3 * (long long)w + d] = lo[d];
+            boxHi[3 * (long long)w + d] = hi[d];
+        }
+        unsafeCell[w] = bad ? 1 : 0;
+    }
+}
+
+__device__ __forceinline__ int hash_find(const unsigned long long* tab, unsigned long long mask, const int* slotCell,
+                                         unsigned long long k) {
+    unsigned long long h = mix(k) & mask;
+    for (unsigned long long probe = 0; probe <= mask; ++probe) {
+        const unsigned long long t = tab[h];
+        if (t == k) return slotCell[h];
+        if (t == kEmpty) return -1;
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// per cell: number (pass 0) or list (pass 1) of occupied neighbour cells
+__global__ void neighbours_kernel(const unsigned long long* cellKey, int C, int D, const unsigned long long* tab,
+                                  unsigned long long mask, const int* slotCell, int* nbCount, const int* nbStart,
+                                  int* nbList, int* nbOwner) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    long long base[3];
+    unpack(cellKey[c], D, base);
+    const int ry = D >= 2 ? kR : 0, rz = D >= 3 ? kR : 0;
+    int k = 0;
+    const int w0 = nbStart ? nbStart[c] : 0;
+    for (int dx = -kR; dx <= kR; ++dx)
+        for (int dy = -ry; dy <= ry; ++dy)
+            for (int dz = -rz; dz <= rz; ++dz) {
+                if (dx == 0 && dy == 0 && dz == 0) continue;
+                long long q[3] = {base[0] + dx, base[1] + dy, base[2] + dz};
+                const int c2 = hash_find(tab, mask, slotCell, pack(q, D));
+                if (c2 < 0) continue;
+                if (nbList) {
+                    nbList[w0 + k] = c2;
+                    nbOwner[w0 + k] = (int)c;
+                }
+                ++k;
+            }
+    if (!nbList) nbCount[c] = k;
+}
+
+// ---- union-find (parent[v] <= v) --------------------------------------------
+__device__ __forceinline__ int uf_find(int* parent, int x) {
+    int cur = __ldcg(parent + x);
+    if (cur != x) {
+        int prev = x, next;
+        while (cur > (next = __ldcg(parent + cur))) {
+            parent[prev] = next;
+            prev = cur;
+            cur = next;
+        }
+    }
+    return cur;
+}
+
+__device__ __forceinline__ void uf_unite(int* parent, int a, int b) {
+    int ra = uf_find(parent, a), rb = uf_find(parent, b);
+    while (ra != rb) {
+        if (ra < rb) { const int t = ra; ra = rb; rb = t; }
+        const int old = atomicCAS(parent + ra, ra, rb);
+        if (old == ra) break;
+        ra = old;
+        rb = uf_find(parent, rb);
+        ra = uf_find(parent, ra);
+    }
+}
+
+// ---- core points (DBSCAN) ----------------------------------------------------
+__global__ void core_kernel(Feat F, Sorted S, const int* cellOf, long long n, const int* nbStart, const int* nbList,
+                            const unsigned char* unsafeCell, double eps, int minPts, unsigned char* core) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cellOf[i];
+    if (c < 0) { core[i] = 0; return; }
+    const int own = S.start[c + 1] - S.start[c];
+    if (!unsafeCell[c] && own >= minPts) { core[i] = 1; return; }
+    double me[3] = {0, 0, 0};
+    for (int d = 0; d < F.D; ++d) me[d] = F.f[d][i];
+    int cnt = 0;
+    auto count_cell = [&](int cell) {
+        for (int p = S.start[cell]; p < S.start[cell + 1] && cnt < minPts; ++p) {
+            double v[3];
+            S.load(p, v);
+            if (sqrt(dist2(me, v, S.D)) <= eps) ++cnt;
+        }
+    };
+    if (!unsafeCell[c]) cnt = own;  // one cell is within eps of itself
+    else count_cell(c);
+    for (int e = nbStart[c]; e < nbStart[c + 1] && cnt < minPts; ++e) count_cell(nbList[e]);
+    core[i] = cnt >= minPts ? 1 : 0;
+}
+
+// warp per cell: link every core point of a safe cell to its smallest core
+// point; exact pair tests inside unsafe cells. rep[c] = smallest core index or -1.
+__global__ void intra_cell_kernel(Sorted S, int C, const unsigned char* core, const unsigned char* unsafeCell,
+                                  double eps, int* parent, int* rep) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= C) return;
+    const int b = S.start[w], e = S.start[w + 1];
+    int m = 0x7fffffff;
+    for (int p = b + lane; p < e; p += 32) {
+        const int i = S.order[p];
+        if (core[i]) m = min(m, i);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) rep[w] = m == 0x7fffffff ? -1 : m;
+    if (m == 0x7fffffff) return;
+    if (!unsafeCell[w]) {
+        for (int p = b + lane; p < e; p += 32) {
+            const int i = S.order[p];
+            if (core[i] && i != m) parent[i] = m;  // i is still a root: nothing else has linked it yet
+        }
+        return;
+    }
+    for (int p = b; p < e; ++p) {
+        const int i = S.order[p];
+        if (!core[i]) continue;
+        double a[3];
+        S.load(p, a);
+        for (int q = p + 1 + lane; q < e; q += 32) {
+            const int j = S.order[q];
+            if (!core[j]) continue;
+            double v[3];
+            S.load(q, v);
+            if (sqrt(dist2(a, v, S.D)) <= eps) uf_unite(parent, i, j);
+        }
+    }
+}
+
+__device__ __forceinline__ double box_gap2(const double* v, const double* lo, const double* hi, int D) {
+    double s = 0.0;
+    for (int d = 0; d < D; ++d) {
+        double g = 0.0;
+        if (v[d] < lo[d]) g = lo[d] - v[d];
+        else if (v[d] > hi[d]) g = v[d] - hi[d];
+        s = s + g * g;
+    }
+    return s;
+}
+
+// warp per (cell, neighbour cell) entry with neighbour > cell: unite the two
+// cells' core points if any core pair is within eps.
+__global__ void cross_cell_kernel(Sorted S, const int* nbOwner, const int* nbList, long long E,
+                                  const unsigned char* core, const unsigned char* unsafeCell, const int* rep,
+                                  const double* boxLo, const double* boxHi, double eps, int* parent) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= E) return;
+    const int ca = nbOwner[w], cb = nbList[w];
+    if (cb <= ca) return;
+    if (rep[ca] < 0 || rep[cb] < 0) return;
+    const bool safe = !unsafeCell[ca] && !unsafeCell[cb];
+    if (safe && uf_find(parent, rep[ca]) == uf_find(parent, rep[cb])) return;
+    const double* lo = boxLo + 3 * (long long)cb;
+    const double* hi = boxHi + 3 * (long long)cb;
+    const double eps2 = eps * eps;
+    for (int p = S.start[ca]; p < S.start[ca + 1]; ++p) {
+        const int i = S.order[p];
+        if (!core[i]) continue;
+        double a[3];
+        S.load(p, a);
+        if (box_gap2(a, lo, hi, S.D) > eps2 * 1.0000001) continue;
+        bool found = false;
+        for (int q0 = S.start[cb]; q0 < S.start[cb + 1]; q0 += 32) {
+            const int q = q0 + lane;
+            bool hit = false;
+            int j = -1;
+            if (q < S.start[cb + 1]) {
+                j = S.order[q];
+                if (core[j]) {
+                    double v[3];
+                    S.load(q, v);
+                    hit = sqrt(dist2(a, v, S.D)) <= eps;
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (bal) {
+                if (safe) {
+                    if (lane == __ffs(bal) - 1) uf_unite(parent, i, j);
+                    found = true;
+                    break;
+                }
+                if (hit) uf_unite(parent, i, j);
+            }
+        }
+        if (found) return;
+    }
+}
+
+__global__ void roots_kernel(int* parent, const unsigned char* core, long long n, int* root) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    root[i] = core[i] ? uf_find(parent, (int)i) : -1;
+}
+
+// ---- numbering: reference-compatible ----------------------------------------
+__global__ void compat_minfix_kernel(const int* root, const int* flags, long long n, int* minFix) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (root[i] >= 0 && flags[i] == -1) atomicMin(&minFix[root[i]], (int)i);
+}
+
+__global__ void compat_marks_kernel(const int* root, const int* minFix, long long n, int* negMark, int* posMark) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (root[i] == (int)i) {
+        if (minFix[i] < n) negMark[minFix[i]] = 1;  // several roots never share a minFix
+        else posMark[i] = 1;
+    }
+}
+
+__global__ void compat_labels_kernel(const int* root, const int* minFix, long long n, const int* negRank,
+                                     const int* posRank, int* labels) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = root[i];
+    if (r < 0) { labels[i] = 0; return; }
+    const int mf = minFix[r];
+    labels[i] = mf < n ? -(negRank[mf] + 1) : posRank[r] + 1;
+}
+
+// ---- numbering: DBSCAN ------------------------------------------------------
+__global__ void root_marks_kernel(const int* root, long long n, int* mark) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    mark[i] = root[i] == (int)i ? 1 : 0;
+}
+
+__global__ void dbscan_labels_kernel(Feat F, Sorted S, const int* cellOf, const int* include, long long n,
+                                     const int* nbStart, const int* nbList, const unsigned char* unsafeCell,
+                                     const unsigned char* core, const int* root, const int* rep, const int* rank,
+                                     double eps, int* labels) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!include[i]) { labels[i] = -2; return; }
+    if (core[i]) { labels[i] = rank[root[i]]; return; }
+    const int c = cellOf[i];
+    double me[3] = {0, 0, 0};
+    for (int d = 0; d < F.D; ++d) me[d] = F.f[d][i];
+    int best = 0x7fffffff;
+    if (!unsafeCell[c] && rep[c] >= 0) best = root[rep[c]];
+    auto scan = [&](int cell) {
+        for (int p = S.start[cell]; p < S.start[cell + 1]; ++p) {
+            const int j = S.order[p];
+            if (!core[j]) continue;
+            const int r = root[j];
+            if (r >= best) continue;
+            double v[3];
+            S.load(p, v);
+            if (sqrt(dist2(me, v, S.D)) <= eps) best = r;
+        }
+    };
+    if (unsafeCell[c]) scan(c);
+    for (int e = nbStart[c]; e < nbStart[c + 1]; ++e) scan(nbList[e]);
+    labels[i] = best == 0x7fffffff ? -1 : rank[best];
+}
+
+__global__ void soa_kernel(const double* F, long long n, int D, double* a, double* b, double* c) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    a[i] = F[i * D];
+    if (D > 1) b[i] = F[i * D + 1];
+    if (D > 2) c[i] = F[i * D + 2];
+}
+
+__global__ void include_kernel(const int* flags, const int* mask, long long n, int compat, int* include) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    include[i] = compat ? (flags[i] != 0) : (mask ? mask[i] != 0 : 1);
+}
+
+__global__ void core_from_include_kernel(const int* include, long long n, unsigned char* core) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) core[i] = include[i] ? 1 : 0;
+}
+
+__global__ void iota_kernel(int* p, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = (int)i;
+}
+
+__global__ void fill_kernel(int* p, long long n, int v) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+#define CK(x)                                                   \
+    do {                                                        \
+        cudaError_t e_ = (x);                                   \
+        if (e_ != cudaSuccess) return cuda_error(e_, #x);       \
+    } while (0)
+#define CKL() CK(cudaGetLastError())
+#define NEED(p) \
+    if (!(p)) return CHAOS_E_NOMEM
+
+// The shared pipeline. compat: flags select the points (flag != 0) and every
+// selected point is core; otherwise mask (may be null) selects them and core
+// points are computed with minPts.
+int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool compat, const int* flags, const int* mask,
+                 int* labels) {
+    cudaStream_t st = c.stream;
+    const int D = F.D;
+    const bool zeroEps = !(eps > 0);
+    const double side = zeroEps ? 1.0 : eps / sqrt((double)D) * (1.0 - 1e-9);
+
+    int* include = (int*)c.alloc(n * sizeof(int));
+    unsigned long long* key = (unsigned long long*)c.alloc(n * sizeof(unsigned long long));
+    unsigned char* unsafePt = (unsigned char*)c.alloc(n);
+    long long* slot = (long long*)c.alloc(n * sizeof(long long));
+    unsigned long long cap = 1;
+    while (cap < (unsigned long long)(2 * n + 2)) cap <<= 1;
+    unsigned long long* tab = (unsigned long long*)c.alloc(cap * sizeof(unsigned long long));
+    int* occ = (int*)c.alloc(cap * sizeof(int));
+    int* slotCell = (int*)c.alloc(cap * sizeof(int));
+    NEED(!c.failed);
+    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include);
+    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, side, key, unsafePt);
+    CK(cudaMemsetAsync(tab, 0xff, cap * sizeof(unsigned long long), st));
+    hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot);
+    occupied_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ);
+    CKL();
+    int C = 0;
+    int rc = exclusive_scan(c, occ, occ, (long long)cap, &C);
+    if (rc) return rc;
+    unsigned long long* cellKey = (unsigned long long*)c.alloc((size_t)(C + 1) * sizeof(unsigned long long));
+    int* cnt = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
+    int* cellOf = (int*)c.alloc(n * sizeof(int));
+    NEED(!c.failed);
+    cell_ids_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ, slotCell, cellKey);
+    CK(cudaMemsetAsync(cnt, 0, (size_t)(C + 1) * sizeof(int), st));
+    point_cell_kernel<<<blocks(n), kTPB, 0, st>>>(slot, n, slotCell, cellOf, cnt);
+    CKL();
+    int used = 0;
+    if ((rc = exclusive_scan(c, cnt, cnt, C + 1, &used))) return rc;  // cnt -> start (C+1 entries)
+    int* start = cnt;
+    int* cursor = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
+    int* order = (int*)c.alloc((size_t)(used + 1) * sizeof(int));
+    double* s0 = (double*)c.alloc((size_t)(used + 1) * sizeof(double));
+    double* s1 = (double*)c.alloc((size_t)(used + 1) * sizeof(double));
+    double* s2 = (double*)c.alloc((size_t)(used + 1) * sizeof(double));
+    NEED(!c.failed);
+    CK(cudaMemsetAsync(cursor, 0, (size_t)(C + 1) * sizeof(int), st));
+    scatter_kernel<<<blocks(n), kTPB, 0, st>>>(F, n, cellOf, start, cursor, order, s0, s1, s2);
+    CKL();
+    Sorted S;
+    S.s[0] = s0;
+    S.s[1] = s1;
+    S.s[2] = s2;
+    S.order = order;
+    S.start = start;
+    S.D = D;
+    double* boxLo = (double*)c.alloc((size_t)(C + 1) * 3 * sizeof(double));
+    double* boxHi = (double*)c.alloc((size_t)(C + 1) * 3 * sizeof(double));
+    unsigned char* unsafeCell = (unsigned char*)c.alloc((size_t)C + 1);
+    int* nbStart = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
+    NEED(!c.failed);
+    if (C > 0) {
+        cell_box_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, unsafePt, boxLo, boxHi, unsafeCell);
+        neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nbStart, nullptr,
+                                                      nullptr, nullptr);
+        CKL();
+    }
+    if (zeroEps && C > 0) CK(cudaMemsetAsync(unsafeCell, 1, (size_t)C, st));
+    CK(cudaMemsetAsync(nbStart + C, 0, sizeof(int), st));
+    int E = 0;
+    if ((rc = exclusive_scan(c, nbStart, nbStart, C + 1, &E))) return rc;
+    int* nbList = (int*)c.alloc((size_t)(E + 1) * sizeof(int));
+    int* nbOwner = (int*)c.alloc((size_t)(E + 1) * sizeof(int));
+    unsigned char* core = (unsigned char*)c.alloc(n);
+    int* parent = (int*)c.alloc(n * sizeof(int));
+    int* rep = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
+    int* root = (int*)c.alloc(n * sizeof(int));
+    NEED(!c.failed);
+    if (C > 0)
+        neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nullptr, nbStart, nbList,
+                                                      nbOwner);
+    if (compat) core_from_include_kernel<<<blocks(n), kTPB, 0, st>>>(include, n, core);
+    else
+        core_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, n, nbStart, nbList, unsafeCell, eps, minPts, core);
+    iota_kernel<<<blocks(n), kTPB, 0, st>>>(parent, n);
+    if (C > 0) intra_cell_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, core, unsafeCell, eps, parent, rep);
+    if (E > 0)
+        cross_cell_kernel<<<blocks((long long)E * 32), kTPB, 0, st>>>(S, nbOwner, nbList, E, core, unsafeCell, rep,
+                                                                      boxLo, boxHi, eps, parent);
+    roots_kernel<<<blocks(n), kTPB, 0, st>>>(parent, core, n, root);
+    CKL();
+    if (compat) {
+        int* minFix = (int*)c.alloc(n * sizeof(int));
+        int* negRank = (int*)c.alloc(n * sizeof(int));
+        int* posRank = (int*)c.alloc(n * sizeof(int));
+        NEED(!c.failed);
+        fill_kernel<<<blocks(n), kTPB, 0, st>>>(minFix, n, (int)n);
+        compat_minfix_kernel<<<blocks(n), kTPB, 0, st>>>(root, flags, n, minFix);
+        CK(cudaMemsetAsync(negRank, 0, n * sizeof(int), st));
+        CK(cudaMemsetAsync(posRank, 0, n * sizeof(int), st));
+        compat_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank);
+        CKL();
+        int t = 0;
+        if ((rc = exclusive_scan(c, negRank, negRank, n, &t))) return rc;
+        if ((rc = exclusive_scan(c, posRank, posRank, n, &t))) return rc;
+        compat_labels_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank, labels);
+        CKL();
+    } else {
+        int* rank = (int*)c.alloc(n * sizeof(int));
+        NEED(!c.failed);
+        root_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, n, rank);
+        CKL();
+        int t = 0;
+        if ((rc = exclusive_scan(c, rank, rank, n, &t))) return rc;
+        dbscan_labels_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, include, n, nbStart, nbList, unsafeCell,
+                                                         core, root, rep, rank, eps, labels);
+        CKL();
+    }
+    return CHAOS_OK;
+}
+
+}  // namespace
+
+int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total) {
+    if (n <= 0) {
+        if (total) *total = 0;
+        return CHAOS_OK;
+    }
+    const long long nb = (n + kScanItems - 1) / kScanItems;
+    int* sums = (int*)c.alloc((size_t)(nb + 1) * sizeof(int));
+    if (!sums) return CHAOS_E_NOMEM;
+    scan_block_kernel<<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n);
+    CK(cudaGetLastError());
+    if (nb > 1) {
+        int rc = exclusive_scan(c, sums, sums, nb, total);
+        if (rc) return rc;
+        add_offsets_kernel<<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n);
+        CK(cudaGetLastError());
+    } else if (total) {
+        CK(cudaMemcpyAsync(total, sums, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+    }
+    return CHAOS_OK;
+}
+
+int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgIntervals, const int* flags, long long n,
+                         double eps, int* labels) {
+    Feat F;
+    F.f[0] = avgPeaks;
+    F.f[1] = avgIntervals;
+    F.f[2] = avgIntervals;
+    F.D = 2;
+    return grid_cluster(c, F, n, eps, 1, true, flags, nullptr, labels);
+}
+
+int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,
+                  int* labels) {
+    double* a = (double*)c.alloc(n * sizeof(double));
+    double* b = (double*)c.alloc(n * sizeof(double));
+    double* d = (double*)c.alloc(n * sizeof(double));
+    if (c.failed) return CHAOS_E_NOMEM;
+    soa_kernel<<<blocks(n), kTPB, 0, c.stream>>>(features, n, dims, a, b, d);
+    CK(cudaGetLastError());
+    Feat F;
+    F.f[0] = a;
+    F.f[1] = b;
+    F.f[2] = d;
+    F.D = dims;
+    return grid_cluster(c, F, n, eps, minPts, false, nullptr, mask, labels);
+}
+
+}  // namespace chaos

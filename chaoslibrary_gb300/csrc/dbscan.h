@@ -1,0 +1,20 @@
+// Grid clustering on the device (dbscan.cu).
+#pragma once
+
+#include "capi_internal.h"
+
+namespace chaos {
+
+// The reference's basin clustering (eps-connected components over flag != 0
+// points, sign classes and canonical numbering); arrays are device pointers.
+int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgIntervals, const int* flags, long long n,
+                         double eps, int* labels);
+
+// DBSCAN with scikit-learn semantics on a row-major n x dims device matrix.
+int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,
+                  int* labels);
+
+// Exclusive prefix sum of n ints (device arrays; in == out allowed).
+int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total);
+
+}  // namespace chaos

@@ -1,0 +1,335 @@
+// Device-side building blocks of the sweep engine: per-launch parameter
+// blocks, the streaming peak detector, the divergence / fixed-point tests and
+// the per-point work functions of the three analyses. Included by the FP64
+// and the FP32 kernel translation units, which instantiate the templates for
+// their arithmetic type.
+//
+// Layout rule for every kernel here: one CUDA thread owns one trajectory; its
+// full state, its parameters and its peak detector live in registers; the
+// trajectory itself never reaches HBM. What a point writes to HBM is its
+// result row (a few scalars, plus its peak list for the bifurcation sweeps).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "launch.h"
+#include "systems.h"
+
+namespace chaos {
+
+template <int S> struct Traits {
+    static constexpr int NX = (S == SYS_SIN2) ? 2 : 3;
+    static constexpr int NA = (S == SYS_CHAMELEON) ? 7 : (S == SYS_ROSSLER_CD) ? 4 : (S == SYS_SIN3) ? 5
+                            : (S == SYS_SIN2 || S == SYS_MEMRISTOR) ? 2 : 3;
+};
+
+// Swept value of grid dimension d for linear point index p (the reference's
+// getValueByIdx, bifurcationCUDA.cu:400-419 / basinsCUDA.cu:185-189):
+// start + n*scale with n = (p / nPts^d) % nPts, multiply and add rounded apart.
+__device__ __forceinline__ double grid_value(const GridSpec& g, long long p, int d) {
+    long long q = p;
+    if (d == 1) q /= g.nPts;
+    const long long n = q % g.nPts;
+    return __dadd_rn(g.start[d], __dmul_rn((double)n, g.scale[d]));
+}
+
+// Divergence test of the bifurcation loop (bifurcationCUDA.cu:445-453):
+// v != v || v == v + 1.0  <=>  !(|v| < 2^53); then |(float)v| > maxValue.
+template <class T> __device__ __forceinline__ bool bif_diverged(T v, const SweepParams& P) {
+    const T av = v < T(0) ? -v : v;
+    if (!(av < T(9007199254740992.0))) return true;
+    return P.checkMax && (double)fabsf((float)v) > P.maxValue;
+}
+// Divergence test of the basins loop (basinsCUDA.cu:350-361): isnan || isinf, then maxValue.
+template <class T> __device__ __forceinline__ T finite_max();
+template <> __device__ __forceinline__ double finite_max<double>() { return 1.7976931348623157e308; }
+template <> __device__ __forceinline__ float finite_max<float>() { return 3.4028234663852886e38f; }
+template <class T> __device__ __forceinline__ bool basins_diverged(T v, const SweepParams& P) {
+    const T av = v < T(0) ? -v : v;
+    if (!(av <= finite_max<T>())) return true;  // NaN or +-inf
+    return P.checkMax && (double)fabsf((float)v) > P.maxValue;
+}
+
+// Streaming form of the reference peakFinder (bifurcationCUDA.cu:469-514).
+// Samples arrive one at a time; a candidate i is judged when d[i+1] arrives
+// and a plateau walk advances one sample per arrival, with exactly the
+// reference's rules: rise > 1e-13 and d[i] >= d[i+1] opens a plateau; a
+// sample above ends it without a peak; a drop > 1e-13 ends it with a peak of
+// value d[j] at time trunc((i+j)/2); after either end the scan resumes at
+// j+2. The first detected peak is dropped and every later one is reported
+// with the interval to its predecessor, (t_k - t_{k-1}) * h.
+template <class T> struct PeakStream {
+    T p2, p1;      // d[k-2], d[k-1]
+    int k;         // index of the next sample
+    int cand;      // scan mode: next candidate index; plateau mode: -1
+    int i0;        // plateau: index of the candidate that opened it
+    int n;         // peaks detected so far (the dropped first one included)
+    int tprev;     // time index of the previous detected peak
+
+    __device__ __forceinline__ void init() { k = 0; cand = 1; i0 = 0; n = 0; tprev = 0; p1 = p2 = T(0); }
+
+    // Pushes d[k] = v; returns true and sets (val, t) when a peak was detected.
+    __device__ __forceinline__ bool push(T v, T& val, int& t) {
+        bool hit = false;
+        if (k >= 2) {
+            if (cand < 0) {  // plateau, j = k-1
+                if (p1 < v) cand = k + 1;
+                else if (p1 - v > T(1e-13)) { hit = true; val = p1; t = (i0 + k - 1) >> 1; cand = k + 1; }
+            } else if (cand == k - 1) {
+                if (p1 - p2 > T(1e-13) && p1 >= v) {
+                    i0 = k - 1;
+                    if (p1 - v > T(1e-13)) { hit = true; val = p1; t = k - 1; cand = k + 1; }
+                    else cand = -1;
+                } else {
+                    cand = k;
+                }
+            }
+        }
+        p2 = p1;
+        p1 = v;
+        ++k;
+        return hit;
+    }
+};
+
+// x[wv] for a run-time wv without indexing the register array (which would
+// move the whole state to local memory).
+template <int NX, class T> __device__ __forceinline__ T pick(const T* x, int wv) {
+    T v = x[0];
+#pragma unroll
+    for (int j = 1; j < NX; ++j)
+        if (j == wv) v = x[j];
+    return v;
+}
+
+// Loads state and parameters of point p of a sweep (mutated parameters or
+// mutated initial-condition components, per P.mutateState).
+template <int S, class T> __device__ __forceinline__ void load_point(const SweepParams& P, long long p, T* x, T* a) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    double v0 = 0.0, v1 = 0.0;
+    v0 = grid_value(P.grid, p, 0);
+    if (P.dim > 1) v1 = grid_value(P.grid, p, 1);
+#pragma unroll
+    for (int i = 0; i < NX; ++i) {
+        double v = P.ic[i];
+        if (P.mutateState) {  // dimension 1 is written last, as in the reference loop
+            if (i == P.mut[0]) v = v0;
+            if (P.dim > 1 && i == P.mut[1]) v = v1;
+        }
+        x[i] = (T)v;
+    }
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+        double v = P.values[i];
+        if (!P.mutateState) {
+            if (i == P.mut[0]) v = v0;
+            if (P.dim > 1 && i == P.mut[1]) v = v1;
+        }
+        a[i] = (T)v;
+    }
+}
+
+// Fixed-point test of the bifurcation loop: sqrtf(fabsf(sum)) < 1e-9 in float.
+template <int NX, class T> __device__ __forceinline__ bool bif_fixed(const T* x, const T* xp) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < NX; ++j) s = s + (x[j] - xp[j]) * (x[j] - xp[j]);
+    return (double)sqrtf(fabsf((float)s)) < 1e-9;
+}
+// Fixed-point test of the basins loop: sqrt(abs(sum)) < 1e-9 in FP64.
+template <int NX, class T> __device__ __forceinline__ bool basins_fixed(const T* x, const T* xp) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < NX; ++j) s = s + (x[j] - xp[j]) * (x[j] - xp[j]);
+    return sqrt(fabs((double)s)) < 1e-9;
+}
+
+// ---------------------------------------------------------------------------
+// Bifurcation point (reference kernels calculateTransTimeCUDA +
+// calculateDiscreteModelCUDA + peakFinderCUDA, bifurcationCUDA.cu:258-371),
+// fused. Writes flags/counts/first and the first `cap` kept peaks/intervals.
+template <int S, class T>
+__device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O, long long p, long long o) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    T x[NX], a[NA], xp[NX];
+    load_point<S, T>(P, p, x, a);
+    const StepCtx<T> c((T)P.h);
+    const int wv = P.wv;
+    int flag = 1;
+    if (P.S > 0) {
+        for (int s = 0; s < P.S; ++s) {
+#pragma unroll
+            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+            step<S>(x, a, c);
+            if (bif_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+        }
+        if (flag == 1 && bif_fixed<NX>(x, xp)) flag = -1;
+    }
+    double first = 0.0;
+    int kept = 0;
+    if (flag == 1) {
+        PeakStream<T> ps;
+        ps.init();
+        first = (double)pick<NX>(x, wv);
+        double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
+        double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
+        for (int i = 0; i < P.B; ++i) {
+#pragma unroll
+            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+            T val;
+            int t;
+            if (ps.push(pick<NX>(x, wv), val, t)) {
+                if (ps.n >= 1) {
+                    const int q = ps.n - 1;
+                    if (q < O.cap) {
+                        if (pk) pk[q] = (double)val;
+                        if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), P.hInterval);
+                    }
+                }
+                ps.tprev = t;
+                ++ps.n;
+            }
+            step<S>(x, a, c);
+            if (bif_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+        }
+        if (flag == 1 && P.B > 0 && bif_fixed<NX>(x, xp)) flag = -1;
+        kept = ps.n > 1 ? ps.n - 1 : 0;
+    } else {
+        flag = 0;  // a transient that ended diverged or fixed is reported as diverged
+    }
+    O.flags[o] = flag;
+    O.counts[o] = flag == 1 ? kept : (flag == -1 ? -1 : 0);
+    if (O.first) O.first[o] = first;
+}
+
+// ---------------------------------------------------------------------------
+// Basins point (reference calculateTransTimeCUDA + calculateDiscreteModelCUDA
+// + avgPeakFinderCUDA, basinsCUDA.cu:233-314 and 818-864), fused.
+template <int S, class T>
+__device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsOut& O, long long p, long long o) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    T x[NX], a[NA], xp[NX];
+    load_point<S, T>(P, p, x, a);
+    const StepCtx<T> c((T)P.h);
+    const int wv = P.wv;
+    for (int s = 0; s < P.S; ++s) step<S>(x, a, c);
+#pragma unroll
+    for (int j = 0; j < NX; ++j) xp[j] = x[j];
+    PeakStream<T> ps;
+    ps.init();
+    int flag = 1;
+    double sp = 0.0, si = 0.0, last = 0.0;
+    for (int i = 0; i < P.B; ++i) {
+#pragma unroll
+        for (int j = 0; j < NX; ++j) xp[j] = x[j];
+        last = (double)pick<NX>(x, wv);
+        T val;
+        int t;
+        if (ps.push(pick<NX>(x, wv), val, t)) {
+            if (ps.n >= 1) {
+                sp = sp + (double)val;
+                si = si + __dmul_rn((double)(t - ps.tprev), P.hInterval);
+            }
+            ps.tprev = t;
+            ++ps.n;
+        }
+        for (int r = 0; r < P.preScaller; ++r) step<S>(x, a, c);
+        if (basins_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+    }
+    if (flag == 1 && P.B > 0 && basins_fixed<NX>(x, xp)) flag = -1;
+    const int kept = ps.n > 1 ? ps.n - 1 : 0;
+    double ap, ai;
+    if (flag == 0) { ap = 999.0; ai = 999.0; }
+    else if (flag == -1) { ap = last; ai = -1.0; }
+    else if (kept <= 0) { ap = 1000.0; ai = 1000.0; }
+    else { ap = sp / (double)kept; ai = si / (double)kept; }
+    O.flags[o] = flag;
+    O.avgPeaks[o] = ap;
+    O.avgIntervals[o] = ai;
+    if (O.counts) O.counts[o] = flag == 1 ? kept : 0;
+}
+
+// ---------------------------------------------------------------------------
+// LLE point, the reference's Benettin scheme (LLECUDA.cu:114-166) in full
+// precision T for both trajectories: calcBlocks+1 blocks of NT steps of x and
+// of its twin q; d = |x-q|/eps; sum += log(d); q = x - (x-q)/d; sum / tMax.
+// The twin starts at x + eps along state component 0.
+template <int S, class T>
+__device__ __forceinline__ double lle_point_full(const LleParams& L, long long p) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    const int i = (int)(p % L.nPts), j = (int)(p / L.nPts);
+    T x[NX], q[NX], a[NA];
+#pragma unroll
+    for (int k = 0; k < NX; ++k) x[k] = (T)L.ic[k];
+    const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
+    const double vb = L.nPts == 1 ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
+#pragma unroll
+    for (int k = 0; k < NA; ++k) {
+        double v = L.values[k];
+        if (k == L.mut[0]) v = va;
+        if (k == L.mut[1]) v = vb;
+        a[k] = (T)v;
+    }
+    const StepCtx<T> c((T)L.h);
+    for (int s = 0; s < L.trans; ++s) step<S>(x, a, c);
+#pragma unroll
+    for (int k = 0; k < NX; ++k) q[k] = x[k];
+    q[0] = x[0] + (T)L.eps;
+    double sum = 0.0;
+    for (int b = 0; b <= L.calcBlocks; ++b) {
+        for (int s = 0; s < L.ntp; ++s) step<S>(x, a, c);
+        for (int s = 0; s < L.ntp; ++s) step<S>(q, a, c);
+        double dist = 0.0;
+#pragma unroll
+        for (int k = 0; k < NX; ++k) {
+            const double df = (double)x[k] - (double)q[k];
+            dist = dist + df * df;
+        }
+        dist = sqrt(dist) / L.eps;
+        sum = sum + log(dist);
+#pragma unroll
+        for (int k = 0; k < NX; ++k) q[k] = (T)((double)x[k] - (((double)x[k] - (double)q[k]) / dist));
+    }
+    return sum / L.tMax;
+}
+
+// LLE point with the twin carried as the exact difference e = q - x (only for
+// the quadratic RK4 systems): x and e in T (FP32), the log-stretch sum in
+// FP64. Same block count, renormalisation and division by tMax as above.
+template <class F, class T>
+__device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p) {
+    const int i = (int)(p % L.nPts), j = (int)(p / L.nPts);
+    T x[3], e[3], a[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[k] = (T)L.ic[k];
+    const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
+    const double vb = L.nPts == 1 ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = L.values[k];
+        if (k == L.mut[0]) v = va;
+        if (k == L.mut[1]) v = vb;
+        a[k] = (T)v;
+    }
+    const RK4H<T> c((T)L.h);
+    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
+    e[0] = (T)L.eps;
+    e[1] = T(0);
+    e[2] = T(0);
+    const T inv_eps = (T)(1.0 / L.eps);
+    double sum = 0.0;
+    for (int b = 0; b <= L.calcBlocks; ++b) {
+        for (int s = 0; s < L.ntp; ++s) rk4_step_twin<F>(x, e, a, c);
+        const T n2 = fmaT(e[0], e[0], fmaT(e[1], e[1], e[2] * e[2]));
+        const T d = sqrtf(n2) * inv_eps;
+        sum += (double)logf(d);
+        const T r = T(1) / d;
+        e[0] *= r;
+        e[1] *= r;
+        e[2] *= r;
+    }
+    return sum / L.tMax;
+}
+
+}  // namespace chaos

@@ -1,0 +1,76 @@
+// FP32 kernels: trajectories in FP32 registers (contraction allowed), peak
+// times, intervals and means in FP64. The LLE kernel carries the twin as the
+// exact difference e = q - x (quadratic RK4 systems only) and accumulates the
+// log-stretch sum in FP64.
+#include "engine.cuh"
+
+namespace chaos {
+
+namespace {
+constexpr int kBlock = 128;
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) bif_kernel_f32(SweepParams P, BifOut O) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= P.nPoints) return;
+    bif_point<S, float>(P, O, P.pBegin + o, o);
+}
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) basins_kernel_f32(SweepParams P, BasinsOut O) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= P.nPoints) return;
+    basins_point<S, float>(P, O, P.pBegin + o, o);
+}
+
+template <class F>
+__global__ void __launch_bounds__(kBlock) lle_twin_kernel_f32(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    out[o] = lle_point_twin<F, float>(L, L.pBegin + o);
+}
+
+inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+#define CHAOS_SYSTEM_SWITCH(sys, CALL) \
+    switch (sys) {                     \
+        case SYS_LORENZ_RK4: CALL(SYS_LORENZ_RK4); break; \
+        case SYS_ROSSLER_RK4: CALL(SYS_ROSSLER_RK4); break; \
+        case SYS_CHEN_RK4: CALL(SYS_CHEN_RK4); break; \
+        case SYS_CHAMELEON: CALL(SYS_CHAMELEON); break; \
+        case SYS_ROSSLER_CD: CALL(SYS_ROSSLER_CD); break; \
+        case SYS_SIN3: CALL(SYS_SIN3); break; \
+        case SYS_SIN2: CALL(SYS_SIN2); break; \
+        case SYS_MEMRISTOR: CALL(SYS_MEMRISTOR); break; \
+        default: return cudaErrorInvalidValue; \
+    }
+}  // namespace
+
+cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
+    if (P.nPoints <= 0) return cudaSuccess;
+#define CALL(S) bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
+    CHAOS_SYSTEM_SWITCH(P.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
+    if (P.nPoints <= 0) return cudaSuccess;
+#define CALL(S) basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
+    CHAOS_SYSTEM_SWITCH(P.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
+    if (L.nPoints <= 0) return cudaSuccess;
+    switch (L.system) {
+        case SYS_LORENZ_RK4: lle_twin_kernel_f32<Lorenz><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
+        case SYS_ROSSLER_RK4: lle_twin_kernel_f32<Rossler><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
+        case SYS_CHEN_RK4: lle_twin_kernel_f32<Chen><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
+        default: return cudaErrorNotSupported;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace chaos

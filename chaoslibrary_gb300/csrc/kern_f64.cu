@@ -1,0 +1,186 @@
+// FP64 kernels: the reference's arithmetic, one rounding per written
+// operation. This translation unit is compiled with --fmad=false, so a*b+c
+// stays two roundings unless the source calls fma(); together with IEEE
+// division and square root the FP64 sweeps reproduce the CPU oracle bit for
+// bit. Also holds the reference-semantics kernels that run on caller arrays
+// (peak finder, per-point dbscan of the 2-D bifurcation).
+#include <climits>
+
+#include "engine.cuh"
+
+namespace chaos {
+
+namespace {
+constexpr int kBlock = 128;
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) bif_kernel(SweepParams P, BifOut O) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= P.nPoints) return;
+    bif_point<S, double>(P, O, P.pBegin + o, o);
+}
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) basins_kernel(SweepParams P, BasinsOut O) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= P.nPoints) return;
+    basins_point<S, double>(P, O, P.pBegin + o, o);
+}
+
+template <int S>
+__global__ void __launch_bounds__(kBlock) lle_kernel(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    out[o] = lle_point_full<S, double>(L, L.pBegin + o);
+}
+
+inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+#define CHAOS_SYSTEM_SWITCH(sys, CALL) \
+    switch (sys) {                     \
+        case SYS_LORENZ_RK4: CALL(SYS_LORENZ_RK4); break; \
+        case SYS_ROSSLER_RK4: CALL(SYS_ROSSLER_RK4); break; \
+        case SYS_CHEN_RK4: CALL(SYS_CHEN_RK4); break; \
+        case SYS_CHAMELEON: CALL(SYS_CHAMELEON); break; \
+        case SYS_ROSSLER_CD: CALL(SYS_ROSSLER_CD); break; \
+        case SYS_SIN3: CALL(SYS_SIN3); break; \
+        case SYS_SIN2: CALL(SYS_SIN2); break; \
+        case SYS_MEMRISTOR: CALL(SYS_MEMRISTOR); break; \
+        default: return cudaErrorInvalidValue; \
+    }
+
+// Peak finder over caller series (the reference's peakFinderCUDA semantics on
+// identical input arrays): one thread streams one series.
+__global__ void peak_array_kernel(const double* __restrict__ data, long long nSeries, int len, double h, int cap,
+                                  int* counts, double* peaks, double* intervals) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nSeries) return;
+    const double* d = data + s * (long long)len;
+    PeakStream<double> ps;
+    ps.init();
+    for (int k = 0; k < len; ++k) {
+        double val;
+        int t;
+        if (ps.push(d[k], val, t)) {
+            if (ps.n >= 1) {
+                const int q = ps.n - 1;
+                if (q < cap) {
+                    peaks[s * (long long)cap + q] = val;
+                    intervals[s * (long long)cap + q] = __dmul_rn((double)(t - ps.tprev), h);
+                }
+            }
+            ps.tprev = t;
+            ++ps.n;
+        }
+    }
+    counts[s] = ps.n > 1 ? ps.n - 1 : 0;
+}
+
+// Per-point dbscan of the 2-D bifurcation (bifurcationCUDA.cu:516-583), one
+// warp per point. The sequential control (new cluster / pop of slot NN-1) is
+// uniform across the warp; each expansion pass over k < P-1 is split across
+// the lanes, which is exact because pass k only reads and writes entry k.
+__global__ void point_dbscan_kernel(const double* __restrict__ intervals, const int* __restrict__ counts, long long n,
+                                    int stride, double eps, int* labScratch, int* slotScratch, int* out) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const int P = counts[w];
+    if (P > stride) {  // more intervals than the row holds: reported, not read
+        if (lane == 0) out[w] = INT_MIN;
+        return;
+    }
+    if (P <= 1) {
+        if (lane == 0) out[w] = P == -1 ? -1 : (P == 0 ? 0 : 1);
+        return;
+    }
+    const double* iv = intervals + w * (long long)stride;
+    int* lab = labScratch + w * (long long)stride;
+    int* slot = slotScratch + w * (long long)stride;
+    for (int k = lane; k < P; k += 32) { lab[k] = 0; slot[k] = 0; }
+    __syncwarp();
+    int cluster = 0, nn = 0;
+    for (int i = 0; i < P; ++i) {
+        bool expand = false;
+        if (nn >= 1) {
+            i = slot[nn - 1];
+            __syncwarp();
+            if (lane == 0) slot[nn - 1] = 0;
+            --nn;
+            expand = true;
+        } else if (lab[i] == 0) {
+            nn = 0;
+            ++cluster;
+            __syncwarp();
+            if (lane == 0) lab[i] = cluster;
+            expand = true;
+        }
+        if (expand) {
+            __syncwarp();
+            const double ivi = iv[i];
+            for (int k0 = 0; k0 < P - 1; k0 += 32) {
+                const int k = k0 + lane;
+                bool hit = false;
+                if (k < P - 1 && k != i && lab[k] == 0) {
+                    const double ivk = iv[k];
+                    const double dist = (ivi == ivk) ? 0.0 : (double)fabsf((float)(ivk - ivi));
+                    if (dist < eps) {
+                        lab[k] = cluster;
+                        slot[k] = k;
+                        hit = true;
+                    }
+                }
+                nn += __popc(__ballot_sync(0xffffffffu, hit));
+            }
+            __syncwarp();
+        }
+    }
+    if (lane == 0) out[w] = cluster - 1;
+}
+
+}  // namespace
+
+bool system_supported(int system) { return system >= 0 && system < SYS_COUNT; }
+int launch_block_size() { return kBlock; }
+
+cudaError_t launch_bif_f64(const SweepParams& P, const BifOut& O, cudaStream_t st) {
+    if (P.nPoints <= 0) return cudaSuccess;
+#define CALL(S) bif_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
+    CHAOS_SYSTEM_SWITCH(P.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
+    if (P.nPoints <= 0) return cudaSuccess;
+#define CALL(S) basins_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
+    CHAOS_SYSTEM_SWITCH(P.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
+    if (L.nPoints <= 0) return cudaSuccess;
+#define CALL(S) lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out)
+    CHAOS_SYSTEM_SWITCH(L.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, double h, int cap, int* counts,
+                               double* peaks, double* intervals, cudaStream_t st) {
+    if (nSeries <= 0) return cudaSuccess;
+    peak_array_kernel<<<grid_for(nSeries), kBlock, 0, st>>>(data, nSeries, len, h, cap, counts, peaks, intervals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long long n, int stride, double eps,
+                                int* labScratch, int* slotScratch, int* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const long long threads = n * 32;
+    point_dbscan_kernel<<<(unsigned)((threads + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        intervals, counts, n, stride, eps, labScratch, slotScratch, out);
+    return cudaGetLastError();
+}
+
+}  // namespace chaos

@@ -1,0 +1,88 @@
+// Parameter blocks passed by value to the sweep kernels, and the launchers
+// the C-ABI layer calls. Every per-call scalar travels in a kernel argument
+// (no __constant__ globals), so calls on different streams never interfere.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace chaos {
+
+constexpr int kMaxState = 12;
+constexpr int kMaxParams = 16;
+
+// Parameter or initial-condition grid of a sweep: point p has coordinate
+// n_d = (p / nPts^d) % nPts in dimension d and value start[d] + n_d*scale[d].
+struct GridSpec {
+    long long nPts;
+    double start[2];
+    double scale[2];
+};
+
+struct SweepParams {
+    int system;
+    int dim;          // 1 or 2 swept dimensions
+    int S;            // transient steps
+    int B;            // recorded samples
+    int preScaller;   // steps per recorded sample (basins); 1 for bifurcation
+    int wv;           // recorded state component
+    int checkMax;     // maxValue != 0
+    int mutateState;  // 1: the grid sets initial conditions (basins); 0: parameters
+    double h;
+    double hInterval;  // h * preScaller, the time unit of peak intervals
+    double maxValue;
+    double ic[kMaxState];
+    double values[kMaxParams];
+    int mut[2];
+    GridSpec grid;
+    long long pBegin;   // first point of this launch
+    long long nPoints;  // points in this launch
+};
+
+// Per-point results of a bifurcation sweep (point-major rows of `cap`).
+struct BifOut {
+    int* counts;        // kept peaks, or -1 fixed point, 0 diverged / none
+    int* flags;         // 1 / 0 / -1
+    double* first;      // first recorded sample (the reference's row for fixed points)
+    double* peaks;      // [n][cap] (may be null)
+    double* intervals;  // [n][cap] (may be null)
+    int cap;
+};
+
+struct BasinsOut {
+    int* flags;
+    double* avgPeaks;
+    double* avgIntervals;
+    int* counts;  // kept peaks (may be null)
+};
+
+struct LleParams {
+    int system;
+    int nPts;
+    int trans, ntp, calcBlocks;
+    double h, eps, tMax;
+    double ic[kMaxState];
+    double values[kMaxParams];
+    int mut[2];
+    double rangeA[2], rangeB[2];
+    double stepA, stepB;  // linspace steps (end - start) / (nPts - 1)
+    long long pBegin, nPoints;
+};
+
+// precision-specific launchers (kern_f64.cu / kern_f32.cu)
+cudaError_t launch_bif_f64(const SweepParams& P, const BifOut& O, cudaStream_t st);
+cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st);
+cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
+cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
+cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
+cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
+// reference-semantics kernels on caller arrays (kern_f64.cu)
+cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, double h, int cap, int* counts,
+                               double* peaks, double* intervals, cudaStream_t st);
+cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long long n, int stride, double eps,
+                                int* labScratch, int* slotScratch, int* out, cudaStream_t st);
+
+bool system_supported(int system);
+int launch_block_size();  // threads per block of the sweep kernels
+
+}  // namespace chaos

@@ -1,0 +1,287 @@
+// Step maps of the dynamical systems the engine integrates.
+//
+// Every system is one in-place step of a discrete map, X <- step(X, a, h), the
+// contract of ChaosLibrary's plug-in `CALC_DISCRETE_MODEL(X, a, h)` with
+// `SIZE_X` / `SIZE_A` (systems/systems.cuh:12-38 in the reference). Here the
+// step is a template over the arithmetic type T so that one definition serves
+//   * the FP64 kernels (T = double; the translation unit is compiled with
+//     contraction off, so every rounding is the one written below),
+//   * the FP32 kernels (T = float; the compiler may contract), and
+//   * the host-side checker (g++ with -ffp-contract=off).
+// Only IEEE-exact operations (+, -, *, /, fma, sqrt) appear in the polynomial
+// systems, so the FP64 results are bit-identical on the GPU and on any host.
+//
+// Systems 0-2 are the classic-RK4 Lorenz, Rossler and Chen flows the benchmark
+// workloads name (the reference ships none of them); systems 3-7 restate the
+// reference's own plug-ins formula by formula (same operation order, same
+// float-typed temporaries where the reference has them), because a plug-in is
+// an interface whose arithmetic must stay the same to be the same system.
+#pragma once
+
+#if defined(__CUDACC__)
+#define CHAOS_HD __host__ __device__ __forceinline__
+#else
+#define CHAOS_HD inline
+#endif
+#if defined(__CUDA_ARCH__)
+#define CHAOS_UNROLL _Pragma("unroll")
+#else
+#define CHAOS_UNROLL
+#endif
+
+#include <math.h>
+
+namespace chaos {
+
+enum SystemId {
+    SYS_LORENZ_RK4 = 0,   // x'=s(y-x), y'=x(r-z)-y, z'=xy-bz; a = {sigma, rho, beta}
+    SYS_ROSSLER_RK4 = 1,  // x'=-y-z, y'=x+ay, z'=b+z(x-c);    a = {a, b, c}
+    SYS_CHEN_RK4 = 2,     // x'=a(y-x), y'=(c-a)x-xz+cy, z'=xy-bz; a = {a, b, c}
+    SYS_CHAMELEON = 3,    // reference systems/systems.cuh:11-39 (7 params)
+    SYS_ROSSLER_CD = 4,   // reference systems/systems.cuh:41-63 (4 params)
+    SYS_SIN3 = 5,         // reference systems/systems.cuh:67-83 (5 params)
+    SYS_SIN2 = 6,         // reference systems/systems.cuh:85-101 (2-D, 2 params)
+    SYS_MEMRISTOR = 7,    // reference systems/systems.cuh:103-178 (Euler, 2 params)
+    SYS_COUNT = 8,
+    SYS_USER = 15         // a reference-format plug-in header compiled in at build time
+};
+
+// State / parameter sizes per system (SIZE_X / SIZE_A of the reference plug-ins).
+CHAOS_HD int system_nx(int s) { return s == SYS_SIN2 ? 2 : 3; }
+CHAOS_HD int system_na(int s) {
+    switch (s) {
+        case SYS_LORENZ_RK4: case SYS_ROSSLER_RK4: case SYS_CHEN_RK4: return 3;
+        case SYS_CHAMELEON: return 7;
+        case SYS_ROSSLER_CD: return 4;
+        case SYS_SIN3: return 5;
+        case SYS_SIN2: return 2;
+        case SYS_MEMRISTOR: return 2;
+        default: return 0;
+    }
+}
+// Systems whose vector field is polynomial (quadratic): they have an exact
+// difference form f(X+e)-f(X), used by the FP32 twin-trajectory LLE.
+CHAOS_HD bool system_has_difference_form(int s) { return s <= SYS_CHEN_RK4; }
+
+// ---- math shims: one name per operation for both precisions ---------------
+CHAOS_HD double fmaT(double a, double b, double c) { return fma(a, b, c); }
+CHAOS_HD float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+CHAOS_HD double cosT(double a) { return cos(a); }
+CHAOS_HD float cosT(float a) { return cosf(a); }
+CHAOS_HD double sinT(double a) { return sin(a); }
+CHAOS_HD float sinT(float a) { return sinf(a); }
+CHAOS_HD double expT(double a) { return exp(a); }
+CHAOS_HD float expT(float a) { return expf(a); }
+CHAOS_HD double atanT(double a) { return atan(a); }
+CHAOS_HD float atanT(float a) { return atanf(a); }
+
+// ---- vector fields of the RK4 systems ---------------------------------------
+struct Lorenz {
+    template <class T> static CHAOS_HD void f(const T* x, const T* a, T* k) {
+        k[0] = a[0] * (x[1] - x[0]);
+        k[1] = fmaT(x[0], a[1] - x[2], -x[1]);
+        k[2] = fmaT(x[0], x[1], -(a[2] * x[2]));
+    }
+    // Exact difference f(x+e) - f(x) of the quadratic field (no cancellation).
+    template <class T> static CHAOS_HD void df(const T* x, const T* e, const T* a, T* d) {
+        d[0] = a[0] * (e[1] - e[0]);
+        d[1] = fmaT(e[0], (a[1] - x[2]) - e[2], -fmaT(x[0], e[2], e[1]));
+        d[2] = fmaT(x[0], e[1], fmaT(e[0], x[1] + e[1], -(a[2] * e[2])));
+    }
+};
+
+struct Rossler {
+    template <class T> static CHAOS_HD void f(const T* x, const T* a, T* k) {
+        k[0] = -(x[1] + x[2]);
+        k[1] = fmaT(a[0], x[1], x[0]);
+        k[2] = fmaT(x[2], x[0] - a[2], a[1]);
+    }
+    template <class T> static CHAOS_HD void df(const T* x, const T* e, const T* a, T* d) {
+        d[0] = -(e[1] + e[2]);
+        d[1] = fmaT(a[0], e[1], e[0]);
+        d[2] = fmaT(x[2], e[0], e[2] * ((x[0] - a[2]) + e[0]));
+    }
+};
+
+struct Chen {
+    template <class T> static CHAOS_HD void f(const T* x, const T* a, T* k) {
+        k[0] = a[0] * (x[1] - x[0]);
+        k[1] = fmaT(x[0], (a[2] - a[0]) - x[2], a[2] * x[1]);
+        k[2] = fmaT(x[0], x[1], -(a[1] * x[2]));
+    }
+    template <class T> static CHAOS_HD void df(const T* x, const T* e, const T* a, T* d) {
+        d[0] = a[0] * (e[1] - e[0]);
+        d[1] = fmaT(e[0], (a[2] - a[0]) - x[2], fmaT(a[2], e[1], -((x[0] + e[0]) * e[2])));
+        d[2] = fmaT(x[0], e[1], fmaT(e[0], x[1] + e[1], -(a[1] * e[2])));
+    }
+};
+
+// Step-size constants of one classic RK4 step, computed once per launch.
+template <class T> struct RK4H {
+    T h, hh, h6;
+    CHAOS_HD RK4H() {}
+    CHAOS_HD explicit RK4H(T h_) : h(h_), hh(h_ * T(0.5)), h6(h_ / T(6)) {}
+};
+
+// Classic fourth-order Runge-Kutta step of a 3-D autonomous field.
+template <class F, class T> CHAOS_HD void rk4_step(T* x, const T* a, const RK4H<T>& c) {
+    T k1[3], k2[3], k3[3], k4[3], y[3];
+    F::f(x, a, k1);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) y[i] = fmaT(c.hh, k1[i], x[i]);
+    F::f(y, a, k2);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) y[i] = fmaT(c.hh, k2[i], x[i]);
+    F::f(y, a, k3);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) y[i] = fmaT(c.h, k3[i], x[i]);
+    F::f(y, a, k4);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) x[i] = fmaT(c.h6, fmaT(T(2), k2[i] + k3[i], k1[i] + k4[i]), x[i]);
+}
+
+// One RK4 step of the base trajectory x together with the exact difference
+// e = p - x of a twin trajectory p. The twin's stages are carried as
+// differences from the base stages, so e keeps full relative precision even
+// when |e| is far below the resolution of x (FP32 with e ~ 1e-8).
+template <class F, class T> CHAOS_HD void rk4_step_twin(T* x, T* e, const T* a, const RK4H<T>& c) {
+    T k1[3], k2[3], k3[3], k4[3], y[3];
+    T d1[3], d2[3], d3[3], d4[3], g[3];
+    F::f(x, a, k1);
+    F::df(x, e, a, d1);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) { y[i] = fmaT(c.hh, k1[i], x[i]); g[i] = fmaT(c.hh, d1[i], e[i]); }
+    F::f(y, a, k2);
+    F::df(y, g, a, d2);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) { y[i] = fmaT(c.hh, k2[i], x[i]); g[i] = fmaT(c.hh, d2[i], e[i]); }
+    F::f(y, a, k3);
+    F::df(y, g, a, d3);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) { y[i] = fmaT(c.h, k3[i], x[i]); g[i] = fmaT(c.h, d3[i], e[i]); }
+    F::f(y, a, k4);
+    F::df(y, g, a, d4);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        x[i] = fmaT(c.h6, fmaT(T(2), k2[i] + k3[i], k1[i] + k4[i]), x[i]);
+        e[i] = fmaT(c.h6, fmaT(T(2), d2[i] + d3[i], d1[i] + d4[i]), e[i]);
+    }
+}
+
+// ---- the reference's own plug-in systems, restated --------------------------
+// Chameleon, semi-implicit two-stage composition (systems/systems.cuh:11-39).
+template <class T> CHAOS_HD void chameleon_step(T* X, const T* a, T h) {
+    T h1 = a[0] * h;
+    T h2 = (T(1) - a[0]) * h;
+    X[0] = fmaT(h1, -a[6] * X[1], X[0]);
+    X[1] = fmaT(h1, a[6] * X[0] + a[1] * X[2], X[1]);
+    T cos_term = cosT(a[5] * X[1]);
+    X[2] = fmaT(h1, a[2] - a[3] * X[2] + a[4] * cos_term, X[2]);
+    X[2] = fmaT(h2, (a[2] + a[4] * cos_term), X[2]) / (T(1) + a[3] * h2);
+    X[1] = fmaT(h2, (a[6] * X[0] + a[1] * X[2]), X[1]);
+    X[0] = fmaT(h2, -a[6] * X[1], X[0]);
+}
+
+// Rossler, "CD" composition (systems/systems.cuh:41-63).
+template <class T> CHAOS_HD void rossler_cd_step(T* x, const T* a, T h) {
+    T h1 = T(0.5) * h + a[0];
+    T h2 = T(0.5) * h - a[0];
+    x[0] = fmaT(h1, -x[1] - x[2], x[0]);
+    x[1] = fmaT(h1, x[0] + a[1] * x[1], x[1]);
+    x[2] = fmaT(h1, a[2] + x[2] * (x[0] - a[3]), x[2]);
+    T temp = fmaT(-h2, x[0] - a[3], T(1));
+    x[2] = fmaT(h2, a[2], x[2]) / temp;
+    temp = fmaT(-h2, a[1], T(1));
+    x[1] = fmaT(h2, x[0], x[1]) / temp;
+    x[0] = fmaT(h2, -x[1] - x[2], x[0]);
+}
+
+// Three sin-coupled oscillators for basins (systems/systems.cuh:67-83). The
+// reference keeps h2 in a float, so it is rounded to float here as well.
+template <class T> CHAOS_HD void sin3_step(T* X, const T* a, T h) {
+    const T h2 = (T)(float)(h * (T(1) - a[0]));
+    X[0] = X[0] + h * (sinT(X[1]) - a[1] * X[0]);
+    X[1] = X[1] + h * (sinT(X[2]) - a[1] * X[1]);
+    X[2] = X[2] + h * (sinT(X[0]) - a[1] * X[2]);
+    X[2] = (X[2] + h2 * sinT(X[0])) / (T(1) + h2 * a[1]);
+    X[1] = (X[1] + h2 * sinT(X[2])) / (T(1) + h2 * a[1]);
+    X[0] = (X[0] + h2 * sinT(X[1])) / (T(1) + h2 * a[1]);
+}
+
+// 2-D sin system for basins (systems/systems.cuh:85-101); h1, h2 and the
+// intermediate z are floats in the reference.
+template <class T> CHAOS_HD void sin2_step(T* X, const T* a, T h) {
+    const T h1 = (T)(float)(h * a[0]);
+    const T h2 = (T)(float)(h * (T(1) - a[0]));
+    X[0] = X[0] + h1 * (-X[1]);
+    X[1] = X[1] + h1 * (a[1] * X[0] + sinT(X[1]));
+    const T z = (T)(float)X[1];
+    X[1] = z + h2 * (a[1] * X[0] + sinT(X[1]));
+    X[0] = X[0] + h2 * (-X[1]);
+}
+
+// Memristor circuit with a tunnel diode, explicit Euler (systems/systems.cuh:103-178).
+template <class T> CHAOS_HD void memristor_step(T* X, const T* a, T h) {
+    const T Vc = X[0], XSV = X[1], t = X[2];
+    const T U1 = T(0.0), U2 = T(-0.04), C1 = T(22e-9);
+    const T Is = T(1.15E-7), Vt = T(1.0) / T(15.0), Vp = T(0.09), Ip = T(2.1e-5), Iv = T(-3e-6);
+    const T D = T(26.0), E = T(0.14);
+    const T Vd = Vc + U2;
+    const T Vm = Vc + U1;
+    const T idiode = Is * (expT(Vd / Vt) - expT(-Vd / Vt));
+    const T itunnel = Ip / Vp * Vd * expT(-(Vd - Vp) / Vp);
+    const T iex = Iv * (atanT(D * (Vd - E)) + atanT(D * (Vd + E)));
+    const T Id = idiode + itunnel + iex;
+    const T Ron = T(1434.0), Roff = T(1e6), Von1 = T(0.28), Voff1 = T(0.14), Von2 = T(-0.12), Voff2 = T(-0.006);
+    const T TAU = T(1e-7), TT = T(2.0), boltz = T(1.380649e-23), echarge = T(1.602176634e-19);
+    const T g = XSV / Ron + (T(1.0) - XSV) / Roff;
+    const T arg1 = -T(1.0) / (TT * boltz / echarge) * (Vm - Von1) * (Vm - Von2);
+    const T arg2 = -T(1.0) / (TT * boltz / echarge) * (Vm - Voff2) * (Vm - Voff1);
+    const T exp1 = expT(arg1), exp2 = expT(arg2);
+    const T f1 = T(1.0) / (T(1.0) + exp1);
+    const T f2 = T(1.0) / (T(1.0) + exp2);
+    const T Ix = (T(1.0) / TAU) * (f1 * (T(1.0) - XSV) - (T(1.0) - f2) * XSV);
+    const T Imem = Vm * g;
+    const T Iin = a[0] * sinT(a[1] * t);
+    const T dVc = (Iin - Imem - Id) / C1;
+    const T dXSV = Ix;
+    X[0] = Vc + h * dVc;
+    X[1] = XSV + h * dXSV;
+    X[2] = t + h;
+}
+
+// Per-launch step constants: the RK4 fractions of h for systems 0-2, plain h otherwise.
+template <class T> struct StepCtx {
+    RK4H<T> rk;
+    CHAOS_HD StepCtx() {}
+    CHAOS_HD explicit StepCtx(T h) : rk(h) {}
+};
+
+// One step of system S (compile-time id).
+template <int S, class T> CHAOS_HD void step(T* x, const T* a, const StepCtx<T>& c) {
+    if (S == SYS_LORENZ_RK4) rk4_step<Lorenz>(x, a, c.rk);
+    else if (S == SYS_ROSSLER_RK4) rk4_step<Rossler>(x, a, c.rk);
+    else if (S == SYS_CHEN_RK4) rk4_step<Chen>(x, a, c.rk);
+    else if (S == SYS_CHAMELEON) chameleon_step(x, a, c.rk.h);
+    else if (S == SYS_ROSSLER_CD) rossler_cd_step(x, a, c.rk.h);
+    else if (S == SYS_SIN3) sin3_step(x, a, c.rk.h);
+    else if (S == SYS_SIN2) sin2_step(x, a, c.rk.h);
+    else if (S == SYS_MEMRISTOR) memristor_step(x, a, c.rk.h);
+}
+
+// Runtime-dispatched step (host checker, tests).
+template <class T> inline void step_dyn(int s, T* x, const T* a, const StepCtx<T>& c) {
+    switch (s) {
+        case SYS_LORENZ_RK4: step<SYS_LORENZ_RK4>(x, a, c); break;
+        case SYS_ROSSLER_RK4: step<SYS_ROSSLER_RK4>(x, a, c); break;
+        case SYS_CHEN_RK4: step<SYS_CHEN_RK4>(x, a, c); break;
+        case SYS_CHAMELEON: step<SYS_CHAMELEON>(x, a, c); break;
+        case SYS_ROSSLER_CD: step<SYS_ROSSLER_CD>(x, a, c); break;
+        case SYS_SIN3: step<SYS_SIN3>(x, a, c); break;
+        case SYS_SIN2: step<SYS_SIN2>(x, a, c); break;
+        case SYS_MEMRISTOR: step<SYS_MEMRISTOR>(x, a, c); break;
+        default: break;
+    }
+}
+
+}  // namespace chaos

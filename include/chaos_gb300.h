@@ -1,0 +1,200 @@
+/*
+ * C ABI of the GB300 (sm_103a) engine for ChaosLibrary's bifurcation / LLE /
+ * basins hot path.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (CHAOS_OK or a negative CHAOS_E_* code; never exits the process) and keeps
+ * the reference's argument names and meaning. The reference's entry points
+ * write CSV files only; these return the same results in caller-owned arrays
+ * (host or device memory, chosen by chaos_exec.memory). The C++ wrappers with
+ * the reference's exact signatures, which write the reference's CSV files,
+ * are declared in chaos_compat.hpp.
+ *
+ * Per-point flags keep the reference's values: 1 = bounded, 0 = diverged
+ * (NaN, |x| >= 2^53 or |x| > maxValue), -1 = fixed point.
+ *
+ * Threading: calls are reentrant (no global device state); calls on one
+ * stream run in order, calls on different streams may overlap.
+ */
+#ifndef CHAOS_GB300_H
+#define CHAOS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHAOS_ABI_VERSION 1
+
+/* status codes */
+#define CHAOS_OK 0
+#define CHAOS_E_ARGS (-1)        /* invalid argument (message in chaos_last_error) */
+#define CHAOS_E_NOMEM (-2)       /* device or host allocation failed */
+#define CHAOS_E_CUDA (-3)        /* CUDA runtime error */
+#define CHAOS_E_IO (-4)          /* file could not be written (compat wrappers) */
+#define CHAOS_E_TIMEOUT (-5)     /* a bounded wait ran out */
+#define CHAOS_E_UNSUPPORTED (-6) /* combination not implemented (e.g. FP32 LLE of a non-polynomial system) */
+#define CHAOS_E_BUSY (-7)        /* admission refused: no slot or HBM budget left */
+#define CHAOS_E_NODEV (-8)       /* no CUDA device */
+
+/* arithmetic of the trajectories */
+#define CHAOS_FP64 0 /* the reference's FP64 arithmetic; bit-identical to the CPU oracle */
+#define CHAOS_FP32 1 /* FP32 state, FP64 accumulation (peak times, means, log-stretch sums) */
+
+/* where the caller's arrays live */
+#define CHAOS_MEM_HOST 0   /* results are copied back and the call returns when they are there */
+#define CHAOS_MEM_DEVICE 1 /* device pointers; the call is asynchronous on `stream` */
+
+/* built-in systems (the reference selects one at compile time in systems/systems.cuh:9) */
+#define CHAOS_SYS_LORENZ_RK4 0  /* x'=s(y-x), y'=x(r-z)-y, z'=xy-bz; a={sigma,rho,beta}; classic RK4 */
+#define CHAOS_SYS_ROSSLER_RK4 1 /* x'=-y-z, y'=x+ay, z'=b+z(x-c); a={a,b,c}; classic RK4 */
+#define CHAOS_SYS_CHEN_RK4 2    /* x'=a(y-x), y'=(c-a)x-xz+cy, z'=xy-bz; a={a,b,c}; classic RK4 */
+#define CHAOS_SYS_CHAMELEON 3   /* reference systems/systems.cuh:11-39 */
+#define CHAOS_SYS_ROSSLER_CD 4  /* reference systems/systems.cuh:41-63 */
+#define CHAOS_SYS_SIN3 5        /* reference systems/systems.cuh:67-83 (USE_SYSTEM_FOR_BASINS) */
+#define CHAOS_SYS_SIN2 6        /* reference systems/systems.cuh:85-101 (USE_SYSTEM_FOR_BASINS_2) */
+#define CHAOS_SYS_MEMRISTOR 7   /* reference systems/systems.cuh:103-178 (USE_DAMIR_SYSTEM) */
+
+typedef struct chaos_exec {
+    int precision; /* CHAOS_FP64 or CHAOS_FP32 */
+    int memory;    /* CHAOS_MEM_HOST or CHAOS_MEM_DEVICE */
+    void* stream;  /* cudaStream_t; NULL = the library's stream for the device */
+    int device;    /* CUDA device ordinal; -1 = the current device */
+} chaos_exec;
+
+/* Library version (CHAOS_ABI_VERSION) and last error message of this thread. */
+int chaos_abi_version(void);
+const char* chaos_last_error(void);
+
+/* SIZE_X / SIZE_A of a built-in system (reference systems/systems.cuh SIZE_X, SIZE_A). */
+int chaos_system_info(int system, int* sizeX, int* sizeA);
+
+/* Waits for the work of `ex` (its stream) to finish. */
+int chaos_synchronize(const chaos_exec* ex);
+
+/*
+ * 1-D bifurcation sweep. Replaces Bifurcation::bifurcation1D
+ * (Bifurcation/include/bifurcationHOST.h:16-30, Bifurcation/src/bifurcationCUDA.cu:587-783).
+ * Point k sweeps values[indicesOfMutVars[0]] over ranges[0..1] (nPts points).
+ * Outputs per point k (arrays of nPts, rows of peakCapacity):
+ *   counts[k]  kept peaks (the reference's amountOfPeaks), -1 fixed point, 0 diverged / none;
+ *              the true count even when it exceeds peakCapacity
+ *   flags[k]   1 / 0 / -1
+ *   firstSample[k]  x[writableVar] at the first recorded sample (the reference's row for -1)
+ *   peaks[k*cap + j], intervals[k*cap + j]  for j < min(counts[k], peakCapacity)
+ * firstSample, peaks and intervals may be NULL.
+ */
+int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, int peakCapacity, int* counts,
+                        int* flags, double* firstSample, double* peaks, double* intervals);
+
+/*
+ * 2-D bifurcation sweep with the per-point interval clustering. Replaces
+ * Bifurcation::bifurcation2D (Bifurcation/include/bifurcationHOST.h:35-50,
+ * Bifurcation/src/bifurcationCUDA.cu:43-256). labels[nPts*nPts] receives the
+ * reference's dbscanCUDA result per point (point k: first swept value index
+ * k % nPts, second k / nPts). counts (may be NULL) as in chaos_bifurcation1d.
+ */
+int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, double eps, int* labels,
+                        int* counts);
+
+/*
+ * Largest-Lyapunov-exponent map. Replaces LLE::LLE2D (LLE/include/LLEHost.h:25-41,
+ * LLE/src/LLECUDA.cu:205-428). lle[j*nPts + i] is the value at
+ * values[indicesOfMutVars[0]] = linspace(ranges[0], ranges[1])[i] and
+ * values[indicesOfMutVars[1]] = linspace(ranges[2], ranges[3])[j]: the
+ * reference CSV's transposed layout (row = second parameter). The twin
+ * trajectory starts at x + eps along state component 0 (the reference draws a
+ * random unit direction with cuRAND). writableVar and maxValue are accepted
+ * and unused, as in the reference. CHAOS_FP32 is supported for the three RK4
+ * systems (exact-difference twin, FP64 log sum).
+ */
+int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nPts, double h, double eps,
+                const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+                const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                const double* values, int amountOfValues, double* lle);
+
+/*
+ * Per-point basin features over the nPts x nPts grid of initial conditions
+ * (initialConditions[indicesOfMutVars[0]] over ranges[0..1] fastest,
+ * initialConditions[indicesOfMutVars[1]] over ranges[2..3]). The first stage
+ * of Basins::basinsOfAttraction_2 (Basins/src/basinsCUDA.cu:602-692, kernels
+ * :233-314 and avgPeakFinderCUDA :818-864): flags, avgPeaks, avgIntervals
+ * with the reference's sentinels (flag 0: 999/999; flag -1: last sample/-1;
+ * no peaks: 1000/1000) and counts = kept peaks (may be NULL).
+ */
+int chaos_basins_features(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                          int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                          const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                          const double* values, int amountOfValues, int preScaller, int* flags, double* avgPeaks,
+                          double* avgIntervals, int* counts);
+
+/*
+ * Basins of attraction. Replaces Basins::basinsOfAttraction_2
+ * (Basins/include/basinsHOST.h:15-30, Basins/src/basinsCUDA.cu:442-813):
+ * features as chaos_basins_features, then the reference's global clustering
+ * (CUDA_dbscan, basinsCUDA.cu:35-179) as chaos_dbscan_compat. Any output
+ * pointer but labels may be NULL.
+ */
+int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double h, int amountOfInitialConditions,
+                 const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                 int writableVar, double maxValue, double transientTime, const double* values, int amountOfValues,
+                 int preScaller, double eps, int* labels, double* avgPeaks, double* avgIntervals, int* flags);
+
+/*
+ * The reference's basin clustering on given feature arrays
+ * (CUDA_dbscan + CUDA_dbscan_kernel, Basins/src/basinsCUDA.cu:35-179, 894-923):
+ * eps-connected components (sqrt(dp^2 + di^2) <= eps, FP64) over the points
+ * with flag != 0. Components that hold a fixed point (flag -1) are numbered
+ * -1, -2, ... in order of their smallest fixed-point index, the others 1, 2,
+ * ... in order of their smallest index; flag-0 points get 0. (The reference
+ * numbers components in a racy seed order; the partition is the same.)
+ */
+int chaos_dbscan_compat(const chaos_exec* ex, const double* avgPeaks, const double* avgIntervals, const int* flags,
+                        long long n, double eps, int* labels);
+
+/*
+ * DBSCAN with scikit-learn semantics on an n x dims feature matrix (row-major,
+ * dims 1..3): core points have >= minPts points (themselves included) within
+ * distance <= eps; clusters are numbered 0, 1, ... by their smallest core
+ * index; a border point joins the lowest-numbered adjacent cluster; noise is
+ * -1; points with mask[i] == 0 (mask may be NULL) are left out and get -2.
+ * No reference counterpart (the reference clusters with chaos_dbscan_compat's rule).
+ */
+int chaos_dbscan(const chaos_exec* ex, const double* features, long long n, int dims, double eps, int minPts,
+                 const int* mask, int* labels);
+
+/*
+ * The reference's peakFinder on caller series (Bifurcation/src/bifurcationCUDA.cu:469-514):
+ * data is nSeries x len (row-major); counts, peaks and intervals as in
+ * chaos_bifurcation1d, with intervals in units of h.
+ */
+int chaos_peak_finder(const chaos_exec* ex, const double* data, long long nSeries, int len, double h,
+                      int peakCapacity, int* counts, double* peaks, double* intervals);
+
+/*
+ * The reference's per-point clustering of the 2-D bifurcation on caller
+ * interval rows (dbscanCUDA + dbscan, Bifurcation/src/bifurcationCUDA.cu:373-398, 516-572):
+ * intervals is n x stride, counts[k] the number of intervals of row k (-1 and
+ * 0 pass through as in the reference). labels[k] = clusters - 1; a row whose
+ * count exceeds stride gets INT_MIN.
+ */
+int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int* counts, long long n, int stride,
+                       double eps, int* labels);
+
+/*
+ * FP32 FMA-pipe probe (no reference counterpart): times `iters` rounds of 8
+ * independent fmaf chains in 2048 threads per SM and returns the elapsed
+ * seconds and the flops executed, the measured denominator of the
+ * integration kernels' roofline.
+ */
+int chaos_fma_probe(const chaos_exec* ex, long long iters, double* seconds, double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHAOS_GB300_H */

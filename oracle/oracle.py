@@ -1,0 +1,273 @@
+"""ctypes front end of the CPU oracle (and of the host build of the reference).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` as the checker. The engine package never
+imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+SRC = HERE / "chaos_oracle.cpp"
+REF_DIR = HERE / "_ref"
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+SYSTEMS = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "rossler_cd": 4, "sin3": 5, "sin2": 6,
+           "memristor": 7}
+
+
+def build(force: bool = False) -> Path:
+    deps = [SRC, HERE.parent / "chaoslibrary_gb300" / "csrc" / "systems.h"]
+    if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return LIB
+    tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+    subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+                    str(SRC), "-o", str(tmp)], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        L = _lib
+        L.orc_steps.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_int]
+        L.orc_trajectory.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.orc_peak_finder.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_int, _ip, _dp, _dp]
+        L.orc_point_dbscan.argtypes = [_dp, _ip, C.c_int, C.c_int, C.c_double, _ip]
+        L.orc_bifurcation.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
+                                      C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_int, C.c_longlong,
+                                      C.c_longlong, _ip, _ip, _dp, _dp, _dp, C.c_void_p, C.c_int]
+        L.orc_lle2d.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, _dp, _dp, _ip,
+                                C.c_double, _dp, C.c_longlong, C.c_longlong, _dp, C.c_int]
+        L.orc_basins_features.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
+                                          C.c_double, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _ip,
+                                          _dp, _dp, C.c_void_p, C.c_int]
+        L.orc_dbscan_compat_bfs.argtypes = [_dp, _dp, _ip, C.c_int, C.c_double, _ip]
+        L.orc_dbscan_compat_grid.argtypes = [_dp, _dp, _ip, C.c_int, C.c_double, _ip]
+        L.orc_dbscan.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, _ip]
+    return _lib
+
+
+def _d(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _i(x):
+    return np.ascontiguousarray(x, dtype=np.int32)
+
+
+def steps(system: int, x0, a, h: float, n: int) -> np.ndarray:
+    x = _d(x0).copy()
+    lib().orc_steps(system, x, _d(a), h, n)
+    return x
+
+
+def trajectory(system: int, x0, a, h: float, n: int) -> np.ndarray:
+    x0 = _d(x0)
+    out = np.zeros((n, x0.size), np.float64)
+    lib().orc_trajectory(system, x0, _d(a), h, n, out)
+    return out
+
+
+def peak_finder(data, h: float, cap: int | None = None):
+    data = _d(np.atleast_2d(data))
+    n, ln = data.shape
+    cap = cap or max(ln, 1)
+    counts = np.zeros(n, np.int32)
+    pk = np.zeros((n, cap), np.float64)
+    iv = np.zeros((n, cap), np.float64)
+    lib().orc_peak_finder(data, n, ln, h, cap, counts, pk, iv)
+    return counts, pk, iv
+
+
+def point_dbscan(intervals, counts, eps: float) -> np.ndarray:
+    intervals = _d(np.atleast_2d(intervals))
+    counts = _i(counts)
+    out = np.zeros(counts.size, np.int32)
+    lib().orc_point_dbscan(intervals, counts, counts.size, intervals.shape[1], eps, out)
+    return out
+
+
+def bifurcation(system: int, dim: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                preScaller=1, eps=0.0, cap=None, p_begin=0, p_end=-1, nthreads=0):
+    """Per point: counts, flags, first, peaks[cap], intervals[cap], labels (dim 2)."""
+    B = int(tMax / h / preScaller)
+    total = nPts ** dim
+    p_end = total if p_end < 0 else p_end
+    n = p_end - p_begin
+    cap = cap or max(B // 2 + 1, 1)
+    counts = np.zeros(n, np.int32)
+    flags = np.zeros(n, np.int32)
+    first = np.zeros(n, np.float64)
+    pk = np.zeros((n, cap), np.float64)
+    iv = np.zeros((n, cap), np.float64)
+    labels = np.zeros(n, np.int32)
+    rc = lib().orc_bifurcation(system, dim, tMax, nPts, h, _d(ic), _d(ranges), _i(mut), wv, maxValue,
+                               transientTime, _d(values), preScaller, eps, cap, p_begin, p_end, counts, flags,
+                               first, pk, iv, labels.ctypes.data if dim == 2 else None, nthreads)
+    if rc:
+        raise ValueError("bad bifurcation arguments")
+    return dict(counts=counts, flags=flags, first=first, peaks=pk, intervals=iv,
+                labels=labels if dim == 2 else None)
+
+
+def lle2d(system: int, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values, p_begin=0, p_end=-1,
+          nthreads=0) -> np.ndarray:
+    total = nPts * nPts
+    p_end = total if p_end < 0 else p_end
+    out = np.zeros(p_end - p_begin, np.float64)
+    rc = lib().orc_lle2d(system, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut), transientTime, _d(values),
+                         p_begin, p_end, out, nthreads)
+    if rc:
+        raise ValueError("bad LLE arguments")
+    return out
+
+
+def basins_features(system: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                    preScaller=1, p_begin=0, p_end=-1, nthreads=0):
+    total = nPts * nPts
+    p_end = total if p_end < 0 else p_end
+    n = p_end - p_begin
+    flags = np.zeros(n, np.int32)
+    ap = np.zeros(n, np.float64)
+    ai = np.zeros(n, np.float64)
+    counts = np.zeros(n, np.int32)
+    rc = lib().orc_basins_features(system, tMax, nPts, h, _d(ic), _d(ranges), _i(mut), wv, maxValue,
+                                   transientTime, _d(values), preScaller, p_begin, p_end, flags, ap, ai,
+                                   counts.ctypes.data, nthreads)
+    if rc:
+        raise ValueError("bad basins arguments")
+    return dict(flags=flags, avg_peaks=ap, avg_intervals=ai, counts=counts)
+
+
+def dbscan_compat(avg_peaks, avg_intervals, flags, eps: float, method: str = "grid") -> np.ndarray:
+    ap, ai, fl = _d(avg_peaks), _d(avg_intervals), _i(flags)
+    out = np.zeros(ap.size, np.int32)
+    fn = lib().orc_dbscan_compat_grid if method == "grid" else lib().orc_dbscan_compat_bfs
+    fn(ap, ai, fl, ap.size, eps, out)
+    return out
+
+
+def dbscan(features, eps: float, min_pts: int, mask=None) -> np.ndarray:
+    f = _d(np.atleast_2d(features))
+    n, d = f.shape
+    out = np.zeros(n, np.int32)
+    m = None if mask is None else _i(mask)
+    lib().orc_dbscan(f, n, d, eps, min_pts, None if m is None else m.ctypes.data, out)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# the reference's own code compiled for the host (only where the sources are)
+
+class RefLib:
+    """Host build of the reference per-thread code for one plug-in system."""
+
+    def __init__(self, name: str):
+        path = REF_DIR / f"libref_{name}.so"
+        if not path.exists():
+            raise FileNotFoundError(path)
+        L = self.L = C.CDLL(str(path))
+        L.refh_steps.argtypes = [_dp, _dp, C.c_double, C.c_int]
+        L.refh_peak_finder.argtypes = [_dp, C.c_int, _dp, _dp, C.c_double]
+        L.refh_point_dbscan.argtypes = [_dp, _dp, _dp, C.c_int, C.c_int, C.c_double]
+        L.refh_bifurcation.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, C.c_int,
+                                       C.c_double, C.c_double, _dp, C.c_int, C.c_int, C.c_double, _ip, _dp, _dp,
+                                       C.c_void_p, C.c_void_p]
+        L.refh_basins.argtypes = [C.c_double, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, C.c_int, C.c_double,
+                                  C.c_double, _dp, C.c_int, C.c_int, _ip, _dp, _dp, _dp]
+        L.refh_basins_dbscan.argtypes = [_dp, _dp, _ip, _ip, C.c_int, C.c_double]
+        L.refh_lle.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _ip,
+                               C.c_double, _dp, C.c_int, _dp]
+
+    def steps(self, x0, a, h, n):
+        x = _d(x0).copy()
+        self.L.refh_steps(x, _d(a), h, n)
+        return x
+
+    def peak_finder(self, series, h):
+        d = _d(series).copy()
+        pk = np.zeros(max(d.size, 1))
+        tm = np.zeros(max(d.size, 1))
+        c = self.L.refh_peak_finder(d, d.size, pk, tm, h)
+        return c, pk[:max(c, 0)], tm[:max(c, 0)]
+
+    def point_dbscan(self, peaks, intervals, count, size_of_block, eps):
+        data = np.zeros(size_of_block)
+        iv = np.zeros(size_of_block)
+        data[:count] = peaks[:count]
+        iv[:count] = intervals[:count]
+        helpful = np.zeros(size_of_block)
+        return self.L.refh_point_dbscan(data, iv, helpful, count, size_of_block, eps)
+
+    def bifurcation(self, dim, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                    preScaller=1, eps=0.0):
+        B = int(tMax / h / preScaller)
+        N = nPts ** dim
+        ic, values = _d(ic), _d(values)
+        amount = np.zeros(N, np.int32)
+        data = np.zeros(N * B)
+        iv = np.zeros(N * B)
+        db = np.zeros(N, np.int32)
+        helpful = np.zeros(N * B)
+        self.L.refh_bifurcation(dim, tMax, nPts, h, ic.size, ic, _d(ranges), _i(mut), wv, maxValue, transientTime,
+                                values, values.size, preScaller, eps, amount, data, iv,
+                                db.ctypes.data if dim == 2 else None, helpful.ctypes.data)
+        return dict(counts=amount, data=data.reshape(N, B), intervals=iv.reshape(N, B),
+                    labels=db if dim == 2 else None)
+
+    def basins(self, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values, preScaller=1):
+        B = int(tMax / h / preScaller)
+        N = nPts * nPts
+        ic, values = _d(ic), _d(values)
+        helpful = np.zeros(N, np.int32)
+        ap = np.zeros(N)
+        ai = np.zeros(N)
+        data = np.zeros(N * B)
+        self.L.refh_basins(tMax, nPts, h, ic.size, ic, _d(ranges), _i(mut), wv, maxValue, transientTime, values,
+                           values.size, preScaller, helpful, ap, ai, data)
+        return dict(flags=helpful, avg_peaks=ap, avg_intervals=ai)
+
+    def basins_dbscan(self, avg_peaks, avg_intervals, flags, eps):
+        ap, ai, fl = _d(avg_peaks).copy(), _d(avg_intervals).copy(), _i(flags).copy()
+        labels = np.zeros(ap.size, np.int32)
+        self.L.refh_basins_dbscan(ap, ai, labels, fl, ap.size, eps)
+        return labels
+
+    def lle(self, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values):
+        ic, values = _d(ic), _d(values)
+        out = np.zeros(nPts * nPts)
+        self.L.refh_lle(tMax, NT, nPts, h, eps, ic.size, ic, _d(ranges), _i(mut), transientTime, values,
+                        values.size, out)
+        return out
+
+
+def ref_available(name: str = "lorenz") -> bool:
+    return (REF_DIR / f"libref_{name}.so").exists()
+
+
+def canonical_labels(labels) -> np.ndarray:
+    """Relabel a compat basin labelling: negative ids numbered -1, -2, ... by
+    their smallest member index, positive ids 1, 2, ... likewise, 0 kept."""
+    labels = np.asarray(labels)
+    out = np.zeros_like(labels)
+    for sign in (-1, 1):
+        ids = np.unique(labels[labels * sign > 0])
+        firsts = sorted((int(np.argmax(labels == v)), v) for v in ids)
+        for rank, (_, v) in enumerate(firsts, start=1):
+            out[labels == v] = sign * rank
+    return out

@@ -1,0 +1,205 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the golden
+fixtures made by the reference's own code and against the CPU oracle.
+
+FP64 polynomial systems are compared bit for bit (peak counts, peak values,
+intervals, flags, features, labels). Systems whose step calls cos/sin/exp are
+compared within tolerances, because CUDA's libm and the host's may differ in
+the last bit and chaos amplifies that."""
+import numpy as np
+import pytest
+
+from conftest import golden, sweep_kwargs
+
+pytestmark = pytest.mark.gpu
+
+SYS = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "sin3": 5}
+
+
+def eng_kw(kw):
+    return dict(tMax=kw["tMax"], nPts=kw["nPts"], h=kw["h"], initialConditions=kw["ic"], ranges=kw["ranges"],
+                indicesOfMutVars=kw["mut"], writableVar=kw["wv"], maxValue=kw["maxValue"],
+                transientTime=kw["transientTime"], values=kw["values"])
+
+
+@pytest.mark.parametrize("name", ["peaks_crafted", "peaks_random"])
+def test_peak_finder_golden(engine, name):
+    g = golden(name)
+    r = engine.peak_finder(g["data"], float(g["h"]), peakCapacity=g["data"].shape[1])
+    assert np.array_equal(r["counts"], g["counts"])
+    for s, c in enumerate(r["counts"]):
+        assert np.array_equal(r["peaks"][s, :c], g["peaks"][s, :c])
+        assert np.array_equal(r["intervals"][s, :c], g["intervals"][s, :c])
+
+
+def test_point_dbscan_golden(engine):
+    g = golden("point_dbscan")
+    out = engine.point_dbscan(g["intervals"], g["counts"], float(g["eps"]))
+    assert np.array_equal(out, g["labels"])
+
+
+@pytest.mark.parametrize("name", ["bif1d_lorenz", "bif2d_lorenz"])
+def test_bifurcation_golden_exact(engine, name):
+    g = golden(name)
+    kw = eng_kw(sweep_kwargs(g))
+    if int(g["dim"]) == 1:
+        r = engine.bifurcation1d("lorenz", **kw)
+        assert np.array_equal(r["counts"], g["counts"])
+        for k, c in enumerate(r["counts"]):
+            if c > 0:
+                assert np.array_equal(r["peaks"][k, :c], g["peaks"][k, :c])
+                assert np.array_equal(r["intervals"][k, :c], g["intervals"][k, :c])
+            if c == -1:
+                assert r["first"][k] == g["first"][k]
+    else:
+        r = engine.bifurcation2d("lorenz", eps=float(g["eps"]), **kw)
+        assert np.array_equal(r["counts"], g["counts"])
+        assert np.array_equal(r["labels"], g["labels"])
+
+
+@pytest.mark.parametrize("name", ["bif1d_chameleon", "bif2d_chameleon"])
+def test_bifurcation_golden_transcendental(engine, name):
+    """Chameleon calls cos(): counts agree on almost every point, peaks closely."""
+    g = golden(name)
+    kw = eng_kw(sweep_kwargs(g))
+    if int(g["dim"]) == 1:
+        r = engine.bifurcation1d("chameleon", **kw)
+        same = r["counts"] == g["counts"]
+        assert same.mean() >= 0.9
+        for k in np.where(same & (r["counts"] > 0))[0]:
+            c = r["counts"][k]
+            np.testing.assert_allclose(r["peaks"][k, :c], g["peaks"][k, :c], rtol=1e-6, atol=1e-9)
+    else:
+        r = engine.bifurcation2d("chameleon", eps=float(g["eps"]), **kw)
+        assert (r["labels"] == g["labels"]).mean() >= 0.9
+
+
+@pytest.mark.parametrize("system, values, ic, mi, rng", [
+    ("lorenz", [10.0, 28.0, 8 / 3], [0.1, 0.1, 0.1], 1, [20.0, 200.0]),
+    ("rossler", [0.2, 0.2, 5.7], [1.0, 1.0, 1.0], 2, [2.0, 10.0]),
+    ("chen", [35.0, 3.0, 28.0], [-10.0, 0.0, 37.0], 2, [20.0, 30.0]),
+])
+def test_bifurcation_vs_oracle_fp64(engine, oracle, system, values, ic, mi, rng):
+    kw = dict(tMax=40.0, nPts=96, h=0.01, initialConditions=ic, ranges=rng, indicesOfMutVars=[mi], writableVar=0,
+              maxValue=1e4, transientTime=20.0, values=values)
+    r = engine.bifurcation1d(system, **kw)
+    o = oracle.bifurcation(SYS[system], 1, kw["tMax"], kw["nPts"], kw["h"], ic, rng, [mi], 0, kw["maxValue"],
+                           kw["transientTime"], values, cap=r["peaks"].shape[1])
+    assert np.array_equal(r["flags"], o["flags"])
+    assert np.array_equal(r["counts"], o["counts"])
+    for k, c in enumerate(r["counts"]):
+        if c > 0:
+            assert np.array_equal(r["peaks"][k, :c], o["peaks"][k, :c])
+            assert np.array_equal(r["intervals"][k, :c], o["intervals"][k, :c])
+        if c == -1:
+            assert r["first"][k] == o["first"][k]
+
+
+def test_bifurcation_small_capacity_reports_true_count(engine, oracle):
+    g = golden("bif1d_lorenz")
+    kw = eng_kw(sweep_kwargs(g))
+    r = engine.bifurcation1d("lorenz", peakCapacity=3, **kw)
+    assert np.array_equal(r["counts"], g["counts"])
+    for k, c in enumerate(r["counts"]):
+        m = min(c, 3)
+        if m > 0:
+            assert np.array_equal(r["peaks"][k, :m], g["peaks"][k, :m])
+
+
+@pytest.mark.parametrize("name", ["basins_lorenz"])
+def test_basins_golden_exact(engine, oracle, name):
+    g = golden(name)
+    kw = eng_kw(sweep_kwargs(g))
+    f = engine.basins_features("lorenz", **kw)
+    assert np.array_equal(f["flags"], g["flags"])
+    assert np.array_equal(f["avg_peaks"], g["avg_peaks"])
+    assert np.array_equal(f["avg_intervals"], g["avg_intervals"])
+    b = engine.basins("lorenz", eps=float(g["eps"]), **kw)
+    assert np.array_equal(oracle.canonical_labels(b["labels"]), oracle.canonical_labels(g["labels"]))
+    o = oracle.dbscan_compat(g["avg_peaks"], g["avg_intervals"], g["flags"], float(g["eps"]))
+    assert np.array_equal(b["labels"], o)  # same canonical numbering as the oracle
+
+
+def test_basins_golden_transcendental(engine, oracle):
+    g = golden("basins_sin3")
+    kw = eng_kw(sweep_kwargs(g))
+    f = engine.basins_features("sin3", **kw)
+    assert (f["flags"] == g["flags"]).mean() >= 0.95
+    close = np.isclose(f["avg_peaks"], g["avg_peaks"], rtol=1e-6, atol=1e-9)
+    assert close.mean() >= 0.9
+
+
+def test_dbscan_compat_golden(engine, oracle):
+    g = golden("dbscan_compat")
+    lab = engine.dbscan_compat(g["avg_peaks"], g["avg_intervals"], g["flags"], float(g["eps"]))
+    assert np.array_equal(oracle.canonical_labels(lab), oracle.canonical_labels(g["labels"]))
+    assert np.array_equal(lab, oracle.dbscan_compat(g["avg_peaks"], g["avg_intervals"], g["flags"], float(g["eps"])))
+
+
+def test_dbscan_sklearn_golden(engine):
+    g = golden("dbscan_sklearn")
+    lab = engine.dbscan(g["X"], float(g["eps"]), int(g["min_pts"]))
+    assert np.array_equal(lab, g["labels"])
+
+
+@pytest.mark.parametrize("n, d, eps, min_pts, seed", [(20000, 2, 0.01, 4, 1), (50000, 3, 0.03, 8, 2),
+                                                      (5000, 1, 0.001, 3, 3), (30000, 3, 0.05, 1, 4)])
+def test_dbscan_random_vs_oracle(engine, oracle, n, d, eps, min_pts, seed):
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0, 1, size=(20, d))
+    X = centres[rng.integers(0, 20, n)] + rng.normal(scale=0.02, size=(n, d))
+    X[: n // 10] = rng.uniform(0, 1, size=(n // 10, d))
+    mask = (rng.random(n) > 0.02).astype(np.int32)
+    lab = engine.dbscan(X, eps, min_pts, mask=mask)
+    ref = oracle.dbscan(X, eps, min_pts, mask=mask)
+    assert np.array_equal(lab, ref)
+
+
+@pytest.mark.parametrize("n, spread, eps, seed", [(100000, 1.0, 0.005, 5), (400000, 3.0, 0.01, 6)])
+def test_dbscan_compat_random_vs_oracle(engine, oracle, n, spread, eps, seed):
+    rng = np.random.default_rng(seed)
+    ap = rng.uniform(0, spread, n)
+    ai = rng.uniform(0, spread, n)
+    ap[:1000] = 7.83  # one dense cell of identical features
+    ai[:1000] = -1.0
+    flags = rng.choice([-1, 0, 1], size=n, p=[0.05, 0.05, 0.9]).astype(np.int32)
+    lab = engine.dbscan_compat(ap, ai, flags, eps)
+    ref = oracle.dbscan_compat(ap, ai, flags, eps)
+    assert np.array_equal(lab, ref)
+
+
+def test_lle_fp64_golden_and_oracle(engine, oracle):
+    g = golden("lle_rossler")
+    kw = dict(tMax=float(g["tMax"]), NT=float(g["NT"]), nPts=int(g["nPts"]), h=float(g["h"]), eps=float(g["eps"]),
+              initialConditions=g["ic"], ranges=g["ranges"], indicesOfMutVars=g["mut"],
+              transientTime=float(g["transientTime"]), values=g["values"])
+    r = engine.lle2d("rossler", precision=engine.FP64, **kw)
+    fin = np.isfinite(g["lle"])
+    assert np.array_equal(np.isfinite(r), fin)
+    assert np.max(np.abs(r[fin] - g["lle"][fin])) < 1e-6
+    o = oracle.lle2d(1, kw["tMax"], kw["NT"], kw["nPts"], kw["h"], kw["eps"], g["ic"], g["ranges"], g["mut"],
+                     kw["transientTime"], g["values"])
+    assert np.max(np.abs(r[fin] - o[fin])) < 1e-12  # same trajectories, libm log may differ in the last bit
+
+
+@pytest.mark.parametrize("system, values, ranges, mut", [
+    ("rossler", [0.2, 0.2, 5.7], [0.1, 0.4, 2.0, 10.0], [0, 2]),
+    ("lorenz", [10.0, 28.0, 8 / 3], [20.0, 60.0, 5.0, 15.0], [1, 0]),
+    ("chen", [35.0, 3.0, 28.0], [30.0, 40.0, 20.0, 30.0], [0, 2]),
+])
+def test_lle_fp32_vs_fp64_oracle(engine, oracle, system, values, ranges, mut):
+    """FP32 twin-difference LLE against the FP64 oracle: regular points (|LLE|
+    small in FP64) agree within 1e-3; every point agrees in classification
+    (chaotic vs not at 0.01)."""
+    ic = [1.0, 1.0, 1.0] if system != "chen" else [-10.0, 0.0, 37.0]
+    kw = dict(tMax=100.0, NT=0.1, nPts=16, h=0.01, eps=1e-8, initialConditions=ic, ranges=ranges,
+              indicesOfMutVars=mut, transientTime=20.0, values=values)
+    r = engine.lle2d(system, precision=engine.FP32, **kw)
+    o = oracle.lle2d(SYS[system], kw["tMax"], kw["NT"], kw["nPts"], kw["h"], kw["eps"], ic, ranges, mut,
+                     kw["transientTime"], values)
+    fin = np.isfinite(o) & (np.abs(o) < 1e3)
+    assert np.isfinite(r[fin]).all()
+    reg = fin & (o < 0.005)
+    if reg.any():
+        assert np.max(np.abs(r[reg] - o[reg])) <= 1e-3
+    chaotic_o, chaotic_r = o[fin] > 0.01, r[fin] > 0.01
+    assert (chaotic_o == chaotic_r).mean() >= 0.97

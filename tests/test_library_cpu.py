@@ -1,0 +1,122 @@
+"""The engine library without a GPU: it builds for sm_103a, loads, exports
+every entry point the public headers declare, and rejects bad arguments on
+the host (CHAOS_E_ARGS) before touching a device."""
+import ctypes as C
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def native():
+    from chaoslibrary_gb300 import build as B
+
+    B.build()
+    from chaoslibrary_gb300 import _native as N
+
+    N.lib()
+    return N
+
+
+def declared_c_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h*"):
+        text = h.read_text()
+        names.update(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(chaos_\w+)\s*\(", text, re.M))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = declared_c_functions()
+    for must in ("chaos_bifurcation1d", "chaos_bifurcation2d", "chaos_lle2d", "chaos_basins", "chaos_dbscan",
+                 "chaos_dbscan_compat", "chaos_peak_finder", "chaos_point_dbscan", "chaos_compat_LLE2D"):
+        assert must in names
+
+
+def test_every_declared_symbol_is_exported(native):
+    L = native.lib()
+    missing = [n for n in declared_c_functions() if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-DC", str(native.lib_path())], capture_output=True, text=True).stdout
+    for cxx in ("Bifurcation::bifurcation1D(", "Bifurcation::bifurcation2D(", "LLE::LLE2D(",
+                "Basins::basinsOfAttraction_2("):
+        assert cxx in out, cxx
+
+
+def test_kernels_built_for_sm_103a(native):
+    out = subprocess.run(["cuobjdump", "--list-elf", str(native.lib_path())], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_abi_version_and_system_info(native):
+    assert native.lib().chaos_abi_version() == 1
+    assert native.system_info("lorenz") == (3, 3)
+    assert native.system_info("chameleon") == (3, 7)
+    assert native.system_info("sin2") == (2, 2)
+    with pytest.raises(native.ChaosError) as e:
+        native.system_info(42)
+    assert e.value.code == -1
+
+
+BIF = dict(tMax=1.0, nPts=8, h=0.01, initialConditions=[0.1, 0.1, 0.1], ranges=[20.0, 200.0],
+           indicesOfMutVars=[1], writableVar=0, maxValue=1e4, transientTime=1.0, values=[10.0, 28.0, 8 / 3])
+
+
+@pytest.mark.parametrize("bad, frag", [
+    (dict(system=99), "unknown system"),
+    (dict(values=[10.0, 28.0]), "amountOfValues"),
+    (dict(initialConditions=[0.1, 0.1]), "amountOfInitialConditions"),
+    (dict(nPts=1), "nPts"),
+    (dict(h=0.0), "h > 0"),
+    (dict(indicesOfMutVars=[5]), "indicesOfMutVars"),
+    (dict(writableVar=3), "writableVar"),
+    (dict(preScaller=0), "preScaller"),
+])
+def test_bifurcation_argument_errors(native, bad, frag):
+    kw = dict(BIF)
+    system = bad.pop("system", "lorenz")
+    kw.update(bad)
+    with pytest.raises(native.ChaosError) as e:
+        native.bifurcation1d(system, **kw)
+    assert e.value.code == -1 and frag in str(e.value)
+
+
+def test_lle_argument_errors(native):
+    kw = dict(tMax=10.0, NT=0.1, nPts=4, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+              ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=5.0, values=[0.2, 0.2, 5.7])
+    with pytest.raises(native.ChaosError, match="NT / h"):
+        native.lle2d("rossler", **{**kw, "NT": 0.001})
+    with pytest.raises(native.ChaosError) as e:
+        native.lle2d("chameleon", **{**kw, "values": [0.5, 3, 0, 2, 1, 18, 1]}, precision=native.FP32)
+    assert e.value.code == -6  # FP32 LLE needs a quadratic system
+
+
+def test_dbscan_argument_errors(native):
+    with pytest.raises(native.ChaosError, match="dims"):
+        native.dbscan(np.zeros((4, 5)), 0.1, 2)
+    with pytest.raises(native.ChaosError, match="minPts"):
+        native.dbscan(np.zeros((4, 2)), 0.1, 0)
+
+
+def test_compat_system_selection(native):
+    L = native.lib()
+    assert L.chaos_compat_set_system(99) == -1
+    assert L.chaos_compat_set_system(0) == 0
+    assert L.chaos_compat_get_system() == 0
+    assert L.chaos_compat_set_system(3) == 0
+
+
+def test_no_cpu_fallback(monkeypatch, tmp_path):
+    """Without the built library the package raises instead of computing."""
+    from chaoslibrary_gb300 import _native as N
+
+    monkeypatch.setattr(N, "_lib", None)
+    monkeypatch.setenv("CHAOS_GB300_LIB", str(tmp_path / "missing.so"))
+    with pytest.raises(N.ChaosError, match="no CPU fallback"):
+        N.bifurcation1d("lorenz", **BIF)
