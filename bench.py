@@ -209,6 +209,8 @@ def reference_arm(args, ws, rank):
 
 
 def config_of(args):
+    if args.npts or args.tmax:
+        return {"workload": f"{args.workload} profiling case (nPts={args.npts}, tMax={args.tmax})"}
     if args.workload == "lle":
         return {"workload": "LLE map, Rossler RK4 h=0.01, a in [0.1,0.4] x c in [2,10], 1024x1024, b=0.2, "
                             "x0=(1,1,1), 5000 transient + 5002 blocks x 10 steps x 2 trajectories",
@@ -419,7 +421,14 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the CPU baseline")
+    ap.add_argument("--npts", type=int, default=None, help="grid resolution override (profiling runs only)")
+    ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()
+    for w in (LLE, BIF1D, BASINS):
+        if args.npts:
+            w["nPts"] = args.npts
+        if args.tmax:
+            w["tMax"] = args.tmax
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         reference_arm(args, ws, rank)

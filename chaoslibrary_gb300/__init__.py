@@ -32,6 +32,7 @@ from ._native import (  # noqa: F401
     bifurcation2d,
     dbscan,
     dbscan_compat,
+    fma_probe,
     lib,
     lib_path,
     lle2d,
@@ -39,10 +40,11 @@ from ._native import (  # noqa: F401
     point_dbscan,
     set_system,
     system_info,
+    trajectory,
 )
 
 __all__ = [
     "FP32", "FP64", "SYSTEMS", "ChaosError", "bifurcation1D", "bifurcation2D", "LLE2D", "basinsOfAttraction_2",
     "Bifurcation", "LLE", "Basins", "bifurcation1d", "bifurcation2d", "lle2d", "basins", "basins_features",
-    "dbscan", "dbscan_compat", "peak_finder", "point_dbscan", "lib", "lib_path", "set_system", "system_info",
+    "dbscan", "dbscan_compat", "fma_probe", "trajectory", "peak_finder", "point_dbscan", "lib", "lib_path", "set_system", "system_info",
 ]

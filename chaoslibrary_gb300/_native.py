@@ -10,6 +10,7 @@ import numpy as np
 
 _PKG = Path(__file__).resolve().parent
 FP64, FP32 = 0, 1
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
 MEM_HOST, MEM_DEVICE = 0, 1
 SYSTEMS = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "rossler_cd": 4, "sin3": 5, "sin2": 6,
            "memristor": 7}
@@ -52,6 +53,7 @@ _SIGS = {
     "chaos_peak_finder": ([_P, _P, _L, _I, _D, _I, _P, _P, _P], _I),
     "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
     "chaos_fma_probe": ([_P, _L, _P, _P], _I),
+    "chaos_trajectory": ([_P, _I, _L, _P, _P, _D, _I, _P], _I),
     "chaos_compat_set_system": ([_I], _I),
     "chaos_compat_set_precision": ([_I], _I),
     "chaos_compat_get_system": ([], _I),
@@ -134,6 +136,8 @@ def _exec(precision, outs: dict, stream=None, device=None) -> Exec:
 
         dev = tensors[0].device
         st = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        if not st:
+            st = CUDA_STREAM_LEGACY  # torch's default stream; NULL would select the library's own stream
         return Exec(_prec(precision), MEM_DEVICE, C.c_void_p(st), dev.index if dev.index is not None else -1)
     return Exec(_prec(precision), MEM_HOST, None, -1 if device is None else int(device))
 
@@ -144,6 +148,20 @@ def fma_probe(iters: int = 200000, device=None) -> float:
     sec, fl = C.c_double(), C.c_double()
     _check(lib().chaos_fma_probe(C.byref(ex), iters, C.byref(sec), C.byref(fl)))
     return fl.value / sec.value
+
+
+def trajectory(system, x0, a, h, n_steps, precision=FP64):
+    """States of trajectories [nTraj, n_steps + 1, SIZE_X] (x0: [nTraj, SIZE_X], a: [nTraj, SIZE_A])."""
+    A = _Args()
+    x0 = np.ascontiguousarray(np.atleast_2d(x0), np.float64)
+    a = np.ascontiguousarray(np.atleast_2d(a), np.float64)
+    n, nx = x0.shape
+    if a.shape[0] == 1 and n > 1:
+        a = np.repeat(a, n, axis=0)
+    out = np.zeros((n, n_steps + 1, nx))
+    ex = _exec(precision, {})
+    _check(lib().chaos_trajectory(C.byref(ex), _sys(system), n, A.d(x0), A.d(a), h, n_steps, _out_ptr(out)))
+    return out
 
 
 def set_system(system) -> None:

@@ -504,4 +504,26 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
     return c.finish(rc);
 }
 
+int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const double* x0, const double* a, double h,
+                     int nSteps, double* out) {
+    if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
+    if (nTraj < 0 || nSteps < 0 || !(h == h) || (nTraj > 0 && (!x0 || !a || !out)))
+        return set_error(CHAOS_E_ARGS, "bad trajectory arguments");
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    if (nTraj == 0) return c.finish(CHAOS_OK);
+    const int nx = system_nx(system), na = system_na(system);
+    const size_t outBytes = (size_t)nTraj * (nSteps + 1) * nx * sizeof(double);
+    const double* dX = (const double*)c.input(x0, (size_t)nTraj * nx * sizeof(double));
+    const double* dA = (const double*)c.input(a, (size_t)nTraj * na * sizeof(double));
+    double* dO = (double*)c.output(out, outBytes);
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_trajectory_f32(system, dX, dA, h, nSteps, dO, nTraj, c.stream)
+                                                 : launch_trajectory_f64(system, dX, dA, h, nSteps, dO, nTraj, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "trajectory kernel"));
+    rc = c.to_host(out, dO, outBytes);
+    return c.finish(rc);
+}
+
 }  // extern "C"

@@ -332,4 +332,27 @@ __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p
     return sum / L.tMax;
 }
 
+// ---------------------------------------------------------------------------
+// Trajectory recorder: nSteps steps of one trajectory per thread, writing the
+// state before the first step and after every step.
+template <int S, class T>
+__device__ __forceinline__ void trajectory_point(const double* x0, const double* a0, double h, int nSteps,
+                                                 double* out, long long t) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    T x[NX], a[NA];
+#pragma unroll
+    for (int j = 0; j < NX; ++j) x[j] = (T)x0[t * NX + j];
+#pragma unroll
+    for (int j = 0; j < NA; ++j) a[j] = (T)a0[t * NA + j];
+    const StepCtx<T> c((T)h);
+    double* o = out + t * (long long)(nSteps + 1) * NX;
+#pragma unroll
+    for (int j = 0; j < NX; ++j) o[j] = (double)x[j];
+    for (int s = 1; s <= nSteps; ++s) {
+        step<S>(x, a, c);
+#pragma unroll
+        for (int j = 0; j < NX; ++j) o[(long long)s * NX + j] = (double)x[j];
+    }
+}
+
 }  // namespace chaos

@@ -30,6 +30,14 @@ __global__ void __launch_bounds__(kBlock) lle_twin_kernel_f32(LleParams L, doubl
     out[o] = lle_point_twin<F, float>(L, L.pBegin + o);
 }
 
+template <int S>
+__global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0, const double* a0, double h, int nSteps,
+                                                       double* out, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    trajectory_point<S, float>(x0, a0, h, nSteps, out, t);
+}
+
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
 #define CHAOS_SYSTEM_SWITCH(sys, CALL) \
@@ -70,6 +78,15 @@ cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
         case SYS_CHEN_RK4: lle_twin_kernel_f32<Chen><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
         default: return cudaErrorNotSupported;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
+                                  double* out, long long n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+#define CALL(S) trajectory_kernel_f32<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n)
+    CHAOS_SYSTEM_SWITCH(system, CALL)
+#undef CALL
     return cudaGetLastError();
 }
 

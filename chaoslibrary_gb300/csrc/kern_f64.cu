@@ -34,6 +34,14 @@ __global__ void __launch_bounds__(kBlock) lle_kernel(LleParams L, double* out) {
     out[o] = lle_point_full<S, double>(L, L.pBegin + o);
 }
 
+template <int S>
+__global__ void __launch_bounds__(kBlock) trajectory_kernel(const double* x0, const double* a0, double h, int nSteps,
+                                                       double* out, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    trajectory_point<S, double>(x0, a0, h, nSteps, out, t);
+}
+
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
 #define CHAOS_SYSTEM_SWITCH(sys, CALL) \
@@ -180,6 +188,15 @@ cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long
     const long long threads = n * 32;
     point_dbscan_kernel<<<(unsigned)((threads + kBlock - 1) / kBlock), kBlock, 0, st>>>(
         intervals, counts, n, stride, eps, labScratch, slotScratch, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0, double h, int nSteps,
+                                  double* out, long long n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+#define CALL(S) trajectory_kernel<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n)
+    CHAOS_SYSTEM_SWITCH(system, CALL)
+#undef CALL
     return cudaGetLastError();
 }
 

@@ -82,6 +82,11 @@ cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, d
 cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long long n, int stride, double eps,
                                 int* labScratch, int* slotScratch, int* out, cudaStream_t st);
 
+cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0, double h, int nSteps,
+                                  double* out, long long n, cudaStream_t st);
+cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
+                                  double* out, long long n, cudaStream_t st);
+
 bool system_supported(int system);
 int launch_block_size();  // threads per block of the sweep kernels
 

@@ -57,7 +57,8 @@ extern "C" {
 typedef struct chaos_exec {
     int precision; /* CHAOS_FP64 or CHAOS_FP32 */
     int memory;    /* CHAOS_MEM_HOST or CHAOS_MEM_DEVICE */
-    void* stream;  /* cudaStream_t; NULL = the library's stream for the device */
+    void* stream;  /* cudaStream_t; NULL = the library's stream for the device (pass
+                      cudaStreamLegacy, not 0, to run on the legacy default stream) */
     int device;    /* CUDA device ordinal; -1 = the current device */
 } chaos_exec;
 
@@ -185,6 +186,16 @@ int chaos_peak_finder(const chaos_exec* ex, const double* data, long long nSerie
  */
 int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int* counts, long long n, int stride,
                        double eps, int* labels);
+
+/*
+ * Trajectories of a built-in system (no reference counterpart; the
+ * reference's phase portraits come from a separate Python script): nTraj
+ * independent trajectories, x0 (nTraj x SIZE_X) and a (nTraj x SIZE_A)
+ * row-major, nSteps steps of CALC_DISCRETE_MODEL each. out holds
+ * nTraj x (nSteps + 1) x SIZE_X states: the start and the state after every step.
+ */
+int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const double* x0, const double* a, double h,
+                     int nSteps, double* out);
 
 /*
  * FP32 FMA-pipe probe (no reference counterpart): times `iters` rounds of 8
