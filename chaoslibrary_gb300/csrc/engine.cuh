@@ -295,10 +295,27 @@ __device__ __forceinline__ double lle_point_full(const LleParams& L, long long p
 }
 
 // LLE point with the twin carried as the exact difference e = q - x (only for
-// the quadratic RK4 systems): x and e in T (FP32), the log-stretch sum in
-// FP64. Same block count, renormalisation and division by tMax as above.
+// the quadratic RK4 systems): x and e in FP32 registers. Same block count and
+// division by tMax as above. Per block the stretch is measured as
+// log2(|e|^2 / eps^2) with the SFU (__log2f) and e is rescaled to length eps
+// with rsqrtf; the per-block logs are summed in FP32 over groups of
+// kLleGroup blocks and every group sum is added to an FP64 accumulator, so the
+// FP64 pipe (1/64 of the FP32 rate on this GPU) sees one add per group.
+constexpr int kLleGroup = 16;
+
 template <class F, class T>
+__device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>& c, int n) {
+    int s = 0;
+    for (; s + 2 <= n; s += 2) {
+        rk4_step_twin<F>(x, e, a, c);
+        rk4_step_twin<F>(x, e, a, c);
+    }
+    if (s < n) rk4_step_twin<F>(x, e, a, c);
+}
+
+template <class F>
 __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p) {
+    using T = float;
     const int i = (int)(p % L.nPts), j = (int)(p / L.nPts);
     T x[3], e[3], a[3];
 #pragma unroll
@@ -314,22 +331,28 @@ __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p
     }
     const RK4H<T> c((T)L.h);
     for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
-    e[0] = (T)L.eps;
+    const T eps = (T)L.eps;
+    const T inv_eps2 = (T)(1.0 / (L.eps * L.eps));
+    e[0] = eps;
     e[1] = T(0);
     e[2] = T(0);
-    const T inv_eps = (T)(1.0 / L.eps);
-    double sum = 0.0;
-    for (int b = 0; b <= L.calcBlocks; ++b) {
-        for (int s = 0; s < L.ntp; ++s) rk4_step_twin<F>(x, e, a, c);
-        const T n2 = fmaT(e[0], e[0], fmaT(e[1], e[1], e[2] * e[2]));
-        const T d = sqrtf(n2) * inv_eps;
-        sum += (double)logf(d);
-        const T r = T(1) / d;
-        e[0] *= r;
-        e[1] *= r;
-        e[2] *= r;
+    double sum = 0.0;  // sum of log2(d^2)
+    const int nb = L.calcBlocks + 1;
+    for (int b0 = 0; b0 < nb; b0 += kLleGroup) {
+        const int bn = min(kLleGroup, nb - b0);
+        T part = T(0);
+        for (int b = 0; b < bn; ++b) {
+            twin_steps<F>(x, e, a, c, L.ntp);
+            const T n2 = fmaf(e[0], e[0], fmaf(e[1], e[1], e[2] * e[2]));
+            part += __log2f(n2 * inv_eps2);
+            const T r = eps * rsqrtf(n2);
+            e[0] *= r;
+            e[1] *= r;
+            e[2] *= r;
+        }
+        sum += (double)part;
     }
-    return sum / L.tMax;
+    return sum * (0.5 * 0.69314718055994530942) / L.tMax;  // log2(d^2) -> ln(d)
 }
 
 // ---------------------------------------------------------------------------

@@ -2,6 +2,8 @@
 // times, intervals and means in FP64. The LLE kernel carries the twin as the
 // exact difference e = q - x (quadratic RK4 systems only) and accumulates the
 // log-stretch sum in FP64.
+#include <cstdlib>
+
 #include "engine.cuh"
 
 namespace chaos {
@@ -23,11 +25,14 @@ __global__ void __launch_bounds__(kBlock) basins_kernel_f32(SweepParams P, Basin
     basins_point<S, float>(P, O, P.pBegin + o, o);
 }
 
-template <class F>
-__global__ void __launch_bounds__(kBlock) lle_twin_kernel_f32(LleParams L, double* out) {
+// MINB = resident blocks per SM the register allocation is shaped for:
+// 12 (40 registers, 48 warps/SM) or 16 (32 registers, 64 warps/SM, a few
+// bytes of spill outside the step loop). Picked per system by the tuner.
+template <class F, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) lle_twin_kernel_f32(LleParams L, double* out) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= L.nPoints) return;
-    out[o] = lle_point_twin<F, float>(L, L.pBegin + o);
+    out[o] = lle_point_twin<F>(L, L.pBegin + o);
 }
 
 template <int S>
@@ -39,6 +44,17 @@ __global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0
 }
 
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+// Occupancy variant of the FP32 LLE kernel: CHAOS_LLE_MINB=12|16 forces one,
+// otherwise the measured default.
+int lle_occupancy_variant(int system) {
+    (void)system;
+    static int forced = [] {
+        const char* s = getenv("CHAOS_LLE_MINB");
+        return s ? atoi(s) : 0;
+    }();
+    return forced ? forced : 12;
+}
 
 #define CHAOS_SYSTEM_SWITCH(sys, CALL) \
     switch (sys) {                     \
@@ -70,12 +86,19 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
     return cudaGetLastError();
 }
 
+template <class F>
+static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb) {
+    if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+    else lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+}
+
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
+    const int minb = lle_occupancy_variant(L.system);
     switch (L.system) {
-        case SYS_LORENZ_RK4: lle_twin_kernel_f32<Lorenz><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
-        case SYS_ROSSLER_RK4: lle_twin_kernel_f32<Rossler><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
-        case SYS_CHEN_RK4: lle_twin_kernel_f32<Chen><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); break;
+        case SYS_LORENZ_RK4: launch_twin<Lorenz>(L, out, st, minb); break;
+        case SYS_ROSSLER_RK4: launch_twin<Rossler>(L, out, st, minb); break;
+        case SYS_CHEN_RK4: launch_twin<Chen>(L, out, st, minb); break;
         default: return cudaErrorNotSupported;
     }
     return cudaGetLastError();

@@ -123,21 +123,24 @@ template <class T> struct RK4H {
     CHAOS_HD explicit RK4H(T h_) : h(h_), hh(h_ * T(0.5)), h6(h_ / T(6)) {}
 };
 
-// Classic fourth-order Runge-Kutta step of a 3-D autonomous field.
+// Classic fourth-order Runge-Kutta step of a 3-D autonomous field:
+// x += h/6 (k1 + 2 k2 + 2 k3 + k4), the sum accumulated as the stages are
+// produced (acc = k1; acc += 2 k2; acc += 2 k3; acc += k4), which keeps only
+// one stage vector alive at a time.
 template <class F, class T> CHAOS_HD void rk4_step(T* x, const T* a, const RK4H<T>& c) {
-    T k1[3], k2[3], k3[3], k4[3], y[3];
-    F::f(x, a, k1);
+    T k[3], y[3], acc[3];
+    F::f(x, a, k);
 CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) y[i] = fmaT(c.hh, k1[i], x[i]);
-    F::f(y, a, k2);
+    for (int i = 0; i < 3; ++i) { acc[i] = k[i]; y[i] = fmaT(c.hh, k[i], x[i]); }
+    F::f(y, a, k);
 CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) y[i] = fmaT(c.hh, k2[i], x[i]);
-    F::f(y, a, k3);
+    for (int i = 0; i < 3; ++i) { acc[i] = fmaT(T(2), k[i], acc[i]); y[i] = fmaT(c.hh, k[i], x[i]); }
+    F::f(y, a, k);
 CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) y[i] = fmaT(c.h, k3[i], x[i]);
-    F::f(y, a, k4);
+    for (int i = 0; i < 3; ++i) { acc[i] = fmaT(T(2), k[i], acc[i]); y[i] = fmaT(c.h, k[i], x[i]); }
+    F::f(y, a, k);
 CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) x[i] = fmaT(c.h6, fmaT(T(2), k2[i] + k3[i], k1[i] + k4[i]), x[i]);
+    for (int i = 0; i < 3; ++i) x[i] = fmaT(c.h6, acc[i] + k[i], x[i]);
 }
 
 // One RK4 step of the base trajectory x together with the exact difference
@@ -145,26 +148,40 @@ CHAOS_UNROLL
 // differences from the base stages, so e keeps full relative precision even
 // when |e| is far below the resolution of x (FP32 with e ~ 1e-8).
 template <class F, class T> CHAOS_HD void rk4_step_twin(T* x, T* e, const T* a, const RK4H<T>& c) {
-    T k1[3], k2[3], k3[3], k4[3], y[3];
-    T d1[3], d2[3], d3[3], d4[3], g[3];
-    F::f(x, a, k1);
-    F::df(x, e, a, d1);
-CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) { y[i] = fmaT(c.hh, k1[i], x[i]); g[i] = fmaT(c.hh, d1[i], e[i]); }
-    F::f(y, a, k2);
-    F::df(y, g, a, d2);
-CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) { y[i] = fmaT(c.hh, k2[i], x[i]); g[i] = fmaT(c.hh, d2[i], e[i]); }
-    F::f(y, a, k3);
-    F::df(y, g, a, d3);
-CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) { y[i] = fmaT(c.h, k3[i], x[i]); g[i] = fmaT(c.h, d3[i], e[i]); }
-    F::f(y, a, k4);
-    F::df(y, g, a, d4);
+    T k[3], y[3], acc[3], d[3], g[3], dacc[3];
+    F::f(x, a, k);
+    F::df(x, e, a, d);
 CHAOS_UNROLL
     for (int i = 0; i < 3; ++i) {
-        x[i] = fmaT(c.h6, fmaT(T(2), k2[i] + k3[i], k1[i] + k4[i]), x[i]);
-        e[i] = fmaT(c.h6, fmaT(T(2), d2[i] + d3[i], d1[i] + d4[i]), e[i]);
+        acc[i] = k[i];
+        dacc[i] = d[i];
+        y[i] = fmaT(c.hh, k[i], x[i]);
+        g[i] = fmaT(c.hh, d[i], e[i]);
+    }
+    F::f(y, a, k);
+    F::df(y, g, a, d);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        acc[i] = fmaT(T(2), k[i], acc[i]);
+        dacc[i] = fmaT(T(2), d[i], dacc[i]);
+        y[i] = fmaT(c.hh, k[i], x[i]);
+        g[i] = fmaT(c.hh, d[i], e[i]);
+    }
+    F::f(y, a, k);
+    F::df(y, g, a, d);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        acc[i] = fmaT(T(2), k[i], acc[i]);
+        dacc[i] = fmaT(T(2), d[i], dacc[i]);
+        y[i] = fmaT(c.h, k[i], x[i]);
+        g[i] = fmaT(c.h, d[i], e[i]);
+    }
+    F::f(y, a, k);
+    F::df(y, g, a, d);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        x[i] = fmaT(c.h6, acc[i] + k[i], x[i]);
+        e[i] = fmaT(c.h6, dacc[i] + d[i], e[i]);
     }
 }
 
