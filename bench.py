@@ -251,6 +251,8 @@ def engine_arm(args, ws, rank, local):
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    if args.lle_variant:
+        C.set_tuning(C.TUNE_LLE_F32_VARIANT, args.lle_variant)
     prec = C.FP32 if args.precision == "fp32" else C.FP64
     w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS}[args.workload]
     n_points = w["nPts"] ** (1 if args.workload == "bif1d" else 2)
@@ -267,6 +269,7 @@ def engine_arm(args, ws, rank, local):
         d2h = n_points * 8
         launches_per_step = 1
         tag = f"lle_{args.precision}_rossler_1024"
+        line_extra = {"lle_variant": C.get_tuning(C.TUNE_LLE_F32_VARIANT)}
     elif args.workload == "bif1d":
         steps_pp = sweep_steps_per_point(w)
         cap = 64
@@ -332,6 +335,8 @@ def engine_arm(args, ws, rank, local):
             "config": config_of(args), "clocks": clocks, "wall_s_timed_region": wall}
     if launches_per_step:
         line["gpu_launches"] = launches_per_step * args.steps
+    if args.workload == "lle":
+        line["config"].update(line_extra)
 
     # roofline: FP32 (or FP64) FMA pipe, algorithmic flops of the integration
     if rank == 0:
@@ -421,6 +426,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the CPU baseline")
+    ap.add_argument("--lle-variant", type=int, default=0, help="FP32 LLE kernel variant (0 default, 2, 12, 16)")
     ap.add_argument("--npts", type=int, default=None, help="grid resolution override (profiling runs only)")
     ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()

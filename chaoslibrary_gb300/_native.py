@@ -54,6 +54,8 @@ _SIGS = {
     "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
     "chaos_fma_probe": ([_P, _L, _P, _P], _I),
     "chaos_trajectory": ([_P, _I, _L, _P, _P, _D, _I, _P], _I),
+    "chaos_set_tuning": ([_I, _I], _I),
+    "chaos_get_tuning": ([_I], _I),
     "chaos_compat_set_system": ([_I], _I),
     "chaos_compat_set_precision": ([_I], _I),
     "chaos_compat_get_system": ([], _I),
@@ -162,6 +164,17 @@ def trajectory(system, x0, a, h, n_steps, precision=FP64):
     ex = _exec(precision, {})
     _check(lib().chaos_trajectory(C.byref(ex), _sys(system), n, A.d(x0), A.d(a), h, n_steps, _out_ptr(out)))
     return out
+
+
+TUNE_LLE_F32_VARIANT = 1
+
+
+def set_tuning(knob: int, value: int) -> None:
+    _check(lib().chaos_set_tuning(knob, value))
+
+
+def get_tuning(knob: int) -> int:
+    return lib().chaos_get_tuning(knob)
 
 
 def set_system(system) -> None:

@@ -504,6 +504,17 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
     return c.finish(rc);
 }
 
+int chaos_set_tuning(int knob, int value) {
+    if (knob == CHAOS_TUNE_LLE_F32_VARIANT)
+        return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
+    return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
+}
+
+int chaos_get_tuning(int knob) {
+    if (knob == CHAOS_TUNE_LLE_F32_VARIANT) return get_lle_variant();
+    return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
+}
+
 int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const double* x0, const double* a, double h,
                      int nSteps, double* out) {
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);

@@ -304,7 +304,7 @@ __device__ __forceinline__ double lle_point_full(const LleParams& L, long long p
 constexpr int kLleGroup = 16;
 
 template <class F, class T>
-__device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>& c, int n) {
+__device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>& c, int n) {  // n steps, 2 per trip
     int s = 0;
     for (; s + 2 <= n; s += 2) {
         rk4_step_twin<F>(x, e, a, c);
@@ -353,6 +353,90 @@ __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p
         sum += (double)part;
     }
     return sum * (0.5 * 0.69314718055994530942) / L.tMax;  // log2(d^2) -> ln(d)
+}
+
+// ---------------------------------------------------------------------------
+// Packed pair of FP32 values: two trajectories advanced by one instruction
+// stream with Blackwell's paired FP32 instructions (fma.rn.f32x2,
+// add.rn.f32x2, mul.rn.f32x2). Each lane of the pair is rounded exactly as
+// the scalar FP32 operation would be; the pair halves the instructions the
+// schedulers issue for the same flops.
+struct P2 {
+    float2 v;
+    __device__ __forceinline__ P2() {}
+    __device__ __forceinline__ explicit P2(double s) : v(make_float2((float)s, (float)s)) {}
+    __device__ __forceinline__ P2(float a, float b) : v(make_float2(a, b)) {}
+};
+__device__ __forceinline__ P2 mk(float2 f) { P2 r; r.v = f; return r; }
+__device__ __forceinline__ P2 operator+(P2 a, P2 b) { return mk(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ P2 operator-(P2 a) { return mk(make_float2(-a.v.x, -a.v.y)); }
+__device__ __forceinline__ P2 operator-(P2 a, P2 b) { return mk(__fadd2_rn(a.v, make_float2(-b.v.x, -b.v.y))); }
+__device__ __forceinline__ P2 operator*(P2 a, P2 b) { return mk(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ P2& operator*=(P2& a, P2 b) { a = a * b; return a; }
+__device__ __forceinline__ P2 fmaT(P2 a, P2 b, P2 c) { return mk(__ffma2_rn(a.v, b.v, c.v)); }
+
+// Step constants of a packed pair: rounded exactly as RK4H<float> rounds them.
+template <> struct RK4H<P2> {
+    P2 h, hh, h6;
+    __device__ __forceinline__ explicit RK4H(float h_)
+        : h((double)h_), hh((double)(h_ * 0.5f)), h6((double)(h_ / 6.0f)) {}
+};
+
+// Two LLE points per thread (indices p and q), lanes of P2. Same arithmetic
+// per lane as lle_point_twin with T = float; the per-block log and rescale
+// run per lane on the SFU.
+template <class F>
+__device__ __forceinline__ void lle_pair_twin(const LleParams& L, long long p, long long q, double* outp,
+                                              double* outq) {
+    P2 x[3], e[3], a[3];
+    long long pts[2] = {p, q};
+    float av[2][3];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int i = (int)(pts[t] % L.nPts), j = (int)(pts[t] / L.nPts);
+        const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
+        const double vb = L.nPts == 1 ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double v = L.values[k];
+            if (k == L.mut[0]) v = va;
+            if (k == L.mut[1]) v = vb;
+            av[t][k] = (float)v;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = P2(av[0][k], av[1][k]);
+        x[k] = P2((double)(float)L.ic[k]);
+    }
+    const RK4H<P2> c((float)L.h);
+    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
+    const float eps = (float)L.eps;
+    const float inv_eps2 = (float)(1.0 / (L.eps * L.eps));
+    e[0] = P2((double)eps);
+    e[1] = P2(0.0);
+    e[2] = P2(0.0);
+    double sum0 = 0.0, sum1 = 0.0;
+    const int nb = L.calcBlocks + 1;
+    for (int b0 = 0; b0 < nb; b0 += kLleGroup) {
+        const int bn = min(kLleGroup, nb - b0);
+        float part0 = 0.f, part1 = 0.f;
+        for (int b = 0; b < bn; ++b) {
+            twin_steps<F>(x, e, a, c, L.ntp);
+            const P2 n2 = fmaT(e[0], e[0], fmaT(e[1], e[1], e[2] * e[2]));
+            part0 += __log2f(n2.v.x * inv_eps2);
+            part1 += __log2f(n2.v.y * inv_eps2);
+            const P2 r(eps * rsqrtf(n2.v.x), eps * rsqrtf(n2.v.y));
+            e[0] *= r;
+            e[1] *= r;
+            e[2] *= r;
+        }
+        sum0 += (double)part0;
+        sum1 += (double)part1;
+    }
+    const double k = (0.5 * 0.69314718055994530942) / L.tMax;
+    *outp = sum0 * k;
+    if (outq) *outq = sum1 * k;
 }
 
 // ---------------------------------------------------------------------------

@@ -2,6 +2,7 @@
 // times, intervals and means in FP64. The LLE kernel carries the twin as the
 // exact difference e = q - x (quadratic RK4 systems only) and accumulates the
 // log-stretch sum in FP64.
+#include <atomic>
 #include <cstdlib>
 
 #include "engine.cuh"
@@ -45,10 +46,15 @@ __global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0
 
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
-// Occupancy variant of the FP32 LLE kernel: CHAOS_LLE_MINB=12|16 forces one,
-// otherwise the measured default.
+// Variant of the FP32 LLE kernel: 12 / 16 = one point per thread shaped for
+// 12 or 16 resident blocks per SM; 2 = two points per thread in packed
+// FP32x2 lanes. CHAOS_LLE_MINB forces one, otherwise the measured default.
+std::atomic<int> g_lle_variant{0};
+
 int lle_occupancy_variant(int system) {
     (void)system;
+    const int set = g_lle_variant.load(std::memory_order_relaxed);
+    if (set) return set;
     static int forced = [] {
         const char* s = getenv("CHAOS_LLE_MINB");
         return s ? atoi(s) : 0;
@@ -86,11 +92,28 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
     return cudaGetLastError();
 }
 
+// Two points per thread in packed FP32x2 lanes.
+template <class F>
+__global__ void __launch_bounds__(kBlock) lle_pair_kernel_f32(LleParams L, double* out) {
+    const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (o >= L.nPoints) return;
+    const bool two = o + 1 < L.nPoints;
+    lle_pair_twin<F>(L, L.pBegin + o, L.pBegin + (two ? o + 1 : o), out + o, two ? out + o + 1 : nullptr);
+}
+
 template <class F>
 static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb) {
-    if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+    if (minb == 2) lle_pair_kernel_f32<F><<<grid_for((L.nPoints + 1) / 2), kBlock, 0, st>>>(L, out);
+    else if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
     else lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
 }
+
+int set_lle_variant(int v) {
+    if (v != 0 && v != 2 && v != 12 && v != 16) return -1;
+    g_lle_variant.store(v);
+    return 0;
+}
+int get_lle_variant() { return lle_occupancy_variant(0); }
 
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;

@@ -87,6 +87,11 @@ cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0
 cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st);
 
+// FP32 LLE kernel variant (kern_f32.cu): 0 = default, 2 = two points per
+// thread (packed FP32x2), 12 / 16 = one point per thread at that occupancy.
+int set_lle_variant(int v);
+int get_lle_variant();
+
 bool system_supported(int system);
 int launch_block_size();  // threads per block of the sweep kernels
 

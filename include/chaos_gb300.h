@@ -198,6 +198,16 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
                      int nSteps, double* out);
 
 /*
+ * Kernel-shape knobs (no reference counterpart). CHAOS_TUNE_LLE_F32_VARIANT:
+ * 2 = two grid points per thread in packed FP32x2 instructions, 12 / 16 = one
+ * point per thread with registers shaped for 12 / 16 resident blocks per SM,
+ * 0 = the library default. Process-wide; results do not depend on it.
+ */
+#define CHAOS_TUNE_LLE_F32_VARIANT 1
+int chaos_set_tuning(int knob, int value);
+int chaos_get_tuning(int knob);
+
+/*
  * FP32 FMA-pipe probe (no reference counterpart): times `iters` rounds of 8
  * independent fmaf chains in 2048 threads per SM and returns the elapsed
  * seconds and the flops executed, the measured denominator of the

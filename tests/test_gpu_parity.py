@@ -238,3 +238,25 @@ def test_fp64_trajectory_1e3_steps(engine, oracle, name):
 
 SYS_ALL = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "rossler_cd": 4, "sin3": 5, "sin2": 6,
            "memristor": 7}
+
+
+@pytest.mark.parametrize("system, values, ranges, mut", [
+    ("rossler", [0.2, 0.2, 5.7], [0.1, 0.4, 2.0, 10.0], [0, 2]),
+    ("lorenz", [10.0, 28.0, 8 / 3], [20.0, 60.0, 5.0, 15.0], [1, 0]),
+])
+def test_lle_fp32_variants_identical(engine, system, values, ranges, mut):
+    """The packed two-points-per-thread kernel and the one-point kernels give
+    bit-identical maps (each FP32x2 lane rounds as the scalar instruction)."""
+    kw = dict(tMax=30.0, NT=0.1, nPts=15, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0], ranges=ranges,
+              indicesOfMutVars=mut, transientTime=5.0, values=values)
+    knob = engine.TUNE_LLE_F32_VARIANT
+    old = engine.get_tuning(knob)
+    try:
+        maps = {}
+        for v in (12, 16, 2):
+            engine.set_tuning(knob, v)
+            maps[v] = engine.lle2d(system, precision=engine.FP32, **kw)
+    finally:
+        engine.set_tuning(knob, 0 if old == 12 else old)
+    for v in (16, 2):
+        assert np.array_equal(maps[v], maps[12], equal_nan=True), v
