@@ -434,9 +434,8 @@ __device__ __forceinline__ void lle_pair_twin(const LleParams& L, long long p, l
         sum0 += (double)part0;
         sum1 += (double)part1;
     }
-    const double k = (0.5 * 0.69314718055994530942) / L.tMax;
-    *outp = sum0 * k;
-    if (outq) *outq = sum1 * k;
+    *outp = sum0 * (0.5 * 0.69314718055994530942) / L.tMax;
+    if (outq) *outq = sum1 * (0.5 * 0.69314718055994530942) / L.tMax;
 }
 
 // ---------------------------------------------------------------------------

@@ -59,7 +59,7 @@ int lle_occupancy_variant(int system) {
         const char* s = getenv("CHAOS_LLE_MINB");
         return s ? atoi(s) : 0;
     }();
-    return forced ? forced : 12;
+    return forced ? forced : 2;
 }
 
 #define CHAOS_SYSTEM_SWITCH(sys, CALL) \
