@@ -24,6 +24,7 @@ SOURCES = [
     ("dbscan.cu", ["--fmad=false", "--extended-lambda"]),
     ("capi.cu", []),
     ("probe.cu", []),
+    ("noalloc.cu", []),
     ("compat.cpp", []),
 ]
 

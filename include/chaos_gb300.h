@@ -188,6 +188,22 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
                        double eps, int* labels);
 
 /*
+ * chaos_point_dbscan without any allocation. No counterpart in the reference:
+ * for callers that must not allocate device memory during the call (work
+ * captured into a CUDA graph, latency-critical loops, hosts that reserve
+ * device memory through their own allocator). Every array is a device
+ * pointer (ex->memory must be CHAOS_MEM_DEVICE); ex->stream NULL means the
+ * legacy default stream; the call is asynchronous. The scratch rows live in
+ * one fixed array compiled into the library (8 MiB per GPU that loads it, kept
+ * until exit), so n * stride is limited to 1,048,576 (larger sizes return
+ * CHAOS_E_ARGS). All calls share that array: calls whose kernels overlap on the
+ * GPU race and must be serialised by the caller. The first call on a device
+ * looks up the array's device address; make it before any stream capture.
+ */
+int chaos_point_dbscan_noalloc(const chaos_exec* ex, const double* intervals, const int* counts, long long n,
+                               int stride, double eps, int* labels);
+
+/*
  * Trajectories of a built-in system (no reference counterpart; the
  * reference's phase portraits come from a separate Python script): nTraj
  * independent trajectories, x0 (nTraj x SIZE_X) and a (nTraj x SIZE_A)
