@@ -50,6 +50,51 @@ BASINS = dict(system="lorenz", sysid=0, flops=71, tMax=50.0, nPts=2048, h=0.01, 
               transientTime=200.0, values=[10.0, 24.0, 8.0 / 3.0], eps=0.05)
 
 
+SYS_FLOPS = {"lorenz": 71, "rossler": 63, "chen": 79}
+SYS_ID = {"lorenz": 0, "rossler": 1, "chen": 2}
+
+
+def batch_jobs(seed: int = 2024, n_jobs: int = 256):
+    """The heterogeneous batch: n_jobs jobs, point counts log-uniform in
+    [1e3, 1e6], system uniform over Lorenz / Rossler / Chen (a=35, b=3, c swept
+    20..30), transients uniform in [2000, 20000] steps, alternately a 1-D
+    bifurcation (tMax 100: 10,000 recorded steps, 64 peaks kept per point) and
+    a 2-D LLE map (sqrt(N) x sqrt(N) points, tMax 100, NT 0.1, eps 1e-8)."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(n_jobs):
+        n = int(round(10 ** rng.uniform(3, 6)))
+        system = ["lorenz", "rossler", "chen"][int(rng.integers(0, 3))]
+        trans = int(rng.integers(2000, 20001)) * 0.01
+        if system == "lorenz":
+            vals, ic, bif_mut, bif_rng, lle_mut, lle_rng = [10.0, 28.0, 8 / 3], [0.1, 0.1, 0.1], [1], [20.0, 200.0], \
+                [1, 0], [20.0, 200.0, 5.0, 15.0]
+        elif system == "rossler":
+            vals, ic, bif_mut, bif_rng, lle_mut, lle_rng = [0.2, 0.2, 5.7], [1.0, 1.0, 1.0], [2], [2.0, 10.0], \
+                [0, 2], [0.1, 0.4, 2.0, 10.0]
+        else:
+            vals, ic, bif_mut, bif_rng, lle_mut, lle_rng = [35.0, 3.0, 28.0], [-10.0, 0.0, 37.0], [2], [20.0, 30.0], \
+                [2, 0], [20.0, 30.0, 30.0, 40.0]
+        if k % 2 == 0:
+            jobs.append(("bif", system, dict(tMax=100.0, nPts=n, h=0.01, initialConditions=ic, ranges=bif_rng,
+                                             indicesOfMutVars=bif_mut, writableVar=0, maxValue=1e4,
+                                             transientTime=trans, values=vals)))
+        else:
+            m = max(int(round(n ** 0.5)), 2)
+            jobs.append(("lle", system, dict(tMax=100.0, NT=0.1, nPts=m, h=0.01, eps=1e-8, initialConditions=ic,
+                                             ranges=lle_rng, indicesOfMutVars=lle_mut, transientTime=trans,
+                                             values=vals)))
+    return jobs
+
+
+def job_points_steps(kind, kw):
+    if kind == "bif":
+        return kw["nPts"], int(kw["transientTime"] / kw["h"]) + int(kw["tMax"] / kw["h"])
+    ntp = int(kw["NT"] / kw["h"])
+    calc = int(kw["tMax"] / kw["h"]) // ntp + 1
+    return kw["nPts"] ** 2, int(kw["transientTime"] / kw["h"]) + 2 * ntp * (calc + 1)
+
+
 def lle_steps_per_point(w) -> int:
     ntp = int(w["NT"] / w["h"])
     calc = int(w["tMax"] / w["h"]) // ntp + 1
@@ -192,8 +237,8 @@ def cpu_sample_sweep(w, kind, target_s=10.0):
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
-    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS}[args.workload]
-    fn = (lambda: cpu_sample_lle(w, args.cpu_seconds)) if args.workload == "lle" else \
+    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS, "batch": LLE}[args.workload]
+    fn = (lambda: cpu_sample_lle(w, args.cpu_seconds)) if args.workload in ("lle", "batch") else \
         (lambda: cpu_sample_sweep(w, args.workload, args.cpu_seconds))
     vals, last = [], None
     for _ in range(args.steps):
@@ -244,6 +289,119 @@ def traffic_from_profiles(kernel_tag: str):
 
 
 # ---- engine arm ----------------------------------------------------------------------------
+def batch_arm(args, ws, rank, local):
+    """The heterogeneous batch as one prepared submission (CUDA graph of the
+    grouped persistent kernels), against the same jobs run one by one."""
+    import torch
+
+    import chaoslibrary_gb300 as C
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    jobs = batch_jobs()
+    total_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in jobs)
+    flops = sum(SYS_FLOPS[s_] * float(np.prod(job_points_steps(k, kw))) for k, s_, kw in jobs)
+    b = C.Batch(device=True)
+    for kind, system, kw in jobs:
+        if kind == "bif":
+            b.add_bifurcation1d(system, peakCapacity=64, **kw)
+        else:
+            b.add_lle2d(system, **kw)
+    b.prepare()
+    for _ in range(args.warmup):
+        b.replay()
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks([local] if ws == 1 else list(range(ws))) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            b.replay()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+    ms = [a.elapsed_time(c) for a, c in ev]
+    t_total = max_over_ranks(ws, sum(ms) / 1e3)
+    value = ws * total_steps * args.steps / t_total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded job list)",
+            "config": {"workload": "256 heterogeneous jobs (seed 2024): N log-uniform 1e3..1e6, systems "
+                                   "Lorenz/Rossler/Chen, transients 2000..20000 steps, half 1-D bifurcation "
+                                   "(10000 recorded steps), half LLE maps (tMax 100, NT 0.1)",
+                       "total_steps": float(total_steps), "jobs": len(jobs),
+                       "l2": "256 MB buffer written between timed steps"},
+            "clocks": clk.summary()}
+    if rank == 0:
+        mean_s = statistics.mean(ms) / 1e3
+        peak = C.fma_probe() / 1e12
+        line["roofline"] = {"bound": "fp32_fma", "achieved": flops / mean_s / 1e12, "peak": peak,
+                            "unit": "TFLOP/s", "frac": flops / mean_s / 1e12 / peak, "traffic": None,
+                            "algorithmic": "71/63/79 flops per Lorenz/Rossler/Chen RK4 step",
+                            "peak_source": "measured in this run: chaos_fma_probe"}
+    # e2e: one-shot host-memory submission (descriptor upload, launch, results copied back)
+    bh = C.Batch(device=False)
+    for kind, system, kw in jobs:
+        if kind == "bif":
+            bh.add_bifurcation1d(system, peakCapacity=64, **kw)
+        else:
+            bh.add_lle2d(system, **kw)
+    bh.run()
+    t0 = time.perf_counter()
+    bh.run()
+    e2e_s = max_over_ranks(ws, time.perf_counter() - t0)
+    d2h = sum(sum(v.nbytes for v in o.values()) for o in bh.outputs)
+    line["e2e"] = {"value": ws * total_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": d2h}
+    if rank == 0 and not args.no_extras:
+        # the same jobs one at a time through the single-sweep FP32 entry points (device outputs)
+        outs = []
+        for kind, system, kw in jobs:
+            n, _ = job_points_steps(kind, kw)
+            if kind == "bif":
+                outs.append(dict(counts=torch.empty(n, dtype=torch.int32, device=dev),
+                                 flags=torch.empty(n, dtype=torch.int32, device=dev),
+                                 first=torch.empty(n, dtype=torch.float64, device=dev),
+                                 peaks=torch.empty(n * 64, dtype=torch.float64, device=dev),
+                                 intervals=torch.empty(n * 64, dtype=torch.float64, device=dev)))
+            else:
+                outs.append(torch.empty(n, dtype=torch.float64, device=dev))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for (kind, system, kw), o in zip(jobs, outs):
+            if kind == "bif":
+                C.bifurcation1d(system, precision=C.FP32, peakCapacity=64, out=o, **kw)
+            else:
+                C.lle2d(system, precision=C.FP32, out=o, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        t_seq = e0.elapsed_time(e1) / 1e3
+        # plain FP64 single-sweep kernel on every 16th job
+        sample = jobs[::16]
+        s_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in sample)
+        e0.record()
+        for kind, system, kw in sample:
+            if kind == "bif":
+                C.bifurcation1d(system, precision=C.FP64, peakCapacity=64, **kw)
+            else:
+                C.lle2d(system, precision=C.FP64, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1) / 1e3
+        line["one_by_one_fp32"] = {"value": total_steps / t_seq, "unit": UNIT,
+                                   "batched_speedup": t_seq / (statistics.mean(ms) / 1e3)}
+        line["fp64_plain"] = {"value": s_steps / t64, "unit": UNIT, "sample": "every 16th job, one by one",
+                              "batched_fp32_speedup": value / (s_steps / t64)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    b.close()
+
+
 def engine_arm(args, ws, rank, local):
     import torch
 
@@ -422,7 +580,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "basins"])
+    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "basins", "batch"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the CPU baseline")
@@ -438,6 +596,8 @@ def main():
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         reference_arm(args, ws, rank)
+    elif args.workload == "batch":
+        batch_arm(args, ws, rank, local)
     else:
         engine_arm(args, ws, rank, local)
     if ws > 1:

@@ -15,6 +15,7 @@ raises.
 from __future__ import annotations
 
 from ._native import (  # noqa: F401
+    Batch,
     FP32,
     FP64,
     SYSTEMS,
@@ -24,6 +25,7 @@ from ._native import (  # noqa: F401
     Bifurcation,
     LLE,
     basins,
+    basins_dbscan,
     basins_features,
     basinsOfAttraction_2,
     bifurcation1D,
@@ -47,7 +49,7 @@ from ._native import (  # noqa: F401
 )
 
 __all__ = [
-    "FP32", "FP64", "SYSTEMS", "ChaosError", "bifurcation1D", "bifurcation2D", "LLE2D", "basinsOfAttraction_2",
-    "Bifurcation", "LLE", "Basins", "bifurcation1d", "bifurcation2d", "lle2d", "basins", "basins_features",
+    "Batch", "FP32", "FP64", "SYSTEMS", "ChaosError", "bifurcation1D", "bifurcation2D", "LLE2D", "basinsOfAttraction_2",
+    "Bifurcation", "LLE", "Basins", "bifurcation1d", "bifurcation2d", "lle2d", "basins", "basins_dbscan", "basins_features",
     "dbscan", "dbscan_compat", "fma_probe", "trajectory", "get_tuning", "set_tuning", "TUNE_LLE_F32_VARIANT", "peak_finder", "point_dbscan", "lib", "lib_path", "set_system", "system_info",
 ]

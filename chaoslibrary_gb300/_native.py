@@ -28,6 +28,20 @@ class Exec(C.Structure):
     _fields_ = [("precision", C.c_int), ("memory", C.c_int), ("stream", C.c_void_p), ("device", C.c_int)]
 
 
+JOB_BIF1D, JOB_LLE2D, JOB_BASINS = 1, 2, 3
+
+
+class Job(C.Structure):
+    """chaos_job of include/chaos_gb300.h."""
+    _fields_ = [("kind", C.c_int), ("system", C.c_int), ("tMax", C.c_double), ("nPts", C.c_int),
+                ("h", C.c_double), ("initialConditions", C.c_void_p), ("ranges", C.c_void_p),
+                ("indicesOfMutVars", C.c_void_p), ("writableVar", C.c_int), ("maxValue", C.c_double),
+                ("transientTime", C.c_double), ("values", C.c_void_p), ("preScaller", C.c_int),
+                ("NT", C.c_double), ("eps", C.c_double), ("peakCapacity", C.c_int), ("counts", C.c_void_p),
+                ("flags", C.c_void_p), ("first", C.c_void_p), ("peaks", C.c_void_p), ("intervals", C.c_void_p),
+                ("lle", C.c_void_p), ("avgPeaks", C.c_void_p), ("avgIntervals", C.c_void_p)]
+
+
 def lib_path() -> Path:
     return Path(os.environ.get("CHAOS_GB300_LIB", _PKG / "lib" / "libchaos_gb300.so"))
 
@@ -49,12 +63,17 @@ _SIGS = {
     "chaos_basins_features": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _P, _P, _P, _P], _I),
     "chaos_basins": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P, _P, _P], _I),
     "chaos_dbscan_compat": ([_P, _P, _P, _P, _L, _D, _P], _I),
+    "chaos_basins_dbscan": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _I, _P, _P, _P], _I),
     "chaos_dbscan": ([_P, _P, _L, _I, _D, _I, _P, _P], _I),
     "chaos_peak_finder": ([_P, _P, _L, _I, _D, _I, _P, _P, _P], _I),
     "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
     "chaos_fma_probe": ([_P, _L, _P, _P], _I),
     "chaos_trajectory": ([_P, _I, _L, _P, _P, _D, _I, _P], _I),
     "chaos_set_tuning": ([_I, _I], _I),
+    "chaos_run_batch": ([_P, _P, _I], _I),
+    "chaos_batch_create": ([_P, _P, _I, _P], _I),
+    "chaos_batch_run": ([_P], _I),
+    "chaos_batch_destroy": ([_P], _I),
     "chaos_get_tuning": ([_I], _I),
     "chaos_compat_set_system": ([_I], _I),
     "chaos_compat_set_precision": ([_I], _I),
@@ -177,6 +196,121 @@ def get_tuning(knob: int) -> int:
     return lib().chaos_get_tuning(knob)
 
 
+class Batch:
+    """Many sweeps run by one submission (chaos_run_batch / chaos_batch_*).
+
+    add_bifurcation1d / add_lle2d / add_basins take the same arguments as the
+    array functions and return the dict of output arrays (numpy, or CUDA
+    tensors when device=True) that the batch fills."""
+
+    def __init__(self, device: bool = False):
+        self.device = device
+        self.jobs = []
+        self.keep = _Args()
+        self.outputs = []
+        self._plan = None
+
+    def _alloc(self, shape, dtype):
+        if self.device:
+            import torch
+
+            tdt = {np.float64: torch.float64, np.int32: torch.int32}[dtype]
+            return torch.zeros(shape, dtype=tdt, device="cuda")
+        return np.zeros(shape, dtype)
+
+    def _common(self, kind, system, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                preScaller):
+        j = Job()
+        j.kind, j.system, j.tMax, j.nPts, j.h = kind, _sys(system), tMax, nPts, h
+        j.initialConditions = self.keep.d(ic)
+        j.ranges = self.keep.d(ranges)
+        j.indicesOfMutVars = self.keep.i(mut)
+        j.writableVar, j.maxValue, j.transientTime = wv, maxValue, transientTime
+        j.values = self.keep.d(values)
+        j.preScaller = preScaller
+        return j
+
+    def add_bifurcation1d(self, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar,
+                          maxValue, transientTime, values, preScaller=1, peakCapacity=64):
+        j = self._common(JOB_BIF1D, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars,
+                         writableVar, maxValue, transientTime, values, preScaller)
+        out = dict(counts=self._alloc(nPts, np.int32), flags=self._alloc(nPts, np.int32),
+                   first=self._alloc(nPts, np.float64), peaks=self._alloc((nPts, peakCapacity), np.float64),
+                   intervals=self._alloc((nPts, peakCapacity), np.float64))
+        j.peakCapacity = peakCapacity
+        j.counts, j.flags, j.first = _out_ptr(out["counts"]), _out_ptr(out["flags"]), _out_ptr(out["first"])
+        j.peaks, j.intervals = _out_ptr(out["peaks"]), _out_ptr(out["intervals"])
+        self.jobs.append(j)
+        self.outputs.append(out)
+        return out
+
+    def add_lle2d(self, system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime,
+                  values):
+        j = self._common(JOB_LLE2D, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, 0, 0.0,
+                         transientTime, values, 1)
+        j.NT, j.eps = NT, eps
+        out = dict(lle=self._alloc(nPts * nPts, np.float64))
+        j.lle = _out_ptr(out["lle"])
+        self.jobs.append(j)
+        self.outputs.append(out)
+        return out
+
+    def add_basins(self, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                   transientTime, values, preScaller=1):
+        j = self._common(JOB_BASINS, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars,
+                         writableVar, maxValue, transientTime, values, preScaller)
+        n = nPts * nPts
+        out = dict(flags=self._alloc(n, np.int32), avg_peaks=self._alloc(n, np.float64),
+                   avg_intervals=self._alloc(n, np.float64), counts=self._alloc(n, np.int32))
+        j.flags, j.avgPeaks = _out_ptr(out["flags"]), _out_ptr(out["avg_peaks"])
+        j.avgIntervals, j.counts = _out_ptr(out["avg_intervals"]), _out_ptr(out["counts"])
+        self.jobs.append(j)
+        self.outputs.append(out)
+        return out
+
+    def _exec(self):
+        if self.device:
+            import torch
+
+            st = torch.cuda.current_stream().cuda_stream or CUDA_STREAM_LEGACY
+            return Exec(FP32, MEM_DEVICE, C.c_void_p(st), torch.cuda.current_device())
+        return Exec(FP32, MEM_HOST, None, -1)
+
+    def run(self):
+        """One-shot submission (chaos_run_batch)."""
+        arr = (Job * len(self.jobs))(*self.jobs)
+        ex = self._exec()
+        _check(lib().chaos_run_batch(C.byref(ex), arr, len(self.jobs)))
+        return self.outputs
+
+    def prepare(self):
+        """Uploads descriptors and captures the launch in a CUDA graph (chaos_batch_create)."""
+        if self._plan is None:
+            arr = (Job * len(self.jobs))(*self.jobs)
+            ex = self._exec()
+            plan = C.c_void_p()
+            _check(lib().chaos_batch_create(C.byref(ex), arr, len(self.jobs), C.byref(plan)))
+            self._plan = plan
+        return self
+
+    def replay(self):
+        """Runs the prepared graph (chaos_batch_run)."""
+        self.prepare()
+        _check(lib().chaos_batch_run(self._plan))
+        return self.outputs
+
+    def close(self):
+        if self._plan is not None:
+            lib().chaos_batch_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def set_system(system) -> None:
     """System used by the reference-signature wrappers (bifurcation1D, ...)."""
     _check(lib().chaos_compat_set_system(_sys(system)))
@@ -270,6 +404,24 @@ def basins(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, w
                               A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size,
                               preScaller, eps, _out_ptr(out["labels"]), _out_ptr(out.get("avg_peaks")),
                               _out_ptr(out.get("avg_intervals")), _out_ptr(out.get("flags"))))
+    return out
+
+
+def basins_dbscan(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                  transientTime, values, preScaller=1, eps=0.05, minPts=8, precision=FP64, out=None, stream=None):
+    """Basins with normalised (amplitude, peak count, interval) features and
+    textbook DBSCAN; labels 0.. clusters, -1 noise, -2 diverged."""
+    A = _Args()
+    n = nPts * nPts
+    if out is None:
+        out = dict(labels=np.zeros(n, np.int32), features=np.zeros((n, 3)), flags=np.zeros(n, np.int32))
+    ex = _exec(precision, out, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_basins_dbscan(C.byref(ex), _sys(system), tMax, nPts, h, ic.size, A.d(ic), A.d(ranges),
+                                     A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals),
+                                     vals.size, preScaller, eps, minPts, _out_ptr(out["labels"]),
+                                     _out_ptr(out.get("features")), _out_ptr(out.get("flags"))))
     return out
 
 

@@ -22,7 +22,10 @@ SOURCES = [
     ("kern_f64.cu", ["--fmad=false"]),
     ("kern_f32.cu", []),
     ("dbscan.cu", ["--fmad=false", "--extended-lambda"]),
+    ("basins_dbscan.cu", ["--fmad=false"]),
     ("capi.cu", []),
+    ("batch.cu", []),
+    ("batch_host.cu", []),
     ("probe.cu", []),
     ("noalloc.cu", []),
     ("compat.cpp", []),

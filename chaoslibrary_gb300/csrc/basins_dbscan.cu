@@ -1,0 +1,93 @@
+// Normalised feature matrix of the basins map for the textbook DBSCAN mode:
+// per point (amplitude, kept peak count, mean interval) -- amplitude is the
+// mean peak value, or the last recorded sample for a point without peaks --
+// min-max scaled to [0, 1] per feature over the points with flag != 0.
+// Integer and FP64 work, two passes over n points (memory-bound).
+#include <cuda_runtime.h>
+
+#include <cfloat>
+
+#include "launch.h"
+
+namespace chaos {
+namespace {
+
+constexpr int kTPB = 256;
+
+__device__ __forceinline__ void raw_features(const BasinsOut& O, long long i, double* f) {
+    const int c = O.counts[i];
+    f[0] = c > 0 ? O.avgPeaks[i] : O.last[i];
+    f[1] = (double)c;
+    f[2] = c > 0 ? O.avgIntervals[i] : 0.0;
+}
+
+// order-preserving map of a double to an unsigned 64-bit key (for atomicMin/Max)
+__device__ __forceinline__ unsigned long long okey(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ounkey(unsigned long long k) {
+    const unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void minmax_init_kernel(unsigned long long* mm) {
+    if (threadIdx.x < 3) mm[threadIdx.x] = ~0ull;        // min keys
+    else if (threadIdx.x < 6) mm[threadIdx.x] = 0ull;    // max keys
+}
+
+__global__ void minmax_kernel(BasinsOut O, long long n, unsigned long long* mm, int* mask) {
+    __shared__ unsigned long long smin[3], smax[3];
+    if (threadIdx.x < 3) { smin[threadIdx.x] = ~0ull; smax[threadIdx.x] = 0ull; }
+    __syncthreads();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int in = O.flags[i] != 0;
+        mask[i] = in;
+        if (!in) continue;
+        double f[3];
+        raw_features(O, i, f);
+        for (int d = 0; d < 3; ++d) {
+            atomicMin(&smin[d], okey(f[d]));
+            atomicMax(&smax[d], okey(f[d]));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        atomicMin(&mm[threadIdx.x], smin[threadIdx.x]);
+        atomicMax(&mm[3 + threadIdx.x], smax[threadIdx.x]);
+    }
+}
+
+__global__ void normalise_kernel(BasinsOut O, long long n, const unsigned long long* mm, double* F) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double f[3];
+    raw_features(O, i, f);
+    for (int d = 0; d < 3; ++d) {
+        double v = 0.0;
+        if (O.flags[i] != 0 && mm[d] != ~0ull) {
+            const double lo = ounkey(mm[d]), hi = ounkey(mm[3 + d]);
+            v = hi > lo ? (f[d] - lo) / (hi - lo) : 0.0;
+        }
+        F[i * 3 + d] = v;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double* minmax, double* features, int* mask,
+                                        cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    unsigned long long* mm = reinterpret_cast<unsigned long long*>(minmax);
+    minmax_init_kernel<<<1, 32, 0, st>>>(mm);
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long need = (n + kTPB - 1) / kTPB;
+    const unsigned grid = (unsigned)(need < (long long)sms * 8 ? need : (long long)sms * 8);
+    minmax_kernel<<<grid, kTPB, 0, st>>>(O, n, mm, mask);
+    normalise_kernel<<<(unsigned)need, kTPB, 0, st>>>(O, n, mm, features);
+    return cudaGetLastError();
+}
+
+}  // namespace chaos

@@ -27,6 +27,7 @@ struct DeviceCtx {
     bool ready = false;
     cudaStream_t stream = nullptr;
     cudaMemPool_t pool = nullptr;
+    std::vector<cudaStream_t> aux;  // for concurrent branches of one call (batched groups)
 };
 std::mutex g_mu;
 std::vector<DeviceCtx> g_dev;
@@ -74,6 +75,21 @@ static int device_ctx(int dev, DeviceCtx** out) {
         c.ready = true;
     }
     *out = &c;
+    return CHAOS_OK;
+}
+
+int aux_streams(int dev, std::vector<cudaStream_t>& out) {
+    DeviceCtx* c = nullptr;
+    int rc = device_ctx(dev, &c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_mu);
+    while (c->aux.size() < 8) {
+        cudaStream_t s = nullptr;
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_error(e, "stream create");
+        c->aux.push_back(s);
+    }
+    out = c->aux;
     return CHAOS_OK;
 }
 
@@ -201,6 +217,46 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     return CHAOS_OK;
 }
 
+int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double h, double eps,
+             const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+             const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues) {
+    int rc = check_system(system, amountOfInitialConditions, amountOfValues);
+    if (rc) return rc;
+    if (!initialConditions || !ranges || !indicesOfMutVars || !values) return set_error(CHAOS_E_ARGS, "null argument");
+    if (nPts < 1) return set_error(CHAOS_E_ARGS, "nPts must be >= 1");
+    if (!(h > 0) || !(tMax > 0) || !(NT > 0) || !(transientTime >= 0) || !(eps > 0))
+        return set_error(CHAOS_E_ARGS, "need h, tMax, NT, eps > 0 and transientTime >= 0");
+    for (int d = 0; d < 2; ++d)
+        if (indicesOfMutVars[d] < 0 || indicesOfMutVars[d] >= amountOfValues)
+            return set_error(CHAOS_E_ARGS, "indicesOfMutVars[%d] out of range", d);
+    if (NT / h > 2.0e9 || tMax / h > 2.0e9 || transientTime / h > 2.0e9)
+        return set_error(CHAOS_E_ARGS, "step counts must fit in int");
+    memset(&L, 0, sizeof L);
+    L.system = system;
+    L.nPts = nPts;
+    L.ntp = static_cast<int>(NT / h);
+    L.trans = static_cast<int>(transientTime / h);
+    const int all = static_cast<int>(tMax / h);
+    if (L.ntp < 1) return set_error(CHAOS_E_ARGS, "NT / h must be >= 1");
+    L.calcBlocks = all / L.ntp + 1;
+    L.h = h;
+    L.eps = eps;
+    L.tMax = tMax;
+    for (int i = 0; i < amountOfInitialConditions; ++i) L.ic[i] = initialConditions[i];
+    for (int i = 0; i < amountOfValues; ++i) L.values[i] = values[i];
+    L.mut[0] = indicesOfMutVars[0];
+    L.mut[1] = indicesOfMutVars[1];
+    L.rangeA[0] = ranges[0];
+    L.rangeA[1] = ranges[1];
+    L.rangeB[0] = ranges[2];
+    L.rangeB[1] = ranges[3];
+    L.stepA = nPts > 1 ? (ranges[1] - ranges[0]) / (nPts - 1) : 0.0;
+    L.stepB = nPts > 1 ? (ranges[3] - ranges[2]) / (nPts - 1) : 0.0;
+    L.pBegin = 0;
+    L.nPoints = (long long)nPts * nPts;
+    return CHAOS_OK;
+}
+
 size_t scratch_budget_bytes() {
     const char* s = getenv("CHAOS_SCRATCH_BUDGET_MB");
     size_t mb = s ? (size_t)strtoull(s, nullptr, 10) : 8192;
@@ -315,42 +371,12 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
                 const double* values, int amountOfValues, double* lle) {
     (void)writableVar;
     (void)maxValue;
-    int rc = check_system(system, amountOfInitialConditions, amountOfValues);
-    if (rc) return rc;
-    if (!initialConditions || !ranges || !indicesOfMutVars || !values || !lle)
-        return set_error(CHAOS_E_ARGS, "null argument");
-    if (nPts < 1) return set_error(CHAOS_E_ARGS, "nPts must be >= 1");
-    if (!(h > 0) || !(tMax > 0) || !(NT > 0) || !(transientTime >= 0) || !(eps > 0))
-        return set_error(CHAOS_E_ARGS, "need h, tMax, NT, eps > 0 and transientTime >= 0");
-    for (int d = 0; d < 2; ++d)
-        if (indicesOfMutVars[d] < 0 || indicesOfMutVars[d] >= amountOfValues)
-            return set_error(CHAOS_E_ARGS, "indicesOfMutVars[%d] out of range", d);
-    if (NT / h > 2.0e9 || tMax / h > 2.0e9 || transientTime / h > 2.0e9)
-        return set_error(CHAOS_E_ARGS, "step counts must fit in int");
+    int rc = CHAOS_OK;
+    if (!lle) return set_error(CHAOS_E_ARGS, "null argument");
     LleParams L;
-    memset(&L, 0, sizeof L);
-    L.system = system;
-    L.nPts = nPts;
-    L.ntp = static_cast<int>(NT / h);
-    L.trans = static_cast<int>(transientTime / h);
-    const int all = static_cast<int>(tMax / h);
-    if (L.ntp < 1) return set_error(CHAOS_E_ARGS, "NT / h must be >= 1");
-    L.calcBlocks = all / L.ntp + 1;
-    L.h = h;
-    L.eps = eps;
-    L.tMax = tMax;
-    for (int i = 0; i < amountOfInitialConditions; ++i) L.ic[i] = initialConditions[i];
-    for (int i = 0; i < amountOfValues; ++i) L.values[i] = values[i];
-    L.mut[0] = indicesOfMutVars[0];
-    L.mut[1] = indicesOfMutVars[1];
-    L.rangeA[0] = ranges[0];
-    L.rangeA[1] = ranges[1];
-    L.rangeB[0] = ranges[2];
-    L.rangeB[1] = ranges[3];
-    L.stepA = nPts > 1 ? (ranges[1] - ranges[0]) / (nPts - 1) : 0.0;
-    L.stepB = nPts > 1 ? (ranges[3] - ranges[2]) / (nPts - 1) : 0.0;
-    L.pBegin = 0;
-    L.nPoints = (long long)nPts * nPts;
+    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                       indicesOfMutVars, transientTime, values, amountOfValues)))
+        return rc;
     if (ex && ex->precision == CHAOS_FP32 && !system_has_difference_form(system))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
     Call c;
@@ -382,6 +408,7 @@ int chaos_basins_features(const chaos_exec* ex, int system, double tMax, int nPt
     O.avgPeaks = (double*)c.output(avgPeaks, n * sizeof(double));
     O.avgIntervals = (double*)c.output(avgIntervals, n * sizeof(double));
     O.counts = (int*)c.output(counts, n * sizeof(int));
+    O.last = nullptr;
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "basins kernel"));
@@ -411,6 +438,7 @@ int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double
     O.avgPeaks = avgPeaks ? (double*)c.output(avgPeaks, n * sizeof(double)) : (double*)c.alloc(n * sizeof(double));
     O.avgIntervals = avgIntervals ? (double*)c.output(avgIntervals, n * sizeof(double)) : (double*)c.alloc(n * sizeof(double));
     O.counts = nullptr;
+    O.last = nullptr;
     int* dLabels = (int*)c.output(labels, n * sizeof(int));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
@@ -420,6 +448,43 @@ int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double
     if (!rc && flags) rc = c.to_host(flags, O.flags, n * sizeof(int));
     if (!rc && avgPeaks) rc = c.to_host(avgPeaks, O.avgPeaks, n * sizeof(double));
     if (!rc && avgIntervals) rc = c.to_host(avgIntervals, O.avgIntervals, n * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_basins_dbscan(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, double eps, int minPts,
+                        int* labels, double* features, int* flags) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 2, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        true);
+    if (rc) return rc;
+    if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
+    if (!(eps > 0) || minPts < 1) return set_error(CHAOS_E_ARGS, "need eps > 0 and minPts >= 1");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const long long n = P.nPoints;
+    BasinsOut O;
+    O.flags = flags ? (int*)c.output(flags, n * sizeof(int)) : (int*)c.alloc(n * sizeof(int));
+    O.avgPeaks = (double*)c.alloc(n * sizeof(double));
+    O.avgIntervals = (double*)c.alloc(n * sizeof(double));
+    O.counts = (int*)c.alloc(n * sizeof(int));
+    O.last = (double*)c.alloc(n * sizeof(double));
+    double* F = features ? (double*)c.output(features, (size_t)n * 3 * sizeof(double))
+                         : (double*)c.alloc((size_t)n * 3 * sizeof(double));
+    int* mask = (int*)c.alloc(n * sizeof(int));
+    double* minmax = (double*)c.alloc(6 * sizeof(double));
+    int* dLabels = (int*)c.output(labels, n * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
+    if (e == cudaSuccess) e = launch_basin_feature_matrix(O, n, minmax, F, mask, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "basins feature kernels"));
+    rc = dbscan_device(c, F, n, 3, eps, minPts, mask, dLabels);
+    if (!rc) rc = c.to_host(labels, dLabels, n * sizeof(int));
+    if (!rc && features) rc = c.to_host(features, F, (size_t)n * 3 * sizeof(double));
+    if (!rc && flags) rc = c.to_host(flags, O.flags, n * sizeof(int));
     return c.finish(rc);
 }
 

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/chaos_gb300.h"
+#include "launch.h"
 
 namespace chaos {
 
@@ -30,5 +31,16 @@ struct Call {
     int to_host(void* host, const void* dev, size_t bytes);  // copy back (host-memory calls)
     int finish(int rc);
 };
+
+// The device's auxiliary streams (8, created on first use) for concurrent branches.
+int aux_streams(int device, std::vector<cudaStream_t>& out);
+
+// Argument checks + parameter blocks shared by the entry points (capi.cu).
+int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, double h, int nIC, const double* ic,
+               const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
+               const double* values, int nValues, int preScaller, bool basins);
+int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double h, double eps,
+             const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+             const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues);
 
 }  // namespace chaos

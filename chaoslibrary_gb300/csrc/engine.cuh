@@ -248,6 +248,7 @@ __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsO
     O.avgPeaks[o] = ap;
     O.avgIntervals[o] = ai;
     if (O.counts) O.counts[o] = flag == 1 ? kept : 0;
+    if (O.last) O.last[o] = last;
 }
 
 // ---------------------------------------------------------------------------

@@ -53,7 +53,8 @@ struct BasinsOut {
     int* flags;
     double* avgPeaks;
     double* avgIntervals;
-    int* counts;  // kept peaks (may be null)
+    int* counts;   // kept peaks (may be null)
+    double* last;  // x[writableVar] at the last recorded sample (may be null)
 };
 
 struct LleParams {
@@ -86,6 +87,11 @@ cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0
                                   double* out, long long n, cudaStream_t st);
 cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st);
+
+// Basin features in normalised form (basins_dbscan.cu): per point (amplitude,
+// peak count, mean interval), min-max scaled over the points with flag != 0.
+cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double* minmax, double* features,
+                                        int* mask, cudaStream_t st);
 
 // FP32 LLE kernel variant (kern_f32.cu): 0 = default, 2 = two points per
 // thread (packed FP32x2), 12 / 16 = one point per thread at that occupancy.

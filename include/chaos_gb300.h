@@ -147,6 +147,22 @@ int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double
                  int preScaller, double eps, int* labels, double* avgPeaks, double* avgIntervals, int* flags);
 
 /*
+ * Basins of attraction with the features and clustering of the benchmark's
+ * basins workload (no reference counterpart; the reference clusters with the
+ * rule of chaos_dbscan_compat): per grid point the features (mean peak
+ * amplitude, kept peak count, mean peak interval) of the reference's peak
+ * rules, with a point without peaks taking (last sample, 0, 0); each feature
+ * min-max scaled to [0, 1] over the points with flag != 0; then chaos_dbscan
+ * (eps, minPts) on that n x 3 matrix. labels: clusters 0.., noise -1,
+ * diverged points (flag 0) -2. features (n x 3, normalised) and flags may be NULL.
+ */
+int chaos_basins_dbscan(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, double eps, int minPts,
+                        int* labels, double* features, int* flags);
+
+/*
  * The reference's basin clustering on given feature arrays
  * (CUDA_dbscan + CUDA_dbscan_kernel, Basins/src/basinsCUDA.cu:35-179, 894-923):
  * eps-connected components (sqrt(dp^2 + di^2) <= eps, FP64) over the points
@@ -186,6 +202,59 @@ int chaos_peak_finder(const chaos_exec* ex, const double* data, long long nSerie
  */
 int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int* counts, long long n, int stride,
                        double eps, int* labels);
+
+/*
+ * Batched sweeps (no reference counterpart: the reference compiles one system
+ * in and runs one sweep per call). Many independent jobs of different kinds,
+ * systems, sizes and transients run in ONE persistent launch that pulls
+ * chunks of points from a device work queue. FP32 trajectories with FP64
+ * accumulation (ex->precision is ignored); a point's result is bit-identical
+ * to the single-job FP32 call's. Arguments mean what they mean in the
+ * single-job entry points; outputs are host or device arrays per ex->memory.
+ */
+#define CHAOS_JOB_BIF1D 1  /* chaos_bifurcation1d: counts, flags, first?, peaks?, intervals? */
+#define CHAOS_JOB_LLE2D 2  /* chaos_lle2d (RK4 systems): lle */
+#define CHAOS_JOB_BASINS 3 /* chaos_basins_features: flags, avgPeaks, avgIntervals, counts? */
+
+typedef struct chaos_job {
+    int kind;
+    int system;
+    double tMax;
+    int nPts;
+    double h;
+    const double* initialConditions; /* SIZE_X host values */
+    const double* ranges;            /* 2 (bifurcation) or 4 values */
+    const int* indicesOfMutVars;     /* 1 or 2 indices */
+    int writableVar;
+    double maxValue;
+    double transientTime;
+    const double* values;            /* SIZE_A host values */
+    int preScaller;
+    double NT;                       /* LLE */
+    double eps;                      /* LLE */
+    int peakCapacity;                /* bifurcation */
+    int* counts;
+    int* flags;
+    double* first;
+    double* peaks;
+    double* intervals;
+    double* lle;
+    double* avgPeaks;
+    double* avgIntervals;
+} chaos_job;
+
+/* Runs the jobs in one persistent launch (chunks ordered longest work first). */
+int chaos_run_batch(const chaos_exec* ex, const chaos_job* jobs, int nJobs);
+
+/*
+ * A prepared batch: descriptors uploaded and the launch captured in a CUDA
+ * graph once, replayed by chaos_batch_run (outputs rewritten every run).
+ * Outputs must stay valid while the plan exists.
+ */
+typedef struct chaos_batch chaos_batch;
+int chaos_batch_create(const chaos_exec* ex, const chaos_job* jobs, int nJobs, chaos_batch** plan);
+int chaos_batch_run(chaos_batch* plan);
+int chaos_batch_destroy(chaos_batch* plan);
 
 /*
  * chaos_point_dbscan without any allocation. No counterpart in the reference:

@@ -357,11 +357,12 @@ int orc_lle2d(int sys, double tMax, double NT, int nPts, double h, double eps, c
 // Basins features over the nPts^2 grid of initial conditions
 // (Basins/src/basinsCUDA.cu:233-314 + 818-864): flags, avgPeaks, avgIntervals
 // (the reference's sentinels: flag 0 -> 999/999, flag -1 -> last sample/-1,
-// no peaks -> 1000/1000) and the kept peak count (counts, may be null).
+// no peaks -> 1000/1000), the kept peak count (counts, may be null) and the
+// last recorded sample (last, may be null; meaningful for flag != 0).
 int orc_basins_features(int sys, double tMax, int nPts, double h, const double* ic, const double* ranges,
                         const int* mut, int wv, double maxValue, double transientTime, const double* values,
                         int preScaller, long long pBegin, long long pEnd, int* flags, double* avgPeaks,
-                        double* avgIntervals, int* counts, int nthreads) {
+                        double* avgIntervals, int* counts, double* last, int nthreads) {
     const int B = (int)(tMax / h / preScaller);
     const int S = (int)(transientTime / h);
     const int nx = chaos::system_nx(sys), na = chaos::system_na(sys);
@@ -398,6 +399,7 @@ int orc_basins_features(int sys, double tMax, int nPts, double h, const double* 
                 }
             }
             if (counts) counts[o] = cnt;
+            if (last) last[o] = data[flag == 0 ? 0 : B - 1];
         }
     }
     return 0;

@@ -55,7 +55,7 @@ def lib() -> C.CDLL:
                                 C.c_double, _dp, C.c_longlong, C.c_longlong, _dp, C.c_int]
         L.orc_basins_features.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
                                           C.c_double, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _ip,
-                                          _dp, _dp, C.c_void_p, C.c_int]
+                                          _dp, _dp, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_dbscan_compat_bfs.argtypes = [_dp, _dp, _ip, C.c_int, C.c_double, _ip]
         L.orc_dbscan_compat_grid.argtypes = [_dp, _dp, _ip, C.c_int, C.c_double, _ip]
         L.orc_dbscan.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, _ip]
@@ -146,12 +146,39 @@ def basins_features(system: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue, t
     ap = np.zeros(n, np.float64)
     ai = np.zeros(n, np.float64)
     counts = np.zeros(n, np.int32)
+    last = np.zeros(n, np.float64)
     rc = lib().orc_basins_features(system, tMax, nPts, h, _d(ic), _d(ranges), _i(mut), wv, maxValue,
                                    transientTime, _d(values), preScaller, p_begin, p_end, flags, ap, ai,
-                                   counts.ctypes.data, nthreads)
+                                   counts.ctypes.data, last.ctypes.data, nthreads)
     if rc:
         raise ValueError("bad basins arguments")
-    return dict(flags=flags, avg_peaks=ap, avg_intervals=ai, counts=counts)
+    return dict(flags=flags, avg_peaks=ap, avg_intervals=ai, counts=counts, last=last)
+
+
+def basin_feature_matrix(feat: dict):
+    """(amplitude, kept peak count, mean interval) per point -- the mean peak,
+    or the last sample without peaks -- min-max scaled over flag != 0 points;
+    returns (features n x 3, mask)."""
+    c = feat["counts"]
+    f = np.stack([np.where(c > 0, feat["avg_peaks"], feat["last"]), c.astype(np.float64),
+                  np.where(c > 0, feat["avg_intervals"], 0.0)], axis=1)
+    mask = (feat["flags"] != 0).astype(np.int32)
+    out = np.zeros_like(f)
+    if mask.any():
+        lo = f[mask == 1].min(axis=0)
+        hi = f[mask == 1].max(axis=0)
+        for d in range(3):
+            if hi[d] > lo[d]:
+                out[:, d] = np.where(mask == 1, (f[:, d] - lo[d]) / (hi[d] - lo[d]), 0.0)
+    return out, mask
+
+
+def basins_dbscan(system: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values, preScaller=1,
+                  eps=0.05, min_pts=8, nthreads=0):
+    feat = basins_features(system, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                           preScaller=preScaller, nthreads=nthreads)
+    F, mask = basin_feature_matrix(feat)
+    return dbscan(F, eps, min_pts, mask=mask), F, feat
 
 
 def dbscan_compat(avg_peaks, avg_intervals, flags, eps: float, method: str = "grid") -> np.ndarray:

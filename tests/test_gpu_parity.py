@@ -260,3 +260,83 @@ def test_lle_fp32_variants_identical(engine, system, values, ranges, mut):
         engine.set_tuning(knob, 0)
     for v in (16, 2):
         assert np.array_equal(maps[v], maps[12], equal_nan=True), (v, np.nanmax(np.abs(maps[v] - maps[12])))
+
+
+@pytest.mark.parametrize("precision", ["fp64"])
+def test_basins_dbscan_vs_oracle(engine, oracle, precision):
+    """BASELINE-mode basins (normalised features, DBSCAN eps/minPts) bit for bit
+    against the oracle's features and DBSCAN on a small Lorenz rho=24 grid."""
+    kw = dict(tMax=10.0, nPts=40, h=0.01, initialConditions=[0.0, 0.0, 27.0], ranges=[-30.0, 30.0, -30.0, 30.0],
+              indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8, transientTime=20.0, values=[10.0, 24.0, 8 / 3])
+    g = engine.basins_dbscan("lorenz", eps=0.05, minPts=8, **kw)
+    lab, F, feat = oracle.basins_dbscan(0, kw["tMax"], kw["nPts"], kw["h"], kw["initialConditions"], kw["ranges"],
+                                        kw["indicesOfMutVars"], kw["writableVar"], kw["maxValue"],
+                                        kw["transientTime"], kw["values"], eps=0.05, min_pts=8)
+    assert np.array_equal(g["flags"], feat["flags"])
+    assert np.array_equal(g["features"], F)
+    assert np.array_equal(g["labels"], lab)
+
+
+def _batch_jobs():
+    """A small mixed batch: every kind, four systems, uneven sizes."""
+    return [
+        ("bif", "lorenz", dict(tMax=20.0, nPts=300, h=0.01, initialConditions=[0.1, 0.1, 0.1], ranges=[20.0, 200.0],
+                               indicesOfMutVars=[1], writableVar=0, maxValue=1e4, transientTime=5.0,
+                               values=[10.0, 28.0, 8 / 3])),
+        ("lle", "rossler", dict(tMax=20.0, NT=0.1, nPts=23, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+                                ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=10.0,
+                                values=[0.2, 0.2, 5.7])),
+        ("bif", "chen", dict(tMax=10.0, nPts=129, h=0.01, initialConditions=[-10.0, 0.0, 37.0], ranges=[20.0, 30.0],
+                             indicesOfMutVars=[2], writableVar=0, maxValue=1e4, transientTime=20.0,
+                             values=[35.0, 3.0, 28.0])),
+        ("lle", "lorenz", dict(tMax=10.0, NT=0.2, nPts=16, h=0.01, eps=1e-8, initialConditions=[0.1, 0.1, 0.1],
+                               ranges=[20.0, 60.0, 5.0, 15.0], indicesOfMutVars=[1, 0], transientTime=3.0,
+                               values=[10.0, 28.0, 8 / 3])),
+        ("basins", "lorenz", dict(tMax=4.0, nPts=20, h=0.01, initialConditions=[0.0, 0.0, 27.0],
+                                  ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1], writableVar=0,
+                                  maxValue=1e8, transientTime=10.0, values=[10.0, 24.0, 8 / 3])),
+        ("bif", "chameleon", dict(tMax=10.0, nPts=77, h=0.01, initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0],
+                                  indicesOfMutVars=[3], writableVar=0, maxValue=1e4, transientTime=5.0,
+                                  values=[0.5, 3, 0, 2, 1, 18, 1])),
+    ]
+
+
+@pytest.mark.parametrize("mode", ["run", "graph", "device"])
+def test_batch_equals_single_jobs(engine, mode):
+    """Every job of a mixed batch (one submission, persistent group kernels)
+    is bit-identical to the same job run alone through its FP32 entry point;
+    a captured plan gives the same results when replayed twice."""
+    b = engine.Batch(device=(mode == "device"))
+    outs = []
+    for kind, system, kw in _batch_jobs():
+        if kind == "bif":
+            outs.append(b.add_bifurcation1d(system, peakCapacity=32, **kw))
+        elif kind == "lle":
+            outs.append(b.add_lle2d(system, **kw))
+        else:
+            outs.append(b.add_basins(system, **kw))
+    runs = 2 if mode == "graph" else 1
+    for _ in range(runs):
+        if mode == "graph":
+            b.replay()
+        else:
+            b.run()
+        if mode == "device":
+            import torch
+            torch.cuda.synchronize()
+        for (kind, system, kw), o in zip(_batch_jobs(), outs):
+            got = {k: (v.cpu().numpy() if hasattr(v, "cpu") else v) for k, v in o.items()}
+            if kind == "bif":
+                ref = engine.bifurcation1d(system, precision=engine.FP32, peakCapacity=32, **kw)
+                assert np.array_equal(got["counts"], ref["counts"]), system
+                assert np.array_equal(got["flags"], ref["flags"])
+                assert np.array_equal(got["peaks"], ref["peaks"].reshape(got["peaks"].shape))
+                assert np.array_equal(got["intervals"], ref["intervals"].reshape(got["intervals"].shape))
+            elif kind == "lle":
+                ref = engine.lle2d(system, precision=engine.FP32, **kw)
+                assert np.array_equal(got["lle"], ref, equal_nan=True), system
+            else:
+                ref = engine.basins_features(system, precision=engine.FP32, **kw)
+                for k in ("flags", "avg_peaks", "avg_intervals", "counts"):
+                    assert np.array_equal(got[k], ref[k]), k
+    b.close()

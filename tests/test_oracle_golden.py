@@ -81,3 +81,15 @@ def test_lle_golden(oracle):
     assert np.array_equal(fin, np.isfinite(o))
     # the reference sums float logs (__logf); the oracle sums FP64 logs
     assert np.max(np.abs(o[fin] - g["lle"][fin])) < 1e-6
+
+
+def test_basin_features_dbscan_matches_sklearn(oracle):
+    """The oracle's DBSCAN on real basin features (Lorenz rho=24) equals
+    scikit-learn's labels."""
+    sk = pytest.importorskip("sklearn.cluster")
+    lab, F, feat = oracle.basins_dbscan(0, 6.0, 30, 0.01, [0.0, 0.0, 27.0], [-30.0, 30.0, -30.0, 30.0], [0, 1], 0,
+                                        1e8, 10.0, [10.0, 24.0, 8 / 3], eps=0.05, min_pts=8)
+    m = feat["flags"] != 0
+    ref = sk.DBSCAN(eps=0.05, min_samples=8).fit(F[m]).labels_
+    assert np.array_equal(lab[m], ref)
+    assert np.all(lab[~m] == -2)
