@@ -128,18 +128,26 @@ void make_chunks(const std::vector<JobDesc>& jobs, std::vector<Chunk>& chunks, s
 // Resets the group counters on `st`, forks one branch per group onto the
 // auxiliary streams, launches each group's persistent kernel and joins the
 // branches back into `st` (works the same inside a stream capture).
-int launch_groups(const std::vector<Group>& groups, const JobDesc* dJobs, const Chunk* dChunks, int* dCounters,
-                  int device, cudaStream_t st, const std::vector<cudaStream_t>& aux,
+// Grid of every group's persistent kernel: resident blocks, at most one per chunk
+// (queried before any capture: occupancy queries are not allowed inside one).
+std::vector<int> group_grids(const std::vector<Group>& groups, int device) {
+    std::vector<int> grid(groups.size());
+    for (size_t g = 0; g < groups.size(); ++g)
+        grid[g] = std::max(1, std::min(groups[g].count, group_resident_blocks(groups[g].kind, groups[g].system, device)));
+    return grid;
+}
+
+int launch_groups(const std::vector<Group>& groups, const std::vector<int>& grids, const JobDesc* dJobs,
+                  const Chunk* dChunks, int* dCounters, cudaStream_t st, const std::vector<cudaStream_t>& aux,
                   const std::vector<cudaEvent_t>& events) {
     cudaError_t e = reset_counters(dCounters, (int)groups.size(), st);
     if (e == cudaSuccess) e = cudaEventRecord(events[0], st);
     for (size_t g = 0; g < groups.size() && e == cudaSuccess; ++g) {
         cudaStream_t s = aux[g % aux.size()];
         e = cudaStreamWaitEvent(s, events[0], 0);
-        const int grid = std::min(groups[g].count, group_resident_blocks(groups[g].kind, groups[g].system, device));
         if (e == cudaSuccess)
             e = launch_group(groups[g].kind, groups[g].system, dJobs, dChunks + groups[g].begin, groups[g].count,
-                             dCounters + g, grid, s);
+                             dCounters + g, grids[g], s);
         if (e == cudaSuccess) e = cudaEventRecord(events[1 + g], s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, events[1 + g], 0);
     }
@@ -164,7 +172,9 @@ void destroy_events(std::vector<cudaEvent_t>& ev) {
 struct chaos_batch {
     chaos_exec ex{};
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t user = nullptr;    // the caller's stream: runs are ordered after its earlier work
+    cudaStream_t stream = nullptr;  // the plan's own stream (a default stream cannot be captured)
+    cudaEvent_t in = nullptr, out = nullptr;
     std::vector<void*> buffers;  // cudaMalloc'd, freed by destroy
     std::vector<HostOut> outs;
     JobDesc* dJobs = nullptr;
@@ -206,7 +216,7 @@ int chaos_run_batch(const chaos_exec* ex, const chaos_job* jobs, int nJobs) {
     std::vector<cudaStream_t> aux;
     if ((rc = aux_streams(c.device, aux))) return c.finish(rc);
     std::vector<cudaEvent_t> events = make_events(1 + (int)groups.size());
-    rc = launch_groups(groups, dJobs, dChunks, counters, c.device, c.stream, aux, events);
+    rc = launch_groups(groups, group_grids(groups, c.device), dJobs, dChunks, counters, c.stream, aux, events);
     for (const HostOut& o : outs)
         if (!rc) rc = c.to_host(o.host, o.dev, o.bytes);
     // the host-side descriptor arrays are copied asynchronously: wait before they go out of scope
@@ -228,7 +238,13 @@ int chaos_batch_create(const chaos_exec* ex, const chaos_job* jobs, int nJobs, c
     if (!b) return c.finish(set_error(CHAOS_E_NOMEM, "host allocation"));
     b->ex = c.ex;
     b->device = c.device;
-    b->stream = c.stream;
+    b->user = c.stream;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->out, cudaEventDisableTiming) != cudaSuccess) {
+        chaos_batch_destroy(b);
+        return c.finish(set_error(CHAOS_E_CUDA, "stream or event create"));
+    }
     auto dalloc = [&](size_t bytes) -> void* {
         void* p = nullptr;
         if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
@@ -260,9 +276,10 @@ int chaos_batch_create(const chaos_exec* ex, const chaos_job* jobs, int nJobs, c
         cudaMemcpy(b->dJobs, desc.data(), desc.size() * sizeof(JobDesc), cudaMemcpyHostToDevice);
         cudaMemcpy(b->dChunks, chunks.data(), chunks.size() * sizeof(Chunk), cudaMemcpyHostToDevice);
         b->events = make_events(1 + (int)b->groups.size());
+        const std::vector<int> grids = group_grids(b->groups, b->device);
         cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            int lrc = launch_groups(b->groups, b->dJobs, b->dChunks, b->dCounters, b->device, b->stream, b->aux,
+            int lrc = launch_groups(b->groups, grids, b->dJobs, b->dChunks, b->dCounters, b->stream, b->aux,
                                     b->events);
             e = cudaStreamEndCapture(b->stream, &b->graph);
             if (lrc != CHAOS_OK && e == cudaSuccess) e = cudaErrorUnknown;
@@ -283,10 +300,14 @@ int chaos_batch_run(chaos_batch* b) {
     int prev = 0;
     cudaGetDevice(&prev);
     if (prev != b->device) cudaSetDevice(b->device);
-    cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+    cudaError_t e = cudaEventRecord(b->in, b->user);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->in, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(b->exec, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->out, b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->user, b->out, 0);
     for (const HostOut& o : b->outs)
-        if (e == cudaSuccess) e = cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, b->stream);
-    if (e == cudaSuccess && b->ex.memory == CHAOS_MEM_HOST) e = cudaStreamSynchronize(b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, b->user);
+    if (e == cudaSuccess && b->ex.memory == CHAOS_MEM_HOST) e = cudaStreamSynchronize(b->user);
     if (prev != b->device) cudaSetDevice(prev);
     return e == cudaSuccess ? CHAOS_OK : cuda_error(e, "batch run");
 }
@@ -298,6 +319,9 @@ int chaos_batch_destroy(chaos_batch* b) {
     if (prev != b->device) cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->in) cudaEventDestroy(b->in);
+    if (b->out) cudaEventDestroy(b->out);
+    if (b->stream) cudaStreamDestroy(b->stream);
     if (b->graph) cudaGraphDestroy(b->graph);
     destroy_events(b->events);
     for (void* p : b->buffers) cudaFree(p);

@@ -82,6 +82,7 @@ int chaos_synchronize(const chaos_exec* ex);
  *   flags[k]   1 / 0 / -1
  *   firstSample[k]  x[writableVar] at the first recorded sample (the reference's row for -1)
  *   peaks[k*cap + j], intervals[k*cap + j]  for j < min(counts[k], peakCapacity)
+ *              (entries past that are left unspecified, as in the reference)
  * firstSample, peaks and intervals may be NULL.
  */
 int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
@@ -249,7 +250,9 @@ int chaos_run_batch(const chaos_exec* ex, const chaos_job* jobs, int nJobs);
 /*
  * A prepared batch: descriptors uploaded and the launch captured in a CUDA
  * graph once, replayed by chaos_batch_run (outputs rewritten every run).
- * Outputs must stay valid while the plan exists.
+ * Runs are ordered after the earlier work of ex->stream and before its later
+ * work (the graph itself runs on a stream the plan owns). Outputs must stay
+ * valid while the plan exists.
  */
 typedef struct chaos_batch chaos_batch;
 int chaos_batch_create(const chaos_exec* ex, const chaos_job* jobs, int nJobs, chaos_batch** plan);
