@@ -87,7 +87,43 @@ def batch_jobs(seed: int = 2024, n_jobs: int = 256):
     return jobs
 
 
+def serve_requests(seed: int = 7, n: int = 2000):
+    """The served stream: n requests, 40 % 1-D bifurcation, 40 % LLE maps,
+    20 % basins maps (features + reference clustering), systems uniform over
+    Lorenz / Rossler / Chen, grid sizes log-uniform in [1e3, 4e6] points,
+    2000 transient steps and 2000 recorded (or 202 Benettin blocks of 10)."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(n):
+        u = rng.random()
+        kind = "bif" if u < 0.4 else ("lle" if u < 0.8 else "basins")
+        system = ["lorenz", "rossler", "chen"][int(rng.integers(0, 3))]
+        N = int(round(10 ** rng.uniform(3, np.log10(4e6))))
+        m = max(int(round(N ** 0.5)), 2)
+        vals = {"lorenz": [10.0, 28.0, 8 / 3], "rossler": [0.2, 0.2, 5.7], "chen": [35.0, 3.0, 28.0]}[system]
+        ic = {"lorenz": [0.1, 0.1, 0.1], "rossler": [1.0, 1.0, 1.0], "chen": [-10.0, 0.0, 37.0]}[system]
+        if kind == "bif":
+            mut, rg = {"lorenz": ([1], [20.0, 200.0]), "rossler": ([2], [2.0, 10.0]), "chen": ([2], [20.0, 30.0])}[system]
+            reqs.append((kind, system, dict(tMax=20.0, nPts=N, h=0.01, initialConditions=ic, ranges=rg,
+                                            indicesOfMutVars=mut, writableVar=0, maxValue=1e4, transientTime=20.0,
+                                            values=vals)))
+        elif kind == "lle":
+            mut, rg = {"lorenz": ([1, 0], [20.0, 200.0, 5.0, 15.0]), "rossler": ([0, 2], [0.1, 0.4, 2.0, 10.0]),
+                       "chen": ([2, 0], [20.0, 30.0, 30.0, 40.0])}[system]
+            reqs.append((kind, system, dict(tMax=20.0, NT=0.1, nPts=m, h=0.01, eps=1e-8, initialConditions=ic,
+                                            ranges=rg, indicesOfMutVars=mut, transientTime=20.0, values=vals)))
+        else:
+            icb = {"lorenz": [0.0, 0.0, 27.0], "rossler": [0.0, 0.0, 0.5], "chen": [0.0, 0.0, 20.0]}[system]
+            vb = {"lorenz": [10.0, 24.0, 8 / 3], "rossler": [0.2, 0.2, 5.7], "chen": [35.0, 3.0, 28.0]}[system]
+            reqs.append((kind, system, dict(tMax=20.0, nPts=m, h=0.01, initialConditions=icb,
+                                            ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1],
+                                            writableVar=0, maxValue=1e8, transientTime=20.0, values=vb)))
+    return reqs
+
+
 def job_points_steps(kind, kw):
+    if kind == "basins":
+        return kw["nPts"] ** 2, int(kw["transientTime"] / kw["h"]) + int(kw["tMax"] / kw["h"])
     if kind == "bif":
         return kw["nPts"], int(kw["transientTime"] / kw["h"]) + int(kw["tMax"] / kw["h"])
     ntp = int(kw["NT"] / kw["h"])
@@ -237,8 +273,8 @@ def cpu_sample_sweep(w, kind, target_s=10.0):
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
-    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS, "batch": LLE}[args.workload]
-    fn = (lambda: cpu_sample_lle(w, args.cpu_seconds)) if args.workload in ("lle", "batch") else \
+    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS, "batch": LLE, "serve": LLE}[args.workload]
+    fn = (lambda: cpu_sample_lle(w, args.cpu_seconds)) if args.workload in ("lle", "batch", "serve") else \
         (lambda: cpu_sample_sweep(w, args.workload, args.cpu_seconds))
     vals, last = [], None
     for _ in range(args.steps):
@@ -400,6 +436,86 @@ def batch_arm(args, ws, rank, local):
     if rank == 0:
         print(json.dumps(line), flush=True)
     b.close()
+
+
+def serve_arm(args, ws, rank, local):
+    """Poisson arrivals of the served stream into the request loop; reports
+    p50/p99 latency and aggregate throughput."""
+    import threading
+
+    import chaoslibrary_gb300 as C
+
+    reqs = serve_requests(n=args.requests)
+    rng = np.random.default_rng(11)
+    gaps = rng.exponential(1.0 / args.rate, size=len(reqs))
+    srv = C.Server(hbm_budget_bytes=args.hbm_budget_gb << 30, max_active=256, iteration_steps=args.iteration_steps)
+    # warm-up: one request of each kind (kernel loading), not counted
+    w = [srv.submit_bifurcation1d("lorenz", peakCapacity=4, **serve_requests(n=5)[0][2])]
+    for rid, _ in w:
+        srv.wait(rid)
+    srv.close()
+    srv = C.Server(hbm_budget_bytes=args.hbm_budget_gb << 30, max_active=256, iteration_steps=args.iteration_steps)
+    ids = []
+    lock = threading.Lock()
+    done_lat = []
+
+    def waiter():
+        k = 0
+        while True:
+            with lock:
+                if k >= len(ids):
+                    if len(ids) == len(reqs):
+                        return
+                    rid = None
+                else:
+                    rid = ids[k][0]
+            if rid is None:
+                time.sleep(0.001)
+                continue
+            srv.wait(rid, timeout=3600)
+            done_lat.append(srv.latency(rid))
+            with lock:
+                ids[k] = (rid, None)  # drop the output arrays
+            k += 1
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    with Clocks([local]) as clk:
+        t0 = time.perf_counter()
+        t_next = t0
+        for (kind, system, kw), gap in zip(reqs, gaps):
+            t_next += gap
+            d = t_next - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            if kind == "bif":
+                rid, out = srv.submit_bifurcation1d(system, peakCapacity=4, **kw)
+            elif kind == "lle":
+                rid, out = srv.submit_lle2d(system, **kw)
+            else:
+                rid, out = srv.submit_basins(system, eps=0.05, **kw)
+            with lock:
+                ids.append((rid, out))
+        th.join()
+        wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    total_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in reqs)
+    lat = np.array(done_lat)
+    line = {"metric": METRIC, "value": total_steps / wall, "unit": UNIT, "n_gpus": 1, "steps": len(reqs),
+            "warmup": 1, "ms_per_step": 1e3 * wall / len(reqs), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request stream)",
+            "config": {"workload": f"served stream: {len(reqs)} Poisson requests at {args.rate}/s, 40% 1-D "
+                                   "bifurcation, 40% LLE, 20% basins (+clustering), Lorenz/Rossler/Chen, "
+                                   "1e3..4e6 points, 2000 transient + 2000 recorded steps",
+                       "rate_per_s": args.rate, "requests": len(reqs), "hbm_budget_gb": args.hbm_budget_gb,
+                       "iteration_steps": args.iteration_steps},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "mean": float(lat.mean()), "max": float(lat.max())},
+            "server": st, "clocks": clk.summary(), "total_steps": float(total_steps), "wall_s": wall,
+            "e2e": {"value": total_steps / wall, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": None}}
+    print(json.dumps(line), flush=True)
 
 
 def engine_arm(args, ws, rank, local):
@@ -580,7 +696,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "basins", "batch"])
+    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "basins", "batch", "serve"])
+    ap.add_argument("--requests", type=int, default=2000, help="served stream length")
+    ap.add_argument("--rate", type=float, default=100.0, help="served stream arrival rate (requests/s)")
+    ap.add_argument("--hbm-budget-gb", type=int, default=64)
+    ap.add_argument("--iteration-steps", type=float, default=2e10)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the CPU baseline")
@@ -598,6 +718,9 @@ def main():
         reference_arm(args, ws, rank)
     elif args.workload == "batch":
         batch_arm(args, ws, rank, local)
+    elif args.workload == "serve":
+        if rank == 0:
+            serve_arm(args, ws, rank, local)
     else:
         engine_arm(args, ws, rank, local)
     if ws > 1:

@@ -39,7 +39,8 @@ class Job(C.Structure):
                 ("transientTime", C.c_double), ("values", C.c_void_p), ("preScaller", C.c_int),
                 ("NT", C.c_double), ("eps", C.c_double), ("peakCapacity", C.c_int), ("counts", C.c_void_p),
                 ("flags", C.c_void_p), ("first", C.c_void_p), ("peaks", C.c_void_p), ("intervals", C.c_void_p),
-                ("lle", C.c_void_p), ("avgPeaks", C.c_void_p), ("avgIntervals", C.c_void_p)]
+                ("lle", C.c_void_p), ("avgPeaks", C.c_void_p), ("avgIntervals", C.c_void_p),
+                ("labels", C.c_void_p)]
 
 
 def lib_path() -> Path:
@@ -74,6 +75,13 @@ _SIGS = {
     "chaos_batch_create": ([_P, _P, _I, _P], _I),
     "chaos_batch_run": ([_P], _I),
     "chaos_batch_destroy": ([_P], _I),
+    "chaos_server_create": ([_P, C.c_size_t, _I, _D, _P], _I),
+    "chaos_server_submit": ([_P, _P, _P], _I),
+    "chaos_server_poll": ([_P, C.c_longlong, _P], _I),
+    "chaos_server_wait": ([_P, C.c_longlong, _D, _P], _I),
+    "chaos_server_stats": ([_P, _P, _I], _I),
+    "chaos_server_latency": ([_P, C.c_longlong], _D),
+    "chaos_server_destroy": ([_P], _I),
     "chaos_get_tuning": ([_I], _I),
     "chaos_compat_set_system": ([_I], _I),
     "chaos_compat_set_precision": ([_I], _I),
@@ -303,6 +311,85 @@ class Batch:
         if self._plan is not None:
             lib().chaos_batch_destroy(self._plan)
             self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+REQ_PENDING, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+STATS = ["completed", "failed", "pending", "running", "p50_s", "p99_s", "mean_s", "steps", "elapsed_s",
+         "iterations", "peak_hbm_bytes", "max_s"]
+
+
+class Server:
+    """The request loop (chaos_server_*): submit jobs at any time, wait for
+    them, read latency statistics. Outputs are host numpy arrays filled when a
+    request completes."""
+
+    def __init__(self, hbm_budget_bytes=64 << 30, max_active=1024, iteration_steps=2e10, device=None):
+        ex = Exec(FP32, MEM_HOST, None, -1 if device is None else int(device))
+        self._s = C.c_void_p()
+        _check(lib().chaos_server_create(C.byref(ex), int(hbm_budget_bytes), int(max_active),
+                                         float(iteration_steps), C.byref(self._s)))
+        self._keep = {}
+
+    def _submit(self, job, keep, out):
+        rid = C.c_longlong()
+        _check(lib().chaos_server_submit(self._s, C.byref(job), C.byref(rid)))
+        self._keep[rid.value] = (keep, out)
+        return rid.value
+
+    def submit_bifurcation1d(self, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar,
+                             maxValue, transientTime, values, preScaller=1, peakCapacity=16):
+        b = Batch()
+        out = b.add_bifurcation1d(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar,
+                                  maxValue, transientTime, values, preScaller, peakCapacity)
+        return self._submit(b.jobs[0], b, out), out
+
+    def submit_lle2d(self, system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
+                     transientTime, values):
+        b = Batch()
+        out = b.add_lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
+                          transientTime, values)
+        return self._submit(b.jobs[0], b, out), out
+
+    def submit_basins(self, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar,
+                      maxValue, transientTime, values, preScaller=1, eps=0.05):
+        b = Batch()
+        out = b.add_basins(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar,
+                           maxValue, transientTime, values, preScaller)
+        j = b.jobs[0]
+        if eps and eps > 0:
+            out["labels"] = np.zeros(nPts * nPts, np.int32)
+            j.labels = out["labels"].ctypes.data
+            j.eps = eps
+        return self._submit(j, b, out), out
+
+    def wait(self, rid, timeout=600.0):
+        st = C.c_int()
+        _check(lib().chaos_server_wait(self._s, rid, float(timeout), C.byref(st)))
+        return st.value
+
+    def poll(self, rid):
+        st = C.c_int()
+        _check(lib().chaos_server_poll(self._s, rid, C.byref(st)))
+        return st.value
+
+    def latency(self, rid):
+        return lib().chaos_server_latency(self._s, rid)
+
+    def stats(self):
+        arr = (C.c_double * len(STATS))()
+        _check(lib().chaos_server_stats(self._s, arr, len(STATS)))
+        return dict(zip(STATS, list(arr)))
+
+    def close(self):
+        if self._s:
+            lib().chaos_server_destroy(self._s)
+            self._s = C.c_void_p()
 
     def __del__(self):
         try:

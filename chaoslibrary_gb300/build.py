@@ -26,6 +26,7 @@ SOURCES = [
     ("capi.cu", []),
     ("batch.cu", []),
     ("batch_host.cu", []),
+    ("server.cu", []),
     ("probe.cu", []),
     ("noalloc.cu", []),
     ("compat.cpp", []),

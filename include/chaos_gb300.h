@@ -242,6 +242,7 @@ typedef struct chaos_job {
     double* lle;
     double* avgPeaks;
     double* avgIntervals;
+    int* labels; /* basins in a server: with eps > 0, the reference clustering at completion */
 } chaos_job;
 
 /* Runs the jobs in one persistent launch (chunks ordered longest work first). */
@@ -258,6 +259,43 @@ typedef struct chaos_batch chaos_batch;
 int chaos_batch_create(const chaos_exec* ex, const chaos_job* jobs, int nJobs, chaos_batch** plan);
 int chaos_batch_run(chaos_batch* plan);
 int chaos_batch_destroy(chaos_batch* plan);
+
+/*
+ * Serving (no reference counterpart): a request loop on one GPU. Requests
+ * (chaos_job, any kind) are admitted first-come-first-served while their
+ * device memory fits the HBM budget and fewer than maxActive are resident;
+ * their parameters and partial results stay on the device until they are
+ * complete. A scheduler thread runs iterations: each takes block-sized
+ * chunks from the resident requests in arrival order up to a work budget
+ * (iterationSteps trajectory-steps), so requests that arrive while others
+ * run join the next iteration (continuous batching); two iterations are in
+ * flight at a time on two streams. A completion thread copies results back
+ * (host-memory servers), runs the basins clustering for jobs that ask for it,
+ * and records latency (submit -> results ready). A result is bit-identical to
+ * the same job run alone (the same device function computes every point).
+ */
+typedef struct chaos_server chaos_server;
+#define CHAOS_REQ_PENDING 0 /* waiting for admission */
+#define CHAOS_REQ_RUNNING 1
+#define CHAOS_REQ_DONE 2
+#define CHAOS_REQ_FAILED 3
+int chaos_server_create(const chaos_exec* ex, size_t hbmBudgetBytes, int maxActive, double iterationSteps,
+                        chaos_server** server);
+/* Copies the job's parameters; its output arrays must stay valid until the request is done. */
+int chaos_server_submit(chaos_server* server, const chaos_job* job, long long* requestId);
+int chaos_server_poll(chaos_server* server, long long requestId, int* state);
+/* Waits at most timeoutSeconds; CHAOS_E_TIMEOUT when the request is not done by then. */
+int chaos_server_wait(chaos_server* server, long long requestId, double timeoutSeconds, int* state);
+/*
+ * stats[0..11] = completed, failed, pending, running, p50 latency (s), p99 latency (s),
+ * mean latency (s), trajectory-steps completed, seconds since the first submission,
+ * iterations launched, peak HBM bytes in use, max latency (s).
+ */
+int chaos_server_stats(chaos_server* server, double* stats, int n);
+/* Latency (s) of a completed request, -1 otherwise. */
+double chaos_server_latency(chaos_server* server, long long requestId);
+/* Stops admitting, finishes the resident requests, fails the pending ones, frees everything. */
+int chaos_server_destroy(chaos_server* server);
 
 /*
  * chaos_point_dbscan without any allocation. No counterpart in the reference:

@@ -342,3 +342,76 @@ def test_batch_equals_single_jobs(engine, mode):
                 for k in ("flags", "avg_peaks", "avg_intervals", "counts"):
                     assert np.array_equal(got[k], ref[k]), k
     b.close()
+
+
+def test_server_results_equal_alone(engine):
+    """Requests served concurrently (continuous batching, staggered arrivals,
+    several iterations in flight) give exactly the results of the same jobs
+    run alone, including the basins clustering."""
+    import time
+
+    srv = engine.Server(hbm_budget_bytes=1 << 30, max_active=8, iteration_steps=2e8)
+    reqs = []
+    for i, (kind, system, kw) in enumerate(_batch_jobs() * 2):
+        if kind == "bif":
+            rid, out = srv.submit_bifurcation1d(system, peakCapacity=32, **kw)
+        elif kind == "lle":
+            rid, out = srv.submit_lle2d(system, **kw)
+        else:
+            rid, out = srv.submit_basins(system, eps=0.05, **kw)
+        reqs.append((rid, kind, system, kw, out))
+        if i % 3 == 0:
+            time.sleep(0.002)
+    for rid, *_ in reqs:
+        assert srv.wait(rid, timeout=120) == engine._native.REQ_DONE
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["p99_s"] >= st["p50_s"] > 0
+    for rid, kind, system, kw, got in reqs:
+        if kind == "bif":
+            ref = engine.bifurcation1d(system, precision=engine.FP32, peakCapacity=32, **kw)
+            assert np.array_equal(got["counts"], ref["counts"])
+            for r, c in enumerate(ref["counts"]):
+                m = min(int(c), 32)
+                assert np.array_equal(got["peaks"][r, :m], ref["peaks"][r, :m])
+        elif kind == "lle":
+            ref = engine.lle2d(system, precision=engine.FP32, **kw)
+            assert np.array_equal(got["lle"], ref, equal_nan=True)
+        else:
+            ref = engine.basins(system, precision=engine.FP32, eps=0.05, **kw)
+            assert np.array_equal(got["avg_peaks"], ref["avg_peaks"])
+            assert np.array_equal(got["labels"], ref["labels"])
+    srv.close()
+
+
+def test_server_bounded_wait_times_out(engine):
+    """A wait shorter than the request's run returns CHAOS_E_TIMEOUT (the host
+    gives up, the GPU keeps working) and a later wait sees it done."""
+    srv = engine.Server(max_active=2, iteration_steps=1e8)
+    rid, out = srv.submit_lle2d("lorenz", tMax=200.0, NT=0.1, nPts=256, h=0.01, eps=1e-8,
+                                initialConditions=[0.1, 0.1, 0.1], ranges=[20.0, 60.0, 5.0, 15.0],
+                                indicesOfMutVars=[1, 0], transientTime=10.0, values=[10.0, 28.0, 8 / 3])
+    with pytest.raises(engine.ChaosError) as e:
+        srv.wait(rid, timeout=1e-4)
+    assert e.value.code == -5
+    assert srv.wait(rid, timeout=300) == engine._native.REQ_DONE
+    assert np.isfinite(out["lle"]).mean() > 0.99
+    srv.close()
+
+
+def test_server_budget_admission(engine):
+    """With an HBM budget smaller than the sum of the requests, admission
+    queues them and the peak device footprint stays within the budget."""
+    budget = 4 << 20
+    srv = engine.Server(hbm_budget_bytes=budget, max_active=64, iteration_steps=5e7)
+    rids = []
+    for k in range(12):
+        rid, _ = srv.submit_lle2d("rossler", tMax=5.0, NT=0.1, nPts=300, h=0.01, eps=1e-8,
+                                  initialConditions=[1.0, 1.0, 1.0], ranges=[0.1, 0.4, 2.0, 10.0],
+                                  indicesOfMutVars=[0, 2], transientTime=1.0, values=[0.2, 0.2, 5.7])
+        rids.append(rid)
+    for rid in rids:
+        assert srv.wait(rid, timeout=120) == engine._native.REQ_DONE
+    st = srv.stats()
+    assert st["peak_hbm_bytes"] <= budget
+    srv.close()
