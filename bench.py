@@ -449,8 +449,16 @@ def serve_arm(args, ws, rank, local):
     rng = np.random.default_rng(11)
     gaps = rng.exponential(1.0 / args.rate, size=len(reqs))
     srv = C.Server(hbm_budget_bytes=args.hbm_budget_gb << 30, max_active=256, iteration_steps=args.iteration_steps)
-    # warm-up: one request of each kind (kernel loading), not counted
-    w = [srv.submit_bifurcation1d("lorenz", peakCapacity=4, **serve_requests(n=5)[0][2])]
+    # warm-up: a small request of each kind and system (kernel loading), not counted
+    w = []
+    for kind, system, kw in serve_requests(n=60):
+        kw = dict(kw, nPts=min(kw["nPts"], 1000 if kind == "bif" else 32))
+        if kind == "bif":
+            w.append(srv.submit_bifurcation1d(system, peakCapacity=4, **kw))
+        elif kind == "lle":
+            w.append(srv.submit_lle2d(system, **kw))
+        else:
+            w.append(srv.submit_basins(system, eps=0.05, **kw))
     for rid, _ in w:
         srv.wait(rid)
     srv.close()

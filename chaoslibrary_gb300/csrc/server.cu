@@ -110,7 +110,7 @@ bool admit_locked(chaos_server* S) {
     bool any = false;
     while (!S->pending.empty() && !S->freeSlots.empty()) {
         Request* r = S->pending.front();
-        if (S->used + r->bytes > S->budget && !S->active.empty()) break;  // a lone request may use it all
+        if (S->used + r->bytes > S->budget && S->used > 0) break;  // a request alone on the device may exceed it
         void* block = nullptr;
         if (r->bytes && cudaMallocFromPoolAsync(&block, r->bytes, S->pool, S->setup) != cudaSuccess) break;
         S->pending.pop_front();
