@@ -6,8 +6,8 @@
 // HBM budget and maxActive) and launches iterations; a completion thread
 // copies finished requests back, runs the basins clustering when asked, frees
 // their memory and records latency. An iteration is a list of block-sized
-// chunks taken first-come-first-served from the resident requests up to a
-// work budget, run by the grouped persistent kernels of batched mode; two
+// chunks shared fairly among the resident requests up to a work budget, run
+// by the grouped persistent kernels of batched mode; two
 // iterations are in flight on two streams, so new requests enter the next
 // iteration while the current one runs. All waits on the host are bounded.
 #include <cuda_runtime.h>
@@ -142,24 +142,37 @@ bool admit_locked(chaos_server* S) {
     return any;
 }
 
-// Chunks of this iteration, first-come-first-served up to the work budget
-// (called with mu held).
-void take_chunks_locked(chaos_server* S, Iteration& I, std::vector<JobDesc>& descs, std::vector<Chunk>& chunks) {
+// Chunks of this iteration (called with mu held): first every resident
+// request with points left gets an equal share of the work budget (at least
+// one chunk), in admission order; what is left of the budget then goes to
+// the oldest requests first. Small requests therefore finish within a few
+// iterations even while large ones are resident (processor sharing).
+void take_chunks_locked(chaos_server* S, Iteration& I, std::vector<Chunk>& chunks) {
     I.work.clear();
+    int waiting = 0;
+    for (Request* r : S->active)
+        if (r->next < r->nPoints) ++waiting;
+    if (!waiting) return;
     double budget = S->iterationSteps;
-    for (Request* r : S->active) {
-        if (budget <= 0) break;
-        long long taken = 0;
-        while (r->next < r->nPoints && budget > 0) {
+    const double share = budget / waiting;
+    std::vector<long long> taken(S->active.size(), 0);
+    auto take = [&](size_t idx, double limit) {
+        Request* r = S->active[idx];
+        double used = 0;
+        while (r->next < r->nPoints && used < limit && budget > 0) {
             const int cnt = (int)std::min<long long>(r->chunk, r->nPoints - r->next);
             chunks.push_back(Chunk{r->slot, cnt, r->next});
             r->next += cnt;
-            taken += cnt;
-            budget -= (double)cnt * (double)r->perPoint;
+            taken[idx] += cnt;
+            const double w = (double)cnt * (double)r->perPoint;
+            used += w;
+            budget -= w;
         }
-        if (taken) I.work.push_back({r, taken});
-    }
-    (void)descs;
+    };
+    for (size_t i = 0; i < S->active.size() && budget > 0; ++i) take(i, share);
+    for (size_t i = 0; i < S->active.size() && budget > 0; ++i) take(i, budget);
+    for (size_t i = 0; i < S->active.size(); ++i)
+        if (taken[i]) I.work.push_back({S->active[i], taken[i]});
 }
 
 // Marks an iteration's work finished; hands completed requests over.
@@ -221,7 +234,6 @@ void scheduler_main(chaos_server* S) {
     cudaSetDevice(S->device);
     int k = 0;
     std::vector<Chunk> chunks;
-    std::vector<JobDesc> descs;
     std::vector<Request*> slotOwner(S->maxActive, nullptr);
     for (;;) {
         Iteration& I = S->it[k & 1];
@@ -236,7 +248,7 @@ void scheduler_main(chaos_server* S) {
             std::unique_lock<std::mutex> lk(S->mu);
             admit_locked(S);
             for (Request* r : S->active) slotOwner[r->slot] = r;
-            take_chunks_locked(S, I, descs, chunks);
+            take_chunks_locked(S, I, chunks);
             if (chunks.empty()) {
                 if (other.busy) drainOther = true;
                 else if (S->stop && S->active.empty()) quit = true;

@@ -266,10 +266,11 @@ int chaos_batch_destroy(chaos_batch* plan);
  * device memory fits the HBM budget and fewer than maxActive are resident;
  * their parameters and partial results stay on the device until they are
  * complete. A scheduler thread runs iterations: each takes block-sized
- * chunks from the resident requests in arrival order up to a work budget
- * (iterationSteps trajectory-steps), so requests that arrive while others
- * run join the next iteration (continuous batching); two iterations are in
- * flight at a time on two streams. A completion thread copies results back
+ * chunks from the resident requests up to a work budget (iterationSteps
+ * trajectory-steps), first an equal share for every request with work left,
+ * then the rest oldest-first, so requests that arrive while others run join
+ * the next iteration (continuous batching) and small requests are not held
+ * behind large ones; two iterations are in flight at a time on two streams. A completion thread copies results back
  * (host-memory servers), runs the basins clustering for jobs that ask for it,
  * and records latency (submit -> results ready). A result is bit-identical to
  * the same job run alone (the same device function computes every point).
