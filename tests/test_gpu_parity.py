@@ -415,3 +415,80 @@ def test_server_budget_admission(engine):
     st = srv.stats()
     assert st["peak_hbm_bytes"] <= budget
     srv.close()
+
+
+def _csv_matrix(values, nPts, fmt):
+    """The reference's matrix rule: ', ' before every value but the first and
+    '\\n' (after the ', ') whenever nPts values are on the line."""
+    out, counter = [], 0
+    for v in values:
+        if counter != 0:
+            out.append(", ")
+        if counter == nPts:
+            out.append("\n")
+            counter = 0
+        out.append(fmt(v))
+        counter += 1
+    return "".join(out)
+
+
+def _g(p):
+    return lambda v: ("%." + str(p) + "g") % v
+
+
+def test_compat_csv_bytes(engine, oracle, tmp_path):
+    """The reference-signature wrappers write the reference's CSV bytes:
+    bifurcation1D rows at precision 12 after a precision-6 header,
+    bifurcation2D / LLE2D matrices, basins' four files at precision 15."""
+    L = engine
+    L.set_system("lorenz")
+    vals = np.array([10.0, 28.0, 8 / 3])
+    # 1-D bifurcation
+    p = tmp_path / "bif1d.csv"
+    L.Bifurcation.bifurcation1D(20.0, 40, 0.01, 3, [0.1, 0.1, 0.1], [20.0, 200.0], [1], 0, 1e4, 10.0, vals, 3, 1, p)
+    o = oracle.bifurcation(0, 1, 20.0, 40, 0.01, [0.1, 0.1, 0.1], [20.0, 200.0], [1], 0, 1e4, 10.0, vals)
+    lines = ["%g %g\n" % (20.0, 200.0)]
+    for k in range(40):
+        par = 20.0 + k * ((200.0 - 20.0) / 39)
+        if o["counts"][k] == -1:
+            lines.append("%.12g, %.12g, 0\n" % (par, o["first"][k]))
+        for j in range(max(o["counts"][k], 0)):
+            lines.append("%.12g, %.12g, %.12g\n" % (par, o["peaks"][k, j], o["intervals"][k, j]))
+    assert p.read_text() == "".join(lines)
+    # 2-D bifurcation
+    p = tmp_path / "bif2d.csv"
+    L.Bifurcation.bifurcation2D(5.0, 9, 0.01, 3, [0.1, 0.1, 0.1], [20.0, 200.0, 5.0, 15.0], [1, 0], 0, 1e4, 5.0,
+                                vals, 3, 1, 0.05, p)
+    o = oracle.bifurcation(0, 2, 5.0, 9, 0.01, [0.1, 0.1, 0.1], [20.0, 200.0, 5.0, 15.0], [1, 0], 0, 1e4, 5.0, vals,
+                           eps=0.05)
+    expect = "20 200\n5 15\n" + _csv_matrix(o["labels"], 9, str)
+    assert p.read_text() == expect
+    # LLE (values at the default precision 6, NaN printed as 0)
+    L.set_system("rossler")
+    p = tmp_path / "lle.csv"
+    L.LLE.LLE2D(20.0, 0.1, 7, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, [0.1, 0.4, 2.0, 10.0], [0, 2], 0, 0.0, 5.0,
+                [0.2, 0.2, 5.7], 3, p)
+    o = oracle.lle2d(1, 20.0, 0.1, 7, 0.01, 1e-8, [1.0, 1.0, 1.0], [0.1, 0.4, 2.0, 10.0], [0, 2], 5.0,
+                     [0.2, 0.2, 5.7])
+    expect = "0.1 0.4\n2 10\n" + _csv_matrix(np.nan_to_num(o, nan=0.0), 7, _g(6))
+    got = p.read_text()
+    # values agree to the printed digits except where the last FP64 bit of log differs
+    assert got.count("\n") == expect.count("\n") and got.split("\n")[:2] == expect.split("\n")[:2]
+    g_cells = [c.strip() for c in got.split("\n", 2)[2].replace("\n", "").split(",")]
+    e_cells = [c.strip() for c in expect.split("\n", 2)[2].replace("\n", "").split(",")]
+    assert len(g_cells) == len(e_cells) == 49
+    assert sum(a != b for a, b in zip(g_cells, e_cells)) <= 1
+    # basins: four files, precision 15
+    L.set_system("lorenz")
+    base = tmp_path / "bas"
+    kw = (4.0, 12, 0.01, 3, [0.0, 0.0, 27.0], [-30.0, 30.0, -30.0, 30.0], [0, 1], 0, 1e8, 10.0,
+          [10.0, 24.0, 8 / 3], 3, 1, 0.05)
+    L.Basins.basinsOfAttraction_2(*kw, base)
+    f = oracle.basins_features(0, 4.0, 12, 0.01, [0.0, 0.0, 27.0], [-30.0, 30.0, -30.0, 30.0], [0, 1], 0, 1e8, 10.0,
+                               [10.0, 24.0, 8 / 3])
+    lab = oracle.dbscan_compat(f["avg_peaks"], f["avg_intervals"], f["flags"], 0.05)
+    head = "-30 30\n-30 30\n"
+    assert (tmp_path / "bas").read_text() == head + _csv_matrix(lab, 12, str)
+    assert (tmp_path / "bas_1.csv").read_text() == head + _csv_matrix(f["avg_peaks"], 12, _g(15))
+    assert (tmp_path / "bas_2.csv").read_text() == head + _csv_matrix(f["avg_intervals"], 12, _g(15))
+    assert (tmp_path / "bas_3.csv").read_text() == head + _csv_matrix(f["flags"], 12, str)
