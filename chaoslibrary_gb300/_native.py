@@ -13,7 +13,7 @@ FP64, FP32 = 0, 1
 CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
 MEM_HOST, MEM_DEVICE = 0, 1
 SYSTEMS = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "rossler_cd": 4, "sin3": 5, "sin2": 6,
-           "memristor": 7}
+           "memristor": 7, "user": 15}
 STATUS = {0: "CHAOS_OK", -1: "CHAOS_E_ARGS", -2: "CHAOS_E_NOMEM", -3: "CHAOS_E_CUDA", -4: "CHAOS_E_IO",
           -5: "CHAOS_E_TIMEOUT", -6: "CHAOS_E_UNSUPPORTED", -7: "CHAOS_E_BUSY", -8: "CHAOS_E_NODEV"}
 

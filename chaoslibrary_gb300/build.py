@@ -51,16 +51,29 @@ def up_to_date() -> bool:
     return all(d.stat().st_mtime <= t for d in _deps())
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, user_systems: str | None = None, lib: Path | None = None,
+          build_dir: Path | None = None) -> Path:
+    """Builds the library. user_systems (or the environment variable
+    CHAOS_USER_SYSTEMS) names a reference-format systems.cuh plug-in header to
+    compile in as system CHAOS_SYS_USER; lib / build_dir redirect the output."""
+    user_systems = user_systems or os.environ.get("CHAOS_USER_SYSTEMS")
+    out = Path(lib).resolve() if lib else LIB
+    bdir = Path(build_dir) if build_dir else BUILD
+    if not force and out == LIB and not user_systems and up_to_date():
         return LIB
-    BUILD.mkdir(exist_ok=True)
-    LIBDIR.mkdir(exist_ok=True)
+    bdir.mkdir(parents=True, exist_ok=True)
+    out.parent.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
     procs = []
     objs = []
-    for src, extra in SOURCES:
-        obj = BUILD / (src + ".o")
+    sources = list(SOURCES)
+    if user_systems:
+        hdr = Path(user_systems).resolve()
+        sources.append(("kern_user.cu", ["--fmad=false", f'-DCHAOS_USER_SYSTEM_HEADER="{hdr}"', f"-I{hdr.parent}"]))
+    else:
+        sources.append(("user_stub.cu", []))
+    for src, extra in sources:
+        obj = bdir / (src + ".o")
         objs.append(obj)
         cmd = [cc, *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
         if src.endswith(".cpp"):
@@ -70,20 +83,20 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     failed = []
     for src, p in procs:
-        out, _ = p.communicate()
+        log, _ = p.communicate()
         if p.returncode != 0:
-            failed.append(f"--- {src}\n{out}")
-        elif verbose and out.strip():
-            print(out)
+            failed.append(f"--- {src}\n{log}")
+        elif verbose and log.strip():
+            print(log)
     if failed:
         raise RuntimeError("nvcc failed:\n" + "\n".join(failed))
-    tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+    tmp = out.with_suffix(f".{os.getpid()}.tmp")
     link = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     if verbose:
         print(" ".join(link), flush=True)
     subprocess.run(link, check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, out)
+    return out
 
 
 if __name__ == "__main__":

@@ -42,6 +42,8 @@ int prepare_job(const chaos_job& j, int memory, JobDesc& J, std::vector<HostOut>
         if (d) outs.push_back({user, d, bytes});
         return d;
     };
+    if (j.system == SYS_USER)
+        return set_error(CHAOS_E_UNSUPPORTED, "batched and served jobs use the built-in systems");
     const int nx = system_supported(j.system) ? system_nx(j.system) : 0;
     const int na = system_supported(j.system) ? system_na(j.system) : 0;
     int rc;

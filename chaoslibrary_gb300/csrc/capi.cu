@@ -165,15 +165,42 @@ void* Call::output(void* user, size_t bytes) {
 // ---------------------------------------------------------------------------
 // argument checks shared by the sweeps
 
+static void sizes_of(int system, int* nx, int* na) {
+    if (system == SYS_USER) {
+        user_system_sizes(nx, na);
+    } else {
+        *nx = system_nx(system);
+        *na = system_na(system);
+    }
+}
+
 static int check_system(int system, int nIC, int nValues) {
+    if (system == SYS_USER && !user_system_available())
+        return set_error(CHAOS_E_UNSUPPORTED, "this build has no user plug-in (CHAOS_USER_SYSTEMS at build time)");
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
-    if (nIC != system_nx(system))
-        return set_error(CHAOS_E_ARGS, "amountOfInitialConditions %d != SIZE_X %d of system %d", nIC,
-                         system_nx(system), system);
-    if (nValues != system_na(system))
-        return set_error(CHAOS_E_ARGS, "amountOfValues %d != SIZE_A %d of system %d", nValues, system_na(system),
-                         system);
+    int nx, na;
+    sizes_of(system, &nx, &na);
+    if (nx > kMaxState || na > kMaxParams)
+        return set_error(CHAOS_E_UNSUPPORTED, "plug-in sizes %d/%d exceed %d/%d", nx, na, kMaxState, kMaxParams);
+    if (nIC != nx)
+        return set_error(CHAOS_E_ARGS, "amountOfInitialConditions %d != SIZE_X %d of system %d", nIC, nx, system);
+    if (nValues != na)
+        return set_error(CHAOS_E_ARGS, "amountOfValues %d != SIZE_A %d of system %d", nValues, na, system);
     return CHAOS_OK;
+}
+
+// precision / plug-in dispatch of the sweep kernels
+static cudaError_t run_bif(int prec, const SweepParams& P, const BifOut& O, cudaStream_t st) {
+    if (P.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_bif_user(P, O, st);
+    return prec == CHAOS_FP32 ? launch_bif_f32(P, O, st) : launch_bif_f64(P, O, st);
+}
+static cudaError_t run_basins(int prec, const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
+    if (P.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_basins_user(P, O, st);
+    return prec == CHAOS_FP32 ? launch_basins_f32(P, O, st) : launch_basins_f64(P, O, st);
+}
+static cudaError_t run_lle(int prec, const LleParams& L, double* out, cudaStream_t st) {
+    if (L.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_lle_user(L, out, st);
+    return prec == CHAOS_FP32 ? launch_lle_f32(L, out, st) : launch_lle_f64(L, out, st);
 }
 
 int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, double h, int nIC, const double* ic,
@@ -273,9 +300,13 @@ int chaos_abi_version(void) { return CHAOS_ABI_VERSION; }
 const char* chaos_last_error(void) { return g_err.c_str(); }
 
 int chaos_system_info(int system, int* sizeX, int* sizeA) {
+    if (system == SYS_USER && !user_system_available())
+        return set_error(CHAOS_E_UNSUPPORTED, "this build has no user plug-in");
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
-    if (sizeX) *sizeX = system_nx(system);
-    if (sizeA) *sizeA = system_na(system);
+    int nx, na;
+    sizes_of(system, &nx, &na);
+    if (sizeX) *sizeX = nx;
+    if (sizeA) *sizeA = na;
     return CHAOS_OK;
 }
 
@@ -313,7 +344,7 @@ int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts,
     O.peaks = (double*)c.output(peaks, rowBytes);
     O.intervals = (double*)c.output(intervals, rowBytes);
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_bif_f32(P, O, c.stream) : launch_bif_f64(P, O, c.stream);
+    cudaError_t e = run_bif(c.ex.precision, P, O, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation kernel"));
     rc = c.to_host(counts, O.counts, n * sizeof(int));
     if (!rc) rc = c.to_host(flags, O.flags, n * sizeof(int));
@@ -355,7 +386,7 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
         Q.pBegin = b;
         Q.nPoints = std::min(chunk, n - b);
         BifOut O{dCounts + b, dFlags, nullptr, nullptr, dIv, cap};
-        cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_bif_f32(Q, O, c.stream) : launch_bif_f64(Q, O, c.stream);
+        cudaError_t e = run_bif(c.ex.precision, Q, O, c.stream);
         if (e == cudaSuccess)
             e = launch_point_dbscan(dIv, dCounts + b, Q.nPoints, cap, eps, dLab, dSlot, dLabels + b, c.stream);
         if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation 2-D kernels"));
@@ -377,13 +408,13 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
                        indicesOfMutVars, transientTime, values, amountOfValues)))
         return rc;
-    if (ex && ex->precision == CHAOS_FP32 && !system_has_difference_form(system))
+    if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_difference_form(system)))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
     Call c;
     if ((rc = c.begin(ex))) return rc;
     double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_lle_f32(L, dOut, c.stream) : launch_lle_f64(L, dOut, c.stream);
+    cudaError_t e = run_lle(c.ex.precision, L, dOut, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "LLE kernel"));
     rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
     return c.finish(rc);
@@ -410,7 +441,7 @@ int chaos_basins_features(const chaos_exec* ex, int system, double tMax, int nPt
     O.counts = (int*)c.output(counts, n * sizeof(int));
     O.last = nullptr;
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
+    cudaError_t e = run_basins(c.ex.precision, P, O, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "basins kernel"));
     rc = c.to_host(flags, O.flags, n * sizeof(int));
     if (!rc) rc = c.to_host(avgPeaks, O.avgPeaks, n * sizeof(double));
@@ -441,7 +472,7 @@ int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double
     O.last = nullptr;
     int* dLabels = (int*)c.output(labels, n * sizeof(int));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
+    cudaError_t e = run_basins(c.ex.precision, P, O, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "basins kernel"));
     rc = dbscan_compat_device(c, O.avgPeaks, O.avgIntervals, O.flags, n, eps, dLabels);
     if (!rc) rc = c.to_host(labels, dLabels, n * sizeof(int));
@@ -478,7 +509,7 @@ int chaos_basins_dbscan(const chaos_exec* ex, int system, double tMax, int nPts,
     double* minmax = (double*)c.alloc(6 * sizeof(double));
     int* dLabels = (int*)c.output(labels, n * sizeof(int));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_basins_f32(P, O, c.stream) : launch_basins_f64(P, O, c.stream);
+    cudaError_t e = run_basins(c.ex.precision, P, O, c.stream);
     if (e == cudaSuccess) e = launch_basin_feature_matrix(O, n, minmax, F, mask, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "basins feature kernels"));
     rc = dbscan_device(c, F, n, 3, eps, minPts, mask, dLabels);
@@ -582,6 +613,8 @@ int chaos_get_tuning(int knob) {
 
 int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const double* x0, const double* a, double h,
                      int nSteps, double* out) {
+    if (system == SYS_USER && !user_system_available())
+        return set_error(CHAOS_E_UNSUPPORTED, "this build has no user plug-in");
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
     if (nTraj < 0 || nSteps < 0 || !(h == h) || (nTraj > 0 && (!x0 || !a || !out)))
         return set_error(CHAOS_E_ARGS, "bad trajectory arguments");
@@ -589,14 +622,20 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
     int rc = c.begin(ex);
     if (rc) return rc;
     if (nTraj == 0) return c.finish(CHAOS_OK);
-    const int nx = system_nx(system), na = system_na(system);
+    int nx, na;
+    sizes_of(system, &nx, &na);
     const size_t outBytes = (size_t)nTraj * (nSteps + 1) * nx * sizeof(double);
     const double* dX = (const double*)c.input(x0, (size_t)nTraj * nx * sizeof(double));
     const double* dA = (const double*)c.input(a, (size_t)nTraj * na * sizeof(double));
     double* dO = (double*)c.output(out, outBytes);
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = c.ex.precision == CHAOS_FP32 ? launch_trajectory_f32(system, dX, dA, h, nSteps, dO, nTraj, c.stream)
-                                                 : launch_trajectory_f64(system, dX, dA, h, nSteps, dO, nTraj, c.stream);
+    cudaError_t e;
+    if (system == SYS_USER)
+        e = c.ex.precision == CHAOS_FP32 ? cudaErrorNotSupported
+                                         : launch_trajectory_user(dX, dA, h, nSteps, dO, nTraj, c.stream);
+    else
+        e = c.ex.precision == CHAOS_FP32 ? launch_trajectory_f32(system, dX, dA, h, nSteps, dO, nTraj, c.stream)
+                                         : launch_trajectory_f64(system, dX, dA, h, nSteps, dO, nTraj, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "trajectory kernel"));
     rc = c.to_host(out, dO, outBytes);
     return c.finish(rc);

@@ -25,6 +25,7 @@ int parse_system(const char* s) {
     static const char* names[] = {"lorenz", "rossler", "chen", "chameleon", "rossler_cd", "sin3", "sin2", "memristor"};
     for (int i = 0; i < 8; ++i)
         if (strcmp(s, names[i]) == 0) return i;
+    if (strcmp(s, "user") == 0) return CHAOS_SYS_USER;
     char* end = nullptr;
     long v = strtol(s, &end, 10);
     return (end && *end == 0) ? (int)v : CHAOS_SYS_CHAMELEON;
@@ -73,7 +74,8 @@ template <class T, class F> void write_matrix(std::ofstream& o, const T* v, long
 extern "C" {
 
 int chaos_compat_set_system(int system) {
-    if (system < 0 || system > CHAOS_SYS_MEMRISTOR) return chaos::set_error(CHAOS_E_ARGS, "unknown system %d", system);
+    if ((system < 0 || system > CHAOS_SYS_MEMRISTOR) && system != CHAOS_SYS_USER)
+        return chaos::set_error(CHAOS_E_ARGS, "unknown system %d", system);
     g_system = system;
     return CHAOS_OK;
 }

@@ -23,6 +23,12 @@ template <int S> struct Traits {
     static constexpr int NA = (S == SYS_CHAMELEON) ? 7 : (S == SYS_ROSSLER_CD) ? 4 : (S == SYS_SIN3) ? 5
                             : (S == SYS_SIN2 || S == SYS_MEMRISTOR) ? 2 : 3;
 };
+#if defined(CHAOS_USER_SYSTEM)
+template <> struct Traits<SYS_USER> {
+    static constexpr int NX = CHAOS_USER_NX;
+    static constexpr int NA = CHAOS_USER_NA;
+};
+#endif
 
 // Swept value of grid dimension d for linear point index p (the reference's
 // getValueByIdx, bifurcationCUDA.cu:400-419 / basinsCUDA.cu:185-189):

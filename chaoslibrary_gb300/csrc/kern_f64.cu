@@ -148,7 +148,9 @@ __global__ void point_dbscan_kernel(const double* __restrict__ intervals, const 
 
 }  // namespace
 
-bool system_supported(int system) { return system >= 0 && system < SYS_COUNT; }
+bool system_supported(int system) {
+    return (system >= 0 && system < SYS_COUNT) || (system == SYS_USER && user_system_available());
+}
 int launch_block_size() { return kBlock; }
 
 cudaError_t launch_bif_f64(const SweepParams& P, const BifOut& O, cudaStream_t st) {

@@ -98,6 +98,16 @@ cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double*
 int set_lle_variant(int v);
 int get_lle_variant();
 
+// The build-time user plug-in (kern_user.cu, or user_stub.cu when the build
+// has none): FP64 kernels of system SYS_USER.
+bool user_system_available();
+void user_system_sizes(int* nx, int* na);
+cudaError_t launch_bif_user(const SweepParams& P, const BifOut& O, cudaStream_t st);
+cudaError_t launch_basins_user(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
+cudaError_t launch_lle_user(const LleParams& L, double* out, cudaStream_t st);
+cudaError_t launch_trajectory_user(const double* x0, const double* a0, double h, int nSteps, double* out,
+                                   long long n, cudaStream_t st);
+
 bool system_supported(int system);
 int launch_block_size();  // threads per block of the sweep kernels
 

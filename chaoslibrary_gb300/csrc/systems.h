@@ -267,6 +267,12 @@ template <class T> CHAOS_HD void memristor_step(T* X, const T* a, T h) {
     X[2] = t + h;
 }
 
+#if defined(CHAOS_USER_SYSTEM)
+// The step of a reference-format plug-in header compiled into this build
+// (kern_user.cu): CALC_DISCRETE_MODEL(X, a, h) on doubles.
+template <class T> __device__ void user_step(T* x, const T* a, T h);
+#endif
+
 // Per-launch step constants: the RK4 fractions of h for systems 0-2, plain h otherwise.
 template <class T> struct StepCtx {
     RK4H<T> rk;
@@ -284,6 +290,9 @@ template <int S, class T> CHAOS_HD void step(T* x, const T* a, const StepCtx<T>&
     else if (S == SYS_SIN3) sin3_step(x, a, c.rk.h);
     else if (S == SYS_SIN2) sin2_step(x, a, c.rk.h);
     else if (S == SYS_MEMRISTOR) memristor_step(x, a, c.rk.h);
+#if defined(CHAOS_USER_SYSTEM)
+    else if (S == SYS_USER) user_step(x, a, c.rk.h);
+#endif
 }
 
 // Runtime-dispatched step (host checker, tests).

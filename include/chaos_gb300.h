@@ -53,6 +53,9 @@ extern "C" {
 #define CHAOS_SYS_SIN3 5        /* reference systems/systems.cuh:67-83 (USE_SYSTEM_FOR_BASINS) */
 #define CHAOS_SYS_SIN2 6        /* reference systems/systems.cuh:85-101 (USE_SYSTEM_FOR_BASINS_2) */
 #define CHAOS_SYS_MEMRISTOR 7   /* reference systems/systems.cuh:103-178 (USE_DAMIR_SYSTEM) */
+/* A reference-format plug-in header (SIZE_X, SIZE_A, CALC_DISCRETE_MODEL; systems/systems.cuh:12-38)
+   compiled in at build time (CHAOS_USER_SYSTEMS=<header>); FP64 single sweeps only. */
+#define CHAOS_SYS_USER 15
 
 typedef struct chaos_exec {
     int precision; /* CHAOS_FP64 or CHAOS_FP32 */
