@@ -603,11 +603,13 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
 int chaos_set_tuning(int knob, int value) {
     if (knob == CHAOS_TUNE_LLE_F32_VARIANT)
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
+    if (knob == CHAOS_TUNE_SWEEP_PAIRS) return set_sweep_pairs(value);
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 
 int chaos_get_tuning(int knob) {
     if (knob == CHAOS_TUNE_LLE_F32_VARIANT) return get_lle_variant();
+    if (knob == CHAOS_TUNE_SWEEP_PAIRS) return sweep_pairs() ? 1 : 0;
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 

@@ -446,6 +446,191 @@ __device__ __forceinline__ void lle_pair_twin(const LleParams& L, long long p, l
 }
 
 // ---------------------------------------------------------------------------
+// Two bifurcation / basins points per thread in packed FP32x2 lanes (RK4
+// systems). Each lane keeps its own flag, peak detector and outputs and
+// follows exactly the scalar FP32 path: a lane that diverges stops recording
+// while the pair keeps stepping (its state is then ignored), and the loop
+// ends when neither lane is recording.
+__device__ __forceinline__ float lane(const P2& v, int l) { return l ? v.v.y : v.v.x; }
+
+template <int NX> __device__ __forceinline__ P2 pick2(const P2* x, int wv) {
+    P2 v = x[0];
+#pragma unroll
+    for (int j = 1; j < NX; ++j)
+        if (j == wv) v = x[j];
+    return v;
+}
+
+// sqrtf(fabsf(sum (x - xp)^2)) < 1e-9 per lane, as bif_fixed<NX, float>
+template <int NX> __device__ __forceinline__ bool bif_fixed_lane(const P2* x, const P2* xp, int l) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < NX; ++j) {
+        const float d = lane(x[j], l) - lane(xp[j], l);
+        s = s + d * d;
+    }
+    return (double)sqrtf(fabsf(s)) < 1e-9;
+}
+template <int NX> __device__ __forceinline__ bool basins_fixed_lane(const P2* x, const P2* xp, int l) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < NX; ++j) {
+        const float d = lane(x[j], l) - lane(xp[j], l);
+        s = s + d * d;
+    }
+    return sqrt(fabs((double)s)) < 1e-9;
+}
+
+template <class F>
+__device__ __forceinline__ void load_pair(const SweepParams& P, long long p0, long long p1, P2* x, P2* a) {
+    float xs[2][3], as[2][3];
+    load_point<SYS_LORENZ_RK4, float>(P, p0, xs[0], as[0]);  // any 3-state, 3-parameter system loads alike
+    load_point<SYS_LORENZ_RK4, float>(P, p1, xs[1], as[1]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        x[k] = P2(xs[0][k], xs[1][k]);
+        a[k] = P2(as[0][k], as[1][k]);
+    }
+}
+
+template <class F>
+__device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOut& O, long long p0, long long p1,
+                                               long long o0, long long o1, bool two) {
+    P2 x[3], a[3], xp[3];
+    load_pair<F>(P, p0, p1, x, a);
+    const RK4H<P2> c((float)P.h);
+    const int wv = P.wv;
+    int flag[2] = {1, two ? 1 : 0};
+    if (P.S > 0) {
+        for (int s = 0; s < P.S; ++s) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+            rk4_step<F>(x, a, c);
+            const P2 v = pick2<3>(x, wv);
+            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
+            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
+            if (flag[0] != 1 && flag[1] != 1) break;
+        }
+#pragma unroll
+        for (int l = 0; l < 2; ++l)
+            if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+    }
+    bool rec[2];
+    double first[2] = {0.0, 0.0};  // stays 0 for a lane that does not record (as the scalar path)
+    PeakStream<float> ps[2];
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        rec[l] = flag[l] == 1;
+        if (!rec[l]) flag[l] = 0;
+        ps[l].init();
+    }
+    const long long oo[2] = {o0, o1};
+    if (rec[0] || rec[1]) {
+        {
+            const P2 v = pick2<3>(x, wv);
+            if (rec[0]) first[0] = (double)v.v.x;
+            if (rec[1]) first[1] = (double)v.v.y;
+        }
+        for (int i = 0; i < P.B; ++i) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+            const P2 v = pick2<3>(x, wv);
+#pragma unroll
+            for (int l = 0; l < 2; ++l) {
+                float val;
+                int t;
+                if (rec[l] && ps[l].push(lane(v, l), val, t)) {
+                    if (ps[l].n >= 1) {
+                        const int q = ps[l].n - 1;
+                        if (q < O.cap) {
+                            if (O.peaks) O.peaks[oo[l] * O.cap + q] = (double)val;
+                            if (O.intervals)
+                                O.intervals[oo[l] * O.cap + q] = __dmul_rn((double)(t - ps[l].tprev), P.hInterval);
+                        }
+                    }
+                    ps[l].tprev = t;
+                    ++ps[l].n;
+                }
+            }
+            rk4_step<F>(x, a, c);
+            const P2 w = pick2<3>(x, wv);
+            if (rec[0] && bif_diverged(w.v.x, P)) { rec[0] = false; flag[0] = 0; }
+            if (rec[1] && bif_diverged(w.v.y, P)) { rec[1] = false; flag[1] = 0; }
+            if (!rec[0] && !rec[1]) break;
+        }
+#pragma unroll
+        for (int l = 0; l < 2; ++l)
+            if (rec[l] && P.B > 0 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+    }
+#pragma unroll
+    for (int l = 0; l < (two ? 2 : 1); ++l) {
+        const int kept = ps[l].n > 1 ? ps[l].n - 1 : 0;
+        O.flags[oo[l]] = flag[l];
+        O.counts[oo[l]] = flag[l] == 1 ? kept : (flag[l] == -1 ? -1 : 0);
+        if (O.first) O.first[oo[l]] = first[l];
+    }
+}
+
+template <class F>
+__device__ __forceinline__ void basins_pair_point(const SweepParams& P, const BasinsOut& O, long long p0,
+                                                  long long p1, long long o0, long long o1, bool two) {
+    P2 x[3], a[3], xp[3];
+    load_pair<F>(P, p0, p1, x, a);
+    const RK4H<P2> c((float)P.h);
+    const int wv = P.wv;
+    for (int s = 0; s < P.S; ++s) rk4_step<F>(x, a, c);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) xp[j] = x[j];
+    PeakStream<float> ps[2];
+    int flag[2] = {1, two ? 1 : 0};
+    bool rec[2] = {true, two};
+    double sp[2] = {0.0, 0.0}, si[2] = {0.0, 0.0}, last[2] = {0.0, 0.0};
+    ps[0].init();
+    ps[1].init();
+    for (int i = 0; i < P.B; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) xp[j] = x[j];
+        const P2 v = pick2<3>(x, wv);
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            if (!rec[l]) continue;
+            last[l] = (double)lane(v, l);
+            float val;
+            int t;
+            if (ps[l].push(lane(v, l), val, t)) {
+                if (ps[l].n >= 1) {
+                    sp[l] = sp[l] + (double)val;
+                    si[l] = si[l] + __dmul_rn((double)(t - ps[l].tprev), P.hInterval);
+                }
+                ps[l].tprev = t;
+                ++ps[l].n;
+            }
+        }
+        for (int r = 0; r < P.preScaller; ++r) rk4_step<F>(x, a, c);
+        const P2 w = pick2<3>(x, wv);
+        if (rec[0] && basins_diverged(w.v.x, P)) { rec[0] = false; flag[0] = 0; }
+        if (rec[1] && basins_diverged(w.v.y, P)) { rec[1] = false; flag[1] = 0; }
+        if (!rec[0] && !rec[1]) break;
+    }
+    const long long oo[2] = {o0, o1};
+#pragma unroll
+    for (int l = 0; l < (two ? 2 : 1); ++l) {
+        if (rec[l] && P.B > 0 && basins_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+        const int kept = ps[l].n > 1 ? ps[l].n - 1 : 0;
+        double ap, ai;
+        if (flag[l] == 0) { ap = 999.0; ai = 999.0; }
+        else if (flag[l] == -1) { ap = last[l]; ai = -1.0; }
+        else if (kept <= 0) { ap = 1000.0; ai = 1000.0; }
+        else { ap = sp[l] / (double)kept; ai = si[l] / (double)kept; }
+        O.flags[oo[l]] = flag[l];
+        O.avgPeaks[oo[l]] = ap;
+        O.avgIntervals[oo[l]] = ai;
+        if (O.counts) O.counts[oo[l]] = flag[l] == 1 ? kept : 0;
+        if (O.last) O.last[oo[l]] = last[l];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Trajectory recorder: nSteps steps of one trajectory per thread, writing the
 // state before the first step and after every step.
 template <int S, class T>

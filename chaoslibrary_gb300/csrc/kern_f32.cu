@@ -44,7 +44,26 @@ __global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0
     trajectory_point<S, float>(x0, a0, h, nSteps, out, t);
 }
 
+// Bifurcation / basins, two points per thread in packed FP32x2 lanes (RK4 systems).
+template <class F>
+__global__ void __launch_bounds__(kBlock) bif_pair_kernel_f32(SweepParams P, BifOut O) {
+    const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (o >= P.nPoints) return;
+    const bool two = o + 1 < P.nPoints;
+    bif_pair_point<F>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
+}
+
+template <class F>
+__global__ void __launch_bounds__(kBlock) basins_pair_kernel_f32(SweepParams P, BasinsOut O) {
+    const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (o >= P.nPoints) return;
+    const bool two = o + 1 < P.nPoints;
+    basins_pair_point<F>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
+}
+
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+}  // namespace
+namespace {
 
 // Variant of the FP32 LLE kernel: 12 / 16 = one point per thread shaped for
 // 12 or 16 resident blocks per SM; 2 = two points per thread in packed
@@ -76,8 +95,34 @@ int lle_occupancy_variant(int system) {
     }
 }  // namespace
 
+std::atomic<int> g_sweep_pairs{-1};
+
+// Paired (two points per thread) FP32 sweeps for the RK4 systems: on unless
+// switched off with chaos_set_tuning or CHAOS_SWEEP_PAIRS=0.
+bool sweep_pairs() {
+    const int v = g_sweep_pairs.load(std::memory_order_relaxed);
+    if (v >= 0) return v != 0;
+    static int env = [] {
+        const char* s = getenv("CHAOS_SWEEP_PAIRS");
+        return s ? atoi(s) : 1;
+    }();
+    return env != 0;
+}
+int set_sweep_pairs(int v) {
+    g_sweep_pairs.store(v ? 1 : 0);
+    return 0;
+}
+
+inline unsigned pair_grid(long long n) { return grid_for((n + 1) / 2); }
+
 cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
+    if (sweep_pairs() && P.system <= SYS_CHEN_RK4) {
+        if (P.system == SYS_LORENZ_RK4) bif_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+        else if (P.system == SYS_ROSSLER_RK4) bif_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+        else bif_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+        return cudaGetLastError();
+    }
 #define CALL(S) bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
@@ -86,6 +131,12 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
 
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
+    if (sweep_pairs() && P.system <= SYS_CHEN_RK4) {
+        if (P.system == SYS_LORENZ_RK4) basins_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+        else if (P.system == SYS_ROSSLER_RK4) basins_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+        else basins_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+        return cudaGetLastError();
+    }
 #define CALL(S) basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL

@@ -97,6 +97,9 @@ cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double*
 // thread (packed FP32x2), 12 / 16 = one point per thread at that occupancy.
 int set_lle_variant(int v);
 int get_lle_variant();
+// Paired FP32 bifurcation / basins kernels for the RK4 systems (kern_f32.cu).
+bool sweep_pairs();
+int set_sweep_pairs(int v);
 
 // The build-time user plug-in (kern_user.cu, or user_stub.cu when the build
 // has none): FP64 kernels of system SYS_USER.

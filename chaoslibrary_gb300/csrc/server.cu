@@ -3,9 +3,11 @@
 //
 // Threads: the caller submits; a scheduler thread admits requests into
 // device-resident slots (descriptor table + output buffers, bounded by the
-// HBM budget and maxActive) and launches iterations; a completion thread
-// copies finished requests back, runs the basins clustering when asked, frees
-// their memory and records latency. An iteration is a list of block-sized
+// HBM budget and maxActive) and launches iterations; a pool of completion
+// workers (one copy stream each) copies finished requests back, runs the
+// basins clustering when asked, frees their memory and records latency. A
+// request's descriptor slot is released as soon as its device work is done;
+// its memory counts against the budget until the worker frees it. An iteration is a list of block-sized
 // chunks shared fairly among the resident requests up to a work budget, run
 // by the grouped persistent kernels of batched mode; two
 // iterations are in flight on two streams, so new requests enter the next
@@ -79,7 +81,8 @@ struct chaos_server {
     int maxActive = 0;
     double iterationSteps = 0;
     cudaMemPool_t pool = nullptr;
-    cudaStream_t setup = nullptr, copy = nullptr;
+    cudaStream_t setup = nullptr;
+    std::vector<cudaStream_t> copy;  // one per completion worker
     cudaEvent_t setupDone = nullptr;
     JobDesc* dTable = nullptr;
     std::vector<int> freeSlots;
@@ -98,8 +101,12 @@ struct chaos_server {
     long long stepsDone = 0, iterations = 0, failed = 0;
     bool started = false;
     Clock::time_point tFirst;
-    std::thread scheduler, completer;
+    std::thread scheduler;
+    std::vector<std::thread> completers;
+    int completersRunning = 0;
 };
+
+constexpr int kCompleters = 4;
 
 namespace {
 
@@ -182,6 +189,7 @@ void finalize(chaos_server* S, Iteration& I) {
         w.first->done += w.second;
         if (w.first->done == w.first->nPoints) {
             S->active.erase(std::find(S->active.begin(), S->active.end(), w.first));
+            S->freeSlots.push_back(w.first->slot);  // its descriptor is no longer read
             S->completed.push_back(w.first);
         }
     }
@@ -291,8 +299,9 @@ void scheduler_main(chaos_server* S) {
     S->cvComplete.notify_all();
 }
 
-void completer_main(chaos_server* S) {
+void completer_main(chaos_server* S, int worker) {
     cudaSetDevice(S->device);
+    cudaStream_t copy = S->copy[worker];
     for (;;) {
         Request* r = nullptr;
         {
@@ -300,7 +309,11 @@ void completer_main(chaos_server* S) {
             S->cvComplete.wait_for(lk, std::chrono::milliseconds(5),
                                    [&] { return !S->completed.empty() || S->schedulerDone; });
             if (S->completed.empty()) {
-                if (S->schedulerDone) break;
+                if (S->schedulerDone) {
+                    S->completersRunning--;
+                    S->cvComplete.notify_all();
+                    break;
+                }
                 continue;
             }
             r = S->completed.front();
@@ -308,24 +321,23 @@ void completer_main(chaos_server* S) {
         }
         int rc = CHAOS_OK;
         if (r->dLabels) {  // the reference clustering of a basins map
-            chaos_exec ex{CHAOS_FP64, CHAOS_MEM_DEVICE, S->copy, S->device};
+            chaos_exec ex{CHAOS_FP64, CHAOS_MEM_DEVICE, copy, S->device};
             Call c;
             rc = c.begin(&ex);
             if (!rc) rc = dbscan_compat_device(c, r->desc.bas.avgPeaks, r->desc.bas.avgIntervals, r->desc.bas.flags,
                                                r->nPoints, r->job.eps, r->dLabels);
             rc = c.finish(rc);
             if (!rc && S->memory == CHAOS_MEM_HOST)
-                cudaMemcpyAsync(r->job.labels, r->dLabels, r->nPoints * sizeof(int), cudaMemcpyDeviceToHost, S->copy);
+                cudaMemcpyAsync(r->job.labels, r->dLabels, r->nPoints * sizeof(int), cudaMemcpyDeviceToHost, copy);
         }
-        for (const HostOut& o : r->outs) cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, S->copy);
-        if (r->devBlock) cudaFreeAsync(r->devBlock, S->copy);
-        cudaError_t e = cudaStreamSynchronize(S->copy);
+        for (const HostOut& o : r->outs) cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, copy);
+        if (r->devBlock) cudaFreeAsync(r->devBlock, copy);
+        cudaError_t e = cudaStreamSynchronize(copy);
         if (e != cudaSuccess && !rc) rc = cuda_error(e, "completion");
         std::lock_guard<std::mutex> lk(S->mu);
         r->state = rc == CHAOS_OK ? CHAOS_REQ_DONE : CHAOS_REQ_FAILED;
         r->latency = seconds(Clock::now() - r->tSubmit);
         S->used -= r->bytes;
-        S->freeSlots.push_back(r->slot);
         if (rc == CHAOS_OK) {
             S->latencies.push_back(r->latency);
             S->stepsDone += r->steps;
@@ -368,7 +380,11 @@ int chaos_server_create(const chaos_exec* ex, size_t hbmBudgetBytes, int maxActi
     S->iterationSteps = iterationSteps;
     S->pool = c.pool;
     cudaError_t e = cudaStreamCreateWithFlags(&S->setup, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy, cudaStreamNonBlocking);
+    for (int w = 0; w < kCompleters && e == cudaSuccess; ++w) {
+        cudaStream_t cs;
+        e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) S->copy.push_back(cs);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->setupDone, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&S->dTable, (size_t)maxActive * sizeof(JobDesc));
     for (Iteration& I : S->it) {
@@ -389,7 +405,8 @@ int chaos_server_create(const chaos_exec* ex, size_t hbmBudgetBytes, int maxActi
     cudaEventRecord(S->setupDone, S->setup);
     for (int i = maxActive - 1; i >= 0; --i) S->freeSlots.push_back(i);
     S->scheduler = std::thread(scheduler_main, S);
-    S->completer = std::thread(completer_main, S);
+    S->completersRunning = kCompleters;
+    for (int w = 0; w < kCompleters; ++w) S->completers.emplace_back(completer_main, S, w);
     *server = S;
     return CHAOS_OK;
 }
@@ -510,7 +527,8 @@ int chaos_server_destroy(chaos_server* S) {
     }
     if (S->scheduler.joinable()) S->scheduler.join();
     else S->schedulerDone = true;
-    if (S->completer.joinable()) S->completer.join();
+    for (std::thread& t : S->completers)
+        if (t.joinable()) t.join();
     cudaSetDevice(S->device);
     for (Iteration& I : S->it) {
         if (I.stream) cudaStreamSynchronize(I.stream);
@@ -523,11 +541,11 @@ int chaos_server_destroy(chaos_server* S) {
         if (I.stream) cudaStreamDestroy(I.stream);
     }
     if (S->setup) cudaStreamSynchronize(S->setup);
-    if (S->copy) cudaStreamSynchronize(S->copy);
+    for (cudaStream_t cs : S->copy) cudaStreamSynchronize(cs);
     if (S->dTable) cudaFree(S->dTable);
     if (S->setupDone) cudaEventDestroy(S->setupDone);
     if (S->setup) cudaStreamDestroy(S->setup);
-    if (S->copy) cudaStreamDestroy(S->copy);
+    for (cudaStream_t cs : S->copy) cudaStreamDestroy(cs);
     delete S;
     return CHAOS_OK;
 }

@@ -334,6 +334,9 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
  * 0 = the library default. Process-wide; results do not depend on it.
  */
 #define CHAOS_TUNE_LLE_F32_VARIANT 1
+/* CHAOS_TUNE_SWEEP_PAIRS: 1 = FP32 bifurcation / basins sweeps of the RK4
+   systems run two points per thread in packed FP32x2 lanes, 0 = one point. */
+#define CHAOS_TUNE_SWEEP_PAIRS 2
 int chaos_set_tuning(int knob, int value);
 int chaos_get_tuning(int knob);
 

@@ -492,3 +492,39 @@ def test_compat_csv_bytes(engine, oracle, tmp_path):
     assert (tmp_path / "bas_1.csv").read_text() == head + _csv_matrix(f["avg_peaks"], 12, _g(15))
     assert (tmp_path / "bas_2.csv").read_text() == head + _csv_matrix(f["avg_intervals"], 12, _g(15))
     assert (tmp_path / "bas_3.csv").read_text() == head + _csv_matrix(f["flags"], 12, str)
+
+
+@pytest.mark.parametrize("system, values, ic, mi, rng, maxv", [
+    ("lorenz", [10.0, 28.0, 8 / 3], [0.1, 0.1, 0.1], 1, [20.0, 200.0], 40.0),   # many points diverge (|x| > 40)
+    ("rossler", [0.2, 0.2, 5.7], [1.0, 1.0, 1.0], 2, [2.0, 10.0], 1e4),
+    ("chen", [35.0, 3.0, 28.0], [-10.0, 0.0, 37.0], 2, [20.0, 30.0], 1e4),
+])
+def test_paired_sweeps_identical(engine, system, values, ic, mi, rng, maxv):
+    """FP32 bifurcation and basins sweeps give bit-identical results with two
+    points per thread (packed FP32x2 lanes) and with one, including lanes that
+    diverge while their partner keeps recording and an odd point count."""
+    knob = engine.TUNE_SWEEP_PAIRS
+    kw = dict(tMax=15.0, nPts=101, h=0.01, initialConditions=ic, ranges=rng, indicesOfMutVars=[mi], writableVar=0,
+              maxValue=maxv, transientTime=5.0, values=values)
+    bk = dict(tMax=6.0, nPts=23, h=0.01, initialConditions=ic, ranges=[-20.0, 20.0, -20.0, 20.0],
+              indicesOfMutVars=[0, 1], writableVar=0, maxValue=maxv * 2, transientTime=3.0, values=values)
+    res = {}
+    try:
+        for v in (0, 1):
+            engine.set_tuning(knob, v)
+            res[v] = (engine.bifurcation1d(system, precision=engine.FP32, peakCapacity=40, **kw),
+                      engine.basins_features(system, precision=engine.FP32, preScaller=2, **bk))
+    finally:
+        engine.set_tuning(knob, 1)
+    (b0, f0), (b1, f1) = res[0], res[1]
+    assert np.array_equal(b0["flags"], b1["flags"]) and np.array_equal(b0["counts"], b1["counts"])
+    assert np.array_equal(b0["first"], b1["first"])
+    for r, c in enumerate(b0["counts"]):
+        m = min(int(c), 40)
+        if m > 0:
+            assert np.array_equal(b0["peaks"][r, :m], b1["peaks"][r, :m])
+            assert np.array_equal(b0["intervals"][r, :m], b1["intervals"][r, :m])
+    for k in ("flags", "avg_peaks", "avg_intervals", "counts"):
+        assert np.array_equal(f0[k], f1[k]), k
+    if system == "lorenz":
+        assert (b0["flags"] == 0).any() and (b0["flags"] == 1).any()
