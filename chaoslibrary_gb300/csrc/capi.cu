@@ -230,6 +230,8 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     P.h = h;
     P.hInterval = h * (double)preScaller;
     P.maxValue = maxValue;
+    P.maxValueF = (float)maxValue;
+    if ((double)P.maxValueF > maxValue) P.maxValueF = nextafterf(P.maxValueF, -INFINITY);
     for (int i = 0; i < nIC; ++i) P.ic[i] = ic[i];
     for (int i = 0; i < nValues; ++i) P.values[i] = values[i];
     P.mut[0] = mut[0];

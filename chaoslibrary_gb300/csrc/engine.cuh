@@ -47,6 +47,12 @@ template <class T> __device__ __forceinline__ bool bif_diverged(T v, const Sweep
     if (!(av < T(9007199254740992.0))) return true;
     return P.checkMax && (double)fabsf((float)v) > P.maxValue;
 }
+// The same test for a float v without FP64 instructions (GB300's FP64 pipe
+// runs at 1/64 of the FP32 rate): |v| > maxValue <=> |v| > maxValueF.
+template <> __device__ __forceinline__ bool bif_diverged<float>(float v, const SweepParams& P) {
+    const float av = fabsf(v);
+    return !(av < 9007199254740992.0f) || (P.checkMax && av > P.maxValueF);
+}
 // Divergence test of the basins loop (basinsCUDA.cu:350-361): isnan || isinf, then maxValue.
 template <class T> __device__ __forceinline__ T finite_max();
 template <> __device__ __forceinline__ double finite_max<double>() { return 1.7976931348623157e308; }
@@ -55,6 +61,10 @@ template <class T> __device__ __forceinline__ bool basins_diverged(T v, const Sw
     const T av = v < T(0) ? -v : v;
     if (!(av <= finite_max<T>())) return true;  // NaN or +-inf
     return P.checkMax && (double)fabsf((float)v) > P.maxValue;
+}
+template <> __device__ __forceinline__ bool basins_diverged<float>(float v, const SweepParams& P) {
+    const float av = fabsf(v);
+    return !(av <= 3.4028234663852886e38f) || (P.checkMax && av > P.maxValueF);
 }
 
 // Streaming form of the reference peakFinder (bifurcationCUDA.cu:469-514).

@@ -2,6 +2,7 @@
 // times, intervals and means in FP64. The LLE kernel carries the twin as the
 // exact difference e = q - x (quadratic RK4 systems only) and accumulates the
 // log-stretch sum in FP64.
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 
@@ -97,8 +98,9 @@ int lle_occupancy_variant(int system) {
 
 std::atomic<int> g_sweep_pairs{-1};
 
-// Paired (two points per thread) FP32 sweeps for the RK4 systems: on unless
-// switched off with chaos_set_tuning or CHAOS_SWEEP_PAIRS=0.
+// Paired (two points per thread) FP32 sweeps for the RK4 systems: on (for
+// sweeps of at least 4 x SMs x 1024 points) unless switched off with
+// chaos_set_tuning or CHAOS_SWEEP_PAIRS=0.
 bool sweep_pairs() {
     const int v = g_sweep_pairs.load(std::memory_order_relaxed);
     if (v >= 0) return v != 0;
@@ -115,9 +117,21 @@ int set_sweep_pairs(int v) {
 
 inline unsigned pair_grid(long long n) { return grid_for((n + 1) / 2); }
 
+// Pairs halve the threads: worth it when the sweep fills the GPU several
+// times over, not for small (latency-bound) sweeps.
+bool pairs_for(long long nPoints) {
+    static long long threshold = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return 4LL * std::max(sms, 1) * 1024;
+    }();
+    return nPoints >= threshold;
+}
+
 cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-    if (sweep_pairs() && P.system <= SYS_CHEN_RK4) {
+    if (sweep_pairs() && P.system <= SYS_CHEN_RK4 && pairs_for(P.nPoints)) {
         if (P.system == SYS_LORENZ_RK4) bif_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
         else if (P.system == SYS_ROSSLER_RK4) bif_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
         else bif_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
@@ -131,7 +145,7 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
 
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-    if (sweep_pairs() && P.system <= SYS_CHEN_RK4) {
+    if (sweep_pairs() && P.system <= SYS_CHEN_RK4 && pairs_for(P.nPoints)) {
         if (P.system == SYS_LORENZ_RK4) basins_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
         else if (P.system == SYS_ROSSLER_RK4) basins_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
         else basins_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);

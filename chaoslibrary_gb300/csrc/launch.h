@@ -31,6 +31,7 @@ struct SweepParams {
     double h;
     double hInterval;  // h * preScaller, the time unit of peak intervals
     double maxValue;
+    float maxValueF;   // the largest float <= maxValue: for a float v, |v| > maxValue <=> |v| > maxValueF
     double ic[kMaxState];
     double values[kMaxParams];
     int mut[2];
