@@ -353,12 +353,14 @@ def batch_arm(args, ws, rank, local):
     with Clocks([local] if ws == 1 else list(range(ws))) as clk:
         barrier(ws)
         torch.cuda.synchronize()
+        l0 = C.launch_count()
         for k in range(args.steps):
             flush.fill_(k & 0xff)
             ev[k][0].record(stream)
             b.replay()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
+        launches = C.launch_count() - l0
         barrier(ws)
     ms = [a.elapsed_time(c) for a, c in ev]
     t_total = max_over_ranks(ws, sum(ms) / 1e3)
@@ -371,7 +373,7 @@ def batch_arm(args, ws, rank, local):
                                    "(10000 recorded steps), half LLE maps (tMax 100, NT 0.1)",
                        "total_steps": float(total_steps), "jobs": len(jobs),
                        "l2": "256 MB buffer written between timed steps"},
-            "clocks": clk.summary()}
+            "clocks": clk.summary(), "gpu_launches": launches}
     if rank == 0:
         mean_s = statistics.mean(ms) / 1e3
         peak = C.fma_probe() / 1e12
@@ -489,6 +491,7 @@ def serve_arm(args, ws, rank, local):
     th = threading.Thread(target=waiter)
     th.start()
     with Clocks([local]) as clk:
+        l0 = C.launch_count()
         t0 = time.perf_counter()
         t_next = t0
         for (kind, system, kw), gap in zip(reqs, gaps):
@@ -506,6 +509,7 @@ def serve_arm(args, ws, rank, local):
                 ids.append((rid, out))
         th.join()
         wall = time.perf_counter() - t0
+        launches = C.launch_count() - l0
     st = srv.stats()
     srv.close()
     total_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in reqs)
@@ -521,6 +525,7 @@ def serve_arm(args, ws, rank, local):
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "mean": float(lat.mean()), "max": float(lat.max())},
             "server": st, "clocks": clk.summary(), "total_steps": float(total_steps), "wall_s": wall,
+            "gpu_launches": launches,
             "e2e": {"value": total_steps / wall, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": None}}
     print(json.dumps(line), flush=True)
@@ -549,7 +554,6 @@ def engine_arm(args, ws, rank, local):
         def step_host():
             return C.lle2d(w["system"], precision=prec, **kw)
         d2h = n_points * 8
-        launches_per_step = 1
         tag = f"lle_{args.precision}_rossler_1024"
         line_extra = {"lle_variant": C.get_tuning(C.TUNE_LLE_F32_VARIANT)}
     elif args.workload == "bif1d":
@@ -568,7 +572,6 @@ def engine_arm(args, ws, rank, local):
         def step_host():
             return C.bifurcation1d(w["system"], precision=prec, peakCapacity=cap, **kw)
         d2h = n_points * (4 + 4 + 8 + 16 * cap)
-        launches_per_step = 1
         tag = f"bif1d_{args.precision}_lorenz_1000"
     else:
         steps_pp = sweep_steps_per_point(w)
@@ -584,7 +587,6 @@ def engine_arm(args, ws, rank, local):
         def step_host():
             return C.basins(w["system"], precision=prec, **kw)
         d2h = n_points * (4 + 8 + 8 + 4)
-        launches_per_step = None
         tag = f"basins_{args.precision}_lorenz_2048"
     steps_per_call = n_points * steps_pp
     for _ in range(args.warmup):
@@ -597,12 +599,14 @@ def engine_arm(args, ws, rank, local):
         barrier(ws)
         torch.cuda.synchronize()
         wall0 = time.perf_counter()
+        l0 = C.launch_count()
         for k in range(args.steps):
             flush.fill_(k & 0xff)
             ev[k][0].record(stream)
             step()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
+        launches = C.launch_count() - l0
         barrier(ws)
         wall = time.perf_counter() - wall0
     ms = [a.elapsed_time(b) for a, b in ev]
@@ -614,9 +618,7 @@ def engine_arm(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == C.FP32 else "f64",
             "data": "synthetic (deterministic parameter / initial-condition grids)",
-            "config": config_of(args), "clocks": clocks, "wall_s_timed_region": wall}
-    if launches_per_step:
-        line["gpu_launches"] = launches_per_step * args.steps
+            "config": config_of(args), "clocks": clocks, "wall_s_timed_region": wall, "gpu_launches": launches}
     if args.workload == "lle":
         line["config"].update(line_extra)
 

@@ -69,6 +69,7 @@ _SIGS = {
     "chaos_peak_finder": ([_P, _P, _L, _I, _D, _I, _P, _P, _P], _I),
     "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
     "chaos_fma_probe": ([_P, _L, _P, _P], _I),
+    "chaos_launch_count": ([_P], _I),
     "chaos_trajectory": ([_P, _I, _L, _P, _P, _D, _I, _P], _I),
     "chaos_set_tuning": ([_I, _I], _I),
     "chaos_run_batch": ([_P, _P, _I], _I),
@@ -177,6 +178,13 @@ def fma_probe(iters: int = 200000, device=None) -> float:
     sec, fl = C.c_double(), C.c_double()
     _check(lib().chaos_fma_probe(C.byref(ex), iters, C.byref(sec), C.byref(fl)))
     return fl.value / sec.value
+
+
+def launch_count() -> int:
+    """Kernels the library has launched in this process so far."""
+    n = C.c_longlong()
+    _check(lib().chaos_launch_count(C.byref(n)))
+    return n.value
 
 
 def trajectory(system, x0, a, h, n_steps, precision=FP64):

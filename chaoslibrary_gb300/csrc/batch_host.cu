@@ -31,6 +31,7 @@ struct chaos_batch {
     std::vector<cudaEvent_t> events;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;  // kernel nodes of the graph (launches per replay)
 };
 
 extern "C" {
@@ -131,6 +132,18 @@ int chaos_batch_create(const chaos_exec* ex, const chaos_job* jobs, int nJobs, c
             if (lrc != CHAOS_OK && e == cudaSuccess) e = cudaErrorUnknown;
         }
         if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e == cudaSuccess) {
+            // captured launches ran nothing: count them at each replay instead
+            size_t nodes = 0;
+            cudaGraphGetNodes(b->graph, nullptr, &nodes);
+            std::vector<cudaGraphNode_t> list(nodes);
+            if (nodes) cudaGraphGetNodes(b->graph, list.data(), &nodes);
+            for (cudaGraphNode_t nd : list) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++b->kernels;
+            }
+            note_launch(-b->kernels);
+        }
         if (e != cudaSuccess) rc = cuda_error(e, "batch graph capture");
     }
     if (rc != CHAOS_OK) {
@@ -149,6 +162,7 @@ int chaos_batch_run(chaos_batch* b) {
     cudaError_t e = cudaEventRecord(b->in, b->user);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->in, 0);
     if (e == cudaSuccess) e = cudaGraphLaunch(b->exec, b->stream);
+    if (e == cudaSuccess) note_launch(b->kernels);
     if (e == cudaSuccess) e = cudaEventRecord(b->out, b->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->user, b->out, 0);
     for (const HostOut& o : b->outs)

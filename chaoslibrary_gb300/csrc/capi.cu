@@ -2,6 +2,8 @@
 // host<->device copies and kernel launches. Declared in include/chaos_gb300.h.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -31,7 +33,11 @@ struct DeviceCtx {
 };
 std::mutex g_mu;
 std::vector<DeviceCtx> g_dev;
+std::atomic<long long> g_launches{0};
 }  // namespace
+
+void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 int set_error(int code, const char* fmt, ...) {
     char buf[512];
@@ -300,6 +306,12 @@ extern "C" {
 
 int chaos_abi_version(void) { return CHAOS_ABI_VERSION; }
 const char* chaos_last_error(void) { return g_err.c_str(); }
+
+int chaos_launch_count(long long* count) {
+    if (!count) return set_error(CHAOS_E_ARGS, "null count");
+    *count = launch_count();
+    return CHAOS_OK;
+}
 
 int chaos_system_info(int system, int* sizeX, int* sizeA) {
     if (system == SYS_USER && !user_system_available())
@@ -605,13 +617,14 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
 int chaos_set_tuning(int knob, int value) {
     if (knob == CHAOS_TUNE_LLE_F32_VARIANT)
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
-    if (knob == CHAOS_TUNE_SWEEP_PAIRS) return set_sweep_pairs(value);
+    if (knob == CHAOS_TUNE_SWEEP_PAIRS)
+        return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1 or 2)", value) : CHAOS_OK;
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 
 int chaos_get_tuning(int knob) {
     if (knob == CHAOS_TUNE_LLE_F32_VARIANT) return get_lle_variant();
-    if (knob == CHAOS_TUNE_SWEEP_PAIRS) return sweep_pairs() ? 1 : 0;
+    if (knob == CHAOS_TUNE_SWEEP_PAIRS) return sweep_pairs();
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 

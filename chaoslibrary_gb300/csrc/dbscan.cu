@@ -566,11 +566,11 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* occ = (int*)c.alloc(cap * sizeof(int));
     int* slotCell = (int*)c.alloc(cap * sizeof(int));
     NEED(!c.failed);
-    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include);
-    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, side, key, unsafePt);
+    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include); ::chaos::note_launch();
+    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, side, key, unsafePt); ::chaos::note_launch();
     CK(cudaMemsetAsync(tab, 0xff, cap * sizeof(unsigned long long), st));
-    hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot);
-    occupied_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ);
+    hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot); ::chaos::note_launch();
+    occupied_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ); ::chaos::note_launch();
     CKL();
     int C = 0;
     int rc = exclusive_scan(c, occ, occ, (long long)cap, &C);
@@ -579,9 +579,9 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* cnt = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
     int* cellOf = (int*)c.alloc(n * sizeof(int));
     NEED(!c.failed);
-    cell_ids_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ, slotCell, cellKey);
+    cell_ids_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ, slotCell, cellKey); ::chaos::note_launch();
     CK(cudaMemsetAsync(cnt, 0, (size_t)(C + 1) * sizeof(int), st));
-    point_cell_kernel<<<blocks(n), kTPB, 0, st>>>(slot, n, slotCell, cellOf, cnt);
+    point_cell_kernel<<<blocks(n), kTPB, 0, st>>>(slot, n, slotCell, cellOf, cnt); ::chaos::note_launch();
     CKL();
     int used = 0;
     if ((rc = exclusive_scan(c, cnt, cnt, C + 1, &used))) return rc;  // cnt -> start (C+1 entries)
@@ -593,7 +593,7 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     double* s2 = (double*)c.alloc((size_t)(used + 1) * sizeof(double));
     NEED(!c.failed);
     CK(cudaMemsetAsync(cursor, 0, (size_t)(C + 1) * sizeof(int), st));
-    scatter_kernel<<<blocks(n), kTPB, 0, st>>>(F, n, cellOf, start, cursor, order, s0, s1, s2);
+    scatter_kernel<<<blocks(n), kTPB, 0, st>>>(F, n, cellOf, start, cursor, order, s0, s1, s2); ::chaos::note_launch();
     CKL();
     Sorted S;
     S.s[0] = s0;
@@ -608,9 +608,9 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* nbStart = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
     NEED(!c.failed);
     if (C > 0) {
-        cell_box_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, unsafePt, boxLo, boxHi, unsafeCell);
+        cell_box_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, unsafePt, boxLo, boxHi, unsafeCell); ::chaos::note_launch();
         neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nbStart, nullptr,
-                                                      nullptr, nullptr);
+                                                      nullptr, nullptr); ::chaos::note_launch();
         CKL();
     }
     if (zeroEps && C > 0) CK(cudaMemsetAsync(unsafeCell, 1, (size_t)C, st));
@@ -625,43 +625,43 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* root = (int*)c.alloc(n * sizeof(int));
     NEED(!c.failed);
     if (C > 0)
-        neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nullptr, nbStart, nbList,
-                                                      nbOwner);
-    if (compat) core_from_include_kernel<<<blocks(n), kTPB, 0, st>>>(include, n, core);
+        { neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nullptr, nbStart, nbList,
+                                                      nbOwner); ::chaos::note_launch(); }
+    if (compat) { core_from_include_kernel<<<blocks(n), kTPB, 0, st>>>(include, n, core); ::chaos::note_launch(); }
     else
-        core_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, n, nbStart, nbList, unsafeCell, eps, minPts, core);
-    iota_kernel<<<blocks(n), kTPB, 0, st>>>(parent, n);
-    if (C > 0) intra_cell_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, core, unsafeCell, eps, parent, rep);
+        { core_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, n, nbStart, nbList, unsafeCell, eps, minPts, core); ::chaos::note_launch(); }
+    iota_kernel<<<blocks(n), kTPB, 0, st>>>(parent, n); ::chaos::note_launch();
+    if (C > 0) { intra_cell_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, core, unsafeCell, eps, parent, rep); ::chaos::note_launch(); }
     if (E > 0)
-        cross_cell_kernel<<<blocks((long long)E * 32), kTPB, 0, st>>>(S, nbOwner, nbList, E, core, unsafeCell, rep,
-                                                                      boxLo, boxHi, eps, parent);
-    roots_kernel<<<blocks(n), kTPB, 0, st>>>(parent, core, n, root);
+        { cross_cell_kernel<<<blocks((long long)E * 32), kTPB, 0, st>>>(S, nbOwner, nbList, E, core, unsafeCell, rep,
+                                                                      boxLo, boxHi, eps, parent); ::chaos::note_launch(); }
+    roots_kernel<<<blocks(n), kTPB, 0, st>>>(parent, core, n, root); ::chaos::note_launch();
     CKL();
     if (compat) {
         int* minFix = (int*)c.alloc(n * sizeof(int));
         int* negRank = (int*)c.alloc(n * sizeof(int));
         int* posRank = (int*)c.alloc(n * sizeof(int));
         NEED(!c.failed);
-        fill_kernel<<<blocks(n), kTPB, 0, st>>>(minFix, n, (int)n);
-        compat_minfix_kernel<<<blocks(n), kTPB, 0, st>>>(root, flags, n, minFix);
+        fill_kernel<<<blocks(n), kTPB, 0, st>>>(minFix, n, (int)n); ::chaos::note_launch();
+        compat_minfix_kernel<<<blocks(n), kTPB, 0, st>>>(root, flags, n, minFix); ::chaos::note_launch();
         CK(cudaMemsetAsync(negRank, 0, n * sizeof(int), st));
         CK(cudaMemsetAsync(posRank, 0, n * sizeof(int), st));
-        compat_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank);
+        compat_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank); ::chaos::note_launch();
         CKL();
         int t = 0;
         if ((rc = exclusive_scan(c, negRank, negRank, n, &t))) return rc;
         if ((rc = exclusive_scan(c, posRank, posRank, n, &t))) return rc;
-        compat_labels_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank, labels);
+        compat_labels_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank, labels); ::chaos::note_launch();
         CKL();
     } else {
         int* rank = (int*)c.alloc(n * sizeof(int));
         NEED(!c.failed);
-        root_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, n, rank);
+        root_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, n, rank); ::chaos::note_launch();
         CKL();
         int t = 0;
         if ((rc = exclusive_scan(c, rank, rank, n, &t))) return rc;
         dbscan_labels_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, include, n, nbStart, nbList, unsafeCell,
-                                                         core, root, rep, rank, eps, labels);
+                                                         core, root, rep, rank, eps, labels); ::chaos::note_launch();
         CKL();
     }
     return CHAOS_OK;
@@ -677,12 +677,12 @@ int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total) {
     const long long nb = (n + kScanItems - 1) / kScanItems;
     int* sums = (int*)c.alloc((size_t)(nb + 1) * sizeof(int));
     if (!sums) return CHAOS_E_NOMEM;
-    scan_block_kernel<<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n);
+    scan_block_kernel<<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n); ::chaos::note_launch();
     CK(cudaGetLastError());
     if (nb > 1) {
         int rc = exclusive_scan(c, sums, sums, nb, total);
         if (rc) return rc;
-        add_offsets_kernel<<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n);
+        add_offsets_kernel<<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n); ::chaos::note_launch();
         CK(cudaGetLastError());
     } else if (total) {
         CK(cudaMemcpyAsync(total, sums, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -707,7 +707,7 @@ int dbscan_device(Call& c, const double* features, long long n, int dims, double
     double* b = (double*)c.alloc(n * sizeof(double));
     double* d = (double*)c.alloc(n * sizeof(double));
     if (c.failed) return CHAOS_E_NOMEM;
-    soa_kernel<<<blocks(n), kTPB, 0, c.stream>>>(features, n, dims, a, b, d);
+    soa_kernel<<<blocks(n), kTPB, 0, c.stream>>>(features, n, dims, a, b, d); ::chaos::note_launch();
     CK(cudaGetLastError());
     Feat F;
     F.f[0] = a;

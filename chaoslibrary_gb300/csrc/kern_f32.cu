@@ -98,20 +98,24 @@ int lle_occupancy_variant(int system) {
 
 std::atomic<int> g_sweep_pairs{-1};
 
-// Paired (two points per thread) FP32 sweeps for the RK4 systems: on (for
-// sweeps of at least 4 x SMs x 1024 points) unless switched off with
-// chaos_set_tuning or CHAOS_SWEEP_PAIRS=0.
-bool sweep_pairs() {
+// Paired (two points per thread) FP32 sweeps for the RK4 systems. Mode 1
+// (default): pairs for bifurcation sweeps of at least 4 x SMs x 1024 points
+// (measured on GB300: +1..3 % there, slower below; basins sweeps measured
+// no faster paired at any size); 2: always; 0: never. Set with
+// chaos_set_tuning or CHAOS_SWEEP_PAIRS.
+int sweep_pairs() {
     const int v = g_sweep_pairs.load(std::memory_order_relaxed);
-    if (v >= 0) return v != 0;
+    if (v >= 0) return v;
     static int env = [] {
         const char* s = getenv("CHAOS_SWEEP_PAIRS");
-        return s ? atoi(s) : 1;
+        const int m = s ? atoi(s) : 1;
+        return m < 0 || m > 2 ? 1 : m;
     }();
-    return env != 0;
+    return env;
 }
 int set_sweep_pairs(int v) {
-    g_sweep_pairs.store(v ? 1 : 0);
+    if (v < 0 || v > 2) return -1;
+    g_sweep_pairs.store(v);
     return 0;
 }
 
@@ -119,25 +123,29 @@ inline unsigned pair_grid(long long n) { return grid_for((n + 1) / 2); }
 
 // Pairs halve the threads: worth it when the sweep fills the GPU several
 // times over, not for small (latency-bound) sweeps.
-bool pairs_for(long long nPoints) {
+bool use_pairs(const SweepParams& P, bool basins) {
+    if (P.system > SYS_CHEN_RK4) return false;
+    const int mode = sweep_pairs();
+    if (mode != 1) return mode == 2;
+    if (basins) return false;
     static long long threshold = [] {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         return 4LL * std::max(sms, 1) * 1024;
     }();
-    return nPoints >= threshold;
+    return P.nPoints >= threshold;
 }
 
 cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-    if (sweep_pairs() && P.system <= SYS_CHEN_RK4 && pairs_for(P.nPoints)) {
-        if (P.system == SYS_LORENZ_RK4) bif_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
-        else if (P.system == SYS_ROSSLER_RK4) bif_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
-        else bif_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+    if (use_pairs(P, false)) {
+        if (P.system == SYS_LORENZ_RK4) { bif_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+        else if (P.system == SYS_ROSSLER_RK4) { bif_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+        else { bif_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
         return cudaGetLastError();
     }
-#define CALL(S) bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
+#define CALL(S) (bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), ::chaos::note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -145,13 +153,13 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
 
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-    if (sweep_pairs() && P.system <= SYS_CHEN_RK4 && pairs_for(P.nPoints)) {
-        if (P.system == SYS_LORENZ_RK4) basins_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
-        else if (P.system == SYS_ROSSLER_RK4) basins_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
-        else basins_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+    if (use_pairs(P, true)) {
+        if (P.system == SYS_LORENZ_RK4) { basins_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+        else if (P.system == SYS_ROSSLER_RK4) { basins_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+        else { basins_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
         return cudaGetLastError();
     }
-#define CALL(S) basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O)
+#define CALL(S) (basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), ::chaos::note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -168,9 +176,9 @@ __global__ void __launch_bounds__(kBlock) lle_pair_kernel_f32(LleParams L, doubl
 
 template <class F>
 static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb) {
-    if (minb == 2) lle_pair_kernel_f32<F><<<grid_for((L.nPoints + 1) / 2), kBlock, 0, st>>>(L, out);
-    else if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
-    else lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+    if (minb == 2) { lle_pair_kernel_f32<F><<<grid_for((L.nPoints + 1) / 2), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
+    else if (minb >= 16) { lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
+    else { lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
 }
 
 int set_lle_variant(int v) {
@@ -195,7 +203,7 @@ cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
 cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-#define CALL(S) trajectory_kernel_f32<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n)
+#define CALL(S) (trajectory_kernel_f32<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n), ::chaos::note_launch())
     CHAOS_SYSTEM_SWITCH(system, CALL)
 #undef CALL
     return cudaGetLastError();

@@ -8,6 +8,11 @@
 
 namespace chaos {
 
+// Kernels launched by this library (all devices and threads): every launch
+// site adds one; a captured CUDA graph adds its kernel nodes at each replay.
+void note_launch(long long n = 1);
+long long launch_count();
+
 constexpr int kMaxState = 12;
 constexpr int kMaxParams = 16;
 
@@ -99,7 +104,7 @@ cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double*
 int set_lle_variant(int v);
 int get_lle_variant();
 // Paired FP32 bifurcation / basins kernels for the RK4 systems (kern_f32.cu).
-bool sweep_pairs();
+int sweep_pairs();  // 0 never, 1 large sweeps, 2 always
 int set_sweep_pairs(int v);
 
 // The build-time user plug-in (kern_user.cu, or user_stub.cu when the build

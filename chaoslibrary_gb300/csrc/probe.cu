@@ -38,8 +38,10 @@ extern "C" int chaos_fma_probe(const chaos_exec* ex, long long iters, double* se
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     fma_probe_kernel<<<grid, 256, 0, c.stream>>>(iters / 8 + 1, sink);  // warm-up
+    note_launch();
     cudaEventRecord(e0, c.stream);
     fma_probe_kernel<<<grid, 256, 0, c.stream>>>(iters, sink);
+    note_launch();
     cudaEventRecord(e1, c.stream);
     cudaError_t e = cudaEventSynchronize(e1);
     float ms = 0.f;

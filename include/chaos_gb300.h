@@ -69,6 +69,11 @@ typedef struct chaos_exec {
 int chaos_abi_version(void);
 const char* chaos_last_error(void);
 
+/* Number of kernels this library has launched in the process so far (all
+ * devices and threads; a plan replay adds the kernels of its graph). No
+ * reference counterpart: lets a caller count the launches of a region. */
+int chaos_launch_count(long long* count);
+
 /* SIZE_X / SIZE_A of a built-in system (reference systems/systems.cuh SIZE_X, SIZE_A). */
 int chaos_system_info(int system, int* sizeX, int* sizeA);
 
@@ -334,8 +339,10 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
  * 0 = the library default. Process-wide; results do not depend on it.
  */
 #define CHAOS_TUNE_LLE_F32_VARIANT 1
-/* CHAOS_TUNE_SWEEP_PAIRS: 1 = FP32 bifurcation / basins sweeps of the RK4
-   systems run two points per thread in packed FP32x2 lanes, 0 = one point. */
+/* CHAOS_TUNE_SWEEP_PAIRS: FP32 bifurcation / basins sweeps of the RK4 systems
+   run two points per thread in packed FP32x2 lanes: 1 (default) for
+   bifurcation sweeps of at least 4 x SMs x 1024 points, 2 always, 0 never
+   (one point per thread). Results are identical in every mode. */
 #define CHAOS_TUNE_SWEEP_PAIRS 2
 int chaos_set_tuning(int knob, int value);
 int chaos_get_tuning(int knob);

@@ -510,13 +510,13 @@ def test_paired_sweeps_identical(engine, system, values, ic, mi, rng, maxv):
               indicesOfMutVars=[0, 1], writableVar=0, maxValue=maxv * 2, transientTime=3.0, values=values)
     res = {}
     try:
-        for v in (0, 1):
+        for v in (0, 2):
             engine.set_tuning(knob, v)
             res[v] = (engine.bifurcation1d(system, precision=engine.FP32, peakCapacity=40, **kw),
                       engine.basins_features(system, precision=engine.FP32, preScaller=2, **bk))
     finally:
         engine.set_tuning(knob, 1)
-    (b0, f0), (b1, f1) = res[0], res[1]
+    (b0, f0), (b1, f1) = res[0], res[2]
     assert np.array_equal(b0["flags"], b1["flags"]) and np.array_equal(b0["counts"], b1["counts"])
     assert np.array_equal(b0["first"], b1["first"])
     for r, c in enumerate(b0["counts"]):
@@ -528,3 +528,26 @@ def test_paired_sweeps_identical(engine, system, values, ic, mi, rng, maxv):
         assert np.array_equal(f0[k], f1[k]), k
     if system == "lorenz":
         assert (b0["flags"] == 0).any() and (b0["flags"] == 1).any()
+
+
+def test_launch_count(engine):
+    """chaos_launch_count grows by one for a single-kernel sweep and by the
+    graph's kernels (counter reset + one per (kind, system) group) for each
+    replay of a prepared batch, not at capture."""
+    lle = dict(tMax=1.0, NT=0.1, nPts=8, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+               ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=0.5, values=[0.2, 0.2, 5.7])
+    n0 = engine.launch_count()
+    engine.lle2d("rossler", precision=engine.FP32, **lle)
+    assert engine.launch_count() - n0 == 1
+    b = engine.Batch(device=False)
+    b.add_lle2d("rossler", **lle)
+    b.add_bifurcation1d("lorenz", tMax=1.0, nPts=50, h=0.01, initialConditions=[0.1, 0.1, 0.1], ranges=[20.0, 30.0],
+                        indicesOfMutVars=[1], writableVar=0, maxValue=1e4, transientTime=0.5,
+                        values=[10.0, 28.0, 8 / 3], peakCapacity=8)
+    n1 = engine.launch_count()
+    b.prepare()
+    assert engine.launch_count() == n1
+    b.replay()
+    b.replay()
+    assert engine.launch_count() - n1 == 2 * 3
+    b.close()
