@@ -47,7 +47,7 @@ BIF1D = dict(system="lorenz", sysid=0, flops=71, tMax=100.0, nPts=1000, h=0.01, 
              values=[10.0, 28.0, 8.0 / 3.0])
 BASINS = dict(system="lorenz", sysid=0, flops=71, tMax=50.0, nPts=2048, h=0.01, initialConditions=[0.0, 0.0, 27.0],
               ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8,
-              transientTime=200.0, values=[10.0, 24.0, 8.0 / 3.0], eps=0.05)
+              transientTime=200.0, values=[10.0, 24.0, 8.0 / 3.0], eps=0.05, minPts=8)
 
 
 SYS_FLOPS = {"lorenz": 71, "rossler": 63, "chen": 79}
@@ -267,7 +267,9 @@ def cpu_sample_sweep(w, kind, target_s=10.0):
     run(b, b + n)
     dt = time.perf_counter() - t
     return {"value": n * sweep_steps_per_point(w) / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n} of {n_all} grid points, full horizon, FP64, {dt:.1f} s"}
+            "sample": f"{n} of {n_all} grid points, full horizon, FP64, {dt:.1f} s"
+                      + ("; per-point integration and features (the clustering needs the whole map and is not "
+                         "in the sample)" if kind == "basins" else "")}
 
 
 def reference_arm(args, ws, rank):
@@ -304,7 +306,8 @@ def config_of(args):
                 "steps_per_point": sweep_steps_per_point(BIF1D), "precision": args.precision,
                 "l2": "256 MB buffer written between timed steps"}
     return {"workload": "basins, Lorenz rho=24 RK4 h=0.01, 2048x2048 ICs x,y in [-30,30], z=27, 20000 transient + "
-                        "5000 recorded steps, features + reference clustering eps=0.05",
+                        "5000 recorded steps, features (mean peak of x, peak count, mean interval) min-max "
+                        "normalised, DBSCAN eps=0.05 minPts=8",
             "grid_points": 2048 * 2048, "steps_per_point": sweep_steps_per_point(BASINS),
             "precision": args.precision, "l2": "256 MB buffer written between timed steps"}
 
@@ -574,19 +577,20 @@ def engine_arm(args, ws, rank, local):
         d2h = n_points * (4 + 4 + 8 + 16 * cap)
         tag = f"bif1d_{args.precision}_lorenz_1000"
     else:
+        # the basins map as specified: (amplitude, peak count, interval) features
+        # min-max normalised, textbook DBSCAN eps=0.05, minPts=8
         steps_pp = sweep_steps_per_point(w)
         outs = dict(labels=torch.empty(n_points, dtype=torch.int32, device=dev),
-                    avg_peaks=torch.empty(n_points, dtype=torch.float64, device=dev),
-                    avg_intervals=torch.empty(n_points, dtype=torch.float64, device=dev),
+                    features=torch.empty((n_points, 3), dtype=torch.float64, device=dev),
                     flags=torch.empty(n_points, dtype=torch.int32, device=dev))
         kw = kw_of(w)
 
         def step(o=None):
-            return C.basins(w["system"], precision=prec, out=outs, **kw)
+            return C.basins_dbscan(w["system"], precision=prec, out=outs, **kw)
 
         def step_host():
-            return C.basins(w["system"], precision=prec, **kw)
-        d2h = n_points * (4 + 8 + 8 + 4)
+            return C.basins_dbscan(w["system"], precision=prec, **kw)
+        d2h = n_points * (4 + 24 + 4)
         tag = f"basins_{args.precision}_lorenz_2048"
     steps_per_call = n_points * steps_pp
     for _ in range(args.warmup):
@@ -648,6 +652,8 @@ def engine_arm(args, ws, rank, local):
 
     if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras:
         line.update(lle_precision_report(C, prec, dev))
+    if rank == 0 and ws == 1 and args.workload == "basins" and not args.no_extras:
+        line.update(basins_extras(C, prec, dev, w))
     if rank == 0 and ws == 1 and not args.no_extras:
         try:
             if args.workload == "lle":
@@ -658,6 +664,75 @@ def engine_arm(args, ws, rank, local):
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def label_agreement(a, b, fixed=()):
+    """Fraction of points with the same label in a and b after the best
+    one-to-one matching of cluster ids; labels listed in `fixed` (noise,
+    diverged) match only themselves."""
+    from scipy.optimize import linear_sum_assignment
+
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    same_fixed = sum(int(np.sum((a == f) & (b == f))) for f in fixed)
+    m = ~np.isin(a, fixed) & ~np.isin(b, fixed)
+    if not m.any():
+        return same_fixed / a.size
+    ua, ia = np.unique(a[m], return_inverse=True)
+    ub, ib = np.unique(b[m], return_inverse=True)
+    M = np.zeros((ua.size, ub.size), np.int64)
+    np.add.at(M, (ia, ib), 1)
+    r, c = linear_sum_assignment(-M)
+    return (same_fixed + int(M[r, c].sum())) / a.size
+
+
+def basins_extras(C, prec, dev, w):
+    """The reference's own clustering (2 raw features, eps-components) on the
+    same 2048^2 map, and the label agreement of the FP32 map with the FP64
+    map (same engine, same inputs) on a 512^2 grid over the same ranges."""
+    import torch
+
+    out = {}
+    kw = {k: v for k, v in kw_of(w).items() if k != "minPts"}
+    n = w["nPts"] ** 2
+    o = dict(labels=torch.empty(n, dtype=torch.int32, device=dev),
+             avg_peaks=torch.empty(n, dtype=torch.float64, device=dev),
+             avg_intervals=torch.empty(n, dtype=torch.float64, device=dev),
+             flags=torch.empty(n, dtype=torch.int32, device=dev))
+    C.basins(w["system"], precision=prec, out=o, **kw)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    C.basins(w["system"], precision=prec, out=o, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    out["reference_clustering_mode"] = {"value": n * sweep_steps_per_point(w) / t, "unit": UNIT,
+                                        "ms_per_map": 1e3 * t,
+                                        "clusters": "2 raw features (mean peak, mean interval), eps-connected "
+                                                    "components, fixed-point components negative"}
+    small = dict(kw_of(w), nPts=512)
+    res = {}
+    t_small = {}
+    for p in (C.FP64, C.FP32):
+        C.basins_dbscan(w["system"], precision=p, **dict(small, nPts=16))
+        t0 = time.perf_counter()
+        r1 = C.basins_dbscan(w["system"], precision=p, **small)
+        t_small[p] = time.perf_counter() - t0
+        r2 = C.basins(w["system"], precision=p, **{k: v for k, v in small.items() if k != "minPts"})
+        res[p] = (r1, r2)
+    (b64, c64), (b32, c32) = res[C.FP64], res[C.FP32]
+    steps_small = 512 * 512 * sweep_steps_per_point(w)
+    out["basins_fp32_vs_fp64"] = {
+        "map": "512x512 (same ranges)", "points": 512 * 512,
+        "label_agreement": label_agreement(b32["labels"], b64["labels"], fixed=(-1, -2)),
+        "reference_clustering_label_agreement": label_agreement(c32["labels"], c64["labels"], fixed=(0,)),
+        "flag_agreement": float(np.mean(b32["flags"] == b64["flags"])),
+        "clusters_fp64": int(len(set(b64["labels"].tolist()) - {-1, -2})),
+        "clusters_fp32": int(len(set(b32["labels"].tolist()) - {-1, -2})),
+        "fp64_plain": {"value": steps_small / t_small[C.FP64], "unit": UNIT},
+        "fp32": {"value": steps_small / t_small[C.FP32], "unit": UNIT}}
+    return out
 
 
 def lle_precision_report(C, prec, dev):

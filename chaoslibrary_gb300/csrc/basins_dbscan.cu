@@ -79,14 +79,17 @@ cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double*
                                         cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     unsigned long long* mm = reinterpret_cast<unsigned long long*>(minmax);
-    minmax_init_kernel<<<1, 32, 0, st>>>(mm); ::chaos::note_launch();
+    minmax_init_kernel<<<1, 32, 0, st>>>(mm);
+    note_launch();
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long need = (n + kTPB - 1) / kTPB;
     const unsigned grid = (unsigned)(need < (long long)sms * 8 ? need : (long long)sms * 8);
-    minmax_kernel<<<grid, kTPB, 0, st>>>(O, n, mm, mask); ::chaos::note_launch();
-    normalise_kernel<<<(unsigned)need, kTPB, 0, st>>>(O, n, mm, features); ::chaos::note_launch();
+    minmax_kernel<<<grid, kTPB, 0, st>>>(O, n, mm, mask);
+    note_launch();
+    normalise_kernel<<<(unsigned)need, kTPB, 0, st>>>(O, n, mm, features);
+    note_launch();
     return cudaGetLastError();
 }
 

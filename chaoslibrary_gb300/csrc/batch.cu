@@ -139,7 +139,8 @@ int group_resident_blocks(int kind, int system, int device) {
 }
 
 cudaError_t reset_counters(int* counters, int n, cudaStream_t st) {
-    reset_counters_kernel<<<1, 32, 0, st>>>(counters, n); ::chaos::note_launch();
+    reset_counters_kernel<<<1, 32, 0, st>>>(counters, n);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -148,7 +149,8 @@ cudaError_t launch_group(int kind, int system, const JobDesc* jobs, const Chunk*
     GroupKernel k = group_kernel_for(kind, system);
     if (!k) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;
-    k<<<gridBlocks, kBatchBlock, 0, st>>>(jobs, chunks, count, counter); ::chaos::note_launch();
+    k<<<gridBlocks, kBatchBlock, 0, st>>>(jobs, chunks, count, counter);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -11,12 +11,15 @@
 //      for everything that follows);
 //   3. per cell: bounding box and the list of occupied neighbour cells;
 //   4. (DBSCAN) core flags: a cell holding >= minPts points makes all of them
-//      core; otherwise neighbours are counted exactly, with early exit;
+//      core; otherwise neighbours are counted exactly, with early exit, whole
+//      cells counted or skipped by their bounding boxes;
 //   5. union-find over points (parent[v] <= v, lock-free hooking with
 //      atomicCAS): every cell's core points are linked to its smallest one,
 //      then one warp per neighbouring cell pair looks for a core pair within
-//      eps (lanes stride over the second cell, per-point box pruning, early
-//      exit), so the root of a component is its smallest core index;
+//      eps (lanes stride over the larger cell, box tests per cell pair and per
+//      point, early exit) in two passes: bounded probes first, then
+//      exhaustive scans of the pairs that still separate two components. The
+//      root of a component is its smallest core index;
 //   6. numbering by prefix sums over the root indices.
 // Distances are sqrt(sum of squared differences) <= eps in FP64, in dimension
 // order, each operation rounded on its own (this file is compiled with
@@ -219,37 +222,87 @@ struct Sorted {
     }
 };
 
-// warp per cell: bounding box and the unsafe flag
-__global__ void cell_box_kernel(Sorted S, int C, const unsigned char* unsafePt, double* boxLo, double* boxHi,
-                                unsigned char* unsafeCell) {
-    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// ---- per-cell reductions over the cell-sorted points ---------------------------
+// One thread per sorted position; a cell's positions are contiguous, so a warp
+// reduces each run of equal cells with shuffles and the run's first lane
+// folds it into the cell with one atomic. Work is even however unequal the
+// cells are (a basin map can put a quarter of a million points in one cell).
+__device__ __forceinline__ unsigned long long okey(double v) {  // order-preserving, for atomicMin/atomicMax
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unkey(unsigned long long k) {
+    const unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// reduction of the lanes [lane, end of its run) holding the same cell
+template <class T, class Op> __device__ __forceinline__ T run_reduce(T v, int cell, Op op) {
     const int lane = threadIdx.x & 31;
-    if (w >= C) return;
-    const int b = S.start[w], e = S.start[w + 1];
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    int bad = 0;
-    for (int p = b + lane; p < e; p += 32) {
+    for (int o = 1; o < 32; o <<= 1) {
+        const T u = __shfl_down_sync(0xffffffffu, v, o);
+        const int c2 = __shfl_down_sync(0xffffffffu, cell, o);
+        if (lane + o < 32 && c2 == cell) v = op(v, u);
+    }
+    return v;
+}
+
+__device__ __forceinline__ bool run_head(int cell) {
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(0xffffffffu, cell, 1);
+    return cell >= 0 && (lane == 0 || prev != cell);
+}
+
+__global__ void cell_init_kernel(int C, unsigned long long* keyLo, unsigned long long* keyHi, int* bad, int* rep) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    for (int d = 0; d < 3; ++d) {
+        keyLo[3 * c + d] = ~0ull;
+        keyHi[3 * c + d] = 0ull;
+    }
+    bad[c] = 0;
+    rep[c] = 0x7fffffff;
+}
+
+// bounding box (NaN features ignored) and unsafe flag of every cell
+__global__ void box_reduce_kernel(Sorted S, long long used, const int* cellOf, const unsigned char* unsafePt,
+                                  unsigned long long* keyLo, unsigned long long* keyHi, int* bad) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1, b = 0;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (p < used) {
+        const int i = S.order[p];
+        c = cellOf[i];
+        b = unsafePt[i];
         for (int d = 0; d < S.D; ++d) {
             const double v = S.s[d][p];
-            lo[d] = fmin(lo[d], v);
-            hi[d] = fmax(hi[d], v);
+            lo[d] = v != v ? INFINITY : v;
+            hi[d] = v != v ? -INFINITY : v;
         }
-        bad |= unsafePt[S.order[p]];
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        for (int d = 0; d < 3; ++d) {
-            lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-            hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    for (int d = 0; d < S.D; ++d) {
+        lo[d] = run_reduce(lo[d], c, [](double x, double y) { return fmin(x, y); });
+        hi[d] = run_reduce(hi[d], c, [](double x, double y) { return fmax(x, y); });
+    }
+    b = run_reduce(b, c, [](int x, int y) { return x | y; });
+    if (run_head(c)) {
+        for (int d = 0; d < S.D; ++d) {
+            atomicMin(&keyLo[3 * (long long)c + d], okey(lo[d]));
+            atomicMax(&keyHi[3 * (long long)c + d], okey(hi[d]));
         }
-        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+        if (b) atomicOr(&bad[c], 1);
     }
-    if (lane == 0) {
-        for (int d = 0; d < 3; ++d) {
-            boxLo[3 * (long long)w + d] = lo[d];
-            boxHi[3 * (long long)w + d] = hi[d];
-        }
-        unsafeCell[w] = bad ? 1 : 0;
+}
+
+__global__ void box_final_kernel(int C, int D, const unsigned long long* keyLo, const unsigned long long* keyHi,
+                                 const int* bad, double* boxLo, double* boxHi, unsigned char* unsafeCell) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    for (int d = 0; d < 3; ++d) {
+        boxLo[3 * c + d] = d < D ? unkey(keyLo[3 * c + d]) : 0.0;
+        boxHi[3 * c + d] = d < D ? unkey(keyHi[3 * c + d]) : 0.0;
     }
+    unsafeCell[c] = bad[c] ? 1 : 0;
 }
 
 __device__ __forceinline__ int hash_find(const unsigned long long* tab, unsigned long long mask, const int* slotCell,
@@ -317,9 +370,32 @@ __device__ __forceinline__ void uf_unite(int* parent, int a, int b) {
     }
 }
 
+// ---- cell bounding boxes ---------------------------------------------------------
+// A cell's box holds all its points, so a box farther than eps from a point
+// (or from another box) holds no point within eps, and a box whose farthest
+// corner is within eps holds only points within eps. Both tests keep a
+// relative margin of 1e-7 on the squared distance (far above the rounding of
+// the exact test), so they never change a result, only skip work.
+constexpr double kBoxOut = 1.0000001, kBoxIn = 0.9999999;
+
+__device__ __forceinline__ void box_dist2(const double* v, const double* lo, const double* hi, int D, double& near2,
+                                          double& far2) {
+    near2 = 0.0;
+    far2 = 0.0;
+    for (int d = 0; d < D; ++d) {
+        double g = 0.0;
+        if (v[d] < lo[d]) g = lo[d] - v[d];
+        else if (v[d] > hi[d]) g = v[d] - hi[d];
+        near2 = near2 + g * g;
+        const double f = fmax(fabs(v[d] - lo[d]), fabs(hi[d] - v[d]));
+        far2 = far2 + f * f;
+    }
+}
+
 // ---- core points (DBSCAN) ----------------------------------------------------
 __global__ void core_kernel(Feat F, Sorted S, const int* cellOf, long long n, const int* nbStart, const int* nbList,
-                            const unsigned char* unsafeCell, double eps, int minPts, unsigned char* core) {
+                            const unsigned char* unsafeCell, const double* boxLo, const double* boxHi, double eps,
+                            int minPts, unsigned char* core) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int c = cellOf[i];
@@ -328,8 +404,18 @@ __global__ void core_kernel(Feat F, Sorted S, const int* cellOf, long long n, co
     if (!unsafeCell[c] && own >= minPts) { core[i] = 1; return; }
     double me[3] = {0, 0, 0};
     for (int d = 0; d < F.D; ++d) me[d] = F.f[d][i];
+    const double eps2 = eps * eps;
     int cnt = 0;
     auto count_cell = [&](int cell) {
+        if (!unsafeCell[cell]) {
+            double near2, far2;
+            box_dist2(me, boxLo + 3 * (long long)cell, boxHi + 3 * (long long)cell, S.D, near2, far2);
+            if (near2 > eps2 * kBoxOut) return;
+            if (far2 < eps2 * kBoxIn) {
+                cnt += S.start[cell + 1] - S.start[cell];
+                return;
+            }
+        }
         for (int p = S.start[cell]; p < S.start[cell + 1] && cnt < minPts; ++p) {
             double v[3];
             S.load(p, v);
@@ -342,29 +428,43 @@ __global__ void core_kernel(Feat F, Sorted S, const int* cellOf, long long n, co
     core[i] = cnt >= minPts ? 1 : 0;
 }
 
-// warp per cell: link every core point of a safe cell to its smallest core
-// point; exact pair tests inside unsafe cells. rep[c] = smallest core index or -1.
-__global__ void intra_cell_kernel(Sorted S, int C, const unsigned char* core, const unsigned char* unsafeCell,
-                                  double eps, int* parent, int* rep) {
+// rep[c] = smallest core index of cell c (or -1); every core point of a safe
+// cell is linked to it, the core points of an unsafe cell by exact pair tests.
+__global__ void rep_reduce_kernel(Sorted S, long long used, const int* cellOf, const unsigned char* core,
+                                  int* rep) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int c = -1, m = 0x7fffffff;
+    if (p < used) {
+        const int i = S.order[p];
+        c = cellOf[i];
+        if (core[i]) m = i;
+    }
+    m = run_reduce(m, c, [](int x, int y) { return min(x, y); });
+    if (run_head(c) && m != 0x7fffffff) atomicMin(&rep[c], m);
+}
+
+__global__ void rep_final_kernel(int C, int* rep) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < C && rep[c] == 0x7fffffff) rep[c] = -1;
+}
+
+__global__ void link_kernel(const int* cellOf, long long n, const unsigned char* core,
+                            const unsigned char* unsafeCell, const int* rep, int* parent) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !core[i]) return;
+    const int c = cellOf[i];
+    if (c < 0 || unsafeCell[c]) return;
+    const int m = rep[c];
+    if (m != (int)i) parent[i] = m;  // i is still a root: nothing else has linked it yet
+}
+
+// warp per unsafe cell: exact pair tests between its core points
+__global__ void unsafe_cell_kernel(Sorted S, int C, const unsigned char* core, const unsigned char* unsafeCell,
+                                   double eps, int* parent) {
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (w >= C) return;
+    if (w >= C || !unsafeCell[w]) return;
     const int b = S.start[w], e = S.start[w + 1];
-    int m = 0x7fffffff;
-    for (int p = b + lane; p < e; p += 32) {
-        const int i = S.order[p];
-        if (core[i]) m = min(m, i);
-    }
-    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0) rep[w] = m == 0x7fffffff ? -1 : m;
-    if (m == 0x7fffffff) return;
-    if (!unsafeCell[w]) {
-        for (int p = b + lane; p < e; p += 32) {
-            const int i = S.order[p];
-            if (core[i] && i != m) parent[i] = m;  // i is still a root: nothing else has linked it yet
-        }
-        return;
-    }
     for (int p = b; p < e; ++p) {
         const int i = S.order[p];
         if (!core[i]) continue;
@@ -380,41 +480,89 @@ __global__ void intra_cell_kernel(Sorted S, int C, const unsigned char* core, co
     }
 }
 
-__device__ __forceinline__ double box_gap2(const double* v, const double* lo, const double* hi, int D) {
-    double s = 0.0;
-    for (int d = 0; d < D; ++d) {
-        double g = 0.0;
-        if (v[d] < lo[d]) g = lo[d] - v[d];
-        else if (v[d] > hi[d]) g = v[d] - hi[d];
-        s = s + g * g;
-    }
-    return s;
-}
-
 // warp per (cell, neighbour cell) entry with neighbour > cell: unite the two
-// cells' core points if any core pair is within eps.
+// cells' core points if any core pair is within eps. The smaller cell's points
+// are walked one by one, the larger cell's 32 at a time.
+//
+// Two passes. Pass 0 probes every pair with a bounded amount of work (up to
+// kProbeOuter points of the smaller cell against up to kProbeChunks x 32
+// points of the larger one) and marks the pairs it could not settle. Pass 1
+// settles the marked pairs exhaustively, but first skips every pair whose two
+// cells pass 0 already put into one component. Inside a dense cluster almost
+// every pair is settled by a probe or joined through other pairs, so the
+// exhaustive scans are left to pairs that really separate two components.
+// The components found do not depend on the order of the unions.
+constexpr int kProbeOuter = 32, kProbeChunks = 8;
+
 __global__ void cross_cell_kernel(Sorted S, const int* nbOwner, const int* nbList, long long E,
                                   const unsigned char* core, const unsigned char* unsafeCell, const int* rep,
-                                  const double* boxLo, const double* boxHi, double eps, int* parent) {
+                                  const double* boxLo, const double* boxHi, double eps, int* parent, int pass,
+                                  unsigned char* deferred) {
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= E) return;
-    const int ca = nbOwner[w], cb = nbList[w];
+    int ca = nbOwner[w], cb = nbList[w];
     if (cb <= ca) return;
+    const bool probe = pass == 0;
+    if (!probe && !deferred[w]) return;
     if (rep[ca] < 0 || rep[cb] < 0) return;
     const bool safe = !unsafeCell[ca] && !unsafeCell[cb];
+    if (!safe && probe) {  // unsafe cells unite every core pair within eps: pass 1 only
+        if (lane == 0) deferred[w] = 1;
+        return;
+    }
     if (safe && uf_find(parent, rep[ca]) == uf_find(parent, rep[cb])) return;
+    const double eps2 = eps * eps;
+    const double* loA = boxLo + 3 * (long long)ca;
+    const double* hiA = boxHi + 3 * (long long)ca;
+    const double* loB = boxLo + 3 * (long long)cb;
+    const double* hiB = boxHi + 3 * (long long)cb;
+    double gap2 = 0.0, span2 = 0.0;
+    for (int d = 0; d < S.D; ++d) {
+        double g = 0.0;
+        if (hiA[d] < loB[d]) g = loB[d] - hiA[d];
+        else if (hiB[d] < loA[d]) g = loA[d] - hiB[d];
+        gap2 = gap2 + g * g;
+        const double f = fmax(hiA[d], hiB[d]) - fmin(loA[d], loB[d]);
+        span2 = span2 + f * f;
+    }
+    if (gap2 > eps2 * kBoxOut) return;
+    if (safe && span2 < eps2 * kBoxIn) {  // every point of one cell is within eps of every point of the other
+        if (lane == 0) uf_unite(parent, rep[ca], rep[cb]);
+        return;
+    }
+    if (S.start[ca + 1] - S.start[ca] > S.start[cb + 1] - S.start[cb]) {
+        const int t = ca;
+        ca = cb;
+        cb = t;
+    }
     const double* lo = boxLo + 3 * (long long)cb;
     const double* hi = boxHi + 3 * (long long)cb;
-    const double eps2 = eps * eps;
+    int outerLeft = kProbeOuter;
+    bool cut = false;
     for (int p = S.start[ca]; p < S.start[ca + 1]; ++p) {
         const int i = S.order[p];
         if (!core[i]) continue;
         double a[3];
         S.load(p, a);
-        if (box_gap2(a, lo, hi, S.D) > eps2 * 1.0000001) continue;
+        double near2, far2;
+        box_dist2(a, lo, hi, S.D, near2, far2);
+        if (near2 > eps2 * kBoxOut) continue;
+        if (safe && far2 < eps2 * kBoxIn) {  // every core point of cb is within eps of i
+            if (lane == 0) uf_unite(parent, i, rep[cb]);
+            return;
+        }
+        if (probe && outerLeft-- == 0) {
+            cut = true;
+            break;
+        }
         bool found = false;
+        int chunks = 0;
         for (int q0 = S.start[cb]; q0 < S.start[cb + 1]; q0 += 32) {
+            if (probe && chunks++ == kProbeChunks) {
+                cut = true;
+                break;
+            }
             const int q = q0 + lane;
             bool hit = false;
             int j = -1;
@@ -438,6 +586,7 @@ __global__ void cross_cell_kernel(Sorted S, const int* nbOwner, const int* nbLis
         }
         if (found) return;
     }
+    if (cut && lane == 0) deferred[w] = 1;
 }
 
 __global__ void roots_kernel(int* parent, const unsigned char* core, long long n, int* root) {
@@ -481,8 +630,8 @@ __global__ void root_marks_kernel(const int* root, long long n, int* mark) {
 
 __global__ void dbscan_labels_kernel(Feat F, Sorted S, const int* cellOf, const int* include, long long n,
                                      const int* nbStart, const int* nbList, const unsigned char* unsafeCell,
-                                     const unsigned char* core, const int* root, const int* rep, const int* rank,
-                                     double eps, int* labels) {
+                                     const double* boxLo, const double* boxHi, const unsigned char* core,
+                                     const int* root, const int* rep, const int* rank, double eps, int* labels) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (!include[i]) { labels[i] = -2; return; }
@@ -492,7 +641,20 @@ __global__ void dbscan_labels_kernel(Feat F, Sorted S, const int* cellOf, const 
     for (int d = 0; d < F.D; ++d) me[d] = F.f[d][i];
     int best = 0x7fffffff;
     if (!unsafeCell[c] && rep[c] >= 0) best = root[rep[c]];
+    const double eps2 = eps * eps;
     auto scan = [&](int cell) {
+        if (!unsafeCell[cell]) {  // all core points of a safe cell share one root
+            if (rep[cell] < 0) return;
+            const int r = root[rep[cell]];
+            if (r >= best) return;
+            double near2, far2;
+            box_dist2(me, boxLo + 3 * (long long)cell, boxHi + 3 * (long long)cell, S.D, near2, far2);
+            if (near2 > eps2 * kBoxOut) return;
+            if (far2 < eps2 * kBoxIn) {
+                best = r;
+                return;
+            }
+        }
         for (int p = S.start[cell]; p < S.start[cell + 1]; ++p) {
             const int j = S.order[p];
             if (!core[j]) continue;
@@ -566,11 +728,15 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* occ = (int*)c.alloc(cap * sizeof(int));
     int* slotCell = (int*)c.alloc(cap * sizeof(int));
     NEED(!c.failed);
-    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include); ::chaos::note_launch();
-    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, side, key, unsafePt); ::chaos::note_launch();
+    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include);
+    note_launch();
+    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, side, key, unsafePt);
+    note_launch();
     CK(cudaMemsetAsync(tab, 0xff, cap * sizeof(unsigned long long), st));
-    hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot); ::chaos::note_launch();
-    occupied_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ); ::chaos::note_launch();
+    hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot);
+    note_launch();
+    occupied_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ);
+    note_launch();
     CKL();
     int C = 0;
     int rc = exclusive_scan(c, occ, occ, (long long)cap, &C);
@@ -579,9 +745,11 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* cnt = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
     int* cellOf = (int*)c.alloc(n * sizeof(int));
     NEED(!c.failed);
-    cell_ids_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ, slotCell, cellKey); ::chaos::note_launch();
+    cell_ids_kernel<<<blocks(cap), kTPB, 0, st>>>(tab, cap, occ, slotCell, cellKey);
+    note_launch();
     CK(cudaMemsetAsync(cnt, 0, (size_t)(C + 1) * sizeof(int), st));
-    point_cell_kernel<<<blocks(n), kTPB, 0, st>>>(slot, n, slotCell, cellOf, cnt); ::chaos::note_launch();
+    point_cell_kernel<<<blocks(n), kTPB, 0, st>>>(slot, n, slotCell, cellOf, cnt);
+    note_launch();
     CKL();
     int used = 0;
     if ((rc = exclusive_scan(c, cnt, cnt, C + 1, &used))) return rc;  // cnt -> start (C+1 entries)
@@ -593,7 +761,8 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     double* s2 = (double*)c.alloc((size_t)(used + 1) * sizeof(double));
     NEED(!c.failed);
     CK(cudaMemsetAsync(cursor, 0, (size_t)(C + 1) * sizeof(int), st));
-    scatter_kernel<<<blocks(n), kTPB, 0, st>>>(F, n, cellOf, start, cursor, order, s0, s1, s2); ::chaos::note_launch();
+    scatter_kernel<<<blocks(n), kTPB, 0, st>>>(F, n, cellOf, start, cursor, order, s0, s1, s2);
+    note_launch();
     CKL();
     Sorted S;
     S.s[0] = s0;
@@ -607,10 +776,21 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     unsigned char* unsafeCell = (unsigned char*)c.alloc((size_t)C + 1);
     int* nbStart = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
     NEED(!c.failed);
+    unsigned long long* keyLo = (unsigned long long*)c.alloc((size_t)(C + 1) * 3 * sizeof(unsigned long long));
+    unsigned long long* keyHi = (unsigned long long*)c.alloc((size_t)(C + 1) * 3 * sizeof(unsigned long long));
+    int* bad = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
+    int* rep = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
+    NEED(!c.failed);
     if (C > 0) {
-        cell_box_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, unsafePt, boxLo, boxHi, unsafeCell); ::chaos::note_launch();
+        cell_init_kernel<<<blocks(C), kTPB, 0, st>>>(C, keyLo, keyHi, bad, rep);
+        note_launch();
+        box_reduce_kernel<<<blocks(used), kTPB, 0, st>>>(S, used, cellOf, unsafePt, keyLo, keyHi, bad);
+        note_launch();
+        box_final_kernel<<<blocks(C), kTPB, 0, st>>>(C, D, keyLo, keyHi, bad, boxLo, boxHi, unsafeCell);
+        note_launch();
         neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nbStart, nullptr,
-                                                      nullptr, nullptr); ::chaos::note_launch();
+                                                      nullptr, nullptr);
+        note_launch();
         CKL();
     }
     if (zeroEps && C > 0) CK(cudaMemsetAsync(unsafeCell, 1, (size_t)C, st));
@@ -621,47 +801,76 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     int* nbOwner = (int*)c.alloc((size_t)(E + 1) * sizeof(int));
     unsigned char* core = (unsigned char*)c.alloc(n);
     int* parent = (int*)c.alloc(n * sizeof(int));
-    int* rep = (int*)c.alloc((size_t)(C + 1) * sizeof(int));
     int* root = (int*)c.alloc(n * sizeof(int));
+    unsigned char* deferred = (unsigned char*)c.alloc((size_t)E + 1);
     NEED(!c.failed);
-    if (C > 0)
-        { neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nullptr, nbStart, nbList,
-                                                      nbOwner); ::chaos::note_launch(); }
-    if (compat) { core_from_include_kernel<<<blocks(n), kTPB, 0, st>>>(include, n, core); ::chaos::note_launch(); }
-    else
-        { core_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, n, nbStart, nbList, unsafeCell, eps, minPts, core); ::chaos::note_launch(); }
-    iota_kernel<<<blocks(n), kTPB, 0, st>>>(parent, n); ::chaos::note_launch();
-    if (C > 0) { intra_cell_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, core, unsafeCell, eps, parent, rep); ::chaos::note_launch(); }
-    if (E > 0)
-        { cross_cell_kernel<<<blocks((long long)E * 32), kTPB, 0, st>>>(S, nbOwner, nbList, E, core, unsafeCell, rep,
-                                                                      boxLo, boxHi, eps, parent); ::chaos::note_launch(); }
-    roots_kernel<<<blocks(n), kTPB, 0, st>>>(parent, core, n, root); ::chaos::note_launch();
+    if (C > 0) {
+        neighbours_kernel<<<blocks(C), kTPB, 0, st>>>(cellKey, C, D, tab, cap - 1, slotCell, nullptr, nbStart, nbList,
+                                                      nbOwner);
+        note_launch();
+    }
+    if (compat) {
+        core_from_include_kernel<<<blocks(n), kTPB, 0, st>>>(include, n, core);
+    } else {
+        core_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, n, nbStart, nbList, unsafeCell, boxLo, boxHi, eps,
+                                                minPts, core);
+    }
+    note_launch();
+    iota_kernel<<<blocks(n), kTPB, 0, st>>>(parent, n);
+    note_launch();
+    if (C > 0) {
+        rep_reduce_kernel<<<blocks(used), kTPB, 0, st>>>(S, used, cellOf, core, rep);
+        note_launch();
+        rep_final_kernel<<<blocks(C), kTPB, 0, st>>>(C, rep);
+        note_launch();
+        link_kernel<<<blocks(n), kTPB, 0, st>>>(cellOf, n, core, unsafeCell, rep, parent);
+        note_launch();
+        unsafe_cell_kernel<<<blocks((long long)C * 32), kTPB, 0, st>>>(S, C, core, unsafeCell, eps, parent);
+        note_launch();
+    }
+    if (E > 0) {
+        CK(cudaMemsetAsync(deferred, 0, (size_t)E, st));
+        for (int pass = 0; pass < 2; ++pass) {
+            cross_cell_kernel<<<blocks((long long)E * 32), kTPB, 0, st>>>(S, nbOwner, nbList, E, core, unsafeCell,
+                                                                          rep, boxLo, boxHi, eps, parent, pass,
+                                                                          deferred);
+            note_launch();
+        }
+    }
+    roots_kernel<<<blocks(n), kTPB, 0, st>>>(parent, core, n, root);
+    note_launch();
     CKL();
     if (compat) {
         int* minFix = (int*)c.alloc(n * sizeof(int));
         int* negRank = (int*)c.alloc(n * sizeof(int));
         int* posRank = (int*)c.alloc(n * sizeof(int));
         NEED(!c.failed);
-        fill_kernel<<<blocks(n), kTPB, 0, st>>>(minFix, n, (int)n); ::chaos::note_launch();
-        compat_minfix_kernel<<<blocks(n), kTPB, 0, st>>>(root, flags, n, minFix); ::chaos::note_launch();
+        fill_kernel<<<blocks(n), kTPB, 0, st>>>(minFix, n, (int)n);
+        note_launch();
+        compat_minfix_kernel<<<blocks(n), kTPB, 0, st>>>(root, flags, n, minFix);
+        note_launch();
         CK(cudaMemsetAsync(negRank, 0, n * sizeof(int), st));
         CK(cudaMemsetAsync(posRank, 0, n * sizeof(int), st));
-        compat_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank); ::chaos::note_launch();
+        compat_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank);
+        note_launch();
         CKL();
         int t = 0;
         if ((rc = exclusive_scan(c, negRank, negRank, n, &t))) return rc;
         if ((rc = exclusive_scan(c, posRank, posRank, n, &t))) return rc;
-        compat_labels_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank, labels); ::chaos::note_launch();
+        compat_labels_kernel<<<blocks(n), kTPB, 0, st>>>(root, minFix, n, negRank, posRank, labels);
+        note_launch();
         CKL();
     } else {
         int* rank = (int*)c.alloc(n * sizeof(int));
         NEED(!c.failed);
-        root_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, n, rank); ::chaos::note_launch();
+        root_marks_kernel<<<blocks(n), kTPB, 0, st>>>(root, n, rank);
+        note_launch();
         CKL();
         int t = 0;
         if ((rc = exclusive_scan(c, rank, rank, n, &t))) return rc;
         dbscan_labels_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, include, n, nbStart, nbList, unsafeCell,
-                                                         core, root, rep, rank, eps, labels); ::chaos::note_launch();
+                                                         boxLo, boxHi, core, root, rep, rank, eps, labels);
+        ::chaos::note_launch();
         CKL();
     }
     return CHAOS_OK;
@@ -677,12 +886,14 @@ int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total) {
     const long long nb = (n + kScanItems - 1) / kScanItems;
     int* sums = (int*)c.alloc((size_t)(nb + 1) * sizeof(int));
     if (!sums) return CHAOS_E_NOMEM;
-    scan_block_kernel<<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n); ::chaos::note_launch();
+    scan_block_kernel<<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n);
+    note_launch();
     CK(cudaGetLastError());
     if (nb > 1) {
         int rc = exclusive_scan(c, sums, sums, nb, total);
         if (rc) return rc;
-        add_offsets_kernel<<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n); ::chaos::note_launch();
+        add_offsets_kernel<<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n);
+        note_launch();
         CK(cudaGetLastError());
     } else if (total) {
         CK(cudaMemcpyAsync(total, sums, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -707,7 +918,8 @@ int dbscan_device(Call& c, const double* features, long long n, int dims, double
     double* b = (double*)c.alloc(n * sizeof(double));
     double* d = (double*)c.alloc(n * sizeof(double));
     if (c.failed) return CHAOS_E_NOMEM;
-    soa_kernel<<<blocks(n), kTPB, 0, c.stream>>>(features, n, dims, a, b, d); ::chaos::note_launch();
+    soa_kernel<<<blocks(n), kTPB, 0, c.stream>>>(features, n, dims, a, b, d);
+    note_launch();
     CK(cudaGetLastError());
     Feat F;
     F.f[0] = a;

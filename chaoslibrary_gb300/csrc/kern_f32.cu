@@ -137,15 +137,25 @@ bool use_pairs(const SweepParams& P, bool basins) {
     return P.nPoints >= threshold;
 }
 
+template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, cudaStream_t st) {
+    bif_pair_kernel_f32<F><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+    note_launch();
+}
+
+template <class F> void launch_basins_pairs(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
+    basins_pair_kernel_f32<F><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+    note_launch();
+}
+
 cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
     if (use_pairs(P, false)) {
-        if (P.system == SYS_LORENZ_RK4) { bif_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
-        else if (P.system == SYS_ROSSLER_RK4) { bif_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
-        else { bif_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+        if (P.system == SYS_LORENZ_RK4) launch_bif_pairs<Lorenz>(P, O, st);
+        else if (P.system == SYS_ROSSLER_RK4) launch_bif_pairs<Rossler>(P, O, st);
+        else launch_bif_pairs<Chen>(P, O, st);
         return cudaGetLastError();
     }
-#define CALL(S) (bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), ::chaos::note_launch())
+#define CALL(S) (bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -154,12 +164,12 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
     if (use_pairs(P, true)) {
-        if (P.system == SYS_LORENZ_RK4) { basins_pair_kernel_f32<Lorenz><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
-        else if (P.system == SYS_ROSSLER_RK4) { basins_pair_kernel_f32<Rossler><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
-        else { basins_pair_kernel_f32<Chen><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+        if (P.system == SYS_LORENZ_RK4) launch_basins_pairs<Lorenz>(P, O, st);
+        else if (P.system == SYS_ROSSLER_RK4) launch_basins_pairs<Rossler>(P, O, st);
+        else launch_basins_pairs<Chen>(P, O, st);
         return cudaGetLastError();
     }
-#define CALL(S) (basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), ::chaos::note_launch())
+#define CALL(S) (basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -176,9 +186,10 @@ __global__ void __launch_bounds__(kBlock) lle_pair_kernel_f32(LleParams L, doubl
 
 template <class F>
 static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb) {
-    if (minb == 2) { lle_pair_kernel_f32<F><<<grid_for((L.nPoints + 1) / 2), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
-    else if (minb >= 16) { lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
-    else { lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
+    if (minb == 2) lle_pair_kernel_f32<F><<<grid_for((L.nPoints + 1) / 2), kBlock, 0, st>>>(L, out);
+    else if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+    else lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+    note_launch();
 }
 
 int set_lle_variant(int v) {
@@ -203,7 +214,8 @@ cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
 cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-#define CALL(S) (trajectory_kernel_f32<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n), ::chaos::note_launch())
+#define CALL(S) \
+    (trajectory_kernel_f32<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n), note_launch())
     CHAOS_SYSTEM_SWITCH(system, CALL)
 #undef CALL
     return cudaGetLastError();

@@ -155,7 +155,7 @@ int launch_block_size() { return kBlock; }
 
 cudaError_t launch_bif_f64(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-#define CALL(S) (bif_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), ::chaos::note_launch())
+#define CALL(S) (bif_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -163,7 +163,7 @@ cudaError_t launch_bif_f64(const SweepParams& P, const BifOut& O, cudaStream_t s
 
 cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-#define CALL(S) (basins_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), ::chaos::note_launch())
+#define CALL(S) (basins_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -171,7 +171,7 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
-#define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), ::chaos::note_launch())
+#define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -180,7 +180,8 @@ cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
 cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, double h, int cap, int* counts,
                                double* peaks, double* intervals, cudaStream_t st) {
     if (nSeries <= 0) return cudaSuccess;
-    peak_array_kernel<<<grid_for(nSeries), kBlock, 0, st>>>(data, nSeries, len, h, cap, counts, peaks, intervals); ::chaos::note_launch();
+    peak_array_kernel<<<grid_for(nSeries), kBlock, 0, st>>>(data, nSeries, len, h, cap, counts, peaks, intervals);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -189,14 +190,16 @@ cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long
     if (n <= 0) return cudaSuccess;
     const long long threads = n * 32;
     point_dbscan_kernel<<<(unsigned)((threads + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-        intervals, counts, n, stride, eps, labScratch, slotScratch, out); ::chaos::note_launch();
+        intervals, counts, n, stride, eps, labScratch, slotScratch, out);
+    note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-#define CALL(S) (trajectory_kernel<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n), ::chaos::note_launch())
+#define CALL(S) \
+    (trajectory_kernel<S><<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n), note_launch())
     CHAOS_SYSTEM_SWITCH(system, CALL)
 #undef CALL
     return cudaGetLastError();

@@ -49,20 +49,32 @@ void user_system_sizes(int* nx, int* na) {
     *na = SIZE_A;
 }
 cudaError_t launch_bif_user(const SweepParams& P, const BifOut& O, cudaStream_t st) {
-    if (P.nPoints > 0) { bif_kernel_user<<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+    if (P.nPoints > 0) {
+        bif_kernel_user<<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O);
+        note_launch();
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_basins_user(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
-    if (P.nPoints > 0) { basins_kernel_user<<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O); ::chaos::note_launch(); }
+    if (P.nPoints > 0) {
+        basins_kernel_user<<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O);
+        note_launch();
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_lle_user(const LleParams& L, double* out, cudaStream_t st) {
-    if (L.nPoints > 0) { lle_kernel_user<<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); ::chaos::note_launch(); }
+    if (L.nPoints > 0) {
+        lle_kernel_user<<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+        note_launch();
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_trajectory_user(const double* x0, const double* a0, double h, int nSteps, double* out,
                                    long long n, cudaStream_t st) {
-    if (n > 0) { trajectory_kernel_user<<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n); ::chaos::note_launch(); }
+    if (n > 0) {
+        trajectory_kernel_user<<<grid_for(n), kBlock, 0, st>>>(x0, a0, h, nSteps, out, n);
+        note_launch();
+    }
     return cudaGetLastError();
 }
 

@@ -154,6 +154,29 @@ def test_dbscan_random_vs_oracle(engine, oracle, n, d, eps, min_pts, seed):
     assert np.array_equal(lab, ref)
 
 
+@pytest.mark.parametrize("d, min_pts, seed", [(3, 8, 11), (2, 5, 12)])
+def test_dbscan_concentrated_vs_oracle(engine, oracle, d, min_pts, seed):
+    """Thousands of points on one spot (attractors that are fixed points give
+    identical features), tight blobs, points on shells at eps +- 1e-12 around
+    a spot, and sparse noise: the cell bounding-box shortcuts of the device
+    clustering change no label."""
+    rng = np.random.default_rng(seed)
+    eps = 0.05
+    spot = np.full(d, 0.2)
+    parts = [np.tile(spot, (6000, 1)),
+             np.full(d, 0.7) + rng.normal(scale=1e-7, size=(6000, d)),
+             np.full(d, 0.5) + rng.uniform(-0.02, 0.02, size=(3000, d))]
+    u = rng.normal(size=(400, d))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    parts.append(spot + u * (eps + rng.choice([-1e-12, 1e-12], size=(400, 1))))
+    parts.append(rng.uniform(0, 1, size=(3000 if d == 3 else 300, d)))
+    X = np.concatenate(parts)
+    X = X[rng.permutation(len(X))]
+    lab = engine.dbscan(X, eps, min_pts)
+    ref = oracle.dbscan(X, eps, min_pts)
+    assert np.array_equal(lab, ref)
+
+
 @pytest.mark.parametrize("n, spread, eps, seed", [(100000, 1.0, 0.005, 5), (400000, 3.0, 0.01, 6)])
 def test_dbscan_compat_random_vs_oracle(engine, oracle, n, spread, eps, seed):
     rng = np.random.default_rng(seed)
