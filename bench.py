@@ -759,7 +759,23 @@ def lle_precision_report(C, prec, dev):
     e1.record()
     torch.cuda.synchronize()
     t32 = e0.elapsed_time(e1) / 1e3
+    # FP32 map with the FP64 sign re-check of the points within 0.01 of zero
+    # (short check over tMax / 10 time units)
+    C.lle2d_checked("rossler", **dict(kw, nPts=64))
+    e0.record()
+    oc, n_checked, n_replaced = C.lle2d_checked("rossler", band=0.01, checkTMax=w["tMax"] / 10, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    tc = e0.elapsed_time(e1) / 1e3
     a, b = o64.cpu().numpy(), o32.cpu().numpy()
+
+    def cls(v):
+        return np.where(~np.isfinite(v), -1, (v > 0).astype(int))
+    recheck = {"band": 0.01, "check_tmax": w["tMax"] / 10, "points_checked": n_checked,
+               "points_replaced": n_replaced, "value": n * lle_steps_per_point(w) / tc, "unit": UNIT,
+               "time_vs_fp32": tc / t32,
+               "sign_class_agreement_with_fp64": {"fp32": float(np.mean(cls(b) == cls(a))),
+                                                  "fp32_rechecked": float(np.mean(cls(oc) == cls(a)))}}
     fin = np.isfinite(a) & np.isfinite(b)
     d = np.abs(a[fin] - b[fin])
     reg = a[fin] < 0.005
@@ -772,7 +788,8 @@ def lle_precision_report(C, prec, dev):
                                   "regular_points": int(reg.sum()),
                                   "regular_max": float(d[reg].max()) if reg.any() else None,
                                   "chaotic_class_agreement": float(np.mean((a[fin] > 0.01) == (b[fin] > 0.01))),
-                                  "nonfinite_mismatch": int(np.sum(np.isfinite(a) != np.isfinite(b)))}}
+                                  "nonfinite_mismatch": int(np.sum(np.isfinite(a) != np.isfinite(b)))},
+            "fp64_sign_recheck": recheck}
 
 
 def main():

@@ -61,6 +61,7 @@ _SIGS = {
     "chaos_bifurcation1d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _P], _I),
     "chaos_bifurcation2d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P], _I),
     "chaos_lle2d": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, _P], _I),
+    "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
     "chaos_basins_features": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _P, _P, _P, _P], _I),
     "chaos_basins": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P, _P, _P], _I),
     "chaos_dbscan_compat": ([_P, _P, _P, _P, _L, _D, _P], _I),
@@ -467,6 +468,26 @@ def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMu
                              A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size,
                              _out_ptr(out)))
     return out
+
+
+def lle2d_checked(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime,
+                  values, band=0.01, checkTMax=None, out=None, stream=None):
+    """FP32 LLE map whose points with |value| <= band (or not finite) get an
+    FP64 re-check over checkTMax (default tMax / 10) time units; points whose
+    sign class the check contradicts carry their full FP64 value. Returns
+    (lle, n_checked, n_replaced)."""
+    A = _Args()
+    if out is None:
+        out = np.zeros(nPts * nPts)
+    ex = _exec(FP32, {"lle": out}, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    nc, nr = C.c_longlong(), C.c_longlong()
+    _check(lib().chaos_lle2d_checked(C.byref(ex), _sys(system), tMax, NT, nPts, h, eps, A.d(ic), ic.size,
+                                     A.d(ranges), A.i(indicesOfMutVars), transientTime, A.d(vals), vals.size, band,
+                                     tMax / 10 if checkTMax is None else checkTMax, _out_ptr(out), C.byref(nc),
+                                     C.byref(nr)))
+    return out, nc.value, nr.value
 
 
 def basins_features(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,

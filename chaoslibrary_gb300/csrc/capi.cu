@@ -434,6 +434,60 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     return c.finish(rc);
 }
 
+int chaos_lle2d_checked(const chaos_exec* ex, int system, double tMax, double NT, int nPts, double h, double eps,
+                        const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+                        const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
+                        double band, double checkTMax, double* lle, long long* nChecked, long long* nReplaced) {
+    int rc = CHAOS_OK;
+    if (!lle) return set_error(CHAOS_E_ARGS, "null argument");
+    if (!(band >= 0) || !(checkTMax > 0)) return set_error(CHAOS_E_ARGS, "need band >= 0 and checkTMax > 0");
+    LleParams L, Lc;
+    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                       indicesOfMutVars, transientTime, values, amountOfValues)))
+        return rc;
+    const bool fullCheck = checkTMax >= tMax;
+    if ((rc = fill_lle(Lc, system, fullCheck ? tMax : checkTMax, NT, nPts, h, eps, initialConditions,
+                       amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values, amountOfValues)))
+        return rc;
+    if (!system_has_difference_form(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2)");
+    if (L.nPoints > 0x7fffffffLL) return set_error(CHAOS_E_ARGS, "nPts^2 must be < 2^31");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const long long n = L.nPoints;
+    double* dOut = (double*)c.output(lle, n * sizeof(double));
+    int* counts = (int*)c.alloc(2 * sizeof(int));
+    int* list = (int*)c.alloc(n * sizeof(int));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = launch_lle_f32(L, dOut, c.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, 2 * sizeof(int), c.stream);
+    if (e == cudaSuccess) e = launch_lle_select(dOut, n, band, list, counts, c.stream);
+    int h0[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h0, counts, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "FP32 LLE map and selection"));
+    const long long checked = h0[0];
+    long long replaced = 0;
+    if (checked > 0) {
+        double* check = (double*)c.alloc(checked * sizeof(double));
+        int* list2 = fullCheck ? nullptr : (int*)c.alloc(checked * sizeof(int));
+        if (c.failed) return c.finish(CHAOS_E_NOMEM);
+        e = launch_lle_list_f64(Lc, list, counts, checked, check, false, c.stream);
+        if (e == cudaSuccess)
+            e = launch_lle_flip(dOut, list, counts, checked, check, fullCheck, dOut, list2, counts + 1, c.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h0 + 1, counts + 1, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e == cudaSuccess && !fullCheck && h0[1] > 0)
+            e = launch_lle_list_f64(L, list2, counts + 1, h0[1], dOut, true, c.stream);
+        if (e != cudaSuccess) return c.finish(cuda_error(e, "FP64 re-check"));
+        replaced = h0[1];
+    }
+    if (nChecked) *nChecked = checked;
+    if (nReplaced) *nReplaced = replaced;
+    rc = c.to_host(lle, dOut, n * sizeof(double));
+    return c.finish(rc);
+}
+
 int chaos_basins_features(const chaos_exec* ex, int system, double tMax, int nPts, double h,
                           int amountOfInitialConditions, const double* initialConditions, const double* ranges,
                           const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,

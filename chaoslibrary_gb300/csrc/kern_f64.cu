@@ -34,6 +34,59 @@ __global__ void __launch_bounds__(kBlock) lle_kernel(LleParams L, double* out) {
     out[o] = lle_point_full<S, double>(L, L.pBegin + o);
 }
 
+// FP64 LLE of the points list[0, *count): out[k] (scatter = 0) or out[list[k]]
+// (scatter = 1). The same device function as lle_kernel, so a point's value
+// is the FP64 map's value bit for bit.
+template <int S>
+__global__ void __launch_bounds__(kBlock) lle_list_kernel(LleParams L, const int* list, const int* count,
+                                                          double* out, int scatter) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= *count) return;
+    const int p = list[k];
+    const double v = lle_point_full<S, double>(L, p);
+    out[scatter ? p : k] = v;
+}
+
+// class of an LLE value for the sign re-check: 1 positive, 0 non-positive,
+// -1 not finite
+__device__ __forceinline__ int lle_class(double v) { return !(fabs(v) <= 1.7976931348623157e308) ? -1 : v > 0.0; }
+
+// warp-aggregated append of p to list (one atomic per warp; list may be null
+// to count only)
+__device__ __forceinline__ void append(bool take, int p, int* list, int* count) {
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take && list) list[base + __popc(m & ((1u << lane) - 1))] = p;
+}
+
+// points whose value is within band of zero or not finite
+__global__ void lle_select_kernel(const double* v, long long n, double band, int* list, int* count) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool take = i < n && !(fabs(v[i]) > band);
+    append(take, (int)i, list, count);
+}
+
+// checked points whose FP64 check disagrees in class with the FP32 value are
+// counted in count2 and appended to list2 (when not null); with final = 1
+// (the check ran the full horizon) their check value is stored into out.
+// Every thread of the grid reaches the warp vote.
+__global__ void lle_flip_kernel(const double* v32, const int* list, const int* count, const double* check,
+                                int final_, double* out, int* list2, int* count2) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool take = false;
+    int p = 0;
+    if (k < *count) {
+        p = list[k];
+        take = lle_class(v32[p]) != lle_class(check[k]);
+    }
+    append(take, p, list2, count2);
+    if (take && final_) out[p] = check[k];
+}
+
 template <int S>
 __global__ void __launch_bounds__(kBlock) trajectory_kernel(const double* x0, const double* a0, double h, int nSteps,
                                                        double* out, long long n) {
@@ -174,6 +227,32 @@ cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
 #define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_select(const double* v, long long n, double band, int* list, int* count, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    lle_select_kernel<<<grid_for(n), kBlock, 0, st>>>(v, n, band, list, count);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_list_f64(const LleParams& L, const int* list, const int* count, long long maxCount,
+                                double* out, bool scatter, cudaStream_t st) {
+    if (maxCount <= 0) return cudaSuccess;
+#define CALL(S) \
+    (lle_list_kernel<S><<<grid_for(maxCount), kBlock, 0, st>>>(L, list, count, out, scatter ? 1 : 0), note_launch())
+    CHAOS_SYSTEM_SWITCH(L.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_flip(const double* v32, const int* list, const int* count, long long maxCount,
+                            const double* check, bool final_, double* out, int* list2, int* count2, cudaStream_t st) {
+    if (maxCount <= 0) return cudaSuccess;
+    lle_flip_kernel<<<grid_for(maxCount), kBlock, 0, st>>>(v32, list, count, check, final_ ? 1 : 0, out, list2,
+                                                            count2);
+    note_launch();
     return cudaGetLastError();
 }
 

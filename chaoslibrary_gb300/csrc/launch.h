@@ -83,6 +83,13 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
+// FP64 sign re-check of an FP32 LLE map (kern_f64.cu): select the points with
+// |v| <= band or v not finite, FP64 LLE of a point list, compare classes
+cudaError_t launch_lle_select(const double* v, long long n, double band, int* list, int* count, cudaStream_t st);
+cudaError_t launch_lle_list_f64(const LleParams& L, const int* list, const int* count, long long maxCount,
+                                double* out, bool scatter, cudaStream_t st);
+cudaError_t launch_lle_flip(const double* v32, const int* list, const int* count, long long maxCount,
+                            const double* check, bool final_, double* out, int* list2, int* count2, cudaStream_t st);
 // reference-semantics kernels on caller arrays (kern_f64.cu)
 cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, double h, int cap, int* counts,
                                double* peaks, double* intervals, cudaStream_t st);

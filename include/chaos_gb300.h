@@ -129,6 +129,24 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
                 const double* values, int amountOfValues, double* lle);
 
 /*
+ * LLE map in FP32 with an FP64 sign re-check (no reference counterpart: the
+ * reference computes in FP64 only). Arguments as chaos_lle2d (RK4 systems
+ * 0-2; ex->precision is ignored). The map is computed as chaos_lle2d with
+ * CHAOS_FP32; every point whose FP32 value v has |v| <= band or is not finite
+ * is integrated again in FP64 over a short horizon of checkTMax time units
+ * (same transient, NT and eps). Where the check's class (positive,
+ * non-positive, not finite) differs from v's, the point's value is replaced by
+ * its FP64 value over the full horizon, bit-identical to chaos_lle2d with
+ * CHAOS_FP64 there. checkTMax >= tMax makes the check itself that full run.
+ * nChecked / nReplaced (may be NULL) receive the numbers of points checked and
+ * replaced. The call waits for the selection and the check (two host syncs).
+ */
+int chaos_lle2d_checked(const chaos_exec* ex, int system, double tMax, double NT, int nPts, double h, double eps,
+                        const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+                        const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
+                        double band, double checkTMax, double* lle, long long* nChecked, long long* nReplaced);
+
+/*
  * Per-point basin features over the nPts x nPts grid of initial conditions
  * (initialConditions[indicesOfMutVars[0]] over ranges[0..1] fastest,
  * initialConditions[indicesOfMutVars[1]] over ranges[2..3]). The first stage
