@@ -393,19 +393,47 @@ __device__ __forceinline__ void box_dist2(const double* v, const double* lo, con
 }
 
 // ---- core points (DBSCAN) ----------------------------------------------------
-__global__ void core_kernel(Feat F, Sorted S, const int* cellOf, long long n, const int* nbStart, const int* nbList,
-                            const unsigned char* unsafeCell, const double* boxLo, const double* boxHi, double eps,
-                            int minPts, unsigned char* core) {
+// warp-aggregated append of p to list (one atomic per warp)
+__device__ __forceinline__ void list_append(bool take, int p, int* list, int* count) {
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take) list[base + __popc(m & ((1u << lane) - 1))] = p;
+}
+
+// points of a safe cell holding >= minPts points are core; every other
+// included point is listed for the exact count below
+__global__ void core_kernel(Sorted S, const int* cellOf, long long n, const unsigned char* unsafeCell, int minPts,
+                            unsigned char* core, int* sparse, int* nSparse) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    bool take = false;
+    if (i < n) {
+        const int c = cellOf[i];
+        if (c < 0) core[i] = 0;
+        else if (!unsafeCell[c] && S.start[c + 1] - S.start[c] >= minPts) core[i] = 1;
+        else take = true;
+    }
+    list_append(take, (int)i, sparse, nSparse);
+}
+
+// warp per listed point: neighbours within eps counted 32 at a time, whole
+// safe cells counted or skipped by their bounding boxes, early exit at minPts
+__global__ void core_sparse_kernel(Feat F, Sorted S, const int* cellOf, const int* sparse, int nSparse,
+                                   const int* nbStart, const int* nbList, const unsigned char* unsafeCell,
+                                   const double* boxLo, const double* boxHi, double eps, int minPts,
+                                   unsigned char* core) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nSparse) return;
+    const int i = sparse[w];
     const int c = cellOf[i];
-    if (c < 0) { core[i] = 0; return; }
-    const int own = S.start[c + 1] - S.start[c];
-    if (!unsafeCell[c] && own >= minPts) { core[i] = 1; return; }
     double me[3] = {0, 0, 0};
     for (int d = 0; d < F.D; ++d) me[d] = F.f[d][i];
     const double eps2 = eps * eps;
-    int cnt = 0;
+    int cnt = 0;  // the same in every lane
     auto count_cell = [&](int cell) {
         if (!unsafeCell[cell]) {
             double near2, far2;
@@ -416,16 +444,22 @@ __global__ void core_kernel(Feat F, Sorted S, const int* cellOf, long long n, co
                 return;
             }
         }
-        for (int p = S.start[cell]; p < S.start[cell + 1] && cnt < minPts; ++p) {
-            double v[3];
-            S.load(p, v);
-            if (sqrt(dist2(me, v, S.D)) <= eps) ++cnt;
+        const int end = S.start[cell + 1];
+        for (int p0 = S.start[cell]; p0 < end && cnt < minPts; p0 += 32) {
+            const int p = p0 + lane;
+            bool hit = false;
+            if (p < end) {
+                double v[3];
+                S.load(p, v);
+                hit = sqrt(dist2(me, v, S.D)) <= eps;
+            }
+            cnt += __popc(__ballot_sync(0xffffffffu, hit));
         }
     };
-    if (!unsafeCell[c]) cnt = own;  // one cell is within eps of itself
+    if (!unsafeCell[c]) cnt = S.start[c + 1] - S.start[c];  // one cell is within eps of itself
     else count_cell(c);
     for (int e = nbStart[c]; e < nbStart[c + 1] && cnt < minPts; ++e) count_cell(nbList[e]);
-    core[i] = cnt >= minPts ? 1 : 0;
+    if (lane == 0) core[i] = cnt >= minPts ? 1 : 0;
 }
 
 // rep[c] = smallest core index of cell c (or -1); every core point of a safe
@@ -484,15 +518,18 @@ __global__ void unsafe_cell_kernel(Sorted S, int C, const unsigned char* core, c
 // cells' core points if any core pair is within eps. The smaller cell's points
 // are walked one by one, the larger cell's 32 at a time.
 //
-// Two passes. Pass 0 probes every pair with a bounded amount of work (up to
-// kProbeOuter points of the smaller cell against up to kProbeChunks x 32
-// points of the larger one) and marks the pairs it could not settle. Pass 1
-// settles the marked pairs exhaustively, but first skips every pair whose two
-// cells pass 0 already put into one component. Inside a dense cluster almost
-// every pair is settled by a probe or joined through other pairs, so the
-// exhaustive scans are left to pairs that really separate two components.
-// The components found do not depend on the order of the unions.
-constexpr int kProbeOuter = 32, kProbeChunks = 8;
+// Three passes of growing budget. Pass 0 probes every pair with a small
+// amount of work (kPassOuter points of the smaller cell against kPassChunks
+// x 32 points of the larger one) and marks the pairs it could not settle;
+// each later pass takes the marked pairs only, first skips those whose two
+// cells earlier unions already put into one component, and the last pass
+// scans exhaustively. Inside a dense cluster almost every pair is settled by a
+// probe or joined through other pairs, so the exhaustive scans are left to
+// pairs that really separate two components. The components found do not
+// depend on the order of the unions.
+constexpr int kCrossPasses = 3;
+__constant__ int kPassOuter[kCrossPasses] = {2, 32, 0x7fffffff};
+__constant__ int kPassChunks[kCrossPasses] = {2, 8, 0x7fffffff};
 
 __global__ void cross_cell_kernel(Sorted S, const int* nbOwner, const int* nbList, long long E,
                                   const unsigned char* core, const unsigned char* unsafeCell, const int* rep,
@@ -503,11 +540,16 @@ __global__ void cross_cell_kernel(Sorted S, const int* nbOwner, const int* nbLis
     if (w >= E) return;
     int ca = nbOwner[w], cb = nbList[w];
     if (cb <= ca) return;
-    const bool probe = pass == 0;
-    if (!probe && !deferred[w]) return;
+    const bool last = pass == kCrossPasses - 1;
+    if (pass > 0) {
+        const bool todo = deferred[w] != 0;
+        __syncwarp();  // every lane has read the mark before lane 0 clears it
+        if (!todo) return;
+        if (lane == 0) deferred[w] = 0;
+    }
     if (rep[ca] < 0 || rep[cb] < 0) return;
     const bool safe = !unsafeCell[ca] && !unsafeCell[cb];
-    if (!safe && probe) {  // unsafe cells unite every core pair within eps: pass 1 only
+    if (!safe && !last) {  // unsafe cells unite every core pair within eps: last pass only
         if (lane == 0) deferred[w] = 1;
         return;
     }
@@ -538,53 +580,70 @@ __global__ void cross_cell_kernel(Sorted S, const int* nbOwner, const int* nbLis
     }
     const double* lo = boxLo + 3 * (long long)cb;
     const double* hi = boxHi + 3 * (long long)cb;
-    int outerLeft = kProbeOuter;
-    bool cut = false;
-    for (int p = S.start[ca]; p < S.start[ca + 1]; ++p) {
-        const int i = S.order[p];
-        if (!core[i]) continue;
-        double a[3];
-        S.load(p, a);
-        double near2, far2;
-        box_dist2(a, lo, hi, S.D, near2, far2);
-        if (near2 > eps2 * kBoxOut) continue;
-        if (safe && far2 < eps2 * kBoxIn) {  // every core point of cb is within eps of i
-            if (lane == 0) uf_unite(parent, i, rep[cb]);
+    int outerLeft = kPassOuter[pass];
+    const int chunkBudget = kPassChunks[pass];
+    bool cut = false, stop = false;
+    // lanes test 32 points of the smaller cell against cb's box at a time;
+    // the points in reach are then taken one by one against cb's points
+    const int endA = S.start[ca + 1], endB = S.start[cb + 1];
+    for (int p0 = S.start[ca]; p0 < endA && !stop; p0 += 32) {
+        const int p = p0 + lane;
+        int i = -1;
+        double a[3] = {0, 0, 0};
+        bool inReach = false, allIn = false;
+        if (p < endA) {
+            i = S.order[p];
+            if (core[i]) {
+                S.load(p, a);
+                double near2, far2;
+                box_dist2(a, lo, hi, S.D, near2, far2);
+                inReach = near2 <= eps2 * kBoxOut;
+                allIn = safe && far2 < eps2 * kBoxIn;
+            }
+        }
+        const unsigned mAll = __ballot_sync(0xffffffffu, inReach && allIn);
+        if (mAll) {  // every core point of cb is within eps of this one
+            if (lane == __ffs(mAll) - 1) uf_unite(parent, i, rep[cb]);
             return;
         }
-        if (probe && outerLeft-- == 0) {
-            cut = true;
-            break;
-        }
-        bool found = false;
-        int chunks = 0;
-        for (int q0 = S.start[cb]; q0 < S.start[cb + 1]; q0 += 32) {
-            if (probe && chunks++ == kProbeChunks) {
-                cut = true;
+        unsigned todo = __ballot_sync(0xffffffffu, inReach);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            if (outerLeft-- == 0) {
+                cut = stop = true;
                 break;
             }
-            const int q = q0 + lane;
-            bool hit = false;
-            int j = -1;
-            if (q < S.start[cb + 1]) {
-                j = S.order[q];
-                if (core[j]) {
-                    double v[3];
-                    S.load(q, v);
-                    hit = sqrt(dist2(a, v, S.D)) <= eps;
-                }
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, hit);
-            if (bal) {
-                if (safe) {
-                    if (lane == __ffs(bal) - 1) uf_unite(parent, i, j);
-                    found = true;
+            const int ii = __shfl_sync(0xffffffffu, i, src);
+            double aa[3];
+            for (int d = 0; d < 3; ++d) aa[d] = __shfl_sync(0xffffffffu, a[d], src);
+            int chunks = 0;
+            for (int q0 = S.start[cb]; q0 < endB; q0 += 32) {
+                if (chunks++ == chunkBudget) {
+                    cut = true;
                     break;
                 }
-                if (hit) uf_unite(parent, i, j);
+                const int q = q0 + lane;
+                bool hit = false;
+                int j = -1;
+                if (q < endB) {
+                    j = S.order[q];
+                    if (core[j]) {
+                        double v[3];
+                        S.load(q, v);
+                        hit = sqrt(dist2(aa, v, S.D)) <= eps;
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, hit);
+                if (bal) {
+                    if (safe) {
+                        if (lane == __ffs(bal) - 1) uf_unite(parent, ii, j);
+                        return;
+                    }
+                    if (hit) uf_unite(parent, ii, j);
+                }
             }
         }
-        if (found) return;
     }
     if (cut && lane == 0) deferred[w] = 1;
 }
@@ -811,11 +870,23 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     }
     if (compat) {
         core_from_include_kernel<<<blocks(n), kTPB, 0, st>>>(include, n, core);
+        note_launch();
     } else {
-        core_kernel<<<blocks(n), kTPB, 0, st>>>(F, S, cellOf, n, nbStart, nbList, unsafeCell, boxLo, boxHi, eps,
-                                                minPts, core);
+        int* sparse = (int*)c.alloc((n + 1) * sizeof(int));
+        int* nSparse = (int*)c.alloc(sizeof(int));
+        NEED(!c.failed);
+        CK(cudaMemsetAsync(nSparse, 0, sizeof(int), st));
+        core_kernel<<<blocks(n), kTPB, 0, st>>>(S, cellOf, n, unsafeCell, minPts, core, sparse, nSparse);
+        note_launch();
+        int hSparse = 0;
+        CK(cudaMemcpyAsync(&hSparse, nSparse, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hSparse > 0) {
+            core_sparse_kernel<<<blocks((long long)hSparse * 32), kTPB, 0, st>>>(
+                F, S, cellOf, sparse, hSparse, nbStart, nbList, unsafeCell, boxLo, boxHi, eps, minPts, core);
+            note_launch();
+        }
     }
-    note_launch();
     iota_kernel<<<blocks(n), kTPB, 0, st>>>(parent, n);
     note_launch();
     if (C > 0) {
@@ -830,7 +901,7 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     }
     if (E > 0) {
         CK(cudaMemsetAsync(deferred, 0, (size_t)E, st));
-        for (int pass = 0; pass < 2; ++pass) {
+        for (int pass = 0; pass < kCrossPasses; ++pass) {
             cross_cell_kernel<<<blocks((long long)E * 32), kTPB, 0, st>>>(S, nbOwner, nbList, E, core, unsafeCell,
                                                                           rep, boxLo, boxHi, eps, parent, pass,
                                                                           deferred);
