@@ -45,8 +45,13 @@ __device__ __forceinline__ void run_basins(const JobDesc& J, long long b, int cn
     __shared__ SweepParams sP;
     if (threadIdx.x == 0) sP = J.sp;
     __syncthreads();
+    if (sP.preScaller == 1) {
 #pragma unroll 1
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) basins_point<S, float>(sP, J.bas, b + t, b + t);
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) basins_point<S, float, true>(sP, J.bas, b + t, b + t);
+    } else {
+#pragma unroll 1
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) basins_point<S, float, false>(sP, J.bas, b + t, b + t);
+    }
 }
 
 // The job's parameter block is staged in shared memory for the chunk: read

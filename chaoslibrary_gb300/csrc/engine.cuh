@@ -190,12 +190,13 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
         first = (double)pick<NX>(x, wv);
         double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
         double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
+        T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
         for (int i = 0; i < P.B; ++i) {
 #pragma unroll
             for (int j = 0; j < NX; ++j) xp[j] = x[j];
             T val;
             int t;
-            if (ps.push(pick<NX>(x, wv), val, t)) {
+            if (ps.push(v, val, t)) {
                 if (ps.n >= 1) {
                     const int q = ps.n - 1;
                     if (q < O.cap) {
@@ -207,7 +208,8 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
                 ++ps.n;
             }
             step<S>(x, a, c);
-            if (bif_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+            v = pick<NX>(x, wv);
+            if (bif_diverged(v, P)) { flag = 0; break; }
         }
         if (flag == 1 && P.B > 0 && bif_fixed<NX>(x, xp)) flag = -1;
         kept = ps.n > 1 ? ps.n - 1 : 0;
@@ -219,10 +221,43 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
     if (O.first) O.first[o] = first;
 }
 
+// Sums over the kept peaks of a basins point: peak values and intervals.
+// FP64 path: the reference's per-peak FP64 sums (avgPeakFinderCUDA,
+// basinsCUDA.cu:818-864). FP32 path: no FP64 instruction per peak (the FP64
+// pipe of this GPU is a small fraction of the FP32 rate): the values are
+// summed as an unevaluated float pair with the error-free TwoSum (about 48
+// significant bits), the intervals as the integer time span they telescope
+// to, and both are widened to FP64 once at the end.
+template <class T> struct PeakSums;
+template <> struct PeakSums<double> {
+    double sp = 0.0, si = 0.0;
+    __device__ __forceinline__ void add(double val, int dt, double hI) {
+        sp = sp + val;
+        si = si + __dmul_rn((double)dt, hI);
+    }
+    __device__ __forceinline__ double peaks() const { return sp; }
+    __device__ __forceinline__ double intervals(double) const { return si; }
+};
+template <> struct PeakSums<float> {
+    float hi = 0.f, lo = 0.f;
+    int span = 0;
+    __device__ __forceinline__ void add(float val, int dt, double) {
+        const float s = hi + val;  // TwoSum(hi, val) = s + err exactly
+        const float bv = s - hi;
+        const float err = (hi - (s - bv)) + (val - bv);
+        hi = s;
+        lo = lo + err;
+        span += dt;
+    }
+    __device__ __forceinline__ double peaks() const { return (double)hi + (double)lo; }
+    __device__ __forceinline__ double intervals(double hI) const { return __dmul_rn((double)span, hI); }
+};
+
 // ---------------------------------------------------------------------------
 // Basins point (reference calculateTransTimeCUDA + calculateDiscreteModelCUDA
-// + avgPeakFinderCUDA, basinsCUDA.cu:233-314 and 818-864), fused.
-template <int S, class T>
+// + avgPeakFinderCUDA, basinsCUDA.cu:233-314 and 818-864), fused. PRE1: the
+// sweep has preScaller == 1 (one step per sample, no inner loop).
+template <int S, class T, bool PRE1 = false>
 __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsOut& O, long long p, long long o) {
     constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
     T x[NX], a[NA], xp[NX];
@@ -235,31 +270,34 @@ __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsO
     PeakStream<T> ps;
     ps.init();
     int flag = 1;
-    double sp = 0.0, si = 0.0, last = 0.0;
+    PeakSums<T> sums;
+    T lastT = T(0);  // widened once after the loop (a per-step FP64 convert costs FP64-pipe time)
+    T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
     for (int i = 0; i < P.B; ++i) {
 #pragma unroll
         for (int j = 0; j < NX; ++j) xp[j] = x[j];
-        last = (double)pick<NX>(x, wv);
+        lastT = v;
         T val;
         int t;
-        if (ps.push(pick<NX>(x, wv), val, t)) {
-            if (ps.n >= 1) {
-                sp = sp + (double)val;
-                si = si + __dmul_rn((double)(t - ps.tprev), P.hInterval);
-            }
+        if (ps.push(v, val, t)) {
+            if (ps.n >= 1) sums.add(val, t - ps.tprev, P.hInterval);
             ps.tprev = t;
             ++ps.n;
         }
-        for (int r = 0; r < P.preScaller; ++r) step<S>(x, a, c);
-        if (basins_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+        if (PRE1) step<S>(x, a, c);
+        else
+            for (int r = 0; r < P.preScaller; ++r) step<S>(x, a, c);
+        v = pick<NX>(x, wv);
+        if (basins_diverged(v, P)) { flag = 0; break; }
     }
     if (flag == 1 && P.B > 0 && basins_fixed<NX>(x, xp)) flag = -1;
+    const double last = (double)lastT;
     const int kept = ps.n > 1 ? ps.n - 1 : 0;
     double ap, ai;
     if (flag == 0) { ap = 999.0; ai = 999.0; }
     else if (flag == -1) { ap = last; ai = -1.0; }
     else if (kept <= 0) { ap = 1000.0; ai = 1000.0; }
-    else { ap = sp / (double)kept; ai = si / (double)kept; }
+    else { ap = sums.peaks() / (double)kept; ai = sums.intervals(P.hInterval) / (double)kept; }
     O.flags[o] = flag;
     O.avgPeaks[o] = ap;
     O.avgIntervals[o] = ai;
@@ -541,10 +579,10 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
             if (rec[0]) first[0] = (double)v.v.x;
             if (rec[1]) first[1] = (double)v.v.y;
         }
+        P2 v = pick2<3>(x, wv);  // carried from one step to the next
         for (int i = 0; i < P.B; ++i) {
 #pragma unroll
             for (int j = 0; j < 3; ++j) xp[j] = x[j];
-            const P2 v = pick2<3>(x, wv);
 #pragma unroll
             for (int l = 0; l < 2; ++l) {
                 float val;
@@ -563,9 +601,9 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
                 }
             }
             rk4_step<F>(x, a, c);
-            const P2 w = pick2<3>(x, wv);
-            if (rec[0] && bif_diverged(w.v.x, P)) { rec[0] = false; flag[0] = 0; }
-            if (rec[1] && bif_diverged(w.v.y, P)) { rec[1] = false; flag[1] = 0; }
+            v = pick2<3>(x, wv);
+            if (rec[0] && bif_diverged(v.v.x, P)) { rec[0] = false; flag[0] = 0; }
+            if (rec[1] && bif_diverged(v.v.y, P)) { rec[1] = false; flag[1] = 0; }
             if (!rec[0] && !rec[1]) break;
         }
 #pragma unroll
@@ -581,7 +619,7 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
     }
 }
 
-template <class F>
+template <class F, bool PRE1 = false>
 __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const BasinsOut& O, long long p0,
                                                   long long p1, long long o0, long long o1, bool two) {
     P2 x[3], a[3], xp[3];
@@ -594,49 +632,50 @@ __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const Ba
     PeakStream<float> ps[2];
     int flag[2] = {1, two ? 1 : 0};
     bool rec[2] = {true, two};
-    double sp[2] = {0.0, 0.0}, si[2] = {0.0, 0.0}, last[2] = {0.0, 0.0};
+    PeakSums<float> sums[2];
+    float lastF[2] = {0.f, 0.f};  // widened after the loop
     ps[0].init();
     ps[1].init();
+    P2 v = pick2<3>(x, wv);  // carried from one step to the next
     for (int i = 0; i < P.B; ++i) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) xp[j] = x[j];
-        const P2 v = pick2<3>(x, wv);
 #pragma unroll
         for (int l = 0; l < 2; ++l) {
             if (!rec[l]) continue;
-            last[l] = (double)lane(v, l);
+            lastF[l] = lane(v, l);
             float val;
             int t;
             if (ps[l].push(lane(v, l), val, t)) {
-                if (ps[l].n >= 1) {
-                    sp[l] = sp[l] + (double)val;
-                    si[l] = si[l] + __dmul_rn((double)(t - ps[l].tprev), P.hInterval);
-                }
+                if (ps[l].n >= 1) sums[l].add(val, t - ps[l].tprev, P.hInterval);
                 ps[l].tprev = t;
                 ++ps[l].n;
             }
         }
-        for (int r = 0; r < P.preScaller; ++r) rk4_step<F>(x, a, c);
-        const P2 w = pick2<3>(x, wv);
-        if (rec[0] && basins_diverged(w.v.x, P)) { rec[0] = false; flag[0] = 0; }
-        if (rec[1] && basins_diverged(w.v.y, P)) { rec[1] = false; flag[1] = 0; }
+        if (PRE1) rk4_step<F>(x, a, c);
+        else
+            for (int r = 0; r < P.preScaller; ++r) rk4_step<F>(x, a, c);
+        v = pick2<3>(x, wv);
+        if (rec[0] && basins_diverged(v.v.x, P)) { rec[0] = false; flag[0] = 0; }
+        if (rec[1] && basins_diverged(v.v.y, P)) { rec[1] = false; flag[1] = 0; }
         if (!rec[0] && !rec[1]) break;
     }
     const long long oo[2] = {o0, o1};
 #pragma unroll
     for (int l = 0; l < (two ? 2 : 1); ++l) {
         if (rec[l] && P.B > 0 && basins_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+        const double last = (double)lastF[l];
         const int kept = ps[l].n > 1 ? ps[l].n - 1 : 0;
         double ap, ai;
         if (flag[l] == 0) { ap = 999.0; ai = 999.0; }
-        else if (flag[l] == -1) { ap = last[l]; ai = -1.0; }
+        else if (flag[l] == -1) { ap = last; ai = -1.0; }
         else if (kept <= 0) { ap = 1000.0; ai = 1000.0; }
-        else { ap = sp[l] / (double)kept; ai = si[l] / (double)kept; }
+        else { ap = sums[l].peaks() / (double)kept; ai = sums[l].intervals(P.hInterval) / (double)kept; }
         O.flags[oo[l]] = flag[l];
         O.avgPeaks[oo[l]] = ap;
         O.avgIntervals[oo[l]] = ai;
         if (O.counts) O.counts[oo[l]] = flag[l] == 1 ? kept : 0;
-        if (O.last) O.last[oo[l]] = last[l];
+        if (O.last) O.last[oo[l]] = last;
     }
 }
 

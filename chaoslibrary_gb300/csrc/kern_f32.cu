@@ -20,11 +20,11 @@ __global__ void __launch_bounds__(kBlock) bif_kernel_f32(SweepParams P, BifOut O
     bif_point<S, float>(P, O, P.pBegin + o, o);
 }
 
-template <int S>
+template <int S, bool PRE1>
 __global__ void __launch_bounds__(kBlock) basins_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
-    basins_point<S, float>(P, O, P.pBegin + o, o);
+    basins_point<S, float, PRE1>(P, O, P.pBegin + o, o);
 }
 
 // MINB = resident blocks per SM the register allocation is shaped for:
@@ -54,12 +54,12 @@ __global__ void __launch_bounds__(kBlock) bif_pair_kernel_f32(SweepParams P, Bif
     bif_pair_point<F>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
 }
 
-template <class F>
+template <class F, bool PRE1>
 __global__ void __launch_bounds__(kBlock) basins_pair_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (o >= P.nPoints) return;
     const bool two = o + 1 < P.nPoints;
-    basins_pair_point<F>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
+    basins_pair_point<F, PRE1>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
 }
 
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
@@ -143,7 +143,8 @@ template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, 
 }
 
 template <class F> void launch_basins_pairs(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
-    basins_pair_kernel_f32<F><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+    if (P.preScaller == 1) basins_pair_kernel_f32<F, true><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+    else basins_pair_kernel_f32<F, false><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
     note_launch();
 }
 
@@ -169,7 +170,10 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
         else launch_basins_pairs<Chen>(P, O, st);
         return cudaGetLastError();
     }
-#define CALL(S) (basins_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
+#define CALL(S)                                                                           \
+    (P.preScaller == 1 ? basins_kernel_f32<S, true><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O) \
+                       : basins_kernel_f32<S, false><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), \
+     note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
