@@ -591,7 +591,7 @@ def engine_arm(args, ws, rank, local):
         def step_host():
             return C.basins_dbscan(w["system"], precision=prec, **kw)
         d2h = n_points * (4 + 24 + 4)
-        tag = f"basins_{args.precision}_lorenz_2048"
+        tag = "basins_lorenz_2048" if args.precision == "fp32" else None
     steps_per_call = n_points * steps_pp
     for _ in range(args.warmup):
         step()
@@ -634,7 +634,7 @@ def engine_arm(args, ws, rank, local):
         peak = C.fma_probe() / 1e12 if prec == C.FP32 else None
         line["roofline"] = {"bound": "fp32_fma" if prec == C.FP32 else "fp64_fma", "achieved": achieved,
                             "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
-                            "traffic": traffic_from_profiles(tag),
+                            "traffic": traffic_from_profiles(tag) if tag else None,
                             "algorithmic": f"{w['flops']} flops per RK4 step x {steps_per_call:.4g} steps per launch",
                             "peak_source": "measured in this run: FP32 fmaf-chain probe (chaos_fma_probe), "
                                            "2048 threads/SM; MEASURED_PEAKS.json has only HBM and bf16 tensor peaks"}
