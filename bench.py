@@ -650,6 +650,11 @@ def engine_arm(args, ws, rank, local):
     line["e2e"] = {"value": ws * steps_per_call / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 88,
                    "d2h_bytes_per_step": d2h}
 
+    if rank == 0 and ws == 1 and args.workload in ("lle", "bif1d") and not args.no_extras and not args.npts \
+            and not args.tmax:
+        ref = reference_gpu_run(args.workload, steps_per_call)
+        if ref:
+            line["reference_gpu"] = ref
     if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras:
         line.update(lle_precision_report(C, prec, dev))
     if rank == 0 and ws == 1 and args.workload == "basins" and not args.no_extras:
@@ -664,6 +669,27 @@ def engine_arm(args, ws, rank, local):
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def reference_gpu_run(workload, steps):
+    """The reference's own GPU path on this GPU (its unchanged sources built by
+    oracle/build_ref_gpu.py, when that build is present): wall time of one call
+    of its host entry point on the same configuration, including its own host
+    work (allocation, per-element zeroing copies, copy back, CSV writing)."""
+    exe = ROOT / "oracle" / "_ref" / f"ref_gpu_{ {'lle': 'lle2d', 'bif1d': 'bif1d'}[workload]}"
+    if not exe.exists():
+        return None
+    with tempfile.TemporaryDirectory() as d:
+        try:
+            p = subprocess.run([str(exe), str(Path(d) / "out.csv")], capture_output=True, text=True, timeout=300)
+        except subprocess.TimeoutExpired:
+            return {"value": None, "error": "timed out after 300 s"}
+    if p.returncode != 0:
+        return {"value": None, "error": f"exit {p.returncode}"}
+    s = json.loads(p.stdout.strip().splitlines()[-1])["seconds"]
+    return {"value": steps / s, "unit": UNIT, "seconds": s,
+            "what": "the reference's unchanged sources (its host entry point, FP64, nvcc defaults) built for "
+                    "sm_103a with the same RK4 plug-in, timed around one call incl. its host work"}
 
 
 def label_agreement(a, b, fixed=()):

@@ -204,6 +204,8 @@ def trajectory(system, x0, a, h, n_steps, precision=FP64):
 
 TUNE_LLE_F32_VARIANT = 1
 TUNE_SWEEP_PAIRS = 2
+TUNE_GRID_FMA = 3
+TUNE_LLE_TWIN = 4
 
 
 def set_tuning(knob: int, value: int) -> None:

@@ -87,6 +87,8 @@ int prepare_job(const chaos_job& j, int memory, JobDesc& J, std::vector<HostOut>
             if (rc) return rc;
             if (!system_has_difference_form(j.system))
                 return set_error(CHAOS_E_UNSUPPORTED, "batched LLE jobs need a quadratic RK4 system (0-2)");
+            if (J.lp.twin != 0)
+                return set_error(CHAOS_E_UNSUPPORTED, "batched LLE jobs are FP32: the reference twin start is FP64 only");
             if (!j.lle) return set_error(CHAOS_E_ARGS, "LLE job needs lle");
             J.nPoints = J.lp.nPoints;
             J.lle = (double*)out(j.lle, J.nPoints * sizeof(double));

@@ -34,6 +34,12 @@ struct DeviceCtx {
 std::mutex g_mu;
 std::vector<DeviceCtx> g_dev;
 std::atomic<long long> g_launches{0};
+int env_flag(const char* name) {
+    const char* s = getenv(name);
+    return s && atoi(s) == 1 ? 1 : 0;
+}
+std::atomic<int> g_grid_fma{env_flag("CHAOS_GRID_FMA")};  // CHAOS_TUNE_GRID_FMA
+std::atomic<int> g_lle_twin{env_flag("CHAOS_LLE_TWIN")};  // CHAOS_TUNE_LLE_TWIN
 }  // namespace
 
 void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -243,6 +249,7 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     P.mut[0] = mut[0];
     P.mut[1] = dim > 1 ? mut[1] : -1;
     P.grid.nPts = nPts;
+    P.grid.fused = g_grid_fma.load(std::memory_order_relaxed);
     for (int d = 0; d < dim; ++d) {
         P.grid.start[d] = ranges[2 * d];
         P.grid.scale[d] = (ranges[2 * d + 1] - ranges[2 * d]) / (double)(nPts - 1);
@@ -289,6 +296,7 @@ int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double 
     L.stepB = nPts > 1 ? (ranges[3] - ranges[2]) / (nPts - 1) : 0.0;
     L.pBegin = 0;
     L.nPoints = (long long)nPts * nPts;
+    L.twin = g_lle_twin.load(std::memory_order_relaxed);
     return CHAOS_OK;
 }
 
@@ -424,6 +432,8 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
         return rc;
     if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_difference_form(system)))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
+        return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
     Call c;
     if ((rc = c.begin(ex))) return rc;
     double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
@@ -451,6 +461,7 @@ int chaos_lle2d_checked(const chaos_exec* ex, int system, double tMax, double NT
         return rc;
     if (!system_has_difference_form(system))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2)");
+    if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
     if (L.nPoints > 0x7fffffffLL) return set_error(CHAOS_E_ARGS, "nPts^2 must be < 2^31");
     Call c;
     if ((rc = c.begin(ex))) return rc;
@@ -673,12 +684,19 @@ int chaos_set_tuning(int knob, int value) {
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
     if (knob == CHAOS_TUNE_SWEEP_PAIRS)
         return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1 or 2)", value) : CHAOS_OK;
+    if (knob == CHAOS_TUNE_GRID_FMA || knob == CHAOS_TUNE_LLE_TWIN) {
+        if (value != 0 && value != 1) return set_error(CHAOS_E_ARGS, "knob %d takes 0 or 1", knob);
+        (knob == CHAOS_TUNE_GRID_FMA ? g_grid_fma : g_lle_twin).store(value);
+        return CHAOS_OK;
+    }
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 
 int chaos_get_tuning(int knob) {
     if (knob == CHAOS_TUNE_LLE_F32_VARIANT) return get_lle_variant();
     if (knob == CHAOS_TUNE_SWEEP_PAIRS) return sweep_pairs();
+    if (knob == CHAOS_TUNE_GRID_FMA) return g_grid_fma.load();
+    if (knob == CHAOS_TUNE_LLE_TWIN) return g_lle_twin.load();
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 

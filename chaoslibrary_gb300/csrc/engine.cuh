@@ -32,12 +32,14 @@ template <> struct Traits<SYS_USER> {
 
 // Swept value of grid dimension d for linear point index p (the reference's
 // getValueByIdx, bifurcationCUDA.cu:400-419 / basinsCUDA.cu:185-189):
-// start + n*scale with n = (p / nPts^d) % nPts, multiply and add rounded apart.
+// start + n*scale with n = (p / nPts^d) % nPts, multiply and add rounded apart
+// (the source as written), or as one FMA when g.fused (the reference's own
+// GPU build: nvcc contracts the expression by default).
 __device__ __forceinline__ double grid_value(const GridSpec& g, long long p, int d) {
     long long q = p;
     if (d == 1) q /= g.nPts;
     const long long n = q % g.nPts;
-    return __dadd_rn(g.start[d], __dmul_rn((double)n, g.scale[d]));
+    return g.fused ? __fma_rn((double)n, g.scale[d], g.start[d]) : __dadd_rn(g.start[d], __dmul_rn((double)n, g.scale[d]));
 }
 
 // Divergence test of the bifurcation loop (bifurcationCUDA.cu:445-453):
@@ -330,7 +332,15 @@ __device__ __forceinline__ double lle_point_full(const LleParams& L, long long p
     for (int s = 0; s < L.trans; ++s) step<S>(x, a, c);
 #pragma unroll
     for (int k = 0; k < NX; ++k) q[k] = x[k];
-    q[0] = x[0] + (T)L.eps;
+    if (L.twin == 1) {
+        // the reference's twin start (LLECUDA.cu:97-101): a float FMA of a unit
+        // direction times eps onto the float-rounded state, here with the
+        // direction e_x instead of its cuRAND draw
+#pragma unroll
+        for (int k = 0; k < NX; ++k) q[k] = (T)__fmaf_rn(k == 0 ? 1.0f : 0.0f, (float)L.eps, (float)x[k]);
+    } else {
+        q[0] = x[0] + (T)L.eps;
+    }
     double sum = 0.0;
     for (int b = 0; b <= L.calcBlocks; ++b) {
         for (int s = 0; s < L.ntp; ++s) step<S>(x, a, c);
@@ -429,6 +439,7 @@ __device__ __forceinline__ P2 operator-(P2 a, P2 b) { return mk(__fadd2_rn(a.v, 
 __device__ __forceinline__ P2 operator*(P2 a, P2 b) { return mk(__fmul2_rn(a.v, b.v)); }
 __device__ __forceinline__ P2& operator*=(P2& a, P2 b) { a = a * b; return a; }
 __device__ __forceinline__ P2 fmaT(P2 a, P2 b, P2 c) { return mk(__ffma2_rn(a.v, b.v, c.v)); }
+__device__ __forceinline__ P2 addR(P2 a, P2 b) { return a + b; }
 
 // Step constants of a packed pair: rounded exactly as RK4H<float> rounds them.
 template <> struct RK4H<P2> {

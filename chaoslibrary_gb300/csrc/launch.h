@@ -22,6 +22,7 @@ struct GridSpec {
     long long nPts;
     double start[2];
     double scale[2];
+    int fused;  // 1: start + n*scale as one FMA (what nvcc's default contraction makes of the reference's getValueByIdx)
 };
 
 struct SweepParams {
@@ -74,6 +75,7 @@ struct LleParams {
     double rangeA[2], rangeB[2];
     double stepA, stepB;  // linspace steps (end - start) / (nPts - 1)
     long long pBegin, nPoints;
+    int twin;  // twin start: 0 x + eps e_x; 1 the reference's, every component rounded to float (FP64 only)
 };
 
 // precision-specific launchers (kern_f64.cu / kern_f32.cu)

@@ -75,6 +75,19 @@ CHAOS_HD float expT(float a) { return expf(a); }
 CHAOS_HD double atanT(double a) { return atan(a); }
 CHAOS_HD float atanT(float a) { return atanf(a); }
 
+// A sum that no compiler may merge with a neighbouring product. In FP64
+// device code it is an explicit round-to-nearest add: the plug-in headers
+// put this RK4 step into reference builds, which contract a*b + c into one
+// FMA by default, and the step must round the same way there as here.
+CHAOS_HD double addR(double a, double b) {
+#if defined(__CUDA_ARCH__)
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+CHAOS_HD float addR(float a, float b) { return a + b; }
+
 // ---- vector fields of the RK4 systems ---------------------------------------
 struct Lorenz {
     template <class T> static CHAOS_HD void f(const T* x, const T* a, T* k) {
@@ -140,7 +153,7 @@ CHAOS_UNROLL
     for (int i = 0; i < 3; ++i) { acc[i] = fmaT(T(2), k[i], acc[i]); y[i] = fmaT(c.h, k[i], x[i]); }
     F::f(y, a, k);
 CHAOS_UNROLL
-    for (int i = 0; i < 3; ++i) x[i] = fmaT(c.h6, acc[i] + k[i], x[i]);
+    for (int i = 0; i < 3; ++i) x[i] = fmaT(c.h6, addR(acc[i], k[i]), x[i]);
 }
 
 // One RK4 step of the base trajectory x together with the exact difference

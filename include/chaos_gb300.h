@@ -362,6 +362,19 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
    bifurcation sweeps of at least 4 x SMs x 1024 points, 2 always, 0 never
    (one point per thread). Results are identical in every mode. */
 #define CHAOS_TUNE_SWEEP_PAIRS 2
+/* CHAOS_TUNE_GRID_FMA: 0 (default) swept values start + n*scale with the
+   multiply and the add rounded apart, as the reference's getValueByIdx is
+   written (bifurcationCUDA.cu:400-419); 1 as one fused multiply-add, which is
+   what the reference's own GPU build computes (nvcc contracts the expression
+   by default): with 1, FP64 bifurcation and basins sweeps reproduce that
+   build's output bit for bit (for plug-ins free of contractible products).
+   Initial value from the environment: CHAOS_GRID_FMA=1. */
+#define CHAOS_TUNE_GRID_FMA 3
+/* CHAOS_TUNE_LLE_TWIN: 0 (default) the twin trajectory starts at x + eps*e_x;
+   1 the reference's start (LLECUDA.cu:97-101): every state component rounded
+   to float and eps added along e_x by a float FMA (the reference draws the
+   direction with cuRAND). FP64 only. Initial value: CHAOS_LLE_TWIN=1. */
+#define CHAOS_TUNE_LLE_TWIN 4
 int chaos_set_tuning(int knob, int value);
 int chaos_get_tuning(int knob);
 

@@ -1,0 +1,57 @@
+// Timing harness around the reference's own GPU path: its unchanged sources
+// (staged and compiled by oracle/build_ref_gpu.py) called through its host
+// entry points, exactly as the reference's src/main.cu calls them.
+// MEASUREMENT INFRASTRUCTURE ONLY: never shipped, never called by the engine.
+//
+//   ref_gpu_bif1d <out.csv> [nPts] [tMax]   Bifurcation::bifurcation1D, Lorenz RK4
+//                                           (h 0.01, rho in [20, 200], transient 100)
+//   ref_gpu_lle2d <out.csv> [nPts] [tMax]   LLE::LLE2D, Rossler RK4 (h 0.01, NT 0.1,
+//                                           a in [0.1, 0.4], c in [2, 10], transient 50)
+//
+// One small warm-up call (module loading), then the timed call; prints one
+// JSON line with the wall time of the timed call. The reference's call
+// includes its own host work: device allocation, the per-element zeroing
+// copies of the LLE result rows, the copy back and the CSV writing.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+
+#if defined(REF_BIF1D)
+#include "bifurcationHOST.h"
+#else
+#include "LLEHost.h"
+#endif
+
+static double run(const std::string& out, int nPts, double tMax) {
+    const auto t0 = std::chrono::steady_clock::now();
+#if defined(REF_BIF1D)
+    const double ic[3] = {0.1, 0.1, 0.1}, ranges[2] = {20.0, 200.0}, values[3] = {10.0, 28.0, 8.0 / 3.0};
+    const int mut[1] = {1};
+    Bifurcation::bifurcation1D(tMax, nPts, 0.01, 3, ic, ranges, mut, 0, 1e4, 100.0, values, 3, 1, out);
+#else
+    const double ic[3] = {1.0, 1.0, 1.0}, ranges[4] = {0.1, 0.4, 2.0, 10.0}, values[3] = {0.2, 0.2, 5.7};
+    const int mut[2] = {0, 2};
+    LLE::LLE2D(tMax, 0.1, nPts, 0.01, 1e-8, ic, 3, ranges, mut, 0, 0.0, 50.0, values, 3, out);
+#endif
+    cudaDeviceSynchronize();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int main(int argc, char** argv) {
+    const std::string out = argc > 1 ? argv[1] : "ref_out.csv";
+#if defined(REF_BIF1D)
+    const int nPts = argc > 2 ? atoi(argv[2]) : 1000;
+    const double tMax = argc > 3 ? atof(argv[3]) : 100.0;
+#else
+    const int nPts = argc > 2 ? atoi(argv[2]) : 1024;
+    const double tMax = argc > 3 ? atof(argv[3]) : 500.0;
+#endif
+    cudaFree(nullptr);     // context
+    run(out, 16, 1.0);     // warm-up: module load
+    const double s = run(out, nPts, tMax);
+    printf("{\"nPts\": %d, \"tMax\": %g, \"seconds\": %.6f}\n", nPts, tMax, s);
+    return 0;
+}
