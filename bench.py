@@ -45,6 +45,11 @@ LLE = dict(system="rossler", sysid=1, flops=63, tMax=500.0, NT=0.1, nPts=1024, h
 BIF1D = dict(system="lorenz", sysid=0, flops=71, tMax=100.0, nPts=1000, h=0.01, initialConditions=[0.1, 0.1, 0.1],
              ranges=[20.0, 200.0], indicesOfMutVars=[1], writableVar=0, maxValue=1e4, transientTime=100.0,
              values=[10.0, 28.0, 8.0 / 3.0])
+# the reference's own 2-D bifurcation timing sweep (src/main.cu:447-505): Chameleon,
+# CT 400 (40,000 recorded steps), TT 2000 (200,000 transient steps), eps 0.001, at 300^2
+BIF2D = dict(system="chameleon", sysid=3, flops=None, tMax=400.0, nPts=300, h=0.01,
+             initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0, 0.0, 20.0], indicesOfMutVars=[3, 5], writableVar=0,
+             maxValue=1e4, transientTime=2000.0, values=[0.5, 3, 0, 2, 1, 18, 1], eps=0.001)
 BASINS = dict(system="lorenz", sysid=0, flops=71, tMax=50.0, nPts=2048, h=0.01, initialConditions=[0.0, 0.0, 27.0],
               ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8,
               transientTime=200.0, values=[10.0, 24.0, 8.0 / 3.0], eps=0.05, minPts=8)
@@ -300,6 +305,12 @@ def config_of(args):
                 "grid_points": 1048576, "steps_per_point": lle_steps_per_point(LLE), "eps": 1e-8,
                 "precision": args.precision, "l2": "256 MB buffer written between timed steps; the map's state "
                                                   "lives in registers (inputs: 88 B of parameters)"}
+    if args.workload == "bif2d":
+        return {"workload": "2-D bifurcation (the reference's own timing sweep), Chameleon, 300x300 over "
+                            "(values[3], values[5]) in [0,5] x [0,20], 200000 transient + 40000 recorded steps, "
+                            "per-point interval clustering eps=0.001", "grid_points": 90000,
+                "steps_per_point": sweep_steps_per_point(BIF2D), "precision": args.precision,
+                "l2": "256 MB buffer written between timed steps"}
     if args.workload == "bif1d":
         return {"workload": "1-D bifurcation, Lorenz RK4 h=0.01, rho in [20,200] x 1000, 10000 transient + "
                             "10000 recorded steps, peaks of x", "grid_points": 1000,
@@ -544,7 +555,7 @@ def engine_arm(args, ws, rank, local):
     if args.lle_variant:
         C.set_tuning(C.TUNE_LLE_F32_VARIANT, args.lle_variant)
     prec = C.FP32 if args.precision == "fp32" else C.FP64
-    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS}[args.workload]
+    w = {"lle": LLE, "bif1d": BIF1D, "bif2d": BIF2D, "basins": BASINS}[args.workload]
     n_points = w["nPts"] ** (1 if args.workload == "bif1d" else 2)
     if args.workload == "lle":
         steps_pp = lle_steps_per_point(w)
@@ -576,6 +587,19 @@ def engine_arm(args, ws, rank, local):
             return C.bifurcation1d(w["system"], precision=prec, peakCapacity=cap, **kw)
         d2h = n_points * (4 + 4 + 8 + 16 * cap)
         tag = f"bif1d_{args.precision}_lorenz_1000"
+    elif args.workload == "bif2d":
+        steps_pp = sweep_steps_per_point(w)
+        outs = dict(labels=torch.empty(n_points, dtype=torch.int32, device=dev),
+                    counts=torch.empty(n_points, dtype=torch.int32, device=dev))
+        kw = kw_of(w)
+
+        def step(o=None):
+            return C.bifurcation2d(w["system"], precision=prec, out=outs, **kw)
+
+        def step_host():
+            return C.bifurcation2d(w["system"], precision=prec, **kw)
+        d2h = n_points * 8
+        tag = None
     else:
         # the basins map as specified: (amplitude, peak count, interval) features
         # min-max normalised, textbook DBSCAN eps=0.05, minPts=8
@@ -627,7 +651,10 @@ def engine_arm(args, ws, rank, local):
         line["config"].update(line_extra)
 
     # roofline: FP32 (or FP64) FMA pipe, algorithmic flops of the integration
-    if rank == 0:
+    if rank == 0 and w["flops"] is None:
+        line["roofline"] = {"bound": "latency / SFU (the Chameleon step calls sin, cos and exp)", "achieved": None,
+                            "peak": None, "unit": None, "frac": None, "traffic": None}
+    elif rank == 0:
         mean_s = statistics.mean(ms) / 1e3
         algo = w["flops"] * steps_per_call
         achieved = algo / mean_s / 1e12
@@ -824,7 +851,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "basins", "batch", "serve"])
+    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "bif2d", "basins", "batch", "serve"])
     ap.add_argument("--requests", type=int, default=2000, help="served stream length")
     ap.add_argument("--rate", type=float, default=100.0, help="served stream arrival rate (requests/s)")
     ap.add_argument("--hbm-budget-gb", type=int, default=64)
@@ -836,7 +863,7 @@ def main():
     ap.add_argument("--npts", type=int, default=None, help="grid resolution override (profiling runs only)")
     ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()
-    for w in (LLE, BIF1D, BASINS):
+    for w in (LLE, BIF1D, BIF2D, BASINS):
         if args.npts:
             w["nPts"] = args.npts
         if args.tmax:

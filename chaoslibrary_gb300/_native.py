@@ -206,6 +206,7 @@ TUNE_LLE_F32_VARIANT = 1
 TUNE_SWEEP_PAIRS = 2
 TUNE_GRID_FMA = 3
 TUNE_LLE_TWIN = 4
+TUNE_BIF2D_CAP = 5
 
 
 def set_tuning(knob: int, value: int) -> None:

@@ -40,6 +40,7 @@ int env_flag(const char* name) {
 }
 std::atomic<int> g_grid_fma{env_flag("CHAOS_GRID_FMA")};  // CHAOS_TUNE_GRID_FMA
 std::atomic<int> g_lle_twin{env_flag("CHAOS_LLE_TWIN")};  // CHAOS_TUNE_LLE_TWIN
+std::atomic<int> g_bif2d_cap{0};                          // CHAOS_TUNE_BIF2D_CAP
 }  // namespace
 
 void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -205,6 +206,10 @@ static int check_system(int system, int nIC, int nValues) {
 static cudaError_t run_bif(int prec, const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_bif_user(P, O, st);
     return prec == CHAOS_FP32 ? launch_bif_f32(P, O, st) : launch_bif_f64(P, O, st);
+}
+static cudaError_t run_bif_list(int prec, const SweepParams& P, const BifOut& O, const int* list, int count,
+                                cudaStream_t st) {
+    return prec == CHAOS_FP32 ? launch_bif_list_f32(P, O, list, count, st) : launch_bif_list_f64(P, O, list, count, st);
 }
 static cudaError_t run_basins(int prec, const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_basins_user(P, O, st);
@@ -392,7 +397,33 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
     const long long n = P.nPoints;
     // every detected peak sits at least two samples after the previous one,
     // so B/2 rows hold all kept intervals of a point
-    const int cap = std::max(P.B / 2, 1);
+    const int capFull = std::max(P.B / 2, 1);
+    // Peak-buffer capacity: the kept-peak counts of up to 4096 evenly spread
+    // points, 25 % + 16 above their maximum (or CHAOS_TUNE_BIF2D_CAP: > 0 a
+    // fixed capacity, -1 always B/2). Points with more peaks are run again
+    // with B/2 rows, so the capacity changes memory and speed, never results.
+    int cap = capFull;
+    const int capKnob = g_bif2d_cap.load(std::memory_order_relaxed);
+    const bool adapt = capKnob >= 0 && P.system != SYS_USER && n <= 0x7fffffffLL && capFull > 64;
+    if (adapt && capKnob > 0) {
+        cap = std::min(capKnob, capFull);
+    } else if (adapt) {
+        const int S = (int)std::min<long long>(n, 4096);
+        std::vector<int> idx(S), hc(S);
+        for (int s = 0; s < S; ++s) idx[s] = (int)(n * s / S);
+        int* dIdx = (int*)c.alloc(S * sizeof(int));
+        int* dPc = (int*)c.alloc(S * sizeof(int));
+        int* dPf = (int*)c.alloc(S * sizeof(int));
+        if (c.failed) return c.finish(CHAOS_E_NOMEM);
+        cudaError_t e = cudaMemcpyAsync(dIdx, idx.data(), S * sizeof(int), cudaMemcpyHostToDevice, c.stream);
+        BifOut Op{dPc, dPf, nullptr, nullptr, nullptr, 0};
+        if (e == cudaSuccess) e = run_bif_list(c.ex.precision, P, Op, dIdx, S, c.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), dPc, S * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation 2-D capacity probe"));
+        const int mx = std::max(0, *std::max_element(hc.begin(), hc.end()));
+        cap = (int)std::min<long long>(capFull, (long long)mx + mx / 4 + 16);
+    }
     const size_t perPoint = (size_t)cap * (sizeof(double) + 2 * sizeof(int));
     long long chunk = (long long)std::max<size_t>(scratch_budget_bytes() / perPoint, 1);
     chunk = std::min(chunk, n);
@@ -412,6 +443,35 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
         if (e == cudaSuccess)
             e = launch_point_dbscan(dIv, dCounts + b, Q.nPoints, cap, eps, dLab, dSlot, dLabels + b, c.stream);
         if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation 2-D kernels"));
+    }
+    if (cap < capFull) {  // the points with more kept peaks than the capacity, again with B/2 rows
+        int* dList = (int*)c.alloc(n * sizeof(int));
+        int* dNum = (int*)c.alloc(sizeof(int));
+        if (c.failed) return c.finish(CHAOS_E_NOMEM);
+        int hNum = 0;
+        cudaError_t e = cudaMemsetAsync(dNum, 0, sizeof(int), c.stream);
+        if (e == cudaSuccess) e = launch_overflow_select(dCounts, n, cap, dList, dNum, c.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hNum, dNum, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation 2-D overflow selection"));
+        if (hNum > 0) {
+            const size_t perFull = (size_t)capFull * (sizeof(double) + 2 * sizeof(int)) + 2 * sizeof(int);
+            const int chunk2 = (int)std::min<long long>(hNum, std::max<size_t>(scratch_budget_bytes() / perFull, 1));
+            int* rCounts = (int*)c.alloc(chunk2 * sizeof(int));
+            int* rFlags = (int*)c.alloc(chunk2 * sizeof(int));
+            double* rIv = (double*)c.alloc((size_t)chunk2 * capFull * sizeof(double));
+            int* rLab = (int*)c.alloc((size_t)chunk2 * capFull * sizeof(int));
+            int* rSlot = (int*)c.alloc((size_t)chunk2 * capFull * sizeof(int));
+            if (c.failed) return c.finish(CHAOS_E_NOMEM);
+            for (int b = 0; b < hNum && e == cudaSuccess; b += chunk2) {
+                const int m = std::min(chunk2, hNum - b);
+                BifOut Or{rCounts, rFlags, nullptr, nullptr, rIv, capFull};
+                e = run_bif_list(c.ex.precision, P, Or, dList + b, m, c.stream);
+                if (e == cudaSuccess)
+                    e = launch_point_dbscan(rIv, rCounts, m, capFull, eps, rLab, rSlot, dLabels, c.stream, dList + b);
+            }
+            if (e != cudaSuccess) return c.finish(cuda_error(e, "bifurcation 2-D overflow pass"));
+        }
     }
     rc = c.to_host(labels, dLabels, n * sizeof(int));
     if (!rc && counts) rc = c.to_host(counts, dCounts, n * sizeof(int));
@@ -684,6 +744,11 @@ int chaos_set_tuning(int knob, int value) {
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
     if (knob == CHAOS_TUNE_SWEEP_PAIRS)
         return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1 or 2)", value) : CHAOS_OK;
+    if (knob == CHAOS_TUNE_BIF2D_CAP) {
+        if (value < -1) return set_error(CHAOS_E_ARGS, "bifurcation 2-D capacity: -1, 0 or a row size");
+        g_bif2d_cap.store(value);
+        return CHAOS_OK;
+    }
     if (knob == CHAOS_TUNE_GRID_FMA || knob == CHAOS_TUNE_LLE_TWIN) {
         if (value != 0 && value != 1) return set_error(CHAOS_E_ARGS, "knob %d takes 0 or 1", knob);
         (knob == CHAOS_TUNE_GRID_FMA ? g_grid_fma : g_lle_twin).store(value);
@@ -697,6 +762,7 @@ int chaos_get_tuning(int knob) {
     if (knob == CHAOS_TUNE_SWEEP_PAIRS) return sweep_pairs();
     if (knob == CHAOS_TUNE_GRID_FMA) return g_grid_fma.load();
     if (knob == CHAOS_TUNE_LLE_TWIN) return g_lle_twin.load();
+    if (knob == CHAOS_TUNE_BIF2D_CAP) return g_bif2d_cap.load();
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 

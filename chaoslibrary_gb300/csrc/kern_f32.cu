@@ -20,6 +20,13 @@ __global__ void __launch_bounds__(kBlock) bif_kernel_f32(SweepParams P, BifOut O
     bif_point<S, float>(P, O, P.pBegin + o, o);
 }
 
+template <int S>
+__global__ void __launch_bounds__(kBlock) bif_list_kernel_f32(SweepParams P, BifOut O, const int* list, int count) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    bif_point<S, float>(P, O, list[k], k);
+}
+
 template <int S, bool PRE1>
 __global__ void __launch_bounds__(kBlock) basins_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,6 +164,14 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
         return cudaGetLastError();
     }
 #define CALL(S) (bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
+    CHAOS_SYSTEM_SWITCH(P.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bif_list_f32(const SweepParams& P, const BifOut& O, const int* list, int count, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+#define CALL(S) (bif_list_kernel_f32<S><<<grid_for(count), kBlock, 0, st>>>(P, O, list, count), note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();

@@ -20,6 +20,14 @@ __global__ void __launch_bounds__(kBlock) bif_kernel(SweepParams P, BifOut O) {
     bif_point<S, double>(P, O, P.pBegin + o, o);
 }
 
+// Bifurcation points list[0, count), result row k for list[k].
+template <int S>
+__global__ void __launch_bounds__(kBlock) bif_list_kernel(SweepParams P, BifOut O, const int* list, int count) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    bif_point<S, double>(P, O, list[k], k);
+}
+
 template <int S>
 __global__ void __launch_bounds__(kBlock) basins_kernel(SweepParams P, BasinsOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -142,17 +150,19 @@ __global__ void peak_array_kernel(const double* __restrict__ data, long long nSe
 // uniform across the warp; each expansion pass over k < P-1 is split across
 // the lanes, which is exact because pass k only reads and writes entry k.
 __global__ void point_dbscan_kernel(const double* __restrict__ intervals, const int* __restrict__ counts, long long n,
-                                    int stride, double eps, int* labScratch, int* slotScratch, int* out) {
+                                    int stride, double eps, int* labScratch, int* slotScratch, int* outBase,
+                                    const int* outIdx) {
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= n) return;
+    const long long oi = outIdx ? (long long)outIdx[w] : w;  // where this point's label goes
     const int P = counts[w];
     if (P > stride) {  // more intervals than the row holds: reported, not read
-        if (lane == 0) out[w] = INT_MIN;
+        if (lane == 0) outBase[oi] = INT_MIN;
         return;
     }
     if (P <= 1) {
-        if (lane == 0) out[w] = P == -1 ? -1 : (P == 0 ? 0 : 1);
+        if (lane == 0) outBase[oi] = P == -1 ? -1 : (P == 0 ? 0 : 1);
         return;
     }
     const double* iv = intervals + w * (long long)stride;
@@ -196,7 +206,7 @@ __global__ void point_dbscan_kernel(const double* __restrict__ intervals, const 
             __syncwarp();
         }
     }
-    if (lane == 0) out[w] = cluster - 1;
+    if (lane == 0) outBase[oi] = cluster - 1;
 }
 
 }  // namespace
@@ -227,6 +237,27 @@ cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
 #define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bif_list_f64(const SweepParams& P, const BifOut& O, const int* list, int count, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+#define CALL(S) (bif_list_kernel<S><<<grid_for(count), kBlock, 0, st>>>(P, O, list, count), note_launch())
+    CHAOS_SYSTEM_SWITCH(P.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+// indices of the points whose kept-peak count exceeds cap
+__global__ void overflow_select_kernel(const int* counts, long long n, int cap, int* list, int* count) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    append(i < n && counts[i] > cap, (int)i, list, count);
+}
+
+cudaError_t launch_overflow_select(const int* counts, long long n, int cap, int* list, int* count, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    overflow_select_kernel<<<grid_for(n), kBlock, 0, st>>>(counts, n, cap, list, count);
+    note_launch();
     return cudaGetLastError();
 }
 
@@ -265,11 +296,11 @@ cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, d
 }
 
 cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long long n, int stride, double eps,
-                                int* labScratch, int* slotScratch, int* out, cudaStream_t st) {
+                                int* labScratch, int* slotScratch, int* out, cudaStream_t st, const int* outIdx) {
     if (n <= 0) return cudaSuccess;
     const long long threads = n * 32;
     point_dbscan_kernel<<<(unsigned)((threads + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-        intervals, counts, n, stride, eps, labScratch, slotScratch, out);
+        intervals, counts, n, stride, eps, labScratch, slotScratch, out, outIdx);
     note_launch();
     return cudaGetLastError();
 }

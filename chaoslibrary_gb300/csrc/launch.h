@@ -85,6 +85,11 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
+// bifurcation points of a list (row k for list[k]); points whose kept-peak
+// count exceeds cap (kern_f64.cu / kern_f32.cu)
+cudaError_t launch_bif_list_f64(const SweepParams& P, const BifOut& O, const int* list, int count, cudaStream_t st);
+cudaError_t launch_bif_list_f32(const SweepParams& P, const BifOut& O, const int* list, int count, cudaStream_t st);
+cudaError_t launch_overflow_select(const int* counts, long long n, int cap, int* list, int* count, cudaStream_t st);
 // FP64 sign re-check of an FP32 LLE map (kern_f64.cu): select the points with
 // |v| <= band or v not finite, FP64 LLE of a point list, compare classes
 cudaError_t launch_lle_select(const double* v, long long n, double band, int* list, int* count, cudaStream_t st);
@@ -96,7 +101,8 @@ cudaError_t launch_lle_flip(const double* v32, const int* list, const int* count
 cudaError_t launch_peak_finder(const double* data, long long nSeries, int len, double h, int cap, int* counts,
                                double* peaks, double* intervals, cudaStream_t st);
 cudaError_t launch_point_dbscan(const double* intervals, const int* counts, long long n, int stride, double eps,
-                                int* labScratch, int* slotScratch, int* out, cudaStream_t st);
+                                int* labScratch, int* slotScratch, int* out, cudaStream_t st,
+                                const int* outIdx = nullptr);  // outIdx: label of row w goes to out[outIdx[w]]
 
 cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st);
