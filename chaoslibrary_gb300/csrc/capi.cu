@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -249,6 +250,24 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     P.maxValue = maxValue;
     P.maxValueF = (float)maxValue;
     if ((double)P.maxValueF > maxValue) P.maxValueF = nextafterf(P.maxValueF, -INFINITY);
+    // For a double v, float(v) (round to nearest, ties to even) exceeds maxValueF
+    // exactly when |v| is above the midpoint m of maxValueF and the next float
+    // up (or at m, when that next float is the even one, or infinity).
+    if (!(maxValue == maxValue) || maxValue == INFINITY) {
+        P.maxBits = ~0ull;  // never
+        P.maxTie = 0;
+    } else if (maxValue < 0) {
+        P.maxBits = 0;  // always (|float(v)| >= 0 > maxValue)
+        P.maxTie = 1;
+    } else {
+        const float up = nextafterf(P.maxValueF, INFINITY);
+        const double m = up == INFINITY ? 340282356779733661637539395458142568448.0  // 2^128 - 2^103
+                                        : ((double)P.maxValueF + (double)up) * 0.5;
+        uint32_t upBits;
+        memcpy(&upBits, &up, sizeof upBits);
+        memcpy(&P.maxBits, &m, sizeof P.maxBits);
+        P.maxTie = (up == INFINITY || (upBits & 1u) == 0) ? 1 : 0;
+    }
     for (int i = 0; i < nIC; ++i) P.ic[i] = ic[i];
     for (int i = 0; i < nValues; ++i) P.values[i] = values[i];
     P.mut[0] = mut[0];

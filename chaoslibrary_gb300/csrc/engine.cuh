@@ -42,31 +42,62 @@ __device__ __forceinline__ double grid_value(const GridSpec& g, long long p, int
     return g.fused ? __fma_rn((double)n, g.scale[d], g.start[d]) : __dadd_rn(g.start[d], __dmul_rn((double)n, g.scale[d]));
 }
 
+// The maxValue test of both loops, (double)fabsf((float)v) > maxValue, for a
+// double v on the integer pipe (this GPU's FP64 pipe is its bottleneck in the
+// FP64 sweeps): with b the bits of |v| (not NaN), it holds exactly when
+// b > maxBits, or b == maxBits and maxTie (the host derives maxBits from the
+// rounding boundary of float(v) at maxValue, see fill_sweep).
+__device__ __forceinline__ bool max_exceeded(unsigned long long b, const SweepParams& P) {
+    return b > P.maxBits || (b == P.maxBits && P.maxTie);
+}
+
 // Divergence test of the bifurcation loop (bifurcationCUDA.cu:445-453):
 // v != v || v == v + 1.0  <=>  !(|v| < 2^53); then |(float)v| > maxValue.
-template <class T> __device__ __forceinline__ bool bif_diverged(T v, const SweepParams& P) {
-    const T av = v < T(0) ? -v : v;
-    if (!(av < T(9007199254740992.0))) return true;
-    return P.checkMax && (double)fabsf((float)v) > P.maxValue;
+template <class T> __device__ __forceinline__ bool bif_diverged(T v, const SweepParams& P);
+template <> __device__ __forceinline__ bool bif_diverged<double>(double v, const SweepParams& P) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    if (b >= 0x4340000000000000ull) return true;  // |v| >= 2^53, infinite or NaN
+    return P.checkMax && max_exceeded(b, P);
 }
-// The same test for a float v without FP64 instructions (GB300's FP64 pipe
-// runs at 1/64 of the FP32 rate): |v| > maxValue <=> |v| > maxValueF.
+// The same test for a float v (float compares): |v| > maxValue <=> |v| > maxValueF.
 template <> __device__ __forceinline__ bool bif_diverged<float>(float v, const SweepParams& P) {
     const float av = fabsf(v);
     return !(av < 9007199254740992.0f) || (P.checkMax && av > P.maxValueF);
 }
 // Divergence test of the basins loop (basinsCUDA.cu:350-361): isnan || isinf, then maxValue.
-template <class T> __device__ __forceinline__ T finite_max();
-template <> __device__ __forceinline__ double finite_max<double>() { return 1.7976931348623157e308; }
-template <> __device__ __forceinline__ float finite_max<float>() { return 3.4028234663852886e38f; }
-template <class T> __device__ __forceinline__ bool basins_diverged(T v, const SweepParams& P) {
-    const T av = v < T(0) ? -v : v;
-    if (!(av <= finite_max<T>())) return true;  // NaN or +-inf
-    return P.checkMax && (double)fabsf((float)v) > P.maxValue;
+template <class T> __device__ __forceinline__ bool basins_diverged(T v, const SweepParams& P);
+template <> __device__ __forceinline__ bool basins_diverged<double>(double v, const SweepParams& P) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    if (b > 0x7fefffffffffffffull) return true;  // NaN or +-inf
+    return P.checkMax && max_exceeded(b, P);
 }
 template <> __device__ __forceinline__ bool basins_diverged<float>(float v, const SweepParams& P) {
     const float av = fabsf(v);
     return !(av <= 3.4028234663852886e38f) || (P.checkMax && av > P.maxValueF);
+}
+
+// Comparisons of a new sample v with the previous one p1 through the one
+// difference d = RN(v - p1): RN(p1 - v) = -d exactly, so "p1 < v" is d > 0,
+// "p1 - v > 1e-13" is d < -1e-13 and "v - p1 > 1e-13" is d > 1e-13, all false
+// for NaN as the direct comparisons are; "p1 >= v" is d <= 0, or v == p1 for
+// equal infinities (where d is NaN). For double they run on the integer pipe:
+// the bits of a double order like signed integers on either side of zero.
+struct DiffTest {
+    bool up, ge, above, below;  // p1 < v, p1 >= v, v - p1 > 1e-13, p1 - v > 1e-13
+};
+__device__ __forceinline__ DiffTest diff_test(double v, double p1) {
+    const long long b = __double_as_longlong(v - p1);
+    const unsigned long long a = (unsigned long long)b & 0x7fffffffffffffffull;
+    constexpr unsigned long long kEps = 0x3d3c25c268497682ull;  // bits of 1e-13
+    constexpr unsigned long long kInf = 0x7ff0000000000000ull;
+    if (a <= kInf) return {b > 0, b <= 0, b > (long long)kEps, b < 0 && a > kEps};
+    const long long vb = __double_as_longlong(v);
+    const bool eqInf = vb == __double_as_longlong(p1) && ((unsigned long long)vb & 0x7fffffffffffffffull) == kInf;
+    return {false, eqInf, false, false};
+}
+__device__ __forceinline__ DiffTest diff_test(float v, float p1) {
+    const float d = v - p1;
+    return {d > 0.f, p1 >= v, d > 1e-13f, d < -1e-13f};
 }
 
 // Streaming form of the reference peakFinder (bifurcationCUDA.cu:469-514).
@@ -77,34 +108,39 @@ template <> __device__ __forceinline__ bool basins_diverged<float>(float v, cons
 // value d[j] at time trunc((i+j)/2); after either end the scan resumes at
 // j+2. The first detected peak is dropped and every later one is reported
 // with the interval to its predecessor, (t_k - t_{k-1}) * h.
+//
+// One subtraction per sample (diff_test): the next sample's rise test
+// "d[k] - d[k-1] > 1e-13" is taken when d[k] arrives and kept as a flag.
 template <class T> struct PeakStream {
-    T p2, p1;      // d[k-2], d[k-1]
+    T p1;          // d[k-1]
+    bool rise;     // d[k-1] - d[k-2] > 1e-13
     int k;         // index of the next sample
     int cand;      // scan mode: next candidate index; plateau mode: -1
     int i0;        // plateau: index of the candidate that opened it
     int n;         // peaks detected so far (the dropped first one included)
     int tprev;     // time index of the previous detected peak
 
-    __device__ __forceinline__ void init() { k = 0; cand = 1; i0 = 0; n = 0; tprev = 0; p1 = p2 = T(0); }
+    __device__ __forceinline__ void init() { k = 0; cand = 1; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false; }
 
     // Pushes d[k] = v; returns true and sets (val, t) when a peak was detected.
     __device__ __forceinline__ bool push(T v, T& val, int& t) {
+        const DiffTest c = diff_test(v, p1);
         bool hit = false;
         if (k >= 2) {
             if (cand < 0) {  // plateau, j = k-1
-                if (p1 < v) cand = k + 1;
-                else if (p1 - v > T(1e-13)) { hit = true; val = p1; t = (i0 + k - 1) >> 1; cand = k + 1; }
+                if (c.up) cand = k + 1;
+                else if (c.below) { hit = true; val = p1; t = (i0 + k - 1) >> 1; cand = k + 1; }
             } else if (cand == k - 1) {
-                if (p1 - p2 > T(1e-13) && p1 >= v) {
+                if (rise && c.ge) {
                     i0 = k - 1;
-                    if (p1 - v > T(1e-13)) { hit = true; val = p1; t = k - 1; cand = k + 1; }
+                    if (c.below) { hit = true; val = p1; t = k - 1; cand = k + 1; }
                     else cand = -1;
                 } else {
                     cand = k;
                 }
             }
         }
-        p2 = p1;
+        rise = c.above;
         p1 = v;
         ++k;
         return hit;

@@ -38,6 +38,8 @@ struct SweepParams {
     double hInterval;  // h * preScaller, the time unit of peak intervals
     double maxValue;
     float maxValueF;   // the largest float <= maxValue: for a float v, |v| > maxValue <=> |v| > maxValueF
+    unsigned long long maxBits;  // for a double v: (double)fabsf((float)v) > maxValue <=> bits(|v|) > maxBits,
+    int maxTie;                  //   or == maxBits with maxTie (the rounding boundary of float(v))
     double ic[kMaxState];
     double values[kMaxParams];
     int mut[2];

@@ -8,6 +8,7 @@ Lorenz / Rossler RK4 plug-ins (``chaoslibrary_gb300/plugins/``) standing in
 for ``systems/systems.cuh``:
 
   oracle/_ref/ref_gpu_bif1d   Bifurcation::bifurcation1D with the Lorenz RK4 plug-in
+  oracle/_ref/ref_gpu_bif2d   Bifurcation::bifurcation2D with the reference's own systems.cuh (Chameleon)
   oracle/_ref/ref_gpu_lle2d   LLE::LLE2D with the Rossler RK4 plug-in
 
 Nothing here is shipped or called by the engine; ``bench.py`` runs these
@@ -32,9 +33,11 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FILES = ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp",
          "Bifurcation/include/bifurcationCUDA.cuh", "Bifurcation/include/bifurcationHOST.h",
          "LLE/src/LLECUDA.cu", "LLE/src/LLEHost.cpp", "LLE/include/LLECUDA.cuh", "LLE/include/LLEHost.h",
-         "debri/cudaMacros.cu", "debri/cudaMacros.cuh"]
+         "debri/cudaMacros.cu", "debri/cudaMacros.cuh", "systems/systems.cuh"]
 TARGETS = {
     "bif1d": ("lorenz", "REF_BIF1D", ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp"]),
+    # the reference's own systems.cuh as shipped (its default plug-in, the Chameleon model)
+    "bif2d": (None, "REF_BIF2D", ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp"]),
     "lle2d": ("rossler", "REF_LLE2D", ["LLE/src/LLECUDA.cu", "LLE/src/LLEHost.cpp"]),
 }
 
@@ -59,9 +62,12 @@ def stage() -> None:
 
 def _build_one(name: str, verbose: bool) -> Path:
     system, macro, srcs = TARGETS[name]
-    sysdir = OUT / f"gsys_{system}"
-    sysdir.mkdir(parents=True, exist_ok=True)
-    (sysdir / "systems.cuh").write_text(f'#include "{REPO}/chaoslibrary_gb300/plugins/{system}_rk4.cuh"\n')
+    if system is None:
+        sysdir = STAGE / "systems"
+    else:
+        sysdir = OUT / f"gsys_{system}"
+        sysdir.mkdir(parents=True, exist_ok=True)
+        (sysdir / "systems.cuh").write_text(f'#include "{REPO}/chaoslibrary_gb300/plugins/{system}_rk4.cuh"\n')
     exe = binary(name)
     cmd = [NVCC, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-w", f"-D{macro}",
            f"-I{sysdir}", f"-I{STAGE / 'Bifurcation/include'}", f"-I{STAGE / 'LLE/include'}",

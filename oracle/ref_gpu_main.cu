@@ -5,6 +5,9 @@
 //
 //   ref_gpu_bif1d <out.csv> [nPts] [tMax]   Bifurcation::bifurcation1D, Lorenz RK4
 //                                           (h 0.01, rho in [20, 200], transient 100)
+//   ref_gpu_bif2d <out.csv> [nPts] [tMax]   Bifurcation::bifurcation2D, the reference's own
+//                                           Chameleon model and its timing sweep's settings
+//                                           (src/main.cu:447-505: transient 2000, eps 0.001)
 //   ref_gpu_lle2d <out.csv> [nPts] [tMax]   LLE::LLE2D, Rossler RK4 (h 0.01, NT 0.1,
 //                                           a in [0.1, 0.4], c in [2, 10], transient 50)
 //
@@ -19,7 +22,7 @@
 #include <cstdlib>
 #include <string>
 
-#if defined(REF_BIF1D)
+#if defined(REF_BIF1D) || defined(REF_BIF2D)
 #include "bifurcationHOST.h"
 #else
 #include "LLEHost.h"
@@ -31,6 +34,10 @@ static double run(const std::string& out, int nPts, double tMax) {
     const double ic[3] = {0.1, 0.1, 0.1}, ranges[2] = {20.0, 200.0}, values[3] = {10.0, 28.0, 8.0 / 3.0};
     const int mut[1] = {1};
     Bifurcation::bifurcation1D(tMax, nPts, 0.01, 3, ic, ranges, mut, 0, 1e4, 100.0, values, 3, 1, out);
+#elif defined(REF_BIF2D)
+    const double ic[3] = {3.0, 3.0, 0.0}, ranges[4] = {0.0, 5.0, 0.0, 20.0}, values[7] = {0.5, 3, 0, 2, 1, 18, 1};
+    const int mut[2] = {3, 5};
+    Bifurcation::bifurcation2D(tMax, nPts, 0.01, 3, ic, ranges, mut, 0, 1e4, 2000.0, values, 7, 1, 0.001, out);
 #else
     const double ic[3] = {1.0, 1.0, 1.0}, ranges[4] = {0.1, 0.4, 2.0, 10.0}, values[3] = {0.2, 0.2, 5.7};
     const int mut[2] = {0, 2};
@@ -45,12 +52,26 @@ int main(int argc, char** argv) {
 #if defined(REF_BIF1D)
     const int nPts = argc > 2 ? atoi(argv[2]) : 1000;
     const double tMax = argc > 3 ? atof(argv[3]) : 100.0;
+#elif defined(REF_BIF2D)
+    const int nPts = argc > 2 ? atoi(argv[2]) : 200;
+    const double tMax = argc > 3 ? atof(argv[3]) : 400.0;
+    // The reference indexes its trajectory buffer with int (idx * amountOfPointsInBlock,
+    // bifurcationCUDA.cu:338, 369), and on this GPU's memory one chunk holds every point: a
+    // product past 2^31 would write outside the buffer. Refuse such sizes.
+    if ((double)nPts * nPts * (tMax / 0.01) >= 2147483647.0) {
+        fprintf(stderr, "nPts^2 * tMax/h >= 2^31: the reference's int indexing would overflow\n");
+        return 2;
+    }
 #else
     const int nPts = argc > 2 ? atoi(argv[2]) : 1024;
     const double tMax = argc > 3 ? atof(argv[3]) : 500.0;
 #endif
     cudaFree(nullptr);     // context
+#if defined(REF_BIF2D)
+    run(out, 4, 1.0);      // warm-up: module load
+#else
     run(out, 16, 1.0);     // warm-up: module load
+#endif
     const double s = run(out, nPts, tMax);
     printf("{\"nPts\": %d, \"tMax\": %g, \"seconds\": %.6f}\n", nPts, tMax, s);
     return 0;
