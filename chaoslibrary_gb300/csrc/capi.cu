@@ -417,15 +417,21 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
     // every detected peak sits at least two samples after the previous one,
     // so B/2 rows hold all kept intervals of a point
     const int capFull = std::max(P.B / 2, 1);
-    // Peak-buffer capacity: the kept-peak counts of up to 4096 evenly spread
-    // points, 25 % + 16 above their maximum (or CHAOS_TUNE_BIF2D_CAP: > 0 a
-    // fixed capacity, -1 always B/2). Points with more peaks are run again
-    // with B/2 rows, so the capacity changes memory and speed, never results.
+    // Peak-buffer capacity. B/2 rows when the whole grid fits the scratch
+    // budget with them; else as many rows as let the grid run as one chunk,
+    // when that is at least 512; else the kept-peak counts of up to 4096
+    // evenly spread points, 25 % + 16 above their maximum (a probe whose cost
+    // is one full trajectory). CHAOS_TUNE_BIF2D_CAP: > 0 a fixed capacity, -1
+    // always B/2. Points with more peaks than the capacity are run again with
+    // B/2 rows, so the capacity changes memory and speed, never results.
     int cap = capFull;
     const int capKnob = g_bif2d_cap.load(std::memory_order_relaxed);
     const bool adapt = capKnob >= 0 && P.system != SYS_USER && n <= 0x7fffffffLL && capFull > 64;
+    const long long capBudget = (long long)(scratch_budget_bytes() / ((size_t)n * (sizeof(double) + 2 * sizeof(int))));
     if (adapt && capKnob > 0) {
         cap = std::min(capKnob, capFull);
+    } else if (adapt && capBudget >= 512) {
+        cap = (int)std::min<long long>(capFull, capBudget);
     } else if (adapt) {
         const int S = (int)std::min<long long>(n, 4096);
         std::vector<int> idx(S), hc(S);

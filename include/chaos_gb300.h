@@ -376,10 +376,12 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
    direction with cuRAND). FP64 only. Initial value: CHAOS_LLE_TWIN=1. */
 #define CHAOS_TUNE_LLE_TWIN 4
 /* CHAOS_TUNE_BIF2D_CAP: peak rows per point of the 2-D bifurcation's
-   clustering scratch. 0 (default): measured per call from the kept-peak
-   counts of up to 4096 evenly spread points (+25 % + 16); > 0 that many;
-   -1: B/2, the most a point can keep. Points with more peaks than the
-   capacity are run again with B/2 rows: results never depend on it. */
+   clustering scratch. 0 (default): B/2 (the most a point can keep) when the
+   grid fits the scratch budget with it, else what lets the grid run as one
+   chunk (at least 512), else measured from the kept-peak counts of up to
+   4096 evenly spread points (+25 % + 16); > 0 that many; -1 always B/2.
+   Points with more peaks than the capacity are run again with B/2 rows:
+   results never depend on it. */
 #define CHAOS_TUNE_BIF2D_CAP 5
 int chaos_set_tuning(int knob, int value);
 int chaos_get_tuning(int knob);

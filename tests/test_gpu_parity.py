@@ -607,23 +607,26 @@ def test_lle_sign_recheck(engine):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_bif2d_capacity_never_changes_results(engine, precision):
-    """The 2-D bifurcation's peak-buffer capacity (measured per call, fixed,
-    or B/2) changes memory and speed only: points with more kept peaks than
-    the capacity are run again with B/2 rows, so labels and counts are the
-    same in every mode."""
+def test_bif2d_capacity_never_changes_results(engine, precision, monkeypatch):
+    """The 2-D bifurcation's peak-buffer capacity (B/2, fitted to the scratch
+    budget, measured by a probe under a 1 MB budget, or fixed) changes memory
+    and speed only: points with more kept peaks than the capacity are run
+    again with B/2 rows, so labels and counts are the same in every mode."""
     kw = dict(tMax=40.0, nPts=24, h=0.01, initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0, 0.0, 20.0],
               indicesOfMutVars=[3, 5], writableVar=0, maxValue=1e4, transientTime=20.0,
               values=[0.5, 3, 0, 2, 1, 18, 1], eps=0.001)
     knob = engine.TUNE_BIF2D_CAP
     res = {}
     try:
-        for mode in (-1, 0, 3):
+        for name, mode, budget_mb in (("full", -1, None), ("default", 0, None), ("fixed3", 3, None),
+                                      ("probe", 0, "1")):
+            if budget_mb:
+                monkeypatch.setenv("CHAOS_SCRATCH_BUDGET_MB", budget_mb)
             engine.set_tuning(knob, mode)
-            res[mode] = engine.bifurcation2d("chameleon", precision=precision, **kw)
+            res[name] = engine.bifurcation2d("chameleon", precision=precision, **kw)
     finally:
         engine.set_tuning(knob, 0)
-    assert (res[-1]["counts"] > 3).any()  # the fixed capacity 3 really overflows
-    for mode in (0, 3):
-        assert np.array_equal(res[mode]["labels"], res[-1]["labels"]), mode
-        assert np.array_equal(res[mode]["counts"], res[-1]["counts"]), mode
+    assert (res["full"]["counts"] > 3).any()  # the fixed capacity 3 really overflows
+    for name in ("default", "fixed3", "probe"):
+        assert np.array_equal(res[name]["labels"], res["full"]["labels"]), name
+        assert np.array_equal(res[name]["counts"], res["full"]["counts"]), name
