@@ -677,11 +677,13 @@ def engine_arm(args, ws, rank, local):
     line["e2e"] = {"value": ws * steps_per_call / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 88,
                    "d2h_bytes_per_step": d2h}
 
-    if rank == 0 and ws == 1 and args.workload in ("lle", "bif1d") and not args.no_extras and not args.npts \
-            and not args.tmax:
+    if rank == 0 and ws == 1 and args.workload in ("lle", "bif1d", "bif2d") and not args.no_extras \
+            and not args.npts and not args.tmax:
         ref = reference_gpu_run(args.workload, steps_per_call)
         if ref:
             line["reference_gpu"] = ref
+    if rank == 0 and ws == 1 and args.workload == "bif2d" and not args.no_extras:
+        line.update(bif2d_extras(C, prec, w))
     if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras:
         line.update(lle_precision_report(C, prec, dev))
     if rank == 0 and ws == 1 and args.workload == "basins" and not args.no_extras:
@@ -702,21 +704,48 @@ def reference_gpu_run(workload, steps):
     """The reference's own GPU path on this GPU (its unchanged sources built by
     oracle/build_ref_gpu.py, when that build is present): wall time of one call
     of its host entry point on the same configuration, including its own host
-    work (allocation, per-element zeroing copies, copy back, CSV writing)."""
-    exe = ROOT / "oracle" / "_ref" / f"ref_gpu_{ {'lle': 'lle2d', 'bif1d': 'bif1d'}[workload]}"
+    work (allocation, per-element zeroing copies, copy back, CSV writing). The
+    2-D bifurcation runs at 200^2: at 300^2 the reference's int indexing of its
+    trajectory buffer would overflow."""
+    exe = ROOT / "oracle" / "_ref" / f"ref_gpu_{ {'lle': 'lle2d', 'bif1d': 'bif1d', 'bif2d': 'bif2d'}[workload]}"
     if not exe.exists():
         return None
+    extra = []
+    if workload == "bif2d":
+        extra = ["200"]
+        steps = 200 * 200 * sweep_steps_per_point(BIF2D)
     with tempfile.TemporaryDirectory() as d:
         try:
-            p = subprocess.run([str(exe), str(Path(d) / "out.csv")], capture_output=True, text=True, timeout=300)
+            p = subprocess.run([str(exe), str(Path(d) / "out.csv")] + extra, capture_output=True, text=True,
+                               timeout=300)
         except subprocess.TimeoutExpired:
             return {"value": None, "error": "timed out after 300 s"}
     if p.returncode != 0:
         return {"value": None, "error": f"exit {p.returncode}"}
     s = json.loads(p.stdout.strip().splitlines()[-1])["seconds"]
-    return {"value": steps / s, "unit": UNIT, "seconds": s,
+    return {"value": steps / s, "unit": UNIT, "seconds": s, "steps": float(steps),
             "what": "the reference's unchanged sources (its host entry point, FP64, nvcc defaults) built for "
-                    "sm_103a with the same RK4 plug-in, timed around one call incl. its host work"}
+                    "sm_103a with the same plug-in, timed around one call incl. its host work"}
+
+
+def bif2d_extras(C, prec, w):
+    """The same 300^2 map in plain FP64 (time and labels), and how many FP32
+    labels equal the FP64 ones."""
+    import time as _t
+
+    kw = kw_of(w)
+    other = C.FP64 if prec == C.FP32 else C.FP32
+    C.bifurcation2d(w["system"], precision=other, **dict(kw, nPts=8))
+    t0 = _t.perf_counter()
+    r_other = C.bifurcation2d(w["system"], precision=other, **kw)
+    dt = _t.perf_counter() - t0
+    r_this = C.bifurcation2d(w["system"], precision=prec, **kw)
+    steps = w["nPts"] ** 2 * sweep_steps_per_point(w)
+    name = "fp64_plain" if other == C.FP64 else "fp32"
+    return {name: {"value": steps / dt, "unit": UNIT, "seconds": dt},
+            "labels_fp32_equal_fp64": float(np.mean(r_other["labels"] == r_this["labels"])),
+            "labels_note": "per-point clustering of peak intervals at eps 0.001 (steps of 0.01): one-step shifts "
+                           "of FP32 peak times change the cluster count"}
 
 
 def label_agreement(a, b, fixed=()):
