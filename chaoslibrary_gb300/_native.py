@@ -71,6 +71,7 @@ _SIGS = {
     "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
     "chaos_fma_probe": ([_P, _L, _P, _P], _I),
     "chaos_launch_count": ([_P], _I),
+    "chaos_autotune": ([_P, _P, _I], _I),
     "chaos_trajectory": ([_P, _I, _L, _P, _P, _D, _I, _P], _I),
     "chaos_set_tuning": ([_I, _I], _I),
     "chaos_run_batch": ([_P, _P, _I], _I),
@@ -181,6 +182,17 @@ def fma_probe(iters: int = 200000, device=None) -> float:
     return fl.value / sec.value
 
 
+def autotune(device=None) -> list[dict]:
+    """Times the FP32 sweeps' launch shapes on this GPU and installs the
+    fastest (chaos_autotune); returns one row per (kind, system)."""
+    ex = Exec(FP32, MEM_HOST, None, -1 if device is None else int(device))
+    t = np.zeros((9, 6))
+    _check(lib().chaos_autotune(C.byref(ex), t.ctypes.data, 9))
+    kinds = ("bif1d", "basins", "lle")
+    return [dict(kind=kinds[int(r[0])], system=int(r[1]), form=int(r[2]), block=int(r[3]), best_ms=float(r[4]),
+                 rule_ms=float(r[5])) for r in t]
+
+
 def launch_count() -> int:
     """Kernels the library has launched in this process so far."""
     n = C.c_longlong()
@@ -207,6 +219,7 @@ TUNE_SWEEP_PAIRS = 2
 TUNE_GRID_FMA = 3
 TUNE_LLE_TWIN = 4
 TUNE_BIF2D_CAP = 5
+TUNE_SHAPES = 6
 
 
 def set_tuning(knob: int, value: int) -> None:

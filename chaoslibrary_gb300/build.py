@@ -20,6 +20,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 # the source writes (no multiply-add contraction).
 SOURCES = [
     ("kern_f64.cu", ["--fmad=false"]),
+    ("tune.cu", []),
     ("kern_f32.cu", []),
     ("dbscan.cu", ["--fmad=false", "--extended-lambda"]),
     ("basins_dbscan.cu", ["--fmad=false"]),

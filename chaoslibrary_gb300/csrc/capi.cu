@@ -769,6 +769,12 @@ int chaos_set_tuning(int knob, int value) {
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
     if (knob == CHAOS_TUNE_SWEEP_PAIRS)
         return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1 or 2)", value) : CHAOS_OK;
+    if (knob == CHAOS_TUNE_SHAPES) {
+        if (value != 0) return set_error(CHAOS_E_ARGS, "CHAOS_TUNE_SHAPES takes 0 (forget tuned shapes)");
+        for (int k = 0; k < 3; ++k)
+            for (int s = 0; s <= SYS_CHEN_RK4; ++s) set_launch_shape(k, s, 0);
+        return CHAOS_OK;
+    }
     if (knob == CHAOS_TUNE_BIF2D_CAP) {
         if (value < -1) return set_error(CHAOS_E_ARGS, "bifurcation 2-D capacity: -1, 0 or a row size");
         g_bif2d_cap.store(value);

@@ -11,10 +11,11 @@
 namespace chaos {
 
 namespace {
-constexpr int kBlock = 128;
+constexpr int kBlock = 128;     // default block
+constexpr int kMaxBlock = 256;  // largest block a tuned launch may use
 
 template <int S>
-__global__ void __launch_bounds__(kBlock) bif_kernel_f32(SweepParams P, BifOut O) {
+__global__ void __launch_bounds__(kMaxBlock) bif_kernel_f32(SweepParams P, BifOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
     bif_point<S, float>(P, O, P.pBegin + o, o);
@@ -28,7 +29,7 @@ __global__ void __launch_bounds__(kBlock) bif_list_kernel_f32(SweepParams P, Bif
 }
 
 template <int S, bool PRE1>
-__global__ void __launch_bounds__(kBlock) basins_kernel_f32(SweepParams P, BasinsOut O) {
+__global__ void __launch_bounds__(kMaxBlock) basins_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
     basins_point<S, float, PRE1>(P, O, P.pBegin + o, o);
@@ -54,7 +55,7 @@ __global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0
 
 // Bifurcation / basins, two points per thread in packed FP32x2 lanes (RK4 systems).
 template <class F>
-__global__ void __launch_bounds__(kBlock) bif_pair_kernel_f32(SweepParams P, BifOut O) {
+__global__ void __launch_bounds__(kMaxBlock) bif_pair_kernel_f32(SweepParams P, BifOut O) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (o >= P.nPoints) return;
     const bool two = o + 1 < P.nPoints;
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(kBlock) bif_pair_kernel_f32(SweepParams P, Bif
 }
 
 template <class F, bool PRE1>
-__global__ void __launch_bounds__(kBlock) basins_pair_kernel_f32(SweepParams P, BasinsOut O) {
+__global__ void __launch_bounds__(kMaxBlock) basins_pair_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (o >= P.nPoints) return;
     const bool two = o + 1 < P.nPoints;
@@ -78,16 +79,22 @@ namespace {
 // FP32x2 lanes. CHAOS_LLE_MINB forces one, otherwise the measured default.
 std::atomic<int> g_lle_variant{0};
 
-int lle_occupancy_variant(int system) {
-    (void)system;
-    const int set = g_lle_variant.load(std::memory_order_relaxed);
-    if (set) return set;
+int lle_env_variant() {
     static int forced = [] {
         const char* s = getenv("CHAOS_LLE_MINB");
         return s ? atoi(s) : 0;
     }();
-    return forced ? forced : 2;
+    return forced;
 }
+
+int lle_occupancy_variant(int system) {
+    (void)system;
+    const int set = g_lle_variant.load(std::memory_order_relaxed);
+    if (set) return set;
+    return lle_env_variant() ? lle_env_variant() : 2;
+}
+
+bool lle_variant_forced() { return g_lle_variant.load(std::memory_order_relaxed) != 0 || lle_env_variant() != 0; }
 
 #define CHAOS_SYSTEM_SWITCH(sys, CALL) \
     switch (sys) {                     \
@@ -126,44 +133,71 @@ int set_sweep_pairs(int v) {
     return 0;
 }
 
-inline unsigned pair_grid(long long n) { return grid_for((n + 1) / 2); }
+inline unsigned grid_of(long long threads, int block) { return (unsigned)((threads + block - 1) / block); }
 
-// Pairs halve the threads: worth it when the sweep fills the GPU several
-// times over, not for small (latency-bound) sweeps.
-bool use_pairs(const SweepParams& P, bool basins) {
-    if (P.system > SYS_CHEN_RK4) return false;
-    const int mode = sweep_pairs();
-    if (mode != 1) return mode == 2;
-    if (basins) return false;
+// Launch shapes the self-timing tuner (tune.cu) found, per kind (0 1-D
+// bifurcation, 1 basins, 2 LLE map) and RK4 system: 0 = none (the built-in
+// rules below), else form * 1024 + block with form 1 (one point per thread)
+// or 2 (two points per thread in packed FP32x2 lanes); for the LLE map also
+// form 12 / 16 (one point per thread, registers shaped for 12 / 16 resident
+// blocks per SM, block 128).
+std::atomic<int> g_shape[3][3];
+
+int shape_of(int kind, int system) {
+    return system >= 0 && system <= SYS_CHEN_RK4 ? g_shape[kind][system].load(std::memory_order_relaxed) : 0;
+}
+
+long long pair_threshold() {
     static long long threshold = [] {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         return 4LL * std::max(sms, 1) * 1024;
     }();
-    return P.nPoints >= threshold;
+    return threshold;
 }
 
-template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, cudaStream_t st) {
-    bif_pair_kernel_f32<F><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+struct Launch {
+    bool pairs;
+    int block;
+};
+
+// Pairs halve the threads: worth it when the sweep fills the GPU several
+// times over, not for small (latency-bound) sweeps. An explicit sweep-pairs
+// mode (0 / 2) wins; then a tuned shape; then the measured rule.
+Launch sweep_launch(const SweepParams& P, bool basins) {
+    if (P.system > SYS_CHEN_RK4) return {false, kBlock};
+    const int mode = sweep_pairs();
+    const int shape = shape_of(basins ? 1 : 0, P.system);
+    const int block = shape ? shape % 1024 : kBlock;
+    if (mode != 1) return {mode == 2, block};
+    const bool big = P.nPoints >= pair_threshold();
+    if (shape) return {shape / 1024 == 2 && big, block};
+    return {!basins && big, kBlock};
+}
+
+template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, int block, cudaStream_t st) {
+    bif_pair_kernel_f32<F><<<grid_of((P.nPoints + 1) / 2, block), block, 0, st>>>(P, O);
     note_launch();
 }
 
-template <class F> void launch_basins_pairs(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
-    if (P.preScaller == 1) basins_pair_kernel_f32<F, true><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
-    else basins_pair_kernel_f32<F, false><<<pair_grid(P.nPoints), kBlock, 0, st>>>(P, O);
+template <class F> void launch_basins_pairs(const SweepParams& P, const BasinsOut& O, int block, cudaStream_t st) {
+    const unsigned g = grid_of((P.nPoints + 1) / 2, block);
+    if (P.preScaller == 1) basins_pair_kernel_f32<F, true><<<g, block, 0, st>>>(P, O);
+    else basins_pair_kernel_f32<F, false><<<g, block, 0, st>>>(P, O);
     note_launch();
 }
 
 cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-    if (use_pairs(P, false)) {
-        if (P.system == SYS_LORENZ_RK4) launch_bif_pairs<Lorenz>(P, O, st);
-        else if (P.system == SYS_ROSSLER_RK4) launch_bif_pairs<Rossler>(P, O, st);
-        else launch_bif_pairs<Chen>(P, O, st);
+    const Launch l = sweep_launch(P, false);
+    if (l.pairs) {
+        if (P.system == SYS_LORENZ_RK4) launch_bif_pairs<Lorenz>(P, O, l.block, st);
+        else if (P.system == SYS_ROSSLER_RK4) launch_bif_pairs<Rossler>(P, O, l.block, st);
+        else launch_bif_pairs<Chen>(P, O, l.block, st);
         return cudaGetLastError();
     }
-#define CALL(S) (bif_kernel_f32<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
+#define CALL(S) (bif_kernel_f32<S><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O), note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -179,15 +213,17 @@ cudaError_t launch_bif_list_f32(const SweepParams& P, const BifOut& O, const int
 
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-    if (use_pairs(P, true)) {
-        if (P.system == SYS_LORENZ_RK4) launch_basins_pairs<Lorenz>(P, O, st);
-        else if (P.system == SYS_ROSSLER_RK4) launch_basins_pairs<Rossler>(P, O, st);
-        else launch_basins_pairs<Chen>(P, O, st);
+    const Launch l = sweep_launch(P, true);
+    if (l.pairs) {
+        if (P.system == SYS_LORENZ_RK4) launch_basins_pairs<Lorenz>(P, O, l.block, st);
+        else if (P.system == SYS_ROSSLER_RK4) launch_basins_pairs<Rossler>(P, O, l.block, st);
+        else launch_basins_pairs<Chen>(P, O, l.block, st);
         return cudaGetLastError();
     }
-#define CALL(S)                                                                           \
-    (P.preScaller == 1 ? basins_kernel_f32<S, true><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O) \
-                       : basins_kernel_f32<S, false><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), \
+    const unsigned g = grid_of(P.nPoints, l.block);
+#define CALL(S)                                                                \
+    (P.preScaller == 1 ? basins_kernel_f32<S, true><<<g, l.block, 0, st>>>(P, O) \
+                       : basins_kernel_f32<S, false><<<g, l.block, 0, st>>>(P, O), \
      note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
@@ -196,7 +232,7 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
 
 // Two points per thread in packed FP32x2 lanes.
 template <class F>
-__global__ void __launch_bounds__(kBlock) lle_pair_kernel_f32(LleParams L, double* out) {
+__global__ void __launch_bounds__(kMaxBlock) lle_pair_kernel_f32(LleParams L, double* out) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (o >= L.nPoints) return;
     const bool two = o + 1 < L.nPoints;
@@ -204,11 +240,20 @@ __global__ void __launch_bounds__(kBlock) lle_pair_kernel_f32(LleParams L, doubl
 }
 
 template <class F>
-static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb) {
-    if (minb == 2) lle_pair_kernel_f32<F><<<grid_for((L.nPoints + 1) / 2), kBlock, 0, st>>>(L, out);
+static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb, int block) {
+    if (minb == 2) lle_pair_kernel_f32<F><<<grid_of((L.nPoints + 1) / 2, block), block, 0, st>>>(L, out);
     else if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
     else lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
     note_launch();
+}
+
+int set_launch_shape(int kind, int system, int code) {
+    if (kind < 0 || kind > 2 || system < 0 || system > SYS_CHEN_RK4 || code < 0) return -1;
+    g_shape[kind][system].store(code);
+    return 0;
+}
+int get_launch_shape(int kind, int system) {
+    return kind >= 0 && kind <= 2 ? shape_of(kind, system) : 0;
 }
 
 int set_lle_variant(int v) {
@@ -220,11 +265,17 @@ int get_lle_variant() { return lle_occupancy_variant(0); }
 
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
-    const int minb = lle_occupancy_variant(L.system);
+    // an explicit variant (chaos_set_tuning / CHAOS_LLE_MINB) wins, then a tuned shape
+    int minb = lle_occupancy_variant(L.system), block = kBlock;
+    const int shape = shape_of(2, L.system);
+    if (shape && !lle_variant_forced()) {
+        minb = shape / 1024;
+        block = minb == 2 ? shape % 1024 : kBlock;
+    }
     switch (L.system) {
-        case SYS_LORENZ_RK4: launch_twin<Lorenz>(L, out, st, minb); break;
-        case SYS_ROSSLER_RK4: launch_twin<Rossler>(L, out, st, minb); break;
-        case SYS_CHEN_RK4: launch_twin<Chen>(L, out, st, minb); break;
+        case SYS_LORENZ_RK4: launch_twin<Lorenz>(L, out, st, minb, block); break;
+        case SYS_ROSSLER_RK4: launch_twin<Rossler>(L, out, st, minb, block); break;
+        case SYS_CHEN_RK4: launch_twin<Chen>(L, out, st, minb, block); break;
         default: return cudaErrorNotSupported;
     }
     return cudaGetLastError();

@@ -121,7 +121,11 @@ cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double*
 int set_lle_variant(int v);
 int get_lle_variant();
 // Paired FP32 bifurcation / basins kernels for the RK4 systems (kern_f32.cu).
-int sweep_pairs();  // 0 never, 1 large sweeps, 2 always
+int sweep_pairs();
+// launch shapes found by the tuner (kern_f32.cu): kind 0 bifurcation, 1 basins,
+// 2 LLE map; code 0 = built-in rule, else form * 1024 + block
+int set_launch_shape(int kind, int system, int code);
+int get_launch_shape(int kind, int system);  // 0 never, 1 large sweeps, 2 always
 int set_sweep_pairs(int v);
 
 // The build-time user plug-in (kern_user.cu, or user_stub.cu when the build

@@ -383,8 +383,26 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
    Points with more peaks than the capacity are run again with B/2 rows:
    results never depend on it. */
 #define CHAOS_TUNE_BIF2D_CAP 5
+/* CHAOS_TUNE_SHAPES: 0 forgets the launch shapes chaos_autotune installed
+   (the built-in rules apply again). */
+#define CHAOS_TUNE_SHAPES 6
 int chaos_set_tuning(int knob, int value);
 int chaos_get_tuning(int knob);
+
+/*
+ * Self-timing tuner (no reference counterpart). Times the launch shapes of the
+ * FP32 sweeps of the three RK4 systems -- one or two trajectories per thread,
+ * the LLE map's register shapes, blocks of 64 / 128 / 256 threads -- on probe
+ * sweeps that fill the GPU of ex (about 2-3 s in all), and installs the
+ * fastest per (kind, system) for every later call in the process; a shape
+ * replaces the built-in rule only when at least 1 % faster. Results do not
+ * depend on shapes. An explicit CHAOS_TUNE_SWEEP_PAIRS (0 / 2) or
+ * CHAOS_TUNE_LLE_F32_VARIANT still wins. table (may be NULL) receives nTable
+ * rows (9 fill all) of 6 doubles: kind (0 1-D bifurcation, 1 basins, 2 LLE
+ * map), system, form (0 rule; 1 / 2 trajectories per thread; 12 / 16 LLE
+ * register shapes), block, best ms, the built-in rule's ms.
+ */
+int chaos_autotune(const chaos_exec* ex, double* table, int nTable);
 
 /*
  * FP32 FMA-pipe probe (no reference counterpart): times `iters` rounds of 8

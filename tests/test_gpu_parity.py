@@ -630,3 +630,38 @@ def test_bif2d_capacity_never_changes_results(engine, precision, monkeypatch):
     for name in ("default", "fixed3", "probe"):
         assert np.array_equal(res[name]["labels"], res["full"]["labels"]), name
         assert np.array_equal(res[name]["counts"], res["full"]["counts"]), name
+
+
+def test_autotune_changes_no_result(engine):
+    """chaos_autotune times the FP32 sweeps' launch shapes on this GPU and
+    installs the fastest; bifurcation, basins and LLE results are the same
+    before and after it, and CHAOS_TUNE_SHAPES 0 restores the rules."""
+    bif = dict(tMax=10.0, nPts=3000, h=0.01, initialConditions=[0.1, 0.1, 0.1], ranges=[20.0, 200.0],
+               indicesOfMutVars=[1], writableVar=0, maxValue=1e4, transientTime=5.0, values=[10.0, 28.0, 8 / 3])
+    bas = dict(tMax=5.0, nPts=60, h=0.01, initialConditions=[0.0, 0.0, 27.0], ranges=[-30.0, 30.0, -30.0, 30.0],
+               indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8, transientTime=5.0, values=[10.0, 24.0, 8 / 3])
+    lle = dict(tMax=5.0, NT=0.1, nPts=60, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+               ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=2.0, values=[0.2, 0.2, 5.7])
+
+    def run():
+        return (engine.bifurcation1d("lorenz", precision=engine.FP32, peakCapacity=16, **bif),
+                engine.basins_features("lorenz", precision=engine.FP32, **bas),
+                engine.lle2d("rossler", precision=engine.FP32, **lle))
+
+    before = run()
+    try:
+        table = engine.autotune()
+        assert len(table) == 9 and all(r["best_ms"] > 0 and r["rule_ms"] > 0 for r in table)
+        assert all(r["best_ms"] <= r["rule_ms"] for r in table)
+        after = run()
+    finally:
+        engine.set_tuning(engine.TUNE_SHAPES, 0)
+    (b0, f0, l0), (b1, f1, l1) = before, after
+    for k in ("counts", "flags"):
+        assert np.array_equal(b0[k], b1[k]), k
+    for r, c in enumerate(b0["counts"]):
+        m = min(int(c), 16)
+        assert np.array_equal(b0["peaks"][r, :m], b1["peaks"][r, :m])
+    for k in ("flags", "avg_peaks", "avg_intervals"):
+        assert np.array_equal(f0[k], f1[k]), k
+    assert np.array_equal(l0, l1, equal_nan=True)
