@@ -61,6 +61,8 @@ _SIGS = {
     "chaos_bifurcation1d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _P], _I),
     "chaos_bifurcation2d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P], _I),
     "chaos_lle2d": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, _P], _I),
+    "chaos_lle_sweep": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
+    "chaos_lyapunov_spectrum": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
     "chaos_basins_features": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _P, _P, _P, _P], _I),
     "chaos_basins": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P, _P, _P], _I),
@@ -483,6 +485,40 @@ def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMu
     _check(lib().chaos_lle2d(C.byref(ex), _sys(system), tMax, NT, nPts, h, eps, A.d(ic), ic.size, A.d(ranges),
                              A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size,
                              _out_ptr(out)))
+    return out
+
+
+def lle_sweep(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime,
+              values, mutateState=False, precision=FP64, out=None, stream=None):
+    """LLE over a 1-D (lle[i]) or 2-D (lle[j*nPts + i]) grid of parameters or,
+    with mutateState, of initial conditions (chaos_lle_sweep)."""
+    A = _Args()
+    n = nPts ** dim
+    if out is None:
+        out = np.zeros(n)
+    ex = _exec(precision, {"lle": out}, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_lle_sweep(C.byref(ex), _sys(system), dim, 1 if mutateState else 0, tMax, NT, nPts, h, eps,
+                                 A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), transientTime, A.d(vals),
+                                 vals.size, _out_ptr(out)))
+    return out
+
+
+def lyapunov_spectrum(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
+                      transientTime, values, mutateState=False, precision=FP64, out=None, stream=None):
+    """Lyapunov spectrum [points, SIZE_X] over the grids of lle_sweep
+    (chaos_lyapunov_spectrum)."""
+    A = _Args()
+    ic = np.asarray(initialConditions, np.float64)
+    n = nPts ** dim
+    if out is None:
+        out = np.zeros((n, ic.size))
+    ex = _exec(precision, {"spectrum": out}, stream)
+    vals = np.asarray(values, np.float64)
+    _check(lib().chaos_lyapunov_spectrum(C.byref(ex), _sys(system), dim, 1 if mutateState else 0, tMax, NT, nPts, h,
+                                         eps, A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), transientTime,
+                                         A.d(vals), vals.size, _out_ptr(out)))
     return out
 
 

@@ -285,16 +285,20 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
 
 int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double h, double eps,
              const double* initialConditions, int amountOfInitialConditions, const double* ranges,
-             const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues) {
+             const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues, int dim,
+             int mutateState) {
     int rc = check_system(system, amountOfInitialConditions, amountOfValues);
     if (rc) return rc;
     if (!initialConditions || !ranges || !indicesOfMutVars || !values) return set_error(CHAOS_E_ARGS, "null argument");
     if (nPts < 1) return set_error(CHAOS_E_ARGS, "nPts must be >= 1");
     if (!(h > 0) || !(tMax > 0) || !(NT > 0) || !(transientTime >= 0) || !(eps > 0))
         return set_error(CHAOS_E_ARGS, "need h, tMax, NT, eps > 0 and transientTime >= 0");
-    for (int d = 0; d < 2; ++d)
-        if (indicesOfMutVars[d] < 0 || indicesOfMutVars[d] >= amountOfValues)
+    if (dim != 1 && dim != 2) return set_error(CHAOS_E_ARGS, "dim must be 1 or 2");
+    const int lim = mutateState ? amountOfInitialConditions : amountOfValues;
+    for (int d = 0; d < dim; ++d)
+        if (indicesOfMutVars[d] < 0 || indicesOfMutVars[d] >= lim)
             return set_error(CHAOS_E_ARGS, "indicesOfMutVars[%d] out of range", d);
+    if (dim == 2 && (double)nPts * nPts > 2.0e9) return set_error(CHAOS_E_ARGS, "nPts^2 must be < 2e9");
     if (NT / h > 2.0e9 || tMax / h > 2.0e9 || transientTime / h > 2.0e9)
         return set_error(CHAOS_E_ARGS, "step counts must fit in int");
     memset(&L, 0, sizeof L);
@@ -311,16 +315,18 @@ int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double 
     for (int i = 0; i < amountOfInitialConditions; ++i) L.ic[i] = initialConditions[i];
     for (int i = 0; i < amountOfValues; ++i) L.values[i] = values[i];
     L.mut[0] = indicesOfMutVars[0];
-    L.mut[1] = indicesOfMutVars[1];
+    L.mut[1] = dim == 2 ? indicesOfMutVars[1] : -1;
     L.rangeA[0] = ranges[0];
     L.rangeA[1] = ranges[1];
-    L.rangeB[0] = ranges[2];
-    L.rangeB[1] = ranges[3];
+    L.rangeB[0] = dim == 2 ? ranges[2] : 0.0;
+    L.rangeB[1] = dim == 2 ? ranges[3] : 0.0;
     L.stepA = nPts > 1 ? (ranges[1] - ranges[0]) / (nPts - 1) : 0.0;
-    L.stepB = nPts > 1 ? (ranges[3] - ranges[2]) / (nPts - 1) : 0.0;
+    L.stepB = nPts > 1 && dim == 2 ? (ranges[3] - ranges[2]) / (nPts - 1) : 0.0;
     L.pBegin = 0;
-    L.nPoints = (long long)nPts * nPts;
+    L.nPoints = dim == 2 ? (long long)nPts * nPts : nPts;
     L.twin = g_lle_twin.load(std::memory_order_relaxed);
+    L.dim = dim;
+    L.mutateState = mutateState ? 1 : 0;
     return CHAOS_OK;
 }
 
@@ -526,6 +532,55 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     cudaError_t e = run_lle(c.ex.precision, L, dOut, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "LLE kernel"));
     rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT, int nPts,
+                    double h, double eps, const double* initialConditions, int amountOfInitialConditions,
+                    const double* ranges, const int* indicesOfMutVars, double transientTime, const double* values,
+                    int amountOfValues, double* lle) {
+    int rc = CHAOS_OK;
+    if (!lle) return set_error(CHAOS_E_ARGS, "null argument");
+    LleParams L;
+    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                       indicesOfMutVars, transientTime, values, amountOfValues, dim, mutateState)))
+        return rc;
+    if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_difference_form(system)))
+        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
+        return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = run_lle(c.ex.precision, L, dOut, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "LLE kernel"));
+    rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT,
+                            int nPts, double h, double eps, const double* initialConditions,
+                            int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                            double transientTime, const double* values, int amountOfValues, double* spectrum) {
+    int rc = CHAOS_OK;
+    if (!spectrum) return set_error(CHAOS_E_ARGS, "null argument");
+    if (system == SYS_USER) return set_error(CHAOS_E_UNSUPPORTED, "the spectrum runs on the built-in systems");
+    LleParams L;
+    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                       indicesOfMutVars, transientTime, values, amountOfValues, dim, mutateState)))
+        return rc;
+    const bool fp32 = ex && ex->precision == CHAOS_FP32;
+    if (fp32 && !system_has_difference_form(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "the FP32 spectrum needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    const size_t bytes = (size_t)L.nPoints * system_nx(system) * sizeof(double);
+    double* dOut = (double*)c.output(spectrum, bytes);
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = fp32 ? launch_spectrum_f32(L, dOut, c.stream) : launch_spectrum_f64(L, dOut, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "Lyapunov spectrum kernel"));
+    rc = c.to_host(spectrum, dOut, bytes);
     return c.finish(rc);
 }
 

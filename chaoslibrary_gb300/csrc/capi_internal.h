@@ -41,6 +41,7 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
                const double* values, int nValues, int preScaller, bool basins);
 int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double h, double eps,
              const double* initialConditions, int amountOfInitialConditions, const double* ranges,
-             const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues);
+             const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
+             int dim = 2, int mutateState = 0);
 
 }  // namespace chaos

@@ -348,22 +348,40 @@ __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsO
 // precision T for both trajectories: calcBlocks+1 blocks of NT steps of x and
 // of its twin q; d = |x-q|/eps; sum += log(d); q = x - (x-q)/d; sum / tMax.
 // The twin starts at x + eps along state component 0.
-template <int S, class T>
-__device__ __forceinline__ double lle_point_full(const LleParams& L, long long p) {
-    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
-    const int i = (int)(p % L.nPts), j = (int)(p / L.nPts);
-    T x[NX], q[NX], a[NA];
-#pragma unroll
-    for (int k = 0; k < NX; ++k) x[k] = (T)L.ic[k];
+// State and parameters of point p of an LLE-type sweep: a 1-D grid (p = i)
+// or the 2-D map (p = j*nPts + i), over parameters values[mut] or initial
+// conditions ic[mut] (L.mutateState); the second dimension is written last.
+// Swept values are linspace start + n*step, multiply and add rounded apart.
+template <int NX, int NA, class T>
+__device__ __forceinline__ void lle_load(const LleParams& L, long long p, T* x, T* a) {
+    const long long i = L.dim == 1 ? p : p % L.nPts, j = L.dim == 1 ? 0 : p / L.nPts;
     const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
-    const double vb = L.nPts == 1 ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
+    const double vb = (L.nPts == 1 || L.dim == 1) ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+        double v = L.ic[k];
+        if (L.mutateState) {
+            if (k == L.mut[0]) v = va;
+            if (k == L.mut[1]) v = vb;
+        }
+        x[k] = (T)v;
+    }
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
         double v = L.values[k];
-        if (k == L.mut[0]) v = va;
-        if (k == L.mut[1]) v = vb;
+        if (!L.mutateState) {
+            if (k == L.mut[0]) v = va;
+            if (k == L.mut[1]) v = vb;
+        }
         a[k] = (T)v;
     }
+}
+
+template <int S, class T>
+__device__ __forceinline__ double lle_point_full(const LleParams& L, long long p) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    T x[NX], q[NX], a[NA];
+    lle_load<NX, NA>(L, p, x, a);
     const StepCtx<T> c((T)L.h);
     for (int s = 0; s < L.trans; ++s) step<S>(x, a, c);
 #pragma unroll
@@ -417,19 +435,8 @@ __device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>
 template <class F>
 __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p) {
     using T = float;
-    const int i = (int)(p % L.nPts), j = (int)(p / L.nPts);
     T x[3], e[3], a[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) x[k] = (T)L.ic[k];
-    const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
-    const double vb = L.nPts == 1 ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double v = L.values[k];
-        if (k == L.mut[0]) v = va;
-        if (k == L.mut[1]) v = vb;
-        a[k] = (T)v;
-    }
+    lle_load<3, 3>(L, p, x, a);
     const RK4H<T> c((T)L.h);
     for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
     const T eps = (T)L.eps;
@@ -454,6 +461,123 @@ __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p
         sum += (double)part;
     }
     return sum * (0.5 * 0.69314718055994530942) / L.tMax;  // log2(d^2) -> ln(d)
+}
+
+// ---------------------------------------------------------------------------
+// Lyapunov spectrum of one point: one twin per state dimension, started along
+// the unit vectors (x + eps e_j), integrated NT at a time beside the base
+// trajectory; after every block the differences y_j - x are orthogonalised by
+// classical Gram-Schmidt (b_j = d_j - sum_{m<j} (d_j.b_m / b_m.b_m) b_m), each
+// norm |b_j| adds log(|b_j| / eps) to exponent j and the twins restart at
+// x + eps b_j/|b_j| -- the scheme of the legacy library's spectrum kernel
+// (debri/cudaLibrary.cu:2141-2330). Blocks and the division by tMax are the
+// LLE map's (calcBlocks + 1 blocks), so exponent 0 estimates the same
+// quantity as lle_point_full. out[p*NX + j] = exponent j.
+template <int S>
+__device__ __forceinline__ void spectrum_point_full(const LleParams& L, long long p, double* out) {
+    constexpr int N = Traits<S>::NX, NA = Traits<S>::NA;
+    double x[N], y[N][N], a[NA], sum[N];
+    lle_load<N, NA>(L, p, x, a);
+    const StepCtx<double> c(L.h);
+    for (int s = 0; s < L.trans; ++s) step<S>(x, a, c);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        sum[j] = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) y[j][i] = i == j ? x[i] + L.eps : x[i];
+    }
+    for (int b = 0; b <= L.calcBlocks; ++b) {
+        for (int s = 0; s < L.ntp; ++s) step<S>(x, a, c);
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+            for (int s = 0; s < L.ntp; ++s) step<S>(y[j], a, c);
+        double d[N][N], g[N][N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                d[j][i] = y[j][i] - x[i];
+                g[j][i] = d[j][i];
+            }
+#pragma unroll
+            for (int m = 0; m < j; ++m) {
+                double num = 0.0, den = 0.0;
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    num = num + d[j][i] * g[m][i];
+                    den = den + g[m][i] * g[m][i];
+                }
+                const double frac = den == 0.0 ? 0.0 : num / den;
+#pragma unroll
+                for (int i = 0; i < N; ++i) g[j][i] = g[j][i] - frac * g[m][i];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            double n2 = 0.0;
+#pragma unroll
+            for (int i = 0; i < N; ++i) n2 = n2 + g[j][i] * g[j][i];
+            const double nrm = sqrt(n2);
+            sum[j] = sum[j] + log(nrm / L.eps);
+#pragma unroll
+            for (int i = 0; i < N; ++i) y[j][i] = x[i] + (nrm == 0.0 ? 0.0 : g[j][i] / nrm) * L.eps;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) out[p * N + j] = sum[j] / L.tMax;
+}
+
+// The spectrum in FP32 for the quadratic RK4 systems: the twins carried as
+// exact differences e_j (rk4_step_multi), Gram-Schmidt in FP32, per block
+// log2(|b_j|^2/eps^2) on the SFU summed in FP32 groups of kLleGroup blocks
+// and added into FP64, as the FP32 LLE map does.
+template <class F>
+__device__ __forceinline__ void spectrum_point_twin(const LleParams& L, long long p, double* out) {
+    float x[3], a[3], e[3][3];
+    lle_load<3, 3>(L, p, x, a);
+    const RK4H<float> c((float)L.h);
+    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
+    const float eps = (float)L.eps;
+    const float inv_eps2 = (float)(1.0 / (L.eps * L.eps));
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) e[j][i] = i == j ? eps : 0.f;
+    double sum[3] = {0.0, 0.0, 0.0};
+    const int nb = L.calcBlocks + 1;
+    for (int b0 = 0; b0 < nb; b0 += kLleGroup) {
+        const int bn = min(kLleGroup, nb - b0);
+        float part[3] = {0.f, 0.f, 0.f};
+        for (int b = 0; b < bn; ++b) {
+            for (int s = 0; s < L.ntp; ++s) rk4_step_multi<F, 3>(x, e, a, c);
+            float g[3][3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) g[j][i] = e[j][i];
+#pragma unroll
+                for (int m = 0; m < j; ++m) {
+                    const float num = fmaf(e[j][0], g[m][0], fmaf(e[j][1], g[m][1], e[j][2] * g[m][2]));
+                    const float den = fmaf(g[m][0], g[m][0], fmaf(g[m][1], g[m][1], g[m][2] * g[m][2]));
+                    const float frac = den == 0.f ? 0.f : num / den;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) g[j][i] = fmaf(-frac, g[m][i], g[j][i]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float n2 = fmaf(g[j][0], g[j][0], fmaf(g[j][1], g[j][1], g[j][2] * g[j][2]));
+                part[j] += __log2f(n2 * inv_eps2);
+                const float r = n2 > 0.f ? eps * rsqrtf(n2) : 0.f;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) e[j][i] = g[j][i] * r;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) sum[j] += (double)part[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) out[p * 3 + j] = sum[j] * (0.5 * 0.69314718055994530942) / L.tMax;
 }
 
 // ---------------------------------------------------------------------------
@@ -491,25 +615,13 @@ template <class F>
 __device__ __forceinline__ void lle_pair_twin(const LleParams& L, long long p, long long q, double* outp,
                                               double* outq) {
     P2 x[3], e[3], a[3];
-    long long pts[2] = {p, q};
-    float av[2][3];
-#pragma unroll
-    for (int t = 0; t < 2; ++t) {
-        const int i = (int)(pts[t] % L.nPts), j = (int)(pts[t] / L.nPts);
-        const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
-        const double vb = L.nPts == 1 ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            double v = L.values[k];
-            if (k == L.mut[0]) v = va;
-            if (k == L.mut[1]) v = vb;
-            av[t][k] = (float)v;
-        }
-    }
+    float xs[2][3], as[2][3];
+    lle_load<3, 3>(L, p, xs[0], as[0]);
+    lle_load<3, 3>(L, q, xs[1], as[1]);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        a[k] = P2(av[0][k], av[1][k]);
-        x[k] = P2((double)(float)L.ic[k]);
+        a[k] = P2(as[0][k], as[1][k]);
+        x[k] = P2(xs[0][k], xs[1][k]);
     }
     const RK4H<P2> c((float)L.h);
     for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);

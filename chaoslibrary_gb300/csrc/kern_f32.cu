@@ -53,6 +53,13 @@ __global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0
     trajectory_point<S, float>(x0, a0, h, nSteps, out, t);
 }
 
+template <class F>
+__global__ void __launch_bounds__(kBlock) spectrum_kernel_f32(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    spectrum_point_twin<F>(L, L.pBegin + o, out);
+}
+
 // Bifurcation / basins, two points per thread in packed FP32x2 lanes (RK4 systems).
 template <class F>
 __global__ void __launch_bounds__(kMaxBlock) bif_pair_kernel_f32(SweepParams P, BifOut O) {
@@ -278,6 +285,19 @@ cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
         case SYS_CHEN_RK4: launch_twin<Chen>(L, out, st, minb, block); break;
         default: return cudaErrorNotSupported;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectrum_f32(const LleParams& L, double* out, cudaStream_t st) {
+    if (L.nPoints <= 0) return cudaSuccess;
+    const unsigned g = grid_for(L.nPoints);
+    switch (L.system) {
+        case SYS_LORENZ_RK4: spectrum_kernel_f32<Lorenz><<<g, kBlock, 0, st>>>(L, out); break;
+        case SYS_ROSSLER_RK4: spectrum_kernel_f32<Rossler><<<g, kBlock, 0, st>>>(L, out); break;
+        case SYS_CHEN_RK4: spectrum_kernel_f32<Chen><<<g, kBlock, 0, st>>>(L, out); break;
+        default: return cudaErrorNotSupported;
+    }
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -42,6 +42,14 @@ __global__ void __launch_bounds__(kBlock) lle_kernel(LleParams L, double* out) {
     out[o] = lle_point_full<S, double>(L, L.pBegin + o);
 }
 
+// Lyapunov spectrum, out[p*SIZE_X + j]
+template <int S>
+__global__ void __launch_bounds__(kBlock) spectrum_kernel(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    spectrum_point_full<S>(L, L.pBegin + o, out);
+}
+
 // FP64 LLE of the points list[0, *count): out[k] (scatter = 0) or out[list[k]]
 // (scatter = 1). The same device function as lle_kernel, so a point's value
 // is the FP64 map's value bit for bit.
@@ -235,6 +243,14 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
 #define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
+    CHAOS_SYSTEM_SWITCH(L.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectrum_f64(const LleParams& L, double* out, cudaStream_t st) {
+    if (L.nPoints <= 0) return cudaSuccess;
+#define CALL(S) (spectrum_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
     return cudaGetLastError();

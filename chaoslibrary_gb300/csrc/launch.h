@@ -78,6 +78,8 @@ struct LleParams {
     double stepA, stepB;  // linspace steps (end - start) / (nPts - 1)
     long long pBegin, nPoints;
     int twin;  // twin start: 0 x + eps e_x; 1 the reference's, every component rounded to float (FP64 only)
+    int dim;          // 1: point p = index i of rangeA; 2: p = j*nPts + i (the LLE2D map)
+    int mutateState;  // 0: the grid sets values[mut]; 1: it sets initial conditions ic[mut]
 };
 
 // precision-specific launchers (kern_f64.cu / kern_f32.cu)
@@ -87,6 +89,9 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
+// Lyapunov spectrum, out[p*SIZE_X + j] (FP64: every built-in system; FP32: the RK4 systems)
+cudaError_t launch_spectrum_f64(const LleParams& L, double* out, cudaStream_t st);
+cudaError_t launch_spectrum_f32(const LleParams& L, double* out, cudaStream_t st);
 // bifurcation points of a list (row k for list[k]); points whose kept-peak
 // count exceeds cap (kern_f64.cu / kern_f32.cu)
 cudaError_t launch_bif_list_f64(const SweepParams& P, const BifOut& O, const int* list, int count, cudaStream_t st);

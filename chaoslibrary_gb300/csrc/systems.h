@@ -198,6 +198,62 @@ CHAOS_UNROLL
     }
 }
 
+// The same step for NE twins at once, p_q = x + e[q]: the base stages are
+// evaluated once and each twin adds only its difference stages (the
+// Lyapunov spectrum carries one twin per state dimension).
+template <class F, int NE, class T>
+CHAOS_HD void rk4_step_multi(T* x, T (*e)[3], const T* a, const RK4H<T>& c) {
+    T k[3], y[3], acc[3], d[NE][3], g[NE][3], dacc[NE][3];
+    F::f(x, a, k);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) F::df(x, e[q], a, d[q]);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        acc[i] = k[i];
+        y[i] = fmaT(c.hh, k[i], x[i]);
+CHAOS_UNROLL
+        for (int q = 0; q < NE; ++q) {
+            dacc[q][i] = d[q][i];
+            g[q][i] = fmaT(c.hh, d[q][i], e[q][i]);
+        }
+    }
+    F::f(y, a, k);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) F::df(y, g[q], a, d[q]);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        acc[i] = fmaT(T(2), k[i], acc[i]);
+        y[i] = fmaT(c.hh, k[i], x[i]);
+CHAOS_UNROLL
+        for (int q = 0; q < NE; ++q) {
+            dacc[q][i] = fmaT(T(2), d[q][i], dacc[q][i]);
+            g[q][i] = fmaT(c.hh, d[q][i], e[q][i]);
+        }
+    }
+    F::f(y, a, k);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) F::df(y, g[q], a, d[q]);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        acc[i] = fmaT(T(2), k[i], acc[i]);
+        y[i] = fmaT(c.h, k[i], x[i]);
+CHAOS_UNROLL
+        for (int q = 0; q < NE; ++q) {
+            dacc[q][i] = fmaT(T(2), d[q][i], dacc[q][i]);
+            g[q][i] = fmaT(c.h, d[q][i], e[q][i]);
+        }
+    }
+    F::f(y, a, k);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) F::df(y, g[q], a, d[q]);
+CHAOS_UNROLL
+    for (int i = 0; i < 3; ++i) {
+        x[i] = fmaT(c.h6, acc[i] + k[i], x[i]);
+CHAOS_UNROLL
+        for (int q = 0; q < NE; ++q) e[q][i] = fmaT(c.h6, dacc[q][i] + d[q][i], e[q][i]);
+    }
+}
+
 // ---- the reference's own plug-in systems, restated --------------------------
 // Chameleon, semi-implicit two-stage composition (systems/systems.cuh:11-39).
 template <class T> CHAOS_HD void chameleon_step(T* X, const T* a, T h) {

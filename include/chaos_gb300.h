@@ -129,6 +129,35 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
                 const double* values, int amountOfValues, double* lle);
 
 /*
+ * LLE over a 1-D or 2-D grid of parameters (mutateState 0) or of initial
+ * conditions (mutateState 1): the legacy library's LLE1D, LLE1DIC, LLE2D and
+ * LLE2DIC analyses (debri/hostLibrary.cu:3111-3828) with the Benettin scheme
+ * of chaos_lle2d (twin at x + eps*e_x, calcBlocks + 1 blocks, sum / tMax).
+ * dim 1: ranges[0..1] and indicesOfMutVars[0], lle[i] for i < nPts; dim 2:
+ * ranges[0..3], indicesOfMutVars[0..1], lle[j*nPts + i] as chaos_lle2d (which
+ * is this call with dim 2, mutateState 0). CHAOS_FP32 for the RK4 systems.
+ */
+int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT, int nPts,
+                    double h, double eps, const double* initialConditions, int amountOfInitialConditions,
+                    const double* ranges, const int* indicesOfMutVars, double transientTime, const double* values,
+                    int amountOfValues, double* lle);
+
+/*
+ * Lyapunov spectrum over the same grids (the legacy library's LS1D / LS2D,
+ * debri/hostLibrary.cu:3829-4111, kernel debri/cudaLibrary.cu:2141-2330):
+ * one twin per state dimension started along the unit vectors, classical
+ * Gram-Schmidt of the twin differences after every block of NT, exponent j =
+ * sum of log(|b_j| / eps) / tMax over calcBlocks + 1 blocks (the LLE map's
+ * count; exponent 0 estimates what chaos_lle_sweep estimates).
+ * spectrum[p*SIZE_X + j], p as in chaos_lle_sweep. Built-in systems; FP32
+ * for the RK4 systems (exact-difference twins).
+ */
+int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT,
+                            int nPts, double h, double eps, const double* initialConditions,
+                            int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                            double transientTime, const double* values, int amountOfValues, double* spectrum);
+
+/*
  * LLE map in FP32 with an FP64 sign re-check (no reference counterpart: the
  * reference computes in FP64 only). Arguments as chaos_lle2d (RK4 systems
  * 0-2; ex->precision is ignored). The map is computed as chaos_lle2d with

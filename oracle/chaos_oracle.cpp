@@ -354,6 +354,118 @@ int orc_lle2d(int sys, double tMax, double NT, int nPts, double h, double eps, c
     return 0;
 }
 
+// Grid point p of an LLE-type sweep (1-D: p = i; 2-D: p = j*nPts + i) over
+// parameters (mutateState 0) or initial conditions (1); dimension 1 last.
+static void lle_grid_point(int dim, int mutateState, long long p, int nPts, const double* ranges, const int* mut,
+                           double* x, double* a) {
+    const int i = dim == 1 ? (int)p : (int)(p % nPts), j = dim == 1 ? 0 : (int)(p / nPts);
+    double* tgt = mutateState ? x : a;
+    tgt[mut[0]] = linspace_value(i, nPts, ranges[0], ranges[1]);
+    if (dim == 2) tgt[mut[1]] = linspace_value(j, nPts, ranges[2], ranges[3]);
+}
+
+// LLE over 1-D / 2-D grids of parameters or initial conditions: the scheme
+// of orc_lle2d (which is dim 2, mutateState 0) at every grid point.
+int orc_lle_sweep(int sys, int dim, int mutateState, double tMax, double NT, int nPts, double h, double eps,
+                  const double* ic, const double* ranges, const int* mut, double transientTime,
+                  const double* values, long long pBegin, long long pEnd, double* out, int nthreads) {
+    const int ntp = (int)(NT / h);
+    const int trans = (int)(transientTime / h);
+    const int all = (int)(tMax / h);
+    if (ntp <= 0 || (dim != 1 && dim != 2)) return 1;
+    const int calcBlocks = all / ntp + 1;
+    const int nx = chaos::system_nx(sys), na = chaos::system_na(sys);
+    const long long total = dim == 2 ? (long long)nPts * nPts : nPts;
+    if (pEnd < 0 || pEnd > total) pEnd = total;
+    set_threads(nthreads);
+    const StepCtx<double> c(h);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long p = pBegin; p < pEnd; ++p) {
+        double x[kMaxX], q[kMaxX], a[32];
+        for (int k = 0; k < nx; ++k) x[k] = ic[k];
+        for (int k = 0; k < na; ++k) a[k] = values[k];
+        lle_grid_point(dim, mutateState, p, nPts, ranges, mut, x, a);
+        for (int s = 0; s < trans; ++s) chaos::step_dyn(sys, x, a, c);
+        for (int k = 0; k < nx; ++k) q[k] = x[k];
+        q[0] = x[0] + eps;
+        double sum = 0.0;
+        for (int b = 0; b <= calcBlocks; ++b) {
+            for (int s = 0; s < ntp; ++s) chaos::step_dyn(sys, x, a, c);
+            for (int s = 0; s < ntp; ++s) chaos::step_dyn(sys, q, a, c);
+            double dist = 0.0;
+            for (int k = 0; k < nx; ++k) { double df = x[k] - q[k]; dist += df * df; }
+            dist = std::sqrt(dist) / eps;
+            sum += std::log(dist);
+            for (int k = 0; k < nx; ++k) q[k] = x[k] - ((x[k] - q[k]) / dist);
+        }
+        out[p - pBegin] = sum / tMax;
+    }
+    return 0;
+}
+
+// Lyapunov spectrum (the legacy library's LSKernelCUDA scheme,
+// debri/cudaLibrary.cu:2141-2330, with the LLE map's block count): one twin
+// per dimension from x + eps e_j; after every block of NT steps the twin
+// differences go through classical Gram-Schmidt, exponent j adds
+// log(|b_j| / eps) and twin j restarts at x + eps b_j/|b_j|.
+// out[(p - pBegin)*nx + j].
+int orc_lyapunov_spectrum(int sys, int dim, int mutateState, double tMax, double NT, int nPts, double h,
+                          double eps, const double* ic, const double* ranges, const int* mut, double transientTime,
+                          const double* values, long long pBegin, long long pEnd, double* out, int nthreads) {
+    const int ntp = (int)(NT / h);
+    const int trans = (int)(transientTime / h);
+    const int all = (int)(tMax / h);
+    if (ntp <= 0 || (dim != 1 && dim != 2)) return 1;
+    const int calcBlocks = all / ntp + 1;
+    const int nx = chaos::system_nx(sys), na = chaos::system_na(sys);
+    const long long total = dim == 2 ? (long long)nPts * nPts : nPts;
+    if (pEnd < 0 || pEnd > total) pEnd = total;
+    set_threads(nthreads);
+    const StepCtx<double> c(h);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long p = pBegin; p < pEnd; ++p) {
+        double x[kMaxX], y[kMaxX][kMaxX], a[32], sum[kMaxX];
+        for (int k = 0; k < nx; ++k) x[k] = ic[k];
+        for (int k = 0; k < na; ++k) a[k] = values[k];
+        lle_grid_point(dim, mutateState, p, nPts, ranges, mut, x, a);
+        for (int s = 0; s < trans; ++s) chaos::step_dyn(sys, x, a, c);
+        for (int j = 0; j < nx; ++j) {
+            sum[j] = 0.0;
+            for (int i = 0; i < nx; ++i) y[j][i] = i == j ? x[i] + eps : x[i];
+        }
+        for (int b = 0; b <= calcBlocks; ++b) {
+            for (int s = 0; s < ntp; ++s) chaos::step_dyn(sys, x, a, c);
+            for (int j = 0; j < nx; ++j)
+                for (int s = 0; s < ntp; ++s) chaos::step_dyn(sys, y[j], a, c);
+            double d[kMaxX][kMaxX], g[kMaxX][kMaxX];
+            for (int j = 0; j < nx; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    d[j][i] = y[j][i] - x[i];
+                    g[j][i] = d[j][i];
+                }
+                for (int m = 0; m < j; ++m) {
+                    double num = 0.0, den = 0.0;
+                    for (int i = 0; i < nx; ++i) {
+                        num += d[j][i] * g[m][i];
+                        den += g[m][i] * g[m][i];
+                    }
+                    const double frac = den == 0.0 ? 0.0 : num / den;
+                    for (int i = 0; i < nx; ++i) g[j][i] -= frac * g[m][i];
+                }
+            }
+            for (int j = 0; j < nx; ++j) {
+                double n2 = 0.0;
+                for (int i = 0; i < nx; ++i) n2 += g[j][i] * g[j][i];
+                const double nrm = std::sqrt(n2);
+                sum[j] += std::log(nrm / eps);
+                for (int i = 0; i < nx; ++i) y[j][i] = x[i] + (nrm == 0.0 ? 0.0 : g[j][i] / nrm) * eps;
+            }
+        }
+        for (int j = 0; j < nx; ++j) out[(p - pBegin) * nx + j] = sum[j] / tMax;
+    }
+    return 0;
+}
+
 // Basins features over the nPts^2 grid of initial conditions
 // (Basins/src/basinsCUDA.cu:233-314 + 818-864): flags, avgPeaks, avgIntervals
 // (the reference's sentinels: flag 0 -> 999/999, flag -1 -> last sample/-1,

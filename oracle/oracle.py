@@ -53,6 +53,10 @@ def lib() -> C.CDLL:
                                       C.c_longlong, _ip, _ip, _dp, _dp, _dp, C.c_void_p, C.c_int]
         L.orc_lle2d.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, _dp, _dp, _ip,
                                 C.c_double, _dp, C.c_longlong, C.c_longlong, _dp, C.c_int]
+        for name in ("orc_lle_sweep", "orc_lyapunov_spectrum"):
+            getattr(L, name).argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
+                                         C.c_double, _dp, _dp, _ip, C.c_double, _dp, C.c_longlong, C.c_longlong,
+                                         _dp, C.c_int]
         L.orc_basins_features.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
                                           C.c_double, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _ip,
                                           _dp, _dp, C.c_void_p, C.c_void_p, C.c_int]
@@ -135,6 +139,32 @@ def lle2d(system: int, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, v
     if rc:
         raise ValueError("bad LLE arguments")
     return out
+
+
+def lle_sweep(system: int, dim, mutateState, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values,
+              p_begin=0, p_end=-1, nthreads=0) -> np.ndarray:
+    total = nPts * nPts if dim == 2 else nPts
+    p_end = total if p_end < 0 else p_end
+    out = np.zeros(p_end - p_begin, np.float64)
+    rc = lib().orc_lle_sweep(system, dim, mutateState, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
+                             transientTime, _d(values), p_begin, p_end, out, nthreads)
+    if rc:
+        raise ValueError("bad LLE arguments")
+    return out
+
+
+def lyapunov_spectrum(system: int, dim, mutateState, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime,
+                      values, p_begin=0, p_end=-1, nthreads=0) -> np.ndarray:
+    """[points, SIZE_X] exponents."""
+    total = nPts * nPts if dim == 2 else nPts
+    p_end = total if p_end < 0 else p_end
+    nx = len(ic)
+    out = np.zeros((p_end - p_begin) * nx, np.float64)
+    rc = lib().orc_lyapunov_spectrum(system, dim, mutateState, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
+                                     transientTime, _d(values), p_begin, p_end, out, nthreads)
+    if rc:
+        raise ValueError("bad spectrum arguments")
+    return out.reshape(-1, nx)
 
 
 def basins_features(system: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,

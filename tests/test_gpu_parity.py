@@ -665,3 +665,66 @@ def test_autotune_changes_no_result(engine):
     for k in ("flags", "avg_peaks", "avg_intervals"):
         assert np.array_equal(f0[k], f1[k]), k
     assert np.array_equal(l0, l1, equal_nan=True)
+
+
+LORENZ28 = dict(values=[10.0, 28.0, 8 / 3], initialConditions=[1.0, 1.0, 1.0])
+
+
+@pytest.mark.parametrize("dim, state", [(1, False), (1, True), (2, True)])
+def test_lle_sweep_fp64_vs_oracle(engine, oracle, dim, state):
+    """LLE over 1-D parameter grids and 1-D / 2-D grids of initial conditions
+    (the legacy LLE1D / LLE1DIC / LLE2DIC analyses) against the oracle."""
+    if state:
+        rng, mut = ([-10.0, 10.0, -10.0, 10.0][: 2 * dim], [0, 1][:dim])
+    else:
+        rng, mut = [20.0, 60.0], [1]
+    n = 9 if dim == 2 else 40
+    kw = dict(tMax=20.0, NT=0.1, nPts=n, h=0.01, eps=1e-8, ranges=rng, indicesOfMutVars=mut, transientTime=5.0,
+              **LORENZ28)
+    g = engine.lle_sweep("lorenz", dim, mutateState=state, **kw)
+    o = oracle.lle_sweep(0, dim, int(state), kw["tMax"], kw["NT"], n, kw["h"], kw["eps"], kw["initialConditions"],
+                         rng, mut, kw["transientTime"], kw["values"])
+    assert np.max(np.abs(g - o)) < 1e-12
+
+
+def test_lle_sweep_2d_params_is_lle2d(engine):
+    kw = dict(tMax=10.0, NT=0.1, nPts=12, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+              ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=2.0, values=[0.2, 0.2, 5.7])
+    for p in (engine.FP64, engine.FP32):
+        assert np.array_equal(engine.lle_sweep("rossler", 2, precision=p, **kw),
+                              engine.lle2d("rossler", precision=p, **kw), equal_nan=True)
+
+
+@pytest.mark.parametrize("system, sid, vals, ic", [("lorenz", 0, [10.0, 28.0, 8 / 3], [1.0, 1.0, 1.0]),
+                                                    ("rossler", 1, [0.2, 0.2, 5.7], [1.0, 1.0, 1.0]),
+                                                    ("chameleon", 3, [0.5, 3, 0, 2, 1, 18, 1], [3.0, 3.0, 0.0])])
+def test_spectrum_fp64_vs_oracle(engine, oracle, system, sid, vals, ic):
+    """Lyapunov spectrum (one twin per dimension, classical Gram-Schmidt per
+    block) against the oracle's restatement."""
+    k = 3 if sid == 3 else 0
+    rng, mut = [vals[k] * 0.9, vals[k] * 1.1], [k]
+    kw = dict(tMax=10.0, NT=0.1, nPts=16, h=0.01, eps=1e-8, ranges=rng, indicesOfMutVars=mut, transientTime=2.0)
+    g = engine.lyapunov_spectrum(system, 1, initialConditions=ic, values=vals, **kw)
+    o = oracle.lyapunov_spectrum(sid, 1, 0, kw["tMax"], kw["NT"], 16, kw["h"], kw["eps"], ic, rng, mut,
+                                 kw["transientTime"], vals)
+    fin = np.isfinite(o)
+    assert np.array_equal(fin, np.isfinite(g))
+    # cos: CUDA's libm and glibc may differ in the last bit, which the chaotic
+    # Chameleon flow amplifies over the 1,200 steps (measured 4e-7)
+    tol = 1e-12 if sid <= 2 else 1e-5
+    assert np.max(np.abs(g[fin] - o[fin])) < tol
+
+
+def test_spectrum_lorenz_physics_fp32_and_fp64(engine):
+    """Lorenz at rho = 28: exponents near (0.906, 0, -14.57) and their sum
+    near -(sigma + 1 + beta) times the blocks' span over tMax, in FP64 and in
+    the FP32 exact-difference path."""
+    kw = dict(tMax=200.0, NT=0.1, nPts=4, h=0.01, eps=1e-8, ranges=[28.0, 28.0], indicesOfMutVars=[1],
+              transientTime=20.0, **LORENZ28)
+    span = (int(round(kw["tMax"] / kw["h"])) // 10 + 2) * kw["NT"] / kw["tMax"]
+    for p in (engine.FP64, engine.FP32):
+        s = engine.lyapunov_spectrum("lorenz", 1, precision=p, **kw)
+        assert np.all(np.abs(s[:, 0] - 0.906) < 0.1), s
+        assert np.all(np.abs(s[:, 1]) < 0.05), s
+        assert np.all(np.abs(s[:, 2] + 14.57) < 0.15), s
+        assert np.all(np.abs(s.sum(axis=1) + (10 + 1 + 8 / 3) * span) < 0.02), s
