@@ -33,6 +33,12 @@ from ._native import (  # noqa: F401
     bifurcation1d,
     bifurcation2D,
     bifurcation2d,
+    bifurcation_sweep,
+    GRID_STATE,
+    GRID_LOG0,
+    GRID_LOG1,
+    GRID_LOG_F32,
+    MUT_STEP,
     dbscan,
     dbscan_compat,
     fma_probe,
@@ -52,6 +58,7 @@ from ._native import (  # noqa: F401
     lib,
     lib_path,
     lle2d,
+    old_library,
     peak_finder,
     point_dbscan,
     set_precision,
@@ -62,6 +69,7 @@ from ._native import (  # noqa: F401
 
 __all__ = [
     "Server", "Batch", "FP32", "FP64", "SYSTEMS", "ChaosError", "bifurcation1D", "bifurcation2D", "LLE2D", "basinsOfAttraction_2",
-    "Bifurcation", "LLE", "Basins", "bifurcation1d", "bifurcation2d", "lle2d", "basins", "basins_dbscan", "basins_features",
+    "Bifurcation", "LLE", "Basins", "bifurcation1d", "bifurcation2d", "bifurcation_sweep", "GRID_STATE",
+    "GRID_LOG0", "GRID_LOG1", "GRID_LOG_F32", "MUT_STEP", "lle2d", "old_library", "basins", "basins_dbscan", "basins_features",
     "dbscan", "dbscan_compat", "fma_probe", "autotune", "launch_count", "lle2d_checked", "lle_sweep", "lyapunov_spectrum", "trajectory", "get_tuning", "set_tuning", "TUNE_LLE_F32_VARIANT", "TUNE_SWEEP_PAIRS", "TUNE_GRID_FMA", "TUNE_LLE_TWIN", "TUNE_BIF2D_CAP", "TUNE_SHAPES", "peak_finder", "point_dbscan", "lib", "lib_path", "set_system", "set_precision", "system_info",
 ]

@@ -61,6 +61,8 @@ _SIGS = {
     "chaos_bifurcation1d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _P], _I),
     "chaos_bifurcation2d": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _P, _P], _I),
     "chaos_lle2d": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, _P], _I),
+    "chaos_bifurcation_sweep": ([_P, _I, _I, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _I, _P, _P, _P,
+                                 _P, _P, _P], _I),
     "chaos_lle_sweep": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lyapunov_spectrum": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
@@ -95,6 +97,15 @@ _SIGS = {
     "chaos_compat_bifurcation2D": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, C.c_char_p], _I),
     "chaos_compat_LLE2D": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
     "chaos_compat_basinsOfAttraction_2": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, C.c_char_p], _I),
+    "chaos_compat_bifurcation1DIC": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, C.c_char_p], _I),
+    "chaos_compat_bifurcation2DIC": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, C.c_char_p], _I),
+    "chaos_compat_bifurcation1DForH": ([_D, _I, _I, _P, _P, _I, _D, _D, _P, _I, _I, C.c_char_p], _I),
+    "chaos_compat_LLE1D": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
+    "chaos_compat_LLE1DIC": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
+    "chaos_compat_LLE2DIC": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
+    "chaos_compat_LS1D": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
+    "chaos_compat_LS2D": ([_D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, C.c_char_p], _I),
+    "chaos_compat_basinsOfAttraction": ([_D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, C.c_char_p], _I),
 }
 
 
@@ -215,6 +226,10 @@ def trajectory(system, x0, a, h, n_steps, precision=FP64):
     _check(lib().chaos_trajectory(C.byref(ex), _sys(system), n, A.d(x0), A.d(a), h, n_steps, _out_ptr(out)))
     return out
 
+
+# grid modes (CHAOS_GRID_*) and the step-size axis marker (CHAOS_MUT_STEP)
+GRID_STATE, GRID_LOG0, GRID_LOG1, GRID_LOG_F32 = 1, 2, 4, 8
+MUT_STEP = -1
 
 TUNE_LLE_F32_VARIANT = 1
 TUNE_SWEEP_PAIRS = 2
@@ -473,6 +488,41 @@ def bifurcation2d(system, tMax, nPts, h, initialConditions, ranges, indicesOfMut
     return out
 
 
+def bifurcation_sweep(system, dim, gridMode, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars,
+                      writableVar, maxValue, transientTime, values, preScaller=1, eps=0.001, peakCapacity=None,
+                      precision=FP64, out=None, stream=None):
+    """Bifurcation over parameters or initial conditions (GRID_STATE), linear
+    or log-scale axes, or the step size (indicesOfMutVars[0] = MUT_STEP, dim 1)
+    (chaos_bifurcation_sweep). dim 1: counts, flags, first, peaks, intervals;
+    dim 2: labels, counts."""
+    A = _Args()
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    n = nPts ** dim
+    if dim == 1:
+        h_min = min(ranges[0], ranges[1]) * (1.0 - 1e-9) if indicesOfMutVars[0] == MUT_STEP else h
+        B = int(tMax / h_min / preScaller) if h_min > 0 and preScaller > 0 else 1
+        cap = int(peakCapacity or max(B // 2, 1))
+        if out is None:
+            out = dict(counts=np.zeros(n, np.int32), flags=np.zeros(n, np.int32), first=np.zeros(n),
+                       peaks=np.zeros((n, cap)), intervals=np.zeros((n, cap)))
+        ex = _exec(precision, out, stream)
+        _check(lib().chaos_bifurcation_sweep(
+            C.byref(ex), _sys(system), 1, gridMode, tMax, nPts, h, ic.size, A.d(ic), A.d(ranges),
+            A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size, preScaller, eps, cap,
+            _out_ptr(out["counts"]), _out_ptr(out["flags"]), _out_ptr(out.get("first")),
+            _out_ptr(out.get("peaks")), _out_ptr(out.get("intervals")), None))
+        return out
+    if out is None:
+        out = dict(labels=np.zeros(n, np.int32), counts=np.zeros(n, np.int32))
+    ex = _exec(precision, out, stream)
+    _check(lib().chaos_bifurcation_sweep(
+        C.byref(ex), _sys(system), 2, gridMode, tMax, nPts, h, ic.size, A.d(ic), A.d(ranges), A.i(indicesOfMutVars),
+        writableVar, maxValue, transientTime, A.d(vals), vals.size, preScaller, eps, 0, _out_ptr(out.get("counts")),
+        None, None, None, None, _out_ptr(out["labels"])))
+    return out
+
+
 def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime, values,
           writableVar=0, maxValue=0.0, precision=FP64, out=None, stream=None):
     """LLE map; result[j*nPts + i] (row = second parameter), as the reference CSV."""
@@ -489,9 +539,10 @@ def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMu
 
 
 def lle_sweep(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime,
-              values, mutateState=False, precision=FP64, out=None, stream=None):
+              values, mutateState=False, precision=FP64, out=None, stream=None, gridMode=0):
     """LLE over a 1-D (lle[i]) or 2-D (lle[j*nPts + i]) grid of parameters or,
-    with mutateState, of initial conditions (chaos_lle_sweep)."""
+    with mutateState, of initial conditions; gridMode adds log-scale axes
+    (GRID_LOG0 / LOG1 / LOG_F32) (chaos_lle_sweep)."""
     A = _Args()
     n = nPts ** dim
     if out is None:
@@ -499,14 +550,15 @@ def lle_sweep(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, in
     ex = _exec(precision, {"lle": out}, stream)
     ic = np.asarray(initialConditions, np.float64)
     vals = np.asarray(values, np.float64)
-    _check(lib().chaos_lle_sweep(C.byref(ex), _sys(system), dim, 1 if mutateState else 0, tMax, NT, nPts, h, eps,
+    mode = gridMode | (GRID_STATE if mutateState else 0)
+    _check(lib().chaos_lle_sweep(C.byref(ex), _sys(system), dim, mode, tMax, NT, nPts, h, eps,
                                  A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), transientTime, A.d(vals),
                                  vals.size, _out_ptr(out)))
     return out
 
 
 def lyapunov_spectrum(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
-                      transientTime, values, mutateState=False, precision=FP64, out=None, stream=None):
+                      transientTime, values, mutateState=False, precision=FP64, out=None, stream=None, gridMode=0):
     """Lyapunov spectrum [points, SIZE_X] over the grids of lle_sweep
     (chaos_lyapunov_spectrum)."""
     A = _Args()
@@ -516,7 +568,8 @@ def lyapunov_spectrum(system, dim, tMax, NT, nPts, h, eps, initialConditions, ra
         out = np.zeros((n, ic.size))
     ex = _exec(precision, {"spectrum": out}, stream)
     vals = np.asarray(values, np.float64)
-    _check(lib().chaos_lyapunov_spectrum(C.byref(ex), _sys(system), dim, 1 if mutateState else 0, tMax, NT, nPts, h,
+    mode = gridMode | (GRID_STATE if mutateState else 0)
+    _check(lib().chaos_lyapunov_spectrum(C.byref(ex), _sys(system), dim, mode, tMax, NT, nPts, h,
                                          eps, A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), transientTime,
                                          A.d(vals), vals.size, _out_ptr(out)))
     return out
@@ -695,3 +748,49 @@ def basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, initialCondit
 Bifurcation = SimpleNamespace(bifurcation1D=bifurcation1D, bifurcation2D=bifurcation2D)
 LLE = SimpleNamespace(LLE2D=LLE2D)
 Basins = SimpleNamespace(basinsOfAttraction_2=basinsOfAttraction_2)
+
+
+# ---- the legacy library's analyses (old_library::..., CSV files) -----------------
+
+def _legacy_bif(name, with_eps):
+    def call(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars, writableVar,
+             maxValue, transientTime, values, amountOfValues, preScaller, *rest):
+        A = _Args()
+        tail = (rest[0], str(rest[1]).encode()) if with_eps else (str(rest[0]).encode(),)
+        _check(getattr(lib(), name)(tMax, nPts, h, amountOfInitialConditions, A.d(initialConditions), A.d(ranges),
+                                    A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(values),
+                                    amountOfValues, preScaller, *tail))
+    call.__name__ = name.replace("chaos_compat_", "")
+    return call
+
+
+def _legacy_lle(name):
+    def call(tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges, indicesOfMutVars,
+             writableVar, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH):
+        A = _Args()
+        _check(getattr(lib(), name)(tMax, NT, nPts, h, eps, A.d(initialConditions), amountOfInitialConditions,
+                                    A.d(ranges), A.i(indicesOfMutVars), writableVar, maxValue, transientTime,
+                                    A.d(values), amountOfValues, str(OUT_FILE_PATH).encode()))
+    call.__name__ = name.replace("chaos_compat_", "")
+    return call
+
+
+def bifurcation1DForH(tMax, nPts, amountOfInitialConditions, initialConditions, ranges, writableVar, maxValue,
+                      transientTime, values, amountOfValues, preScaller, OUT_FILE_PATH):
+    A = _Args()
+    _check(lib().chaos_compat_bifurcation1DForH(tMax, nPts, amountOfInitialConditions, A.d(initialConditions),
+                                                A.d(ranges), writableVar, maxValue, transientTime, A.d(values),
+                                                amountOfValues, preScaller, str(OUT_FILE_PATH).encode()))
+
+
+old_library = SimpleNamespace(
+    bifurcation1DIC=_legacy_bif("chaos_compat_bifurcation1DIC", False),
+    bifurcation2DIC=_legacy_bif("chaos_compat_bifurcation2DIC", True),
+    bifurcation1DForH=bifurcation1DForH,
+    basinsOfAttraction=_legacy_bif("chaos_compat_basinsOfAttraction", True),
+    LLE1D=_legacy_lle("chaos_compat_LLE1D"),
+    LLE1DIC=_legacy_lle("chaos_compat_LLE1DIC"),
+    LLE2DIC=_legacy_lle("chaos_compat_LLE2DIC"),
+    LS1D=_legacy_lle("chaos_compat_LS1D"),
+    LS2D=_legacy_lle("chaos_compat_LS2D"),
+)

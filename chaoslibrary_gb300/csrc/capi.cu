@@ -221,18 +221,73 @@ static cudaError_t run_lle(int prec, const LleParams& L, double* out, cudaStream
     return prec == CHAOS_FP32 ? launch_lle_f32(L, out, st) : launch_lle_f64(L, out, st);
 }
 
+// Values of a log-scale axis: the legacy getValueByIdxLog exponent
+// log10(r0) + n*((log10(r1) - log10(r0)) / (nPts - 1)) (debri/cudaLibrary.cu:1191-1196),
+// then 10^x in FP64, or (double)powf(10, (float)x) as the legacy step-size
+// sweep rounds it (debri/cudaLibrary.cu:1001).
+void log_axis_values(double r0, double r1, int nPts, bool f32, std::vector<double>& out) {
+    out.resize(nPts);
+    const double l0 = std::log10(r0);
+    const double step = (std::log10(r1) - l0) / (double)(nPts - 1);
+    for (int n = 0; n < nPts; ++n) {
+        const double x = l0 + (double)n * step;
+        out[n] = f32 ? (double)powf(10.0f, (float)x) : std::pow(10.0, x);
+    }
+}
+
+// Checks a grid mode against the ranges: log-scale axes need positive ends and nPts >= 2.
+static int check_grid_mode(int gridMode, int dim, int nPts, const double* ranges) {
+    if (gridMode & ~(CHAOS_GRID_STATE | CHAOS_GRID_LOG0 | CHAOS_GRID_LOG1 | CHAOS_GRID_LOG_F32))
+        return set_error(CHAOS_E_ARGS, "unknown grid mode bits 0x%x", gridMode);
+    if ((gridMode & CHAOS_GRID_LOG1) && dim < 2) return set_error(CHAOS_E_ARGS, "CHAOS_GRID_LOG1 needs dim 2");
+    for (int d = 0; d < dim; ++d) {
+        if (!(gridMode & (d ? CHAOS_GRID_LOG1 : CHAOS_GRID_LOG0))) continue;
+        if (nPts < 2) return set_error(CHAOS_E_ARGS, "a log-scale axis needs nPts >= 2");
+        if (!(ranges[2 * d] > 0) || !(ranges[2 * d + 1] > 0) || std::isinf(ranges[2 * d]) ||
+            std::isinf(ranges[2 * d + 1]))
+            return set_error(CHAOS_E_ARGS, "a log-scale axis needs finite positive ranges");
+    }
+    return CHAOS_OK;
+}
+
+// Uploads the log-scale axes of a grid mode to scratch of the call; table[d]
+// receives the device array (untouched for linear axes).
+static int upload_log_axes(Call& c, int gridMode, int dim, int nPts, const double* ranges, const double** table) {
+    for (int d = 0; d < dim; ++d) {
+        if (!(gridMode & (d ? CHAOS_GRID_LOG1 : CHAOS_GRID_LOG0))) continue;
+        std::vector<double> v;
+        log_axis_values(ranges[2 * d], ranges[2 * d + 1], nPts, (gridMode & CHAOS_GRID_LOG_F32) != 0, v);
+        double* dv = (double*)c.alloc(v.size() * sizeof(double));
+        if (c.failed) return CHAOS_E_NOMEM;
+        cudaError_t e = cudaMemcpyAsync(dv, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        // (a copy from pageable memory has read v when it returns)
+        if (e != cudaSuccess) return cuda_error(e, "grid table upload");
+        table[d] = dv;
+    }
+    return CHAOS_OK;
+}
+
 int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, double h, int nIC, const double* ic,
                const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
-               const double* values, int nValues, int preScaller, bool basins) {
+               const double* values, int nValues, int preScaller, bool basins, int gridMode) {
     int rc = check_system(system, nIC, nValues);
     if (rc) return rc;
     if (!ic || !ranges || !mut || !values) return set_error(CHAOS_E_ARGS, "null parameter array");
+    const bool state = basins || (gridMode & CHAOS_GRID_STATE);
+    const bool stepAxis = (gridMode & kGridStepAxis) && mut[0] == CHAOS_MUT_STEP;
+    if (stepAxis) {  // the step sweeps dimension 0; the caller's h is not used
+        if (dim != 1 || basins) return set_error(CHAOS_E_ARGS, "the step-size sweep is a 1-D bifurcation");
+        if (!(ranges[0] > 0) || !(ranges[1] > 0) || std::isinf(ranges[0]) || std::isinf(ranges[1]))
+            return set_error(CHAOS_E_ARGS, "the step-size range must be finite and positive");
+        h = std::min(ranges[0], ranges[1]) * (1.0 - 1e-9);  // below every step on the axis: bounds the step counts
+    }
     if (!(h > 0) || !(tMax > 0) || !(transientTime >= 0)) return set_error(CHAOS_E_ARGS, "need h > 0, tMax > 0, transientTime >= 0");
     if (nPts < 2) return set_error(CHAOS_E_ARGS, "nPts must be >= 2");
     if (preScaller < 1) return set_error(CHAOS_E_ARGS, "preScaller must be >= 1");
     if (wv < 0 || wv >= nIC) return set_error(CHAOS_E_ARGS, "writableVar %d out of range", wv);
-    const int lim = basins ? nIC : nValues;
-    for (int d = 0; d < dim; ++d)
+    if ((rc = check_grid_mode(gridMode & ~kGridStepAxis, dim, nPts, ranges))) return rc;
+    const int lim = state ? nIC : nValues;
+    for (int d = stepAxis ? 1 : 0; d < dim; ++d)
         if (mut[d] < 0 || mut[d] >= lim) return set_error(CHAOS_E_ARGS, "indicesOfMutVars[%d] = %d out of range", d, mut[d]);
     const double Bd = tMax / h / preScaller, Sd = transientTime / h;
     if (!(Bd >= 1) || Bd > 2.0e9 || Sd > 2.0e9) return set_error(CHAOS_E_ARGS, "tMax/h/preScaller must be in [1, 2e9]");
@@ -244,7 +299,7 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     P.preScaller = basins ? preScaller : 1;
     P.wv = wv;
     P.checkMax = maxValue != 0;
-    P.mutateState = basins ? 1 : 0;
+    P.mutateState = state ? 1 : 0;
     P.h = h;
     P.hInterval = h * (double)preScaller;
     P.maxValue = maxValue;
@@ -280,13 +335,18 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     }
     P.pBegin = 0;
     P.nPoints = dim == 1 ? (long long)nPts : (long long)nPts * nPts;
+    P.sweepStep = stepAxis ? 1 : 0;
+    P.bPre = preScaller;
+    P.tMax = tMax;
+    P.transientTime = transientTime;
     return CHAOS_OK;
 }
 
 int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double h, double eps,
              const double* initialConditions, int amountOfInitialConditions, const double* ranges,
              const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues, int dim,
-             int mutateState) {
+             int gridMode) {
+    const int mutateState = gridMode & CHAOS_GRID_STATE;
     int rc = check_system(system, amountOfInitialConditions, amountOfValues);
     if (rc) return rc;
     if (!initialConditions || !ranges || !indicesOfMutVars || !values) return set_error(CHAOS_E_ARGS, "null argument");
@@ -294,6 +354,7 @@ int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double 
     if (!(h > 0) || !(tMax > 0) || !(NT > 0) || !(transientTime >= 0) || !(eps > 0))
         return set_error(CHAOS_E_ARGS, "need h, tMax, NT, eps > 0 and transientTime >= 0");
     if (dim != 1 && dim != 2) return set_error(CHAOS_E_ARGS, "dim must be 1 or 2");
+    if ((rc = check_grid_mode(gridMode, dim, nPts, ranges))) return rc;
     const int lim = mutateState ? amountOfInitialConditions : amountOfValues;
     for (int d = 0; d < dim; ++d)
         if (indicesOfMutVars[d] < 0 || indicesOfMutVars[d] >= lim)
@@ -371,21 +432,19 @@ int chaos_synchronize(const chaos_exec* ex) {
     return c.finish(rc);
 }
 
-int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
-                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
-                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
-                        const double* values, int amountOfValues, int preScaller, int peakCapacity, int* counts,
-                        int* flags, double* firstSample, double* peaks, double* intervals) {
-    SweepParams P;
-    int rc = fill_sweep(P, system, 1, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
-                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
-                        false);
-    if (rc) return rc;
+}  // extern "C"
+
+// The 1-D bifurcation of a filled parameter block (log-scale axes of gridMode
+// uploaded here).
+static int bif1d_run(const chaos_exec* ex, SweepParams P, int gridMode, const double* ranges, int peakCapacity,
+                     int* counts, int* flags, double* firstSample, double* peaks, double* intervals) {
+    int rc = CHAOS_OK;
     if (!counts || !flags) return set_error(CHAOS_E_ARGS, "counts and flags are required");
     if (peakCapacity < 0 || ((peaks || intervals) && peakCapacity == 0))
         return set_error(CHAOS_E_ARGS, "peakCapacity must be > 0 when peaks or intervals are requested");
     Call c;
     if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_log_axes(c, gridMode, P.dim, (int)P.grid.nPts, ranges, P.grid.table))) return c.finish(rc);
     const long long n = P.nPoints;
     const size_t rowBytes = (size_t)n * peakCapacity * sizeof(double);
     BifOut O;
@@ -406,19 +465,14 @@ int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts,
     return c.finish(rc);
 }
 
-int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
-                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
-                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
-                        const double* values, int amountOfValues, int preScaller, double eps, int* labels,
-                        int* counts) {
-    SweepParams P;
-    int rc = fill_sweep(P, system, 2, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
-                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
-                        false);
-    if (rc) return rc;
+// The 2-D bifurcation with per-point clustering of a filled parameter block.
+static int bif2d_run(const chaos_exec* ex, SweepParams P, int gridMode, const double* ranges, double eps,
+                     int* labels, int* counts) {
+    int rc = CHAOS_OK;
     if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
     Call c;
     if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_log_axes(c, gridMode, P.dim, (int)P.grid.nPts, ranges, P.grid.table))) return c.finish(rc);
     const long long n = P.nPoints;
     // every detected peak sits at least two samples after the previous one,
     // so B/2 rows hold all kept intervals of a point
@@ -509,6 +563,56 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
     return c.finish(rc);
 }
 
+extern "C" {
+
+int chaos_bifurcation1d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, int peakCapacity, int* counts,
+                        int* flags, double* firstSample, double* peaks, double* intervals) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 1, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        false);
+    if (rc) return rc;
+    return bif1d_run(ex, P, 0, ranges, peakCapacity, counts, flags, firstSample, peaks, intervals);
+}
+
+int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts, double h,
+                        int amountOfInitialConditions, const double* initialConditions, const double* ranges,
+                        const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
+                        const double* values, int amountOfValues, int preScaller, double eps, int* labels,
+                        int* counts) {
+    SweepParams P;
+    int rc = fill_sweep(P, system, 2, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        false);
+    if (rc) return rc;
+    return bif2d_run(ex, P, 0, ranges, eps, labels, counts);
+}
+
+int chaos_bifurcation_sweep(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, int nPts,
+                            double h, int amountOfInitialConditions, const double* initialConditions,
+                            const double* ranges, const int* indicesOfMutVars, int writableVar, double maxValue,
+                            double transientTime, const double* values, int amountOfValues, int preScaller,
+                            double eps, int peakCapacity, int* counts, int* flags, double* firstSample,
+                            double* peaks, double* intervals, int* labels) {
+    if (dim != 1 && dim != 2) return set_error(CHAOS_E_ARGS, "dim must be 1 or 2");
+    if (gridMode & kGridStepAxis) return set_error(CHAOS_E_ARGS, "unknown grid mode bits 0x%x", gridMode);
+    SweepParams P;
+    int rc = fill_sweep(P, system, dim, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        false, gridMode | kGridStepAxis);
+    if (rc) return rc;
+    if (dim == 1) {
+        if (labels) return set_error(CHAOS_E_ARGS, "labels belong to the 2-D sweep");
+        return bif1d_run(ex, P, gridMode, ranges, peakCapacity, counts, flags, firstSample, peaks, intervals);
+    }
+    if (flags || firstSample || peaks || intervals || peakCapacity)
+        return set_error(CHAOS_E_ARGS, "the 2-D sweep returns labels and counts only");
+    return bif2d_run(ex, P, gridMode, ranges, eps, labels, counts);
+}
+
 int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nPts, double h, double eps,
                 const double* initialConditions, int amountOfInitialConditions, const double* ranges,
                 const int* indicesOfMutVars, int writableVar, double maxValue, double transientTime,
@@ -535,7 +639,7 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     return c.finish(rc);
 }
 
-int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT, int nPts,
+int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT, int nPts,
                     double h, double eps, const double* initialConditions, int amountOfInitialConditions,
                     const double* ranges, const int* indicesOfMutVars, double transientTime, const double* values,
                     int amountOfValues, double* lle) {
@@ -543,7 +647,7 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, 
     if (!lle) return set_error(CHAOS_E_ARGS, "null argument");
     LleParams L;
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                       indicesOfMutVars, transientTime, values, amountOfValues, dim, mutateState)))
+                       indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
         return rc;
     if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_difference_form(system)))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
@@ -551,6 +655,7 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, 
         return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
     Call c;
     if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);
     double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e = run_lle(c.ex.precision, L, dOut, c.stream);
@@ -559,7 +664,7 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, 
     return c.finish(rc);
 }
 
-int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT,
+int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
                             int nPts, double h, double eps, const double* initialConditions,
                             int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                             double transientTime, const double* values, int amountOfValues, double* spectrum) {
@@ -568,13 +673,14 @@ int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int mutat
     if (system == SYS_USER) return set_error(CHAOS_E_UNSUPPORTED, "the spectrum runs on the built-in systems");
     LleParams L;
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                       indicesOfMutVars, transientTime, values, amountOfValues, dim, mutateState)))
+                       indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
         return rc;
     const bool fp32 = ex && ex->precision == CHAOS_FP32;
     if (fp32 && !system_has_difference_form(system))
         return set_error(CHAOS_E_UNSUPPORTED, "the FP32 spectrum needs a quadratic RK4 system (0-2); use CHAOS_FP64");
     Call c;
     if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);
     const size_t bytes = (size_t)L.nPoints * system_nx(system) * sizeof(double);
     double* dOut = (double*)c.output(spectrum, bytes);
     if (c.failed) return c.finish(CHAOS_E_NOMEM);

@@ -36,12 +36,17 @@ struct Call {
 int aux_streams(int device, std::vector<cudaStream_t>& out);
 
 // Argument checks + parameter blocks shared by the entry points (capi.cu).
+// gridMode: CHAOS_GRID_* bits; kGridStepAxis lets indicesOfMutVars[0] be
+// CHAOS_MUT_STEP (the step-size sweep of chaos_bifurcation_sweep).
+constexpr int kGridStepAxis = 1 << 16;
 int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, double h, int nIC, const double* ic,
                const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
-               const double* values, int nValues, int preScaller, bool basins);
+               const double* values, int nValues, int preScaller, bool basins, int gridMode = 0);
 int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double h, double eps,
              const double* initialConditions, int amountOfInitialConditions, const double* ranges,
              const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
-             int dim = 2, int mutateState = 0);
+             int dim = 2, int gridMode = 0);
+// Host values of a log-scale axis (the legacy getValueByIdxLog, then 10^x).
+void log_axis_values(double r0, double r1, int nPts, bool f32, std::vector<double>& out);
 
 }  // namespace chaos

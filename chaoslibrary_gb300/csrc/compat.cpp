@@ -4,6 +4,7 @@
 // (default for headers and LLE values, 12 for bifurcation rows, 15 for every
 // basins file), same ", " separators with the reference's line-break rule
 // (a row break is written as ", " then "\n"), NaN LLE values printed as 0.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -192,6 +193,221 @@ int chaos_compat_basinsOfAttraction_2(double tMax, int nPts, double h, int amoun
     return CHAOS_OK;
 }
 
+// ---- the legacy library's analyses (namespace old_library, debri/hostLibrary.cuh) ----
+// Each runs the engine's sweep with the matching grid mode and writes the
+// legacy function's file format.
+
+// Rows "value, peak" per kept peak, precision 12, no header: bifurcation1DIC
+// and bifurcation1DForH (debri/hostLibrary.cu:1447-1460, 1197-1210). The
+// step-size sweep labels its rows with the linear getValueByIdx of the range,
+// not the step it used, as the legacy writer does.
+static int legacy_bif1d(int gridMode, double tMax, int nPts, double h, int amountOfInitialConditions,
+                        const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                        int writableVar, double maxValue, double transientTime, const double* values,
+                        int amountOfValues, int preScaller, const char* OUT_FILE_PATH) {
+    if (nPts < 2 || preScaller < 1) return chaos::set_error(CHAOS_E_ARGS, "bad sweep arguments");
+    const bool stepAxis = indicesOfMutVars && indicesOfMutVars[0] == CHAOS_MUT_STEP;
+    const double hMin = stepAxis ? std::min(ranges[0], ranges[1]) * (1.0 - 1e-9) : h;
+    if (!(hMin > 0)) return chaos::set_error(CHAOS_E_ARGS, "need a positive step");
+    const int B = (int)(tMax / hMin / preScaller);
+    const int cap = B / 2 > 0 ? B / 2 : 1;
+    std::vector<int> counts(nPts), flags(nPts);
+    std::vector<double> peaks((size_t)nPts * cap);
+    chaos_exec ex = active_exec();
+    int rc = chaos_bifurcation_sweep(&ex, active_system(), 1, gridMode, tMax, nPts, h, amountOfInitialConditions,
+                                     initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                                     transientTime, values, amountOfValues, preScaller, 0.0, cap, counts.data(),
+                                     flags.data(), nullptr, peaks.data(), nullptr, nullptr);
+    if (rc) return rc;
+    std::ofstream o(OUT_FILE_PATH);
+    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+    o << std::setprecision(12);
+    for (int k = 0; k < nPts; ++k) {
+        const double p = host_grid_value(k, nPts, ranges[0], ranges[1]);
+        for (int j = 0; j < counts[k] && j < cap; ++j) o << p << ", " << peaks[(size_t)k * cap + j] << '\n';
+    }
+    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+}
+
+// The arithmetic of the LLE-type wrappers: FP32 only where the engine has it.
+static chaos_exec lle_exec() {
+    chaos_exec ex = active_exec();
+    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHEN_RK4) ex.precision = CHAOS_FP64;
+    return ex;
+}
+
+// LLE1D / LLE1DIC: rows "value, lle" at precision 12, no header
+// (debri/hostLibrary.cu:3291-3300, 3508-3517); LLE2DIC: the matrix rule at the
+// default precision, no header (debri/hostLibrary.cu:3793-3805).
+static int legacy_lle(int dim, int gridMode, double tMax, double NT, int nPts, double h, double eps,
+                      const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+                      const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
+                      const char* OUT_FILE_PATH) {
+    if (nPts < 1) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 1");
+    const long long n = dim == 2 ? (long long)nPts * nPts : nPts;
+    std::vector<double> lle(n);
+    chaos_exec ex = lle_exec();
+    int rc = chaos_lle_sweep(&ex, active_system(), dim, gridMode, tMax, NT, nPts, h, eps, initialConditions,
+                             amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
+                             amountOfValues, lle.data());
+    if (rc) return rc;
+    std::ofstream o(OUT_FILE_PATH);
+    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+    if (dim == 1) {
+        o << std::setprecision(12);
+        for (int k = 0; k < nPts; ++k) o << host_grid_value(k, nPts, ranges[0], ranges[1]) << ", " << lle[k] << '\n';
+    } else {
+        write_matrix(o, lle.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
+    }
+    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+}
+
+// LS1D: rows "value, l_0, ..., l_{n-1}" at the default precision, no header
+// (debri/hostLibrary.cu:3927-3936). LS2D: one file per exponent,
+// OUT_FILE_PATH + "<k+1>.csv", the range header then the matrix rule
+// (debri/hostLibrary.cu:4030-4040, 4078-4094).
+static int legacy_ls(int dim, double tMax, double NT, int nPts, double h, double eps,
+                     const double* initialConditions, int amountOfInitialConditions, const double* ranges,
+                     const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
+                     const char* OUT_FILE_PATH) {
+    if (nPts < 1 || amountOfInitialConditions < 1) return chaos::set_error(CHAOS_E_ARGS, "bad sweep arguments");
+    const long long n = dim == 2 ? (long long)nPts * nPts : nPts;
+    const int nx = amountOfInitialConditions;
+    std::vector<double> sp((size_t)n * nx);
+    chaos_exec ex = lle_exec();
+    int rc = chaos_lyapunov_spectrum(&ex, active_system(), dim, 0, tMax, NT, nPts, h, eps, initialConditions,
+                                     amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
+                                     amountOfValues, sp.data());
+    if (rc) return rc;
+    if (dim == 1) {
+        std::ofstream o(OUT_FILE_PATH);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+        for (int k = 0; k < nPts; ++k) {
+            o << host_grid_value(k, nPts, ranges[0], ranges[1]);
+            for (int j = 0; j < nx; ++j) o << ", " << sp[(size_t)k * nx + j];
+            o << '\n';
+        }
+        return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    }
+    std::vector<double> col(n);
+    for (int j = 0; j < nx; ++j) {
+        const std::string path = std::string(OUT_FILE_PATH) + std::to_string(j + 1) + ".csv";
+        std::ofstream o(path);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", path.c_str());
+        o << ranges[0] << " " << ranges[1] << "\n";
+        o << ranges[2] << " " << ranges[3] << "\n";
+        for (long long p = 0; p < n; ++p) col[p] = sp[(size_t)p * nx + j];
+        write_matrix(o, col.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
+        if (!o.good()) return chaos::set_error(CHAOS_E_IO, "write failed: %s", path.c_str());
+    }
+    return CHAOS_OK;
+}
+
+int chaos_compat_bifurcation1DIC(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                 const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                                 int writableVar, double maxValue, double transientTime, const double* values,
+                                 int amountOfValues, int preScaller, const char* OUT_FILE_PATH) {
+    return legacy_bif1d(CHAOS_GRID_STATE, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        OUT_FILE_PATH);
+}
+
+int chaos_compat_bifurcation1DForH(double tMax, int nPts, int amountOfInitialConditions,
+                                   const double* initialConditions, const double* ranges, int writableVar,
+                                   double maxValue, double transientTime, const double* values, int amountOfValues,
+                                   int preScaller, const char* OUT_FILE_PATH) {
+    const int mut[1] = {CHAOS_MUT_STEP};
+    return legacy_bif1d(CHAOS_GRID_LOG0 | CHAOS_GRID_LOG_F32, tMax, nPts, 0.0, amountOfInitialConditions,
+                        initialConditions, ranges, mut, writableVar, maxValue, transientTime, values, amountOfValues,
+                        preScaller, OUT_FILE_PATH);
+}
+
+// bifurcation2DIC writes bifurcation2D's file (debri/hostLibrary.cu:2932-2936, 3058-3076).
+int chaos_compat_bifurcation2DIC(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                 const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                                 int writableVar, double maxValue, double transientTime, const double* values,
+                                 int amountOfValues, int preScaller, double eps, const char* OUT_FILE_PATH) {
+    if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+    const long long n = (long long)nPts * nPts;
+    std::vector<int> labels(n);
+    chaos_exec ex = active_exec();
+    int rc = chaos_bifurcation_sweep(&ex, active_system(), 2, CHAOS_GRID_STATE, tMax, nPts, h,
+                                     amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
+                                     writableVar, maxValue, transientTime, values, amountOfValues, preScaller, eps, 0,
+                                     nullptr, nullptr, nullptr, nullptr, nullptr, labels.data());
+    if (rc) return rc;
+    std::ofstream o(OUT_FILE_PATH);
+    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+    o << ranges[0] << " " << ranges[1] << "\n";
+    o << ranges[2] << " " << ranges[3] << "\n";
+    o << std::setprecision(12);
+    write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+}
+
+int chaos_compat_LLE1D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                       int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                       int writableVar, double maxValue, double transientTime, const double* values,
+                       int amountOfValues, const char* OUT_FILE_PATH) {
+    (void)writableVar;
+    (void)maxValue;
+    return legacy_lle(1, 0, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                      indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+}
+
+int chaos_compat_LLE1DIC(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                         int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                         int writableVar, double maxValue, double transientTime, const double* values,
+                         int amountOfValues, const char* OUT_FILE_PATH) {
+    (void)writableVar;
+    (void)maxValue;
+    return legacy_lle(1, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
+                      ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+}
+
+int chaos_compat_LLE2DIC(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                         int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                         int writableVar, double maxValue, double transientTime, const double* values,
+                         int amountOfValues, const char* OUT_FILE_PATH) {
+    (void)writableVar;
+    (void)maxValue;
+    return legacy_lle(2, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
+                      ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+}
+
+int chaos_compat_LS1D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                      int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                      int writableVar, double maxValue, double transientTime, const double* values,
+                      int amountOfValues, const char* OUT_FILE_PATH) {
+    (void)writableVar;
+    (void)maxValue;
+    return legacy_ls(1, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                     indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+}
+
+int chaos_compat_LS2D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                      int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                      int writableVar, double maxValue, double transientTime, const double* values,
+                      int amountOfValues, const char* OUT_FILE_PATH) {
+    (void)writableVar;
+    (void)maxValue;
+    return legacy_ls(2, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                     indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+}
+
+// The legacy basins map (debri/hostLibrary.cu:4115-4556) writes the four files
+// of basinsOfAttraction_2; its main file holds an array it never fills
+// (the clustering kernel is not launched), here the basin labels.
+int chaos_compat_basinsOfAttraction(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                    const double* initialConditions, const double* ranges,
+                                    const int* indicesOfMutVars, int writableVar, double maxValue,
+                                    double transientTime, const double* values, int amountOfValues, int preScaller,
+                                    double eps, const char* OUT_FILE_PATH) {
+    return chaos_compat_basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                                             indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                             amountOfValues, preScaller, eps, OUT_FILE_PATH);
+}
+
 }  // extern "C"
 
 namespace Bifurcation {
@@ -235,3 +451,55 @@ int basinsOfAttraction_2(const double tMax, const int nPts, const double h, cons
                                              amountOfValues, preScaller, eps, OUT_FILE_PATH.c_str());
 }
 }  // namespace Basins
+
+namespace old_library {
+#define CHAOS_LEGACY_BIF_ARGS                                                                                   \
+    const double tMax, const int nPts, const double h, const int amountOfInitialConditions,                     \
+        const double *initialConditions, const double *ranges, const int *indicesOfMutVars,                     \
+        const int writableVar, const double maxValue, const double transientTime, const double *values,         \
+        const int amountOfValues, const int preScaller
+#define CHAOS_LEGACY_LLE_ARGS                                                                                   \
+    const double tMax, const double NT, const int nPts, const double h, const double eps,                       \
+        const double *initialConditions, const int amountOfInitialConditions, const double *ranges,             \
+        const int *indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,  \
+        const double *values, const int amountOfValues
+#define CHAOS_LEGACY_BIF_PASS                                                                                   \
+    tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue, \
+        transientTime, values, amountOfValues, preScaller
+#define CHAOS_LEGACY_LLE_PASS                                                                                   \
+    tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges, indicesOfMutVars, writableVar, \
+        maxValue, transientTime, values, amountOfValues
+
+int bifurcation1DIC(CHAOS_LEGACY_BIF_ARGS, std::string OUT_FILE_PATH) {
+    return chaos_compat_bifurcation1DIC(CHAOS_LEGACY_BIF_PASS, OUT_FILE_PATH.c_str());
+}
+int bifurcation2DIC(CHAOS_LEGACY_BIF_ARGS, const double eps, std::string OUT_FILE_PATH) {
+    return chaos_compat_bifurcation2DIC(CHAOS_LEGACY_BIF_PASS, eps, OUT_FILE_PATH.c_str());
+}
+int bifurcation1DForH(const double tMax, const int nPts, const int amountOfInitialConditions,
+                      const double* initialConditions, const double* ranges, const int writableVar,
+                      const double maxValue, const double transientTime, const double* values,
+                      const int amountOfValues, const int preScaller, std::string OUT_FILE_PATH) {
+    return chaos_compat_bifurcation1DForH(tMax, nPts, amountOfInitialConditions, initialConditions, ranges,
+                                          writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                                          OUT_FILE_PATH.c_str());
+}
+int LLE1D(CHAOS_LEGACY_LLE_ARGS, std::string OUT_FILE_PATH) {
+    return chaos_compat_LLE1D(CHAOS_LEGACY_LLE_PASS, OUT_FILE_PATH.c_str());
+}
+int LLE1DIC(CHAOS_LEGACY_LLE_ARGS, std::string OUT_FILE_PATH) {
+    return chaos_compat_LLE1DIC(CHAOS_LEGACY_LLE_PASS, OUT_FILE_PATH.c_str());
+}
+int LLE2DIC(CHAOS_LEGACY_LLE_ARGS, std::string OUT_FILE_PATH) {
+    return chaos_compat_LLE2DIC(CHAOS_LEGACY_LLE_PASS, OUT_FILE_PATH.c_str());
+}
+int LS1D(CHAOS_LEGACY_LLE_ARGS, std::string OUT_FILE_PATH) {
+    return chaos_compat_LS1D(CHAOS_LEGACY_LLE_PASS, OUT_FILE_PATH.c_str());
+}
+int LS2D(CHAOS_LEGACY_LLE_ARGS, std::string OUT_FILE_PATH) {
+    return chaos_compat_LS2D(CHAOS_LEGACY_LLE_PASS, OUT_FILE_PATH.c_str());
+}
+int basinsOfAttraction(CHAOS_LEGACY_BIF_ARGS, const double eps, std::string OUT_FILE_PATH) {
+    return chaos_compat_basinsOfAttraction(CHAOS_LEGACY_BIF_PASS, eps, OUT_FILE_PATH.c_str());
+}
+}  // namespace old_library

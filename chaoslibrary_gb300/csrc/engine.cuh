@@ -39,6 +39,7 @@ __device__ __forceinline__ double grid_value(const GridSpec& g, long long p, int
     long long q = p;
     if (d == 1) q /= g.nPts;
     const long long n = q % g.nPts;
+    if (g.table[d]) return g.table[d][n];
     return g.fused ? __fma_rn((double)n, g.scale[d], g.start[d]) : __dadd_rn(g.start[d], __dmul_rn((double)n, g.scale[d]));
 }
 
@@ -208,11 +209,19 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
     constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
     T x[NX], a[NA], xp[NX];
     load_point<S, T>(P, p, x, a);
-    const StepCtx<T> c((T)P.h);
+    double hp = P.h, hI = P.hInterval;
+    int nS = P.S, nB = P.B;
+    if (P.sweepStep) {  // this point's own step and step counts, as the host derives them from h
+        hp = grid_value(P.grid, p, 0);
+        nS = (int)__ddiv_rn(P.transientTime, hp);
+        nB = (int)__ddiv_rn(__ddiv_rn(P.tMax, hp), (double)P.bPre);
+        hI = __dmul_rn(hp, (double)P.bPre);
+    }
+    const StepCtx<T> c((T)hp);
     const int wv = P.wv;
     int flag = 1;
-    if (P.S > 0) {
-        for (int s = 0; s < P.S; ++s) {
+    if (nS > 0) {
+        for (int s = 0; s < nS; ++s) {
 #pragma unroll
             for (int j = 0; j < NX; ++j) xp[j] = x[j];
             step<S>(x, a, c);
@@ -229,7 +238,7 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
         double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
         double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
         T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
-        for (int i = 0; i < P.B; ++i) {
+        for (int i = 0; i < nB; ++i) {
 #pragma unroll
             for (int j = 0; j < NX; ++j) xp[j] = x[j];
             T val;
@@ -239,7 +248,7 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
                     const int q = ps.n - 1;
                     if (q < O.cap) {
                         if (pk) pk[q] = (double)val;
-                        if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), P.hInterval);
+                        if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), hI);
                     }
                 }
                 ps.tprev = t;
@@ -249,7 +258,7 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
             v = pick<NX>(x, wv);
             if (bif_diverged(v, P)) { flag = 0; break; }
         }
-        if (flag == 1 && P.B > 0 && bif_fixed<NX>(x, xp)) flag = -1;
+        if (flag == 1 && nB > 0 && bif_fixed<NX>(x, xp)) flag = -1;
         kept = ps.n > 1 ? ps.n - 1 : 0;
     } else {
         flag = 0;  // a transient that ended diverged or fixed is reported as diverged
@@ -355,8 +364,12 @@ __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsO
 template <int NX, int NA, class T>
 __device__ __forceinline__ void lle_load(const LleParams& L, long long p, T* x, T* a) {
     const long long i = L.dim == 1 ? p : p % L.nPts, j = L.dim == 1 ? 0 : p / L.nPts;
-    const double va = L.nPts == 1 ? L.rangeA[0] : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
-    const double vb = (L.nPts == 1 || L.dim == 1) ? L.rangeB[0] : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
+    const double va = L.table[0]    ? L.table[0][i]
+                      : L.nPts == 1 ? L.rangeA[0]
+                                    : __dadd_rn(L.rangeA[0], __dmul_rn((double)i, L.stepA));
+    const double vb = L.table[1]                      ? L.table[1][j]
+                      : (L.nPts == 1 || L.dim == 1) ? L.rangeB[0]
+                                                    : __dadd_rn(L.rangeB[0], __dmul_rn((double)j, L.stepB));
 #pragma unroll
     for (int k = 0; k < NX; ++k) {
         double v = L.ic[k];

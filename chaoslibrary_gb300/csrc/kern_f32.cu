@@ -173,7 +173,7 @@ struct Launch {
 // times over, not for small (latency-bound) sweeps. An explicit sweep-pairs
 // mode (0 / 2) wins; then a tuned shape; then the measured rule.
 Launch sweep_launch(const SweepParams& P, bool basins) {
-    if (P.system > SYS_CHEN_RK4) return {false, kBlock};
+    if (P.system > SYS_CHEN_RK4 || P.sweepStep) return {false, kBlock};  // a pair shares one step size
     const int mode = sweep_pairs();
     const int shape = shape_of(basins ? 1 : 0, P.system);
     const int block = shape ? shape % 1024 : kBlock;

@@ -18,11 +18,14 @@ constexpr int kMaxParams = 16;
 
 // Parameter or initial-condition grid of a sweep: point p has coordinate
 // n_d = (p / nPts^d) % nPts in dimension d and value start[d] + n_d*scale[d].
+// A dimension with a table (log-scale axes) takes its value from table[d][n_d]
+// instead: nPts values the host computed.
 struct GridSpec {
     long long nPts;
     double start[2];
     double scale[2];
     int fused;  // 1: start + n*scale as one FMA (what nvcc's default contraction makes of the reference's getValueByIdx)
+    const double* table[2];  // device arrays of nPts values, or null (linear axis)
 };
 
 struct SweepParams {
@@ -46,6 +49,12 @@ struct SweepParams {
     GridSpec grid;
     long long pBegin;   // first point of this launch
     long long nPoints;  // points in this launch
+    // Step-size sweep (bifurcation): dimension 0 sets the integration step h of
+    // each point, which then runs (int)(transientTime / h) transient steps and
+    // (int)(tMax / h / bPre) recorded samples with intervals in units h * bPre.
+    int sweepStep;
+    int bPre;  // the caller's preScaller
+    double tMax, transientTime;
 };
 
 // Per-point results of a bifurcation sweep (point-major rows of `cap`).
@@ -80,6 +89,7 @@ struct LleParams {
     int twin;  // twin start: 0 x + eps e_x; 1 the reference's, every component rounded to float (FP64 only)
     int dim;          // 1: point p = index i of rangeA; 2: p = j*nPts + i (the LLE2D map)
     int mutateState;  // 0: the grid sets values[mut]; 1: it sets initial conditions ic[mut]
+    const double* table[2];  // log-scale axes: device arrays of nPts values (null: linspace)
 };
 
 // precision-specific launchers (kern_f64.cu / kern_f32.cu)

@@ -47,6 +47,58 @@ int basinsOfAttraction_2(const double tMax, const int nPts, const double h, cons
                          std::string OUT_FILE_PATH);
 }  // namespace Basins
 
+// The legacy library's analyses (debri/hostLibrary.cuh:30-400, namespace
+// old_library) with their signatures and file formats, on the engine's sweeps:
+// the *IC variants sweep initial conditions (CHAOS_GRID_STATE), the step-size
+// sweep runs the step on the legacy log scale, the LLE / LS analyses use the
+// LLE map's Benettin scheme and the Gram-Schmidt spectrum. Loops, peak rule
+// and clustering are the current library's (the legacy kernels integrate a
+// system hard-wired into the legacy sources).
+namespace old_library {
+// debri/hostLibrary.cu:1243-1486
+int bifurcation1DIC(const double tMax, const int nPts, const double h, const int amountOfInitialConditions,
+                    const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                    const int writableVar, const double maxValue, const double transientTime, const double* values,
+                    const int amountOfValues, const int preScaller, std::string OUT_FILE_PATH);
+// debri/hostLibrary.cu:2819-3107
+int bifurcation2DIC(const double tMax, const int nPts, const double h, const int amountOfInitialConditions,
+                    const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                    const int writableVar, const double maxValue, const double transientTime, const double* values,
+                    const int amountOfValues, const int preScaller, const double eps, std::string OUT_FILE_PATH);
+// debri/hostLibrary.cu:1005-1240: ranges[0..1] is the range of the step h (log scale)
+int bifurcation1DForH(const double tMax, const int nPts, const int amountOfInitialConditions,
+                      const double* initialConditions, const double* ranges, const int writableVar,
+                      const double maxValue, const double transientTime, const double* values,
+                      const int amountOfValues, const int preScaller, std::string OUT_FILE_PATH);
+// debri/hostLibrary.cu:3111-3325, 3328-3542, 3692-3825, 3829-3958, 3961-4111
+int LLE1D(const double tMax, const double NT, const int nPts, const double h, const double eps,
+          const double* initialConditions, const int amountOfInitialConditions, const double* ranges,
+          const int* indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,
+          const double* values, const int amountOfValues, std::string OUT_FILE_PATH);
+int LLE1DIC(const double tMax, const double NT, const int nPts, const double h, const double eps,
+            const double* initialConditions, const int amountOfInitialConditions, const double* ranges,
+            const int* indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,
+            const double* values, const int amountOfValues, std::string OUT_FILE_PATH);
+int LLE2DIC(const double tMax, const double NT, const int nPts, const double h, const double eps,
+            const double* initialConditions, const int amountOfInitialConditions, const double* ranges,
+            const int* indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,
+            const double* values, const int amountOfValues, std::string OUT_FILE_PATH);
+int LS1D(const double tMax, const double NT, const int nPts, const double h, const double eps,
+         const double* initialConditions, const int amountOfInitialConditions, const double* ranges,
+         const int* indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,
+         const double* values, const int amountOfValues, std::string OUT_FILE_PATH);
+int LS2D(const double tMax, const double NT, const int nPts, const double h, const double eps,
+         const double* initialConditions, const int amountOfInitialConditions, const double* ranges,
+         const int* indicesOfMutVars, const int writableVar, const double maxValue, const double transientTime,
+         const double* values, const int amountOfValues, std::string OUT_FILE_PATH);
+// debri/hostLibrary.cu:4115-4556
+int basinsOfAttraction(const double tMax, const int nPts, const double h, const int amountOfInitialConditions,
+                       const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                       const int writableVar, const double maxValue, const double transientTime,
+                       const double* values, const int amountOfValues, const int preScaller, const double eps,
+                       std::string OUT_FILE_PATH);
+}  // namespace old_library
+
 extern "C" {
 // Run-time selection of the system and arithmetic the wrappers above use.
 int chaos_compat_set_system(int system);
@@ -71,6 +123,45 @@ int chaos_compat_basinsOfAttraction_2(double tMax, int nPts, double h, int amoun
                                       const int* indicesOfMutVars, int writableVar, double maxValue,
                                       double transientTime, const double* values, int amountOfValues,
                                       int preScaller, double eps, const char* OUT_FILE_PATH);
+
+// The legacy analyses with a C string path.
+int chaos_compat_bifurcation1DIC(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                 const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                                 int writableVar, double maxValue, double transientTime, const double* values,
+                                 int amountOfValues, int preScaller, const char* OUT_FILE_PATH);
+int chaos_compat_bifurcation2DIC(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                 const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
+                                 int writableVar, double maxValue, double transientTime, const double* values,
+                                 int amountOfValues, int preScaller, double eps, const char* OUT_FILE_PATH);
+int chaos_compat_bifurcation1DForH(double tMax, int nPts, int amountOfInitialConditions,
+                                   const double* initialConditions, const double* ranges, int writableVar,
+                                   double maxValue, double transientTime, const double* values, int amountOfValues,
+                                   int preScaller, const char* OUT_FILE_PATH);
+int chaos_compat_LLE1D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                       int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                       int writableVar, double maxValue, double transientTime, const double* values,
+                       int amountOfValues, const char* OUT_FILE_PATH);
+int chaos_compat_LLE1DIC(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                         int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                         int writableVar, double maxValue, double transientTime, const double* values,
+                         int amountOfValues, const char* OUT_FILE_PATH);
+int chaos_compat_LLE2DIC(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                         int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                         int writableVar, double maxValue, double transientTime, const double* values,
+                         int amountOfValues, const char* OUT_FILE_PATH);
+int chaos_compat_LS1D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                      int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                      int writableVar, double maxValue, double transientTime, const double* values,
+                      int amountOfValues, const char* OUT_FILE_PATH);
+int chaos_compat_LS2D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
+                      int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                      int writableVar, double maxValue, double transientTime, const double* values,
+                      int amountOfValues, const char* OUT_FILE_PATH);
+int chaos_compat_basinsOfAttraction(double tMax, int nPts, double h, int amountOfInitialConditions,
+                                    const double* initialConditions, const double* ranges,
+                                    const int* indicesOfMutVars, int writableVar, double maxValue,
+                                    double transientTime, const double* values, int amountOfValues, int preScaller,
+                                    double eps, const char* OUT_FILE_PATH);
 }
 
 #endif  // CHAOS_COMPAT_HPP

@@ -57,6 +57,18 @@ extern "C" {
    compiled in at build time (CHAOS_USER_SYSTEMS=<header>); FP64 single sweeps only. */
 #define CHAOS_SYS_USER 15
 
+/* Grid modes of the sweep calls that take one (chaos_bifurcation_sweep,
+   chaos_lle_sweep, chaos_lyapunov_spectrum), OR-ed together. */
+#define CHAOS_GRID_STATE 1 /* indicesOfMutVars address initial conditions, not parameters (the *IC analyses) */
+#define CHAOS_GRID_LOG0 2  /* dimension 0 on a log scale: value n = 10^(log10(r0) + n*((log10(r1) - log10(r0)) /
+                              (nPts - 1))), the legacy getValueByIdxLog (debri/cudaLibrary.cu:1191-1196) */
+#define CHAOS_GRID_LOG1 4  /* dimension 1 on a log scale (ranges[2..3]) */
+#define CHAOS_GRID_LOG_F32 8 /* log-scale values rounded as the legacy step-size sweep does,
+                                (double)powf(10, (float)x) (debri/cudaLibrary.cu:1001); else pow in FP64 */
+/* indicesOfMutVars[0] == CHAOS_MUT_STEP: dimension 0 sweeps the integration step h itself
+   (chaos_bifurcation_sweep, dim 1; the legacy bifurcation1DForH, debri/hostLibrary.cu:1005-1240). */
+#define CHAOS_MUT_STEP (-1)
+
 typedef struct chaos_exec {
     int precision; /* CHAOS_FP64 or CHAOS_FP32 */
     int memory;    /* CHAOS_MEM_HOST or CHAOS_MEM_DEVICE */
@@ -113,6 +125,29 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
                         int* counts);
 
 /*
+ * Bifurcation sweep over a 1-D or 2-D grid with a grid mode (CHAOS_GRID_*):
+ * parameters or initial conditions, linear or log-scale axes, or the step
+ * size. The legacy library's bifurcation1DIC / bifurcation2DIC
+ * (debri/hostLibrary.cu:1243-1486, 2819-3107) are gridMode CHAOS_GRID_STATE;
+ * its step-size sweep bifurcation1DForH (debri/hostLibrary.cu:1005-1240) is
+ * dim 1, indicesOfMutVars[0] = CHAOS_MUT_STEP, gridMode CHAOS_GRID_LOG0 |
+ * CHAOS_GRID_LOG_F32 (h is then ignored: point k integrates with its own step
+ * h_k, (int)(transientTime / h_k) transient steps, (int)(tMax / h_k /
+ * preScaller) samples, intervals in units h_k * preScaller). Loop, peak rule
+ * and clustering are chaos_bifurcation1d's / chaos_bifurcation2d's, which are
+ * this call with gridMode 0.
+ * dim 1: outputs as chaos_bifurcation1d (labels must be NULL).
+ * dim 2: labels[nPts*nPts] and counts (may be NULL) as chaos_bifurcation2d;
+ *        flags, firstSample, peaks and intervals must be NULL, peakCapacity 0.
+ */
+int chaos_bifurcation_sweep(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, int nPts,
+                            double h, int amountOfInitialConditions, const double* initialConditions,
+                            const double* ranges, const int* indicesOfMutVars, int writableVar, double maxValue,
+                            double transientTime, const double* values, int amountOfValues, int preScaller,
+                            double eps, int peakCapacity, int* counts, int* flags, double* firstSample,
+                            double* peaks, double* intervals, int* labels);
+
+/*
  * Largest-Lyapunov-exponent map. Replaces LLE::LLE2D (LLE/include/LLEHost.h:25-41,
  * LLE/src/LLECUDA.cu:205-428). lle[j*nPts + i] is the value at
  * values[indicesOfMutVars[0]] = linspace(ranges[0], ranges[1])[i] and
@@ -129,15 +164,17 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
                 const double* values, int amountOfValues, double* lle);
 
 /*
- * LLE over a 1-D or 2-D grid of parameters (mutateState 0) or of initial
- * conditions (mutateState 1): the legacy library's LLE1D, LLE1DIC, LLE2D and
- * LLE2DIC analyses (debri/hostLibrary.cu:3111-3828) with the Benettin scheme
- * of chaos_lle2d (twin at x + eps*e_x, calcBlocks + 1 blocks, sum / tMax).
- * dim 1: ranges[0..1] and indicesOfMutVars[0], lle[i] for i < nPts; dim 2:
- * ranges[0..3], indicesOfMutVars[0..1], lle[j*nPts + i] as chaos_lle2d (which
- * is this call with dim 2, mutateState 0). CHAOS_FP32 for the RK4 systems.
+ * LLE over a 1-D or 2-D grid of parameters (gridMode 0) or of initial
+ * conditions (gridMode CHAOS_GRID_STATE), linear or log-scale axes
+ * (CHAOS_GRID_LOG0 / LOG1 / LOG_F32): the legacy library's LLE1D, LLE1DIC,
+ * LLE2D and LLE2DIC analyses (debri/hostLibrary.cu:3111-3828) with the
+ * Benettin scheme of chaos_lle2d (twin at x + eps*e_x, calcBlocks + 1 blocks,
+ * sum / tMax). dim 1: ranges[0..1] and indicesOfMutVars[0], lle[i] for
+ * i < nPts; dim 2: ranges[0..3], indicesOfMutVars[0..1], lle[j*nPts + i] as
+ * chaos_lle2d (which is this call with dim 2, gridMode 0). CHAOS_FP32 for the
+ * RK4 systems.
  */
-int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT, int nPts,
+int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT, int nPts,
                     double h, double eps, const double* initialConditions, int amountOfInitialConditions,
                     const double* ranges, const int* indicesOfMutVars, double transientTime, const double* values,
                     int amountOfValues, double* lle);
@@ -149,10 +186,10 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int mutateState, 
  * Gram-Schmidt of the twin differences after every block of NT, exponent j =
  * sum of log(|b_j| / eps) / tMax over calcBlocks + 1 blocks (the LLE map's
  * count; exponent 0 estimates what chaos_lle_sweep estimates).
- * spectrum[p*SIZE_X + j], p as in chaos_lle_sweep. Built-in systems; FP32
+ * spectrum[p*SIZE_X + j], p and gridMode as in chaos_lle_sweep. Built-in systems; FP32
  * for the RK4 systems (exact-difference twins).
  */
-int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int mutateState, double tMax, double NT,
+int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
                             int nPts, double h, double eps, const double* initialConditions,
                             int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                             double transientTime, const double* values, int amountOfValues, double* spectrum);

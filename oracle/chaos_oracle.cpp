@@ -65,6 +65,28 @@ inline double grid_value(long long idx, int nPts, double start, double finish, i
     return start + (double)n * scale;
 }
 
+// Log-scale axis value (the legacy getValueByIdxLog, debri/cudaLibrary.cu:1191-1196:
+// log10(start) + n*((log10(finish) - log10(start)) / (nPts - 1))), raised to
+// 10^x in FP64, or through powf as the legacy step-size sweep does
+// (debri/cudaLibrary.cu:1001: (double)powf(10, x)).
+inline double log_value(long long n, int nPts, double start, double finish, bool f32) {
+    const double l0 = std::log10(start);
+    const double x = l0 + (double)n * ((std::log10(finish) - l0) / (double)(nPts - 1));
+    return f32 ? (double)powf(10.0f, (float)x) : std::pow(10.0, x);
+}
+
+// Grid modes (the engine's CHAOS_GRID_* bits): initial conditions instead of
+// parameters, log-scale dimension 0 / 1, FP32 rounding of log values.
+constexpr int kModeState = 1, kModeLog0 = 2, kModeLog1 = 4, kModeLogF32 = 8;
+
+// Value of dimension d at grid point idx of a bifurcation-type sweep.
+inline double sweep_value(long long idx, int nPts, const double* ranges, int d, int mode) {
+    if (!(mode & (d ? kModeLog1 : kModeLog0))) return grid_value(idx, nPts, ranges[2 * d], ranges[2 * d + 1], d);
+    long long div = 1;
+    for (int k = 0; k < d; ++k) div *= nPts;
+    return log_value((idx / div) % nPts, nPts, ranges[2 * d], ranges[2 * d + 1], (mode & kModeLogF32) != 0);
+}
+
 // linspace of LLE/src/LLECUDA.cu:172-203 (host code, no contraction).
 inline double linspace_value(int i, int num, double start, double end) {
     if (num == 1) return start;
@@ -260,23 +282,28 @@ void orc_point_dbscan(const double* intervals, const int* counts, int nSeries, i
 // first recorded sample), the first `cap` peaks and intervals, and for dim 2
 // the per-point dbscan result (labels, may be null).
 // [pBegin, pEnd) restricts the work to a sub-range of points.
-int orc_bifurcation(int sys, int dim, double tMax, int nPts, double h, const double* ic, const double* ranges,
-                    const int* mut, int wv, double maxValue, double transientTime, const double* values,
-                    int preScaller, double eps, int cap, long long pBegin, long long pEnd, int* counts, int* flags,
-                    double* first, double* peaks, double* intervals, int* labels, int nthreads) {
-    const int B = (int)(tMax / h / preScaller);
-    const int S = (int)(transientTime / h);
+// gridMode: kMode* bits; mut[0] == -1 makes dimension 0 the integration step
+// (dim 1): point k runs with its own h_k, (int)(transientTime / h_k)
+// transient steps, (int)(tMax / h_k / preScaller) samples, intervals in units
+// h_k * preScaller (the legacy step-size sweep, debri/hostLibrary.cu:1005-1240).
+int orc_bifurcation_sweep(int sys, int dim, int gridMode, double tMax, int nPts, double h, const double* ic,
+                          const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
+                          const double* values, int preScaller, double eps, int cap, long long pBegin,
+                          long long pEnd, int* counts, int* flags, double* first, double* peaks, double* intervals,
+                          int* labels, int nthreads) {
+    const bool stepAxis = mut[0] == -1;
+    if (stepAxis && (dim != 1 || !(ranges[0] > 0) || !(ranges[1] > 0))) return 1;
+    const double hMin = stepAxis ? std::min(ranges[0], ranges[1]) * (1.0 - 1e-9) : h;
+    const int Bmax = (int)(tMax / hMin / preScaller);
     const int nx = chaos::system_nx(sys), na = chaos::system_na(sys);
     long long total = 1;
     for (int d = 0; d < dim; ++d) total *= nPts;
     if (pEnd < 0 || pEnd > total) pEnd = total;
-    if (B < 1 || nx > kMaxX) return 1;
+    if (Bmax < 1 || nx > kMaxX) return 1;
     set_threads(nthreads);
-    const StepCtx<double> c(h);
-    const double hh = h * (double)preScaller;
 #pragma omp parallel
     {
-        std::vector<double> data(B), pk(B), tm(B);
+        std::vector<double> data(Bmax + 1), pk(Bmax + 1), tm(Bmax + 1);
         std::vector<int> lab, slot;
 #pragma omp for schedule(dynamic, 4)
         for (long long p = pBegin; p < pEnd; ++p) {
@@ -284,7 +311,25 @@ int orc_bifurcation(int sys, int dim, double tMax, int nPts, double h, const dou
             double x[kMaxX], a[32];
             for (int j = 0; j < nx; ++j) x[j] = ic[j];
             for (int j = 0; j < na; ++j) a[j] = values[j];
-            for (int d = 0; d < dim; ++d) a[mut[d]] = grid_value(p, nPts, ranges[2 * d], ranges[2 * d + 1], d);
+            double hp = h;
+            for (int d = 0; d < dim; ++d) {
+                const double v = sweep_value(p, nPts, ranges, d, gridMode);
+                if (d == 0 && stepAxis) hp = v;
+                else if (gridMode & kModeState) x[mut[d]] = v;
+                else a[mut[d]] = v;
+            }
+            const int B = (int)(tMax / hp / preScaller);
+            const int S = (int)(transientTime / hp);
+            const StepCtx<double> c(hp);
+            const double hh = hp * (double)preScaller;
+            if (B < 1) {  // no recorded sample: the transient decides alone
+                int flag = loop_bif(sys, x, a, c, S, nx, wv, maxValue, nullptr);
+                flags[o] = flag == 1 ? 1 : 0;
+                first[o] = 0.0;
+                counts[o] = 0;
+                if (labels) labels[o] = 0;
+                continue;
+            }
             int flag = loop_bif(sys, x, a, c, S, nx, wv, maxValue, nullptr);
             if (flag == 1) flag = loop_bif(sys, x, a, c, B, nx, wv, maxValue, data.data());
             else flag = 0;
@@ -307,6 +352,17 @@ int orc_bifurcation(int sys, int dim, double tMax, int nPts, double h, const dou
         }
     }
     return 0;
+}
+
+// Bifurcation sweep over nPts^dim parameter points: orc_bifurcation_sweep with gridMode 0.
+int orc_bifurcation(int sys, int dim, double tMax, int nPts, double h, const double* ic, const double* ranges,
+                    const int* mut, int wv, double maxValue, double transientTime, const double* values,
+                    int preScaller, double eps, int cap, long long pBegin, long long pEnd, int* counts, int* flags,
+                    double* first, double* peaks, double* intervals, int* labels, int nthreads) {
+    if ((int)(tMax / h / preScaller) < 1) return 1;
+    return orc_bifurcation_sweep(sys, dim, 0, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                                 preScaller, eps, cap, pBegin, pEnd, counts, flags, first, peaks, intervals, labels,
+                                 nthreads);
 }
 
 // LLE map, FP64, the reference's Benettin scheme (LLECUDA.cu:114-166):
@@ -355,18 +411,23 @@ int orc_lle2d(int sys, double tMax, double NT, int nPts, double h, double eps, c
 }
 
 // Grid point p of an LLE-type sweep (1-D: p = i; 2-D: p = j*nPts + i) over
-// parameters (mutateState 0) or initial conditions (1); dimension 1 last.
-static void lle_grid_point(int dim, int mutateState, long long p, int nPts, const double* ranges, const int* mut,
+// parameters or initial conditions (kModeState), linspace or log-scale axes;
+// dimension 1 last.
+static void lle_grid_point(int dim, int gridMode, long long p, int nPts, const double* ranges, const int* mut,
                            double* x, double* a) {
     const int i = dim == 1 ? (int)p : (int)(p % nPts), j = dim == 1 ? 0 : (int)(p / nPts);
-    double* tgt = mutateState ? x : a;
-    tgt[mut[0]] = linspace_value(i, nPts, ranges[0], ranges[1]);
-    if (dim == 2) tgt[mut[1]] = linspace_value(j, nPts, ranges[2], ranges[3]);
+    double* tgt = (gridMode & kModeState) ? x : a;
+    const bool f32 = (gridMode & kModeLogF32) != 0;
+    tgt[mut[0]] = (gridMode & kModeLog0) ? log_value(i, nPts, ranges[0], ranges[1], f32)
+                                         : linspace_value(i, nPts, ranges[0], ranges[1]);
+    if (dim == 2)
+        tgt[mut[1]] = (gridMode & kModeLog1) ? log_value(j, nPts, ranges[2], ranges[3], f32)
+                                             : linspace_value(j, nPts, ranges[2], ranges[3]);
 }
 
 // LLE over 1-D / 2-D grids of parameters or initial conditions: the scheme
-// of orc_lle2d (which is dim 2, mutateState 0) at every grid point.
-int orc_lle_sweep(int sys, int dim, int mutateState, double tMax, double NT, int nPts, double h, double eps,
+// of orc_lle2d (which is dim 2, gridMode 0) at every grid point.
+int orc_lle_sweep(int sys, int dim, int gridMode, double tMax, double NT, int nPts, double h, double eps,
                   const double* ic, const double* ranges, const int* mut, double transientTime,
                   const double* values, long long pBegin, long long pEnd, double* out, int nthreads) {
     const int ntp = (int)(NT / h);
@@ -384,7 +445,7 @@ int orc_lle_sweep(int sys, int dim, int mutateState, double tMax, double NT, int
         double x[kMaxX], q[kMaxX], a[32];
         for (int k = 0; k < nx; ++k) x[k] = ic[k];
         for (int k = 0; k < na; ++k) a[k] = values[k];
-        lle_grid_point(dim, mutateState, p, nPts, ranges, mut, x, a);
+        lle_grid_point(dim, gridMode, p, nPts, ranges, mut, x, a);
         for (int s = 0; s < trans; ++s) chaos::step_dyn(sys, x, a, c);
         for (int k = 0; k < nx; ++k) q[k] = x[k];
         q[0] = x[0] + eps;
@@ -409,7 +470,7 @@ int orc_lle_sweep(int sys, int dim, int mutateState, double tMax, double NT, int
 // differences go through classical Gram-Schmidt, exponent j adds
 // log(|b_j| / eps) and twin j restarts at x + eps b_j/|b_j|.
 // out[(p - pBegin)*nx + j].
-int orc_lyapunov_spectrum(int sys, int dim, int mutateState, double tMax, double NT, int nPts, double h,
+int orc_lyapunov_spectrum(int sys, int dim, int gridMode, double tMax, double NT, int nPts, double h,
                           double eps, const double* ic, const double* ranges, const int* mut, double transientTime,
                           const double* values, long long pBegin, long long pEnd, double* out, int nthreads) {
     const int ntp = (int)(NT / h);
@@ -427,7 +488,7 @@ int orc_lyapunov_spectrum(int sys, int dim, int mutateState, double tMax, double
         double x[kMaxX], y[kMaxX][kMaxX], a[32], sum[kMaxX];
         for (int k = 0; k < nx; ++k) x[k] = ic[k];
         for (int k = 0; k < na; ++k) a[k] = values[k];
-        lle_grid_point(dim, mutateState, p, nPts, ranges, mut, x, a);
+        lle_grid_point(dim, gridMode, p, nPts, ranges, mut, x, a);
         for (int s = 0; s < trans; ++s) chaos::step_dyn(sys, x, a, c);
         for (int j = 0; j < nx; ++j) {
             sum[j] = 0.0;

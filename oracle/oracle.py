@@ -51,6 +51,10 @@ def lib() -> C.CDLL:
         L.orc_bifurcation.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
                                       C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_int, C.c_longlong,
                                       C.c_longlong, _ip, _ip, _dp, _dp, _dp, C.c_void_p, C.c_int]
+        L.orc_bifurcation_sweep.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp,
+                                            _ip, C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_double, C.c_int,
+                                            C.c_longlong, C.c_longlong, _ip, _ip, _dp, _dp, _dp, C.c_void_p,
+                                            C.c_int]
         L.orc_lle2d.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, _dp, _dp, _ip,
                                 C.c_double, _dp, C.c_longlong, C.c_longlong, _dp, C.c_int]
         for name in ("orc_lle_sweep", "orc_lyapunov_spectrum"):
@@ -129,6 +133,47 @@ def bifurcation(system: int, dim: int, tMax, nPts, h, ic, ranges, mut, wv, maxVa
                 labels=labels if dim == 2 else None)
 
 
+# grid modes (the engine's CHAOS_GRID_* bits) and the step-size axis marker
+GRID_STATE, GRID_LOG0, GRID_LOG1, GRID_LOG_F32 = 1, 2, 4, 8
+MUT_STEP = -1
+
+
+def bifurcation_sweep(system: int, dim: int, grid_mode: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue,
+                      transientTime, values, preScaller=1, eps=0.0, cap=None, p_begin=0, p_end=-1, nthreads=0):
+    """bifurcation() over initial conditions, log-scale axes or the step size
+    (mut[0] == MUT_STEP, dim 1). cap defaults to the largest B/2 + 1 on the grid."""
+    if mut[0] == MUT_STEP:
+        h_min = min(ranges[0], ranges[1]) * (1.0 - 1e-9)
+        B = int(tMax / h_min / preScaller)
+    else:
+        B = int(tMax / h / preScaller)
+    total = nPts ** dim
+    p_end = total if p_end < 0 else p_end
+    n = p_end - p_begin
+    cap = cap or max(B // 2 + 1, 1)
+    counts = np.zeros(n, np.int32)
+    flags = np.zeros(n, np.int32)
+    first = np.zeros(n, np.float64)
+    pk = np.zeros((n, cap), np.float64)
+    iv = np.zeros((n, cap), np.float64)
+    labels = np.zeros(n, np.int32)
+    rc = lib().orc_bifurcation_sweep(system, dim, grid_mode, tMax, nPts, h, _d(ic), _d(ranges), _i(mut), wv,
+                                     maxValue, transientTime, _d(values), preScaller, eps, cap, p_begin, p_end,
+                                     counts, flags, first, pk, iv, labels.ctypes.data if dim == 2 else None,
+                                     nthreads)
+    if rc:
+        raise ValueError("bad bifurcation arguments")
+    return dict(counts=counts, flags=flags, first=first, peaks=pk, intervals=iv,
+                labels=labels if dim == 2 else None)
+
+
+def log_axis(r0: float, r1: float, nPts: int, f32: bool = False) -> np.ndarray:
+    """Values of a log-scale axis, computed as the oracle's C code does."""
+    l0 = np.log10(r0)
+    x = l0 + np.arange(nPts, dtype=np.float64) * ((np.log10(r1) - l0) / (nPts - 1))
+    return np.power(np.float32(10.0), x.astype(np.float32)).astype(np.float64) if f32 else np.power(10.0, x)
+
+
 def lle2d(system: int, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values, p_begin=0, p_end=-1,
           nthreads=0) -> np.ndarray:
     total = nPts * nPts
@@ -141,26 +186,26 @@ def lle2d(system: int, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, v
     return out
 
 
-def lle_sweep(system: int, dim, mutateState, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values,
+def lle_sweep(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values,
               p_begin=0, p_end=-1, nthreads=0) -> np.ndarray:
     total = nPts * nPts if dim == 2 else nPts
     p_end = total if p_end < 0 else p_end
     out = np.zeros(p_end - p_begin, np.float64)
-    rc = lib().orc_lle_sweep(system, dim, mutateState, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
+    rc = lib().orc_lle_sweep(system, dim, grid_mode, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
                              transientTime, _d(values), p_begin, p_end, out, nthreads)
     if rc:
         raise ValueError("bad LLE arguments")
     return out
 
 
-def lyapunov_spectrum(system: int, dim, mutateState, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime,
+def lyapunov_spectrum(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime,
                       values, p_begin=0, p_end=-1, nthreads=0) -> np.ndarray:
     """[points, SIZE_X] exponents."""
     total = nPts * nPts if dim == 2 else nPts
     p_end = total if p_end < 0 else p_end
     nx = len(ic)
     out = np.zeros((p_end - p_begin) * nx, np.float64)
-    rc = lib().orc_lyapunov_spectrum(system, dim, mutateState, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
+    rc = lib().orc_lyapunov_spectrum(system, dim, grid_mode, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
                                      transientTime, _d(values), p_begin, p_end, out, nthreads)
     if rc:
         raise ValueError("bad spectrum arguments")

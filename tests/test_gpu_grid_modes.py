@@ -1,0 +1,216 @@
+"""GPU parity of the grid modes (CHAOS_GRID_*): bifurcation and LLE sweeps
+over initial conditions (the legacy *IC analyses), log-scale axes (the legacy
+getValueByIdxLog, debri/cudaLibrary.cu:1191-1196), the step-size sweep (the
+legacy bifurcation1DForH, debri/hostLibrary.cu:1005-1240), and the legacy
+analyses' file formats, against the CPU oracle. FP64 results are compared bit
+for bit."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import _csv_matrix, _g
+
+pytestmark = pytest.mark.gpu
+
+LORENZ = [10.0, 28.0, 8 / 3]
+IC = [0.1, 0.1, 0.1]
+
+
+def _assert_bif_equal(g, o, cap):
+    assert np.array_equal(g["counts"], o["counts"])
+    assert np.array_equal(g["flags"], o["flags"])
+    for k, c in enumerate(g["counts"]):
+        m = min(max(int(c), 0), cap)
+        assert np.array_equal(g["peaks"][k, :m], o["peaks"][k, :m]), k
+        assert np.array_equal(g["intervals"][k, :m], o["intervals"][k, :m]), k
+        if c == -1:
+            assert g["first"][k] == o["first"][k]
+
+
+@pytest.mark.parametrize("mode, rng, mut", [
+    ("state", [-8.0, 8.0], [2]),
+    ("log", [20.0, 200.0], [1]),
+    ("log_f32", [20.0, 200.0], [1]),
+    ("state_log", [0.5, 30.0], [2]),
+])
+def test_bifurcation_1d_modes_fp64_vs_oracle(engine, oracle, mode, rng, mut):
+    gm = {"state": engine.GRID_STATE, "log": engine.GRID_LOG0, "log_f32": engine.GRID_LOG0 | engine.GRID_LOG_F32,
+          "state_log": engine.GRID_STATE | engine.GRID_LOG0}[mode]
+    n, cap = 64, 400
+    kw = dict(tMax=10.0, nPts=n, h=0.01, initialConditions=IC, ranges=rng, indicesOfMutVars=mut, writableVar=0,
+              maxValue=1e4, transientTime=5.0, values=LORENZ)
+    g = engine.bifurcation_sweep("lorenz", 1, gm, peakCapacity=cap, **kw)
+    o = oracle.bifurcation_sweep(0, 1, gm, 10.0, n, 0.01, IC, rng, mut, 0, 1e4, 5.0, LORENZ, cap=cap)
+    _assert_bif_equal(g, o, cap)
+
+
+@pytest.mark.parametrize("mode", ["state", "log1"])
+def test_bifurcation_2d_modes_fp64_vs_oracle(engine, oracle, mode):
+    """2-D sweeps with the per-point clustering: initial conditions (the
+    legacy bifurcation2DIC) and a log-scale second axis."""
+    if mode == "state":
+        gm, rng, mut = engine.GRID_STATE, [-10.0, 10.0, -10.0, 10.0], [0, 1]
+    else:
+        gm, rng, mut = engine.GRID_LOG1, [20.0, 200.0, 1.0, 30.0], [1, 0]
+    n = 24
+    g = engine.bifurcation_sweep("lorenz", 2, gm, tMax=6.0, nPts=n, h=0.01, initialConditions=IC, ranges=rng,
+                                 indicesOfMutVars=mut, writableVar=0, maxValue=1e4, transientTime=4.0, values=LORENZ,
+                                 eps=0.05)
+    o = oracle.bifurcation_sweep(0, 2, gm, 6.0, n, 0.01, IC, rng, mut, 0, 1e4, 4.0, LORENZ, eps=0.05)
+    assert np.array_equal(g["counts"], o["counts"])
+    assert np.array_equal(g["labels"], o["labels"])
+
+
+@pytest.mark.parametrize("mode", ["log_f32", "linear"])
+def test_step_sweep_fp64_vs_oracle(engine, oracle, mode):
+    """Every point integrates with its own step h_k, (int)(transientTime/h_k)
+    transient steps and (int)(tMax/h_k) samples; intervals in units h_k."""
+    gm = engine.GRID_LOG0 | engine.GRID_LOG_F32 if mode == "log_f32" else 0
+    n, cap, rng = 40, 1200, [0.001, 0.03]
+    kw = dict(tMax=20.0, nPts=n, h=0.0, initialConditions=[1.0, 1.0, 1.0], ranges=rng,
+              indicesOfMutVars=[engine.MUT_STEP], writableVar=0, maxValue=1e4, transientTime=10.0,
+              values=[0.2, 0.2, 5.7])
+    g = engine.bifurcation_sweep("rossler", 1, gm, peakCapacity=cap, **kw)
+    o = oracle.bifurcation_sweep(1, 1, gm, 20.0, n, 0.0, [1.0, 1.0, 1.0], rng, [-1], 0, 1e4, 10.0,
+                                 [0.2, 0.2, 5.7], cap=cap)
+    _assert_bif_equal(g, o, cap)
+    assert np.all(g["counts"] > 0)
+
+
+def test_step_sweep_fp32_runs_single_point_kernels(engine):
+    """The FP32 step sweep (one point per thread: a pair would share one step)
+    keeps the FP64 sweep's flags and nearly its peak counts."""
+    kw = dict(tMax=40.0, nPts=2048, h=0.0, initialConditions=[1.0, 1.0, 1.0], ranges=[0.002, 0.02],
+              indicesOfMutVars=[engine.MUT_STEP], writableVar=0, maxValue=1e4, transientTime=10.0,
+              values=[0.2, 0.2, 5.7], peakCapacity=64)
+    old = engine.get_tuning(engine.TUNE_SWEEP_PAIRS)
+    try:
+        engine.set_tuning(engine.TUNE_SWEEP_PAIRS, 2)  # pairs forced on: the step sweep must still run singly
+        g32 = engine.bifurcation_sweep("rossler", 1, engine.GRID_LOG0, precision=engine.FP32, **kw)
+    finally:
+        engine.set_tuning(engine.TUNE_SWEEP_PAIRS, old)
+    g64 = engine.bifurcation_sweep("rossler", 1, engine.GRID_LOG0, **kw)
+    assert np.array_equal(g32["flags"], g64["flags"])
+    assert np.mean(np.abs(g32["counts"] - g64["counts"]) <= 1) > 0.99
+
+
+def test_log_axis_values_are_the_oracles(engine, oracle):
+    """Point k of the engine's log-scale sweep equals the engine's linear
+    sweep over [v_k, v_k] with v_k from the oracle's formula: the device uses
+    exactly these values."""
+    n = 16
+    for f32 in (False, True):
+        gm = engine.GRID_LOG0 | (engine.GRID_LOG_F32 if f32 else 0)
+        vk = oracle.log_axis(20.0, 200.0, n, f32=f32)
+        kw = dict(tMax=8.0, h=0.01, initialConditions=IC, indicesOfMutVars=[1], writableVar=0, maxValue=1e4,
+                  transientTime=4.0, values=LORENZ, peakCapacity=200)
+        g = engine.bifurcation_sweep("lorenz", 1, gm, nPts=n, ranges=[20.0, 200.0], **kw)
+        for k in (0, 7, n - 1):
+            s = engine.bifurcation1d("lorenz", nPts=2, ranges=[vk[k], vk[k]], **kw)
+            assert g["counts"][k] == s["counts"][0]
+            c = max(int(s["counts"][0]), 0)
+            assert np.array_equal(g["peaks"][k, :c], s["peaks"][0, :c])
+
+
+def test_step_sweep_constant_range_is_bifurcation1d(engine):
+    kw = dict(tMax=10.0, initialConditions=IC, writableVar=0, maxValue=1e4, transientTime=5.0, values=LORENZ,
+              peakCapacity=300)
+    g = engine.bifurcation_sweep("lorenz", 1, 0, nPts=3, h=0.0, ranges=[0.01, 0.01],
+                                 indicesOfMutVars=[engine.MUT_STEP], **kw)
+    s = engine.bifurcation1d("lorenz", nPts=3, h=0.01, ranges=[28.0, 28.0], indicesOfMutVars=[1], **kw)
+    for k in ("counts", "flags", "peaks", "intervals"):
+        assert np.array_equal(g[k], s[k]), k
+
+
+@pytest.mark.parametrize("dim, mode", [(1, "log"), (2, "log_state")])
+def test_lle_sweep_log_axes_fp64_vs_oracle(engine, oracle, dim, mode):
+    if mode == "log":
+        gm, rng, mut = engine.GRID_LOG0, [10.0, 100.0], [1]
+    else:
+        gm, rng, mut = engine.GRID_LOG0 | engine.GRID_LOG1 | engine.GRID_STATE, [0.5, 10.0, 0.5, 10.0], [0, 1]
+    n = 24 if dim == 1 else 8
+    kw = dict(tMax=15.0, NT=0.1, nPts=n, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0], ranges=rng,
+              indicesOfMutVars=mut, transientTime=5.0, values=LORENZ)
+    g = engine.lle_sweep("lorenz", dim, gridMode=gm, **kw)
+    o = oracle.lle_sweep(0, dim, gm, 15.0, 0.1, n, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, mut, 5.0, LORENZ)
+    assert np.max(np.abs(g - o)) < 1e-12
+    g32 = engine.lle_sweep("lorenz", dim, gridMode=gm, precision=engine.FP32, **kw)
+    assert np.all(np.isfinite(g32))
+
+
+def test_spectrum_log_axis_fp64_vs_oracle(engine, oracle):
+    kw = dict(tMax=10.0, NT=0.1, nPts=12, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0], ranges=[10.0, 100.0],
+              indicesOfMutVars=[1], transientTime=2.0, values=LORENZ)
+    g = engine.lyapunov_spectrum("lorenz", 1, gridMode=engine.GRID_LOG0, **kw)
+    o = oracle.lyapunov_spectrum(0, 1, engine.GRID_LOG0, 10.0, 0.1, 12, 0.01, 1e-8, [1.0, 1.0, 1.0],
+                                 [10.0, 100.0], [1], 2.0, LORENZ)
+    assert np.max(np.abs(g - o)) < 1e-12
+
+
+def test_legacy_csv_bytes(engine, oracle, tmp_path):
+    """old_library's analyses write the legacy files: bifurcation1DIC /
+    bifurcation1DForH rows 'value, peak' (precision 12, the step sweep
+    labelled with the linear range), bifurcation2DIC's labels matrix,
+    LLE1D / LLE1DIC rows (precision 12), LLE2DIC's matrix and LS1D / LS2D."""
+    L, old = engine, engine.old_library
+    L.set_system("lorenz")
+    L.set_precision(L.FP64)
+    n = 20
+    lin = [-8.0 + k * (16.0 / (n - 1)) for k in range(n)]
+    # bifurcation1DIC
+    p = tmp_path / "bic.csv"
+    old.bifurcation1DIC(8.0, n, 0.01, 3, IC, [-8.0, 8.0], [2], 0, 1e4, 4.0, LORENZ, 3, 1, p)
+    o = oracle.bifurcation_sweep(0, 1, oracle.GRID_STATE, 8.0, n, 0.01, IC, [-8.0, 8.0], [2], 0, 1e4, 4.0, LORENZ)
+    expect = "".join("%.12g, %.12g\n" % (lin[k], o["peaks"][k, j]) for k in range(n)
+                     for j in range(max(int(o["counts"][k]), 0)))
+    assert p.read_text() == expect
+    # bifurcation1DForH (log-scale step, FP32-rounded; rows labelled with the linear range)
+    p = tmp_path / "bh.csv"
+    old.bifurcation1DForH(8.0, n, 3, IC, [0.005, 0.02], 0, 1e4, 4.0, LORENZ, 3, 1, p)
+    o = oracle.bifurcation_sweep(0, 1, oracle.GRID_LOG0 | oracle.GRID_LOG_F32, 8.0, n, 0.0, IC, [0.005, 0.02], [-1],
+                                 0, 1e4, 4.0, LORENZ)
+    hl = [0.005 + k * ((0.02 - 0.005) / (n - 1)) for k in range(n)]
+    expect = "".join("%.12g, %.12g\n" % (hl[k], o["peaks"][k, j]) for k in range(n)
+                     for j in range(max(int(o["counts"][k]), 0)))
+    assert p.read_text() == expect
+    # bifurcation2DIC
+    p = tmp_path / "b2.csv"
+    old.bifurcation2DIC(5.0, 9, 0.01, 3, IC, [-10.0, 10.0, -10.0, 10.0], [0, 1], 0, 1e4, 4.0, LORENZ, 3, 1, 0.05, p)
+    o = oracle.bifurcation_sweep(0, 2, oracle.GRID_STATE, 5.0, 9, 0.01, IC, [-10.0, 10.0, -10.0, 10.0], [0, 1], 0,
+                                 1e4, 4.0, LORENZ, eps=0.05)
+    assert p.read_text() == "-10 10\n-10 10\n" + _csv_matrix(o["labels"], 9, str)
+    # LLE1D / LLE1DIC / LLE2DIC
+    kw = (10.0, 0.1)
+    for name, dim, gm, rng, mut in (("LLE1D", 1, 0, [20.0, 60.0], [1]), ("LLE1DIC", 1, 1, [-8.0, 8.0], [2]),
+                                    ("LLE2DIC", 2, 1, [-8.0, 8.0, -8.0, 8.0], [0, 2])):
+        m = 12 if dim == 1 else 5
+        p = tmp_path / f"{name}.csv"
+        getattr(old, name)(*kw, m, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, rng, mut, 0, 0.0, 5.0, LORENZ, 3, p)
+        o = oracle.lle_sweep(0, dim, gm, 10.0, 0.1, m, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, mut, 5.0, LORENZ)
+        got = p.read_text()
+        if dim == 1:
+            par = [rng[0] + k * ((rng[1] - rng[0]) / (m - 1)) for k in range(m)]
+            expect = "".join("%.12g, %.12g\n" % (par[k], o[k]) for k in range(m))
+            # the last digit of a printed LLE may differ where the last bit of log does
+            assert [ln.split(", ")[0] for ln in got.splitlines()] == [ln.split(", ")[0] for ln in expect.splitlines()]
+            assert np.allclose([float(ln.split(", ")[1]) for ln in got.splitlines()], o, rtol=1e-10, atol=1e-12)
+        else:
+            cells = [float(c) for c in got.replace("\n", "").split(", ")]
+            assert np.allclose(cells, o, rtol=1e-5, atol=1e-6) and got.count("\n") == m - 1
+    # LS1D / LS2D
+    rng = [20.0, 60.0]
+    p = tmp_path / "ls1.csv"
+    old.LS1D(10.0, 0.1, 6, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, rng, [1], 0, 0.0, 5.0, LORENZ, 3, p)
+    o = oracle.lyapunov_spectrum(0, 1, 0, 10.0, 0.1, 6, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, [1], 5.0, LORENZ)
+    rows = [ln.split(", ") for ln in p.read_text().splitlines()]
+    assert [r[0] for r in rows] == [_g(6)(20.0 + k * 8.0) for k in range(6)]
+    assert np.allclose(np.array([[float(x) for x in r[1:]] for r in rows]), o, rtol=1e-5, atol=1e-6)
+    base = tmp_path / "ls2_"
+    old.LS2D(10.0, 0.1, 4, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, [20.0, 60.0, 5.0, 15.0], [1, 0], 0, 0.0, 5.0, LORENZ, 3,
+             base)
+    o = oracle.lyapunov_spectrum(0, 2, 0, 10.0, 0.1, 4, 0.01, 1e-8, [1.0, 1.0, 1.0], [20.0, 60.0, 5.0, 15.0],
+                                 [1, 0], 5.0, LORENZ)
+    for j in range(3):
+        t = (tmp_path / f"ls2_{j + 1}.csv").read_text()
+        assert t.startswith("20 60\n5 15\n")
+        cells = [float(c) for c in t.split("\n", 2)[2].replace("\n", "").split(", ")]
+        assert np.allclose(cells, o[:, j], rtol=1e-5, atol=1e-6)

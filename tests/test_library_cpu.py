@@ -43,7 +43,10 @@ def test_every_declared_symbol_is_exported(native):
     assert not missing, missing
     out = subprocess.run(["nm", "-DC", str(native.lib_path())], capture_output=True, text=True).stdout
     for cxx in ("Bifurcation::bifurcation1D(", "Bifurcation::bifurcation2D(", "LLE::LLE2D(",
-                "Basins::basinsOfAttraction_2("):
+                "Basins::basinsOfAttraction_2(", "old_library::bifurcation1DIC(", "old_library::bifurcation2DIC(",
+                "old_library::bifurcation1DForH(", "old_library::LLE1D(", "old_library::LLE1DIC(",
+                "old_library::LLE2DIC(", "old_library::LS1D(", "old_library::LS2D(",
+                "old_library::basinsOfAttraction("):
         assert cxx in out, cxx
 
 
@@ -102,6 +105,21 @@ def test_dbscan_argument_errors(native):
         native.dbscan(np.zeros((4, 5)), 0.1, 2)
     with pytest.raises(native.ChaosError, match="minPts"):
         native.dbscan(np.zeros((4, 2)), 0.1, 0)
+
+
+def test_grid_mode_argument_errors(native):
+    kw = dict(tMax=5.0, nPts=8, h=0.01, initialConditions=[0.1, 0.1, 0.1], writableVar=0, maxValue=1e4,
+              transientTime=1.0, values=[10.0, 28.0, 8 / 3])
+    with pytest.raises(native.ChaosError, match="positive"):
+        native.bifurcation_sweep("lorenz", 1, native.GRID_LOG0, ranges=[-1.0, 10.0], indicesOfMutVars=[1], **kw)
+    with pytest.raises(native.ChaosError, match="1-D"):
+        native.bifurcation_sweep("lorenz", 2, 0, ranges=[0.01, 0.02, 1.0, 2.0],
+                                 indicesOfMutVars=[native.MUT_STEP, 0], **kw)
+    with pytest.raises(native.ChaosError, match="grid mode"):
+        native.bifurcation_sweep("lorenz", 1, 64, ranges=[1.0, 10.0], indicesOfMutVars=[1], **kw)
+    with pytest.raises(native.ChaosError, match="dim 2"):
+        native.lle_sweep("lorenz", 1, 5.0, 0.1, 8, 0.01, 1e-8, [0.1, 0.1, 0.1], [1.0, 10.0], [1], 1.0,
+                         [10.0, 28.0, 8 / 3], gridMode=native.GRID_LOG1)
 
 
 def test_compat_system_selection(native):
