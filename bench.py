@@ -11,7 +11,8 @@ the FP32 kernel (exact-difference twin, FP64 log-stretch sum); the line also
 carries the plain FP64 kernel's rate and the FP32 map's error against FP64.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
-                  [--workload lle|bif1d|basins] [--precision fp32|fp64]
+                  [--workload lle|bif1d|bif2d|basins|spectrum|batch|serve]
+                  [--precision fp32|fp64]
 
 --impl reference times the CPU path of the reference algorithm (the oracle's
 C++ restatement, OpenMP over all host cores) on a bounded sample of the same
@@ -53,6 +54,13 @@ BIF2D = dict(system="chameleon", sysid=3, flops=None, tMax=400.0, nPts=300, h=0.
 BASINS = dict(system="lorenz", sysid=0, flops=71, tMax=50.0, nPts=2048, h=0.01, initialConditions=[0.0, 0.0, 27.0],
               ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8,
               transientTime=200.0, values=[10.0, 24.0, 8.0 / 3.0], eps=0.05, minPts=8)
+
+# Lyapunov spectrum (the legacy LS2D analysis): Lorenz, (rho, sigma) in [20,200] x [5,15],
+# 1024^2, tMax 100 (1,002 blocks of NT 0.1), 2,000 transient steps; the orbit and one
+# twin per state dimension
+SPECTRUM = dict(system="lorenz", sysid=0, flops=71, tMax=100.0, NT=0.1, nPts=1024, h=0.01, eps=1e-8,
+                initialConditions=[1.0, 1.0, 1.0], ranges=[20.0, 200.0, 5.0, 15.0], indicesOfMutVars=[1, 0],
+                transientTime=20.0, values=[10.0, 28.0, 8.0 / 3.0])
 
 
 SYS_FLOPS = {"lorenz": 71, "rossler": 63, "chen": 79}
@@ -140,6 +148,12 @@ def lle_steps_per_point(w) -> int:
     ntp = int(w["NT"] / w["h"])
     calc = int(w["tMax"] / w["h"]) // ntp + 1
     return int(w["transientTime"] / w["h"]) + 2 * ntp * (calc + 1)
+
+
+def spectrum_steps_per_point(w, nx=3) -> int:
+    ntp = int(w["NT"] / w["h"])
+    calc = int(w["tMax"] / w["h"]) // ntp + 1
+    return int(w["transientTime"] / w["h"]) + (1 + nx) * ntp * (calc + 1)
 
 
 def sweep_steps_per_point(w) -> int:
@@ -247,6 +261,26 @@ def cpu_sample_lle(w, target_s=10.0):
                       f"FP64, {dt:.1f} s"}
 
 
+def cpu_sample_spectrum(w, target_s=10.0):
+    from oracle import oracle as O
+
+    nthreads = os.cpu_count() or 1
+    n_all = w["nPts"] * w["nPts"]
+    args = (w["sysid"], 2, 0, w["tMax"], w["NT"], w["nPts"], w["h"], w["eps"], w["initialConditions"], w["ranges"],
+            w["indicesOfMutVars"], w["transientTime"], w["values"])
+    probe = 2 * nthreads
+    t = time.perf_counter()
+    O.lyapunov_spectrum(*args, p_begin=n_all // 2, p_end=n_all // 2 + probe, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    n = int(min(n_all, max(probe, probe * target_s / max(dt, 1e-3))))
+    begin = n_all // 2 - n // 2
+    t = time.perf_counter()
+    O.lyapunov_spectrum(*args, p_begin=begin, p_end=begin + n, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    return {"value": n * spectrum_steps_per_point(w) / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n} contiguous grid points from the middle of the map, full horizon, FP64, {dt:.1f} s"}
+
+
 def cpu_sample_sweep(w, kind, target_s=10.0):
     from oracle import oracle as O
 
@@ -280,9 +314,14 @@ def cpu_sample_sweep(w, kind, target_s=10.0):
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
-    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS, "batch": LLE, "serve": LLE}[args.workload]
-    fn = (lambda: cpu_sample_lle(w, args.cpu_seconds)) if args.workload in ("lle", "batch", "serve") else \
-        (lambda: cpu_sample_sweep(w, args.workload, args.cpu_seconds))
+    w = {"lle": LLE, "bif1d": BIF1D, "basins": BASINS, "batch": LLE, "serve": LLE, "bif2d": BIF2D,
+         "spectrum": SPECTRUM}[args.workload]
+    if args.workload in ("lle", "batch", "serve"):
+        fn = lambda: cpu_sample_lle(w, args.cpu_seconds)  # noqa: E731
+    elif args.workload == "spectrum":
+        fn = lambda: cpu_sample_spectrum(w, args.cpu_seconds)  # noqa: E731
+    else:
+        fn = lambda: cpu_sample_sweep(w, args.workload, args.cpu_seconds)  # noqa: E731
     vals, last = [], None
     for _ in range(args.steps):
         last = fn()
@@ -305,6 +344,12 @@ def config_of(args):
                 "grid_points": 1048576, "steps_per_point": lle_steps_per_point(LLE), "eps": 1e-8,
                 "precision": args.precision, "l2": "256 MB buffer written between timed steps; the map's state "
                                                   "lives in registers (inputs: 88 B of parameters)"}
+    if args.workload == "spectrum":
+        return {"workload": "Lyapunov spectrum (Gram-Schmidt per block), Lorenz RK4 h=0.01, rho in [20,200] x "
+                            "sigma in [5,15], 1024x1024, beta=8/3, x0=(1,1,1), 2000 transient steps + 1002 blocks "
+                            "x 10 steps x (orbit + 3 twins)", "grid_points": 1048576,
+                "steps_per_point": spectrum_steps_per_point(SPECTRUM), "eps": 1e-8, "precision": args.precision,
+                "l2": "256 MB buffer written between timed steps; state in registers, 24 B written per point"}
     if args.workload == "bif2d":
         return {"workload": "2-D bifurcation (the reference's own timing sweep), Chameleon, 300x300 over "
                             "(values[3], values[5]) in [0,5] x [0,20], 200000 transient + 40000 recorded steps, "
@@ -555,9 +600,21 @@ def engine_arm(args, ws, rank, local):
     if args.lle_variant:
         C.set_tuning(C.TUNE_LLE_F32_VARIANT, args.lle_variant)
     prec = C.FP32 if args.precision == "fp32" else C.FP64
-    w = {"lle": LLE, "bif1d": BIF1D, "bif2d": BIF2D, "basins": BASINS}[args.workload]
+    w = {"lle": LLE, "bif1d": BIF1D, "bif2d": BIF2D, "basins": BASINS, "spectrum": SPECTRUM}[args.workload]
     n_points = w["nPts"] ** (1 if args.workload == "bif1d" else 2)
-    if args.workload == "lle":
+    if args.workload == "spectrum":
+        steps_pp = spectrum_steps_per_point(w)
+        out = torch.empty((n_points, 3), dtype=torch.float64, device=dev)
+        kw = kw_of(w)
+
+        def step(o=None):
+            return C.lyapunov_spectrum(w["system"], 2, precision=prec, out=out, **kw)
+
+        def step_host():
+            return C.lyapunov_spectrum(w["system"], 2, precision=prec, **kw)
+        d2h = n_points * 24
+        tag = f"spectrum_{args.precision}_lorenz_1024"
+    elif args.workload == "lle":
         steps_pp = lle_steps_per_point(w)
         out = torch.empty(n_points, dtype=torch.float64, device=dev)
         kw = kw_of(w)
@@ -692,6 +749,8 @@ def engine_arm(args, ws, rank, local):
         try:
             if args.workload == "lle":
                 line["cpu_baseline"] = cpu_sample_lle(w, args.cpu_seconds)
+            elif args.workload == "spectrum":
+                line["cpu_baseline"] = cpu_sample_spectrum(w, args.cpu_seconds)
             else:
                 line["cpu_baseline"] = cpu_sample_sweep(w, args.workload, args.cpu_seconds)
         except Exception as e:  # the checker is optional at run time
@@ -880,7 +939,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="lle", choices=["lle", "bif1d", "bif2d", "basins", "batch", "serve"])
+    ap.add_argument("--workload", default="lle",
+                    choices=["lle", "bif1d", "bif2d", "basins", "spectrum", "batch", "serve"])
     ap.add_argument("--requests", type=int, default=2000, help="served stream length")
     ap.add_argument("--rate", type=float, default=100.0, help="served stream arrival rate (requests/s)")
     ap.add_argument("--hbm-budget-gb", type=int, default=64)
@@ -892,7 +952,7 @@ def main():
     ap.add_argument("--npts", type=int, default=None, help="grid resolution override (profiling runs only)")
     ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()
-    for w in (LLE, BIF1D, BIF2D, BASINS):
+    for w in (LLE, BIF1D, BIF2D, BASINS, SPECTRUM):
         if args.npts:
             w["nPts"] = args.npts
         if args.tmax:

@@ -49,7 +49,7 @@ def _deps() -> list[Path]:
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not (LIBDIR / "chaos_perf").exists():
         return False
     t = LIB.stat().st_mtime
     return all(d.stat().st_mtime <= t for d in _deps())
@@ -100,7 +100,25 @@ def build(force: bool = False, verbose: bool = False, user_systems: str | None =
         print(" ".join(link), flush=True)
     subprocess.run(link, check=True)
     os.replace(tmp, out)
+    if out == LIB:
+        build_cli(verbose)
     return out
+
+
+CLI = LIBDIR / "chaos_perf"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """Builds chaos_perf, the command-line driver of the reference's
+    performance sweeps, linked against the library beside it."""
+    tmp = CLI.with_suffix(f".{os.getpid()}.tmp")
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", str(CSRC / "perf_main.cpp"), "-o", str(tmp), f"-L{LIBDIR}",
+           "-lchaos_gb300", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

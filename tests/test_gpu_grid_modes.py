@@ -214,3 +214,28 @@ def test_legacy_csv_bytes(engine, oracle, tmp_path):
         assert t.startswith("20 60\n5 15\n")
         cells = [float(c) for c in t.split("\n", 2)[2].replace("\n", "").split(", ")]
         assert np.allclose(cells, o[:, j], rtol=1e-5, atol=1e-6)
+
+
+def test_perf_cli_tables(engine, tmp_path):
+    """chaos_perf runs the reference's three performance sweeps (here at
+    small resolutions and modelling times) and writes the reference's result
+    tables row for row, with the diagram files beside them."""
+    import re
+    import subprocess
+
+    cli = engine.lib_path().parent / "chaos_perf"
+    r = subprocess.run([str(cli), "--suite", "all", "--resolutions", "16,24", "--times", "100,200",
+                        "--fixed-resolution", "16", "--out", str(tmp_path)], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    bif = (tmp_path / "bifurcation_performance_results.csv").read_text().splitlines()
+    assert bif[0] == "Test,Parameter,Value,Library,ExecutionTime_ms,Dimension"
+    assert [ln.rsplit(",", 2)[0] for ln in bif[1:]] == ["Resolution,16,Bifurcation", "Resolution,24,Bifurcation",
+                                                       "ModelingTime,100,Bifurcation", "ModelingTime,200,Bifurcation"]
+    assert all(re.fullmatch(r"\w+,\d+,Bifurcation,\d+,2D", ln) for ln in bif[1:])
+    for name, lib in (("lle", "LLE"), ("basins", "Basins")):
+        t = (tmp_path / f"{name}_performance_results.csv").read_text().splitlines()
+        assert t[0] == "Test,Parameter,Value,Library,ExecutionTime_ms"
+        assert len(t) == 5 and all(re.fullmatch(rf"(Resolution|ModelingTime),\d+,{lib},\d+", ln) for ln in t[1:])
+    assert (tmp_path / "bif2d_res_test_24.csv").read_text().startswith("0 5\n0 20\n")
+    assert (tmp_path / "lle_tt_test_200.csv").exists() and (tmp_path / "basins_res_test_16.csv_3.csv").exists()

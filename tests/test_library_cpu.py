@@ -138,3 +138,14 @@ def test_no_cpu_fallback(monkeypatch, tmp_path):
     monkeypatch.setenv("CHAOS_GB300_LIB", str(tmp_path / "missing.so"))
     with pytest.raises(N.ChaosError, match="no CPU fallback"):
         N.bifurcation1d("lorenz", **BIF)
+
+
+def test_perf_cli_builds_and_parses(native, tmp_path):
+    """chaos_perf (the reference's performance sweeps as a Linux CLI) links
+    against the library and rejects unknown options without touching a GPU."""
+    cli = native.lib_path().parent / "chaos_perf"
+    assert cli.exists()
+    out = subprocess.run([str(cli), "--help"], capture_output=True, text=True)
+    assert out.returncode == 0 and "--suite" in out.stdout
+    bad = subprocess.run([str(cli), "--suite", "nothing"], capture_output=True, text=True)
+    assert bad.returncode == 2
