@@ -625,8 +625,8 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
                        indicesOfMutVars, transientTime, values, amountOfValues)))
         return rc;
-    if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_difference_form(system)))
-        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_fp32_lle(system)))
+        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
         return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
     Call c;
@@ -649,8 +649,8 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
                        indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
         return rc;
-    if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_difference_form(system)))
-        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_fp32_lle(system)))
+        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
         return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
     Call c;

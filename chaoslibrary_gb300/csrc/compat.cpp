@@ -149,7 +149,7 @@ int chaos_compat_LLE2D(double tMax, double NT, int nPts, double h, double eps, c
     const long long n = (long long)nPts * nPts;
     std::vector<double> lle(n);
     chaos_exec ex = active_exec();
-    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHEN_RK4) ex.precision = CHAOS_FP64;
+    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
     std::ofstream o(OUT_FILE_PATH);
     if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
     o << ranges[0] << " " << ranges[1] << "\n";
@@ -229,10 +229,12 @@ static int legacy_bif1d(int gridMode, double tMax, int nPts, double h, int amoun
     return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
 }
 
-// The arithmetic of the LLE-type wrappers: FP32 only where the engine has it.
-static chaos_exec lle_exec() {
+// The arithmetic of the LLE-type wrappers: FP32 only where the engine has it
+// (LLE: the RK4 systems and Chameleon; spectrum: the RK4 systems).
+static chaos_exec lle_exec(bool spectrum = false) {
     chaos_exec ex = active_exec();
-    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHEN_RK4) ex.precision = CHAOS_FP64;
+    const int last = spectrum ? CHAOS_SYS_CHEN_RK4 : CHAOS_SYS_CHAMELEON;
+    if (ex.precision == CHAOS_FP32 && active_system() > last) ex.precision = CHAOS_FP64;
     return ex;
 }
 
@@ -274,7 +276,7 @@ static int legacy_ls(int dim, double tMax, double NT, int nPts, double h, double
     const long long n = dim == 2 ? (long long)nPts * nPts : nPts;
     const int nx = amountOfInitialConditions;
     std::vector<double> sp((size_t)n * nx);
-    chaos_exec ex = lle_exec();
+    chaos_exec ex = lle_exec(true);
     int rc = chaos_lyapunov_spectrum(&ex, active_system(), dim, 0, tMax, NT, nPts, h, eps, initialConditions,
                                      amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
                                      amountOfValues, sp.data());

@@ -445,25 +445,21 @@ __device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>
     if (s < n) rk4_step_twin<F>(x, e, a, c);
 }
 
-template <class F>
-__device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p) {
+// The Benettin blocks of an FP32 twin carried as a difference e (three state
+// components): steps(e, n) advances the orbit and e by n steps.
+template <class Steps>
+__device__ __forceinline__ double lle_twin_blocks(const LleParams& L, Steps&& steps) {
     using T = float;
-    T x[3], e[3], a[3];
-    lle_load<3, 3>(L, p, x, a);
-    const RK4H<T> c((T)L.h);
-    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
     const T eps = (T)L.eps;
     const T inv_eps2 = (T)(1.0 / (L.eps * L.eps));
-    e[0] = eps;
-    e[1] = T(0);
-    e[2] = T(0);
+    T e[3] = {eps, T(0), T(0)};
     double sum = 0.0;  // sum of log2(d^2)
     const int nb = L.calcBlocks + 1;
     for (int b0 = 0; b0 < nb; b0 += kLleGroup) {
         const int bn = min(kLleGroup, nb - b0);
         T part = T(0);
         for (int b = 0; b < bn; ++b) {
-            twin_steps<F>(x, e, a, c, L.ntp);
+            steps(e, L.ntp);
             const T n2 = fmaf(e[0], e[0], fmaf(e[1], e[1], e[2] * e[2]));
             part += __log2f(n2 * inv_eps2);
             const T r = eps * rsqrtf(n2);
@@ -474,6 +470,27 @@ __device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p
         sum += (double)part;
     }
     return sum * (0.5 * 0.69314718055994530942) / L.tMax;  // log2(d^2) -> ln(d)
+}
+
+template <class F>
+__device__ __forceinline__ double lle_point_twin(const LleParams& L, long long p) {
+    float x[3], a[3];
+    lle_load<3, 3>(L, p, x, a);
+    const RK4H<float> c((float)L.h);
+    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
+    return lle_twin_blocks(L, [&](float* e, int n) { twin_steps<F>(x, e, a, c, n); });
+}
+
+// The FP32 LLE point of Chameleon (the reference's default system): the twin
+// as the difference of chameleon_step_twin.
+__device__ __forceinline__ double lle_point_twin_chameleon(const LleParams& L, long long p) {
+    float x[3], a[7];
+    lle_load<3, 7>(L, p, x, a);
+    const float h = (float)L.h;
+    for (int s = 0; s < L.trans; ++s) chameleon_step<float>(x, a, h);
+    return lle_twin_blocks(L, [&](float* e, int n) {
+        for (int s = 0; s < n; ++s) chameleon_step_twin<float>(x, e, a, h);
+    });
 }
 
 // ---------------------------------------------------------------------------

@@ -45,6 +45,12 @@ __global__ void __launch_bounds__(kBlock, MINB) lle_twin_kernel_f32(LleParams L,
     out[o] = lle_point_twin<F>(L, L.pBegin + o);
 }
 
+__global__ void __launch_bounds__(kBlock) lle_chameleon_kernel_f32(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    out[o] = lle_point_twin_chameleon(L, L.pBegin + o);
+}
+
 template <int S>
 __global__ void __launch_bounds__(kBlock) trajectory_kernel_f32(const double* x0, const double* a0, double h, int nSteps,
                                                        double* out, long long n) {
@@ -283,6 +289,10 @@ cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
         case SYS_LORENZ_RK4: launch_twin<Lorenz>(L, out, st, minb, block); break;
         case SYS_ROSSLER_RK4: launch_twin<Rossler>(L, out, st, minb, block); break;
         case SYS_CHEN_RK4: launch_twin<Chen>(L, out, st, minb, block); break;
+        case SYS_CHAMELEON:
+            lle_chameleon_kernel_f32<<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
+            note_launch();
+            break;
         default: return cudaErrorNotSupported;
     }
     return cudaGetLastError();

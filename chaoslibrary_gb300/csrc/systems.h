@@ -62,6 +62,9 @@ CHAOS_HD int system_na(int s) {
 // Systems whose vector field is polynomial (quadratic): they have an exact
 // difference form f(X+e)-f(X), used by the FP32 twin-trajectory LLE.
 CHAOS_HD bool system_has_difference_form(int s) { return s <= SYS_CHEN_RK4; }
+// Systems whose FP32 LLE map carries the twin as an exact difference: the
+// quadratic RK4 systems and Chameleon (chameleon_step_twin).
+CHAOS_HD bool system_has_fp32_lle(int s) { return s <= SYS_CHEN_RK4 || s == SYS_CHAMELEON; }
 
 // ---- math shims: one name per operation for both precisions ---------------
 CHAOS_HD double fmaT(double a, double b, double c) { return fma(a, b, c); }
@@ -266,6 +269,34 @@ template <class T> CHAOS_HD void chameleon_step(T* X, const T* a, T h) {
     X[2] = fmaT(h2, (a[2] + a[4] * cos_term), X[2]) / (T(1) + a[3] * h2);
     X[1] = fmaT(h2, (a[6] * X[0] + a[1] * X[2]), X[1]);
     X[0] = fmaT(h2, -a[6] * X[1], X[0]);
+}
+
+// The Chameleon step of a twin carried as the difference E = Q - X from the
+// orbit X (FP32 LLE map). Every update of the composition is linear in the
+// state except the cos term, whose difference is taken in product form,
+// cos(u + d) - cos(u) = -2 sin(u + d/2) sin(d/2) with u = a5*X1, d = a5*E1:
+// E keeps its full relative precision while |E| is far below the
+// resolution of X. X advances exactly as chameleon_step does.
+template <class T> CHAOS_HD void chameleon_step_twin(T* X, T* E, const T* a, T h) {
+    const T h1 = a[0] * h;
+    const T h2 = (T(1) - a[0]) * h;
+    X[0] = fmaT(h1, -a[6] * X[1], X[0]);
+    E[0] = fmaT(h1, -a[6] * E[1], E[0]);
+    X[1] = fmaT(h1, a[6] * X[0] + a[1] * X[2], X[1]);
+    E[1] = fmaT(h1, a[6] * E[0] + a[1] * E[2], E[1]);
+    const T u = a[5] * X[1];
+    const T half = T(0.5) * (a[5] * E[1]);
+    const T cos_term = cosT(u);
+    const T dcos = T(-2) * sinT(u + half) * sinT(half);
+    X[2] = fmaT(h1, a[2] - a[3] * X[2] + a[4] * cos_term, X[2]);
+    E[2] = fmaT(h1, a[4] * dcos - a[3] * E[2], E[2]);
+    const T den = T(1) + a[3] * h2;
+    X[2] = fmaT(h2, (a[2] + a[4] * cos_term), X[2]) / den;
+    E[2] = fmaT(h2, a[4] * dcos, E[2]) / den;
+    X[1] = fmaT(h2, (a[6] * X[0] + a[1] * X[2]), X[1]);
+    E[1] = fmaT(h2, (a[6] * E[0] + a[1] * E[2]), E[1]);
+    X[0] = fmaT(h2, -a[6] * X[1], X[0]);
+    E[0] = fmaT(h2, -a[6] * E[1], E[0]);
 }
 
 // Rossler, "CD" composition (systems/systems.cuh:41-63).

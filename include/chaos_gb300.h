@@ -156,7 +156,8 @@ int chaos_bifurcation_sweep(const chaos_exec* ex, int system, int dim, int gridM
  * trajectory starts at x + eps along state component 0 (the reference draws a
  * random unit direction with cuRAND). writableVar and maxValue are accepted
  * and unused, as in the reference. CHAOS_FP32 is supported for the three RK4
- * systems (exact-difference twin, FP64 log sum).
+ * systems and Chameleon (the twin carried as an exact difference, FP64 log
+ * sum).
  */
 int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nPts, double h, double eps,
                 const double* initialConditions, int amountOfInitialConditions, const double* ranges,
@@ -172,7 +173,7 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
  * sum / tMax). dim 1: ranges[0..1] and indicesOfMutVars[0], lle[i] for
  * i < nPts; dim 2: ranges[0..3], indicesOfMutVars[0..1], lle[j*nPts + i] as
  * chaos_lle2d (which is this call with dim 2, gridMode 0). CHAOS_FP32 for the
- * RK4 systems.
+ * RK4 systems and Chameleon.
  */
 int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT, int nPts,
                     double h, double eps, const double* initialConditions, int amountOfInitialConditions,

@@ -96,8 +96,8 @@ def test_lle_argument_errors(native):
     with pytest.raises(native.ChaosError, match="NT / h"):
         native.lle2d("rossler", **{**kw, "NT": 0.001})
     with pytest.raises(native.ChaosError) as e:
-        native.lle2d("chameleon", **{**kw, "values": [0.5, 3, 0, 2, 1, 18, 1]}, precision=native.FP32)
-    assert e.value.code == -6  # FP32 LLE needs a quadratic system
+        native.lle2d("rossler_cd", **{**kw, "values": [0.2, 0.2, 5.7, 0.0]}, precision=native.FP32)
+    assert e.value.code == -6  # FP32 LLE needs a quadratic RK4 system or Chameleon
 
 
 def test_dbscan_argument_errors(native):
