@@ -929,7 +929,7 @@ int chaos_set_tuning(int knob, int value) {
     if (knob == CHAOS_TUNE_LLE_F32_VARIANT)
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
     if (knob == CHAOS_TUNE_SWEEP_PAIRS)
-        return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1 or 2)", value) : CHAOS_OK;
+        return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1, 2 or 3)", value) : CHAOS_OK;
     if (knob == CHAOS_TUNE_SHAPES) {
         if (value != 0) return set_error(CHAOS_E_ARGS, "CHAOS_TUNE_SHAPES takes 0 (forget tuned shapes)");
         for (int k = 0; k < 3; ++k)

@@ -304,14 +304,14 @@ template <> struct PeakSums<float> {
 // Basins point (reference calculateTransTimeCUDA + calculateDiscreteModelCUDA
 // + avgPeakFinderCUDA, basinsCUDA.cu:233-314 and 818-864), fused. PRE1: the
 // sweep has preScaller == 1 (one step per sample, no inner loop).
-template <int S, class T, bool PRE1 = false>
-__device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsOut& O, long long p, long long o) {
-    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
-    T x[NX], a[NA], xp[NX];
-    load_point<S, T>(P, p, x, a);
-    const StepCtx<T> c((T)P.h);
+// The recorded part of a basins point, from its state x after the transient:
+// peak detector, divergence and fixed-point tests, features into row o.
+template <int S, class T, bool PRE1>
+__device__ __forceinline__ void basins_record(const SweepParams& P, const BasinsOut& O, T* x, const T* a,
+                                              const StepCtx<T>& c, long long o) {
+    constexpr int NX = Traits<S>::NX;
+    T xp[NX];
     const int wv = P.wv;
-    for (int s = 0; s < P.S; ++s) step<S>(x, a, c);
 #pragma unroll
     for (int j = 0; j < NX; ++j) xp[j] = x[j];
     PeakStream<T> ps;
@@ -350,6 +350,16 @@ __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsO
     O.avgIntervals[o] = ai;
     if (O.counts) O.counts[o] = flag == 1 ? kept : 0;
     if (O.last) O.last[o] = last;
+}
+
+template <int S, class T, bool PRE1 = false>
+__device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsOut& O, long long p, long long o) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    T x[NX], a[NA];
+    load_point<S, T>(P, p, x, a);
+    const StepCtx<T> c((T)P.h);
+    for (int s = 0; s < P.S; ++s) step<S>(x, a, c);
+    basins_record<S, T, PRE1>(P, O, x, a, c, o);
 }
 
 // ---------------------------------------------------------------------------
@@ -865,6 +875,38 @@ __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const Ba
         O.avgIntervals[oo[l]] = ai;
         if (O.counts) O.counts[oo[l]] = flag[l] == 1 ? kept : 0;
         if (O.last) O.last[oo[l]] = last;
+    }
+}
+
+// Two basins points per thread, hybrid: the transient (no tests, 80 % of the
+// steps of a typical map) runs packed, two trajectories per FP32x2
+// instruction; the recorded part then runs lane by lane with the scalar loop,
+// whose per-sample peak detector and divergence test a packed loop would have
+// to run for both lanes anyway. Bit-identical to basins_point.
+template <class F> struct SysOf;
+template <> struct SysOf<Lorenz> { static constexpr int S = SYS_LORENZ_RK4; };
+template <> struct SysOf<Rossler> { static constexpr int S = SYS_ROSSLER_RK4; };
+template <> struct SysOf<Chen> { static constexpr int S = SYS_CHEN_RK4; };
+
+template <class F, bool PRE1 = false>
+__device__ __forceinline__ void basins_hybrid_point(const SweepParams& P, const BasinsOut& O, long long p0,
+                                                    long long p1, long long o0, long long o1, bool two) {
+    P2 x[3], a[3];
+    load_pair<F>(P, p0, p1, x, a);
+    {
+        const RK4H<P2> c((float)P.h);
+        for (int s = 0; s < P.S; ++s) rk4_step<F>(x, a, c);
+    }
+    const StepCtx<float> cs((float)P.h);
+#pragma unroll 1
+    for (int l = 0; l < (two ? 2 : 1); ++l) {
+        float xs[3], as[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            xs[k] = lane(x[k], l);
+            as[k] = lane(a[k], l);
+        }
+        basins_record<SysOf<F>::S, float, PRE1>(P, O, xs, as, cs, l ? o1 : o0);
     }
 }
 

@@ -83,6 +83,14 @@ __global__ void __launch_bounds__(kMaxBlock) basins_pair_kernel_f32(SweepParams 
     basins_pair_point<F, PRE1>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
 }
 
+template <class F, bool PRE1>
+__global__ void __launch_bounds__(kMaxBlock) basins_hybrid_kernel_f32(SweepParams P, BasinsOut O) {
+    const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (o >= P.nPoints) return;
+    const bool two = o + 1 < P.nPoints;
+    basins_hybrid_point<F, PRE1>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
+}
+
 inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 }  // namespace
 namespace {
@@ -126,22 +134,25 @@ bool lle_variant_forced() { return g_lle_variant.load(std::memory_order_relaxed)
 std::atomic<int> g_sweep_pairs{-1};
 
 // Paired (two points per thread) FP32 sweeps for the RK4 systems. Mode 1
-// (default): pairs for bifurcation sweeps of at least 4 x SMs x 1024 points
-// (measured on GB300: +1..3 % there, slower below; basins sweeps measured
-// no faster paired at any size); 2: always; 0: never. Set with
-// chaos_set_tuning or CHAOS_SWEEP_PAIRS.
+// (default): sweeps of at least 4 x SMs x 1024 points run paired --
+// bifurcation fully packed (measured on GB300: +1..3 % there, slower below),
+// basins as hybrid pairs (packed transient, recorded part lane by lane:
+// 150.9 ms for the 2048^2 Lorenz map against 159.6 ms one point per thread
+// and 154.7 ms fully packed); 2: always fully packed; 0: never; 3: basins
+// always hybrid, bifurcation as 1. Set with chaos_set_tuning or
+// CHAOS_SWEEP_PAIRS.
 int sweep_pairs() {
     const int v = g_sweep_pairs.load(std::memory_order_relaxed);
     if (v >= 0) return v;
     static int env = [] {
         const char* s = getenv("CHAOS_SWEEP_PAIRS");
         const int m = s ? atoi(s) : 1;
-        return m < 0 || m > 2 ? 1 : m;
+        return m < 0 || m > 3 ? 1 : m;
     }();
     return env;
 }
 int set_sweep_pairs(int v) {
-    if (v < 0 || v > 2) return -1;
+    if (v < 0 || v > 3) return -1;
     g_sweep_pairs.store(v);
     return 0;
 }
@@ -151,9 +162,10 @@ inline unsigned grid_of(long long threads, int block) { return (unsigned)((threa
 // Launch shapes the self-timing tuner (tune.cu) found, per kind (0 1-D
 // bifurcation, 1 basins, 2 LLE map) and RK4 system: 0 = none (the built-in
 // rules below), else form * 1024 + block with form 1 (one point per thread)
-// or 2 (two points per thread in packed FP32x2 lanes); for the LLE map also
-// form 12 / 16 (one point per thread, registers shaped for 12 / 16 resident
-// blocks per SM, block 128).
+// or 2 (two points per thread in packed FP32x2 lanes); for basins also form 3
+// (two points per thread, packed transient, recorded part lane by lane); for
+// the LLE map also form 12 / 16 (one point per thread, registers shaped for
+// 12 / 16 resident blocks per SM, block 128).
 std::atomic<int> g_shape[3][3];
 
 int shape_of(int kind, int system) {
@@ -171,22 +183,27 @@ long long pair_threshold() {
 }
 
 struct Launch {
-    bool pairs;
+    int form;  // 1 one point per thread, 2 packed pairs, 3 hybrid pairs (basins)
     int block;
 };
 
 // Pairs halve the threads: worth it when the sweep fills the GPU several
 // times over, not for small (latency-bound) sweeps. An explicit sweep-pairs
-// mode (0 / 2) wins; then a tuned shape; then the measured rule.
+// mode (0 / 2 / 3) wins; then a tuned shape; then the measured rule.
 Launch sweep_launch(const SweepParams& P, bool basins) {
-    if (P.system > SYS_CHEN_RK4 || P.sweepStep) return {false, kBlock};  // a pair shares one step size
+    if (P.system > SYS_CHEN_RK4 || P.sweepStep) return {1, kBlock};  // a pair shares one step size
     const int mode = sweep_pairs();
     const int shape = shape_of(basins ? 1 : 0, P.system);
     const int block = shape ? shape % 1024 : kBlock;
-    if (mode != 1) return {mode == 2, block};
     const bool big = P.nPoints >= pair_threshold();
-    if (shape) return {shape / 1024 == 2 && big, block};
-    return {!basins && big, kBlock};
+    if (mode == 0) return {1, block};
+    if (mode == 2) return {2, block};
+    if (mode == 3 && basins) return {3, block};
+    if (shape) {
+        const int form = shape / 1024;
+        return {form == 3 && !basins ? 1 : (form >= 2 && !big ? 1 : form), block};
+    }
+    return {big ? (basins ? 3 : 2) : 1, kBlock};
 }
 
 template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, int block, cudaStream_t st) {
@@ -201,10 +218,17 @@ template <class F> void launch_basins_pairs(const SweepParams& P, const BasinsOu
     note_launch();
 }
 
+template <class F> void launch_basins_hybrid(const SweepParams& P, const BasinsOut& O, int block, cudaStream_t st) {
+    const unsigned g = grid_of((P.nPoints + 1) / 2, block);
+    if (P.preScaller == 1) basins_hybrid_kernel_f32<F, true><<<g, block, 0, st>>>(P, O);
+    else basins_hybrid_kernel_f32<F, false><<<g, block, 0, st>>>(P, O);
+    note_launch();
+}
+
 cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
     const Launch l = sweep_launch(P, false);
-    if (l.pairs) {
+    if (l.form == 2) {
         if (P.system == SYS_LORENZ_RK4) launch_bif_pairs<Lorenz>(P, O, l.block, st);
         else if (P.system == SYS_ROSSLER_RK4) launch_bif_pairs<Rossler>(P, O, l.block, st);
         else launch_bif_pairs<Chen>(P, O, l.block, st);
@@ -227,10 +251,16 @@ cudaError_t launch_bif_list_f32(const SweepParams& P, const BifOut& O, const int
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
     const Launch l = sweep_launch(P, true);
-    if (l.pairs) {
+    if (l.form == 2) {
         if (P.system == SYS_LORENZ_RK4) launch_basins_pairs<Lorenz>(P, O, l.block, st);
         else if (P.system == SYS_ROSSLER_RK4) launch_basins_pairs<Rossler>(P, O, l.block, st);
         else launch_basins_pairs<Chen>(P, O, l.block, st);
+        return cudaGetLastError();
+    }
+    if (l.form == 3) {
+        if (P.system == SYS_LORENZ_RK4) launch_basins_hybrid<Lorenz>(P, O, l.block, st);
+        else if (P.system == SYS_ROSSLER_RK4) launch_basins_hybrid<Rossler>(P, O, l.block, st);
+        else launch_basins_hybrid<Chen>(P, O, l.block, st);
         return cudaGetLastError();
     }
     const unsigned g = grid_of(P.nPoints, l.block);

@@ -425,9 +425,11 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
  */
 #define CHAOS_TUNE_LLE_F32_VARIANT 1
 /* CHAOS_TUNE_SWEEP_PAIRS: FP32 bifurcation / basins sweeps of the RK4 systems
-   run two points per thread in packed FP32x2 lanes: 1 (default) for
-   bifurcation sweeps of at least 4 x SMs x 1024 points, 2 always, 0 never
-   (one point per thread). Results are identical in every mode. */
+   run two points per thread in packed FP32x2 lanes: 1 (default) for sweeps
+   of at least 4 x SMs x 1024 points (bifurcation fully packed, basins as
+   hybrid pairs: packed transient, recorded part lane by lane), 2 always
+   fully packed, 0 never (one point per thread), 3 basins always hybrid and
+   bifurcation as 1. Results are identical in every mode. */
 #define CHAOS_TUNE_SWEEP_PAIRS 2
 /* CHAOS_TUNE_GRID_FMA: 0 (default) swept values start + n*scale with the
    multiply and the add rounded apart, as the reference's getValueByIdx is
@@ -463,11 +465,11 @@ int chaos_get_tuning(int knob);
  * sweeps that fill the GPU of ex (about 2-3 s in all), and installs the
  * fastest per (kind, system) for every later call in the process; a shape
  * replaces the built-in rule only when at least 1 % faster. Results do not
- * depend on shapes. An explicit CHAOS_TUNE_SWEEP_PAIRS (0 / 2) or
+ * depend on shapes. An explicit CHAOS_TUNE_SWEEP_PAIRS (0 / 2 / 3) or
  * CHAOS_TUNE_LLE_F32_VARIANT still wins. table (may be NULL) receives nTable
  * rows (9 fill all) of 6 doubles: kind (0 1-D bifurcation, 1 basins, 2 LLE
- * map), system, form (0 rule; 1 / 2 trajectories per thread; 12 / 16 LLE
- * register shapes), block, best ms, the built-in rule's ms.
+ * map), system, form (0 rule; 1 / 2 trajectories per thread; 3 basins hybrid
+ * pairs; 12 / 16 LLE register shapes), block, best ms, the built-in rule's ms.
  */
 int chaos_autotune(const chaos_exec* ex, double* table, int nTable);
 
