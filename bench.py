@@ -739,6 +739,11 @@ def engine_arm(args, ws, rank, local):
         ref = reference_gpu_run(args.workload, steps_per_call)
         if ref:
             line["reference_gpu"] = ref
+    if rank == 0 and ws == 1 and args.workload == "basins" and not args.no_extras and not args.npts \
+            and not args.tmax:
+        ref = basins_reference_gpu(C)
+        if ref:
+            line["reference_gpu"] = ref
     if rank == 0 and ws == 1 and args.workload == "bif2d" and not args.no_extras:
         line.update(bif2d_extras(C, prec, w))
     if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras:
@@ -785,6 +790,63 @@ def reference_gpu_run(workload, steps):
     return {"value": steps / s, "unit": UNIT, "seconds": s, "steps": float(steps),
             "what": "the reference's unchanged sources (its host entry point, FP64, nvcc defaults) built for "
                     "sm_103a with the same plug-in, timed around one call incl. its host work"}
+
+
+def _csv_matrix_cells(path, skip=2):
+    """Cells of a reference-format matrix file (header lines, then ', '
+    separators with a line break after every row)."""
+    body = Path(path).read_text().split("\n", skip)[skip]
+    return [c for c in body.replace("\n", "").split(", ") if c != ""]
+
+
+def basins_reference_gpu(C, n=200):
+    """The reference's own basins path (its unchanged sources built by
+    oracle/build_ref_gpu.py) on the basins workload's ranges at n^2 -- its
+    host-driven clustering launches one kernel per reached point, so the
+    2048^2 map is out of its reach -- beside the engine's reference-signature
+    entry point (same CSV files) in FP64 and FP32, with the basin-label
+    agreement of each against the reference (after the best one-to-one
+    matching of cluster ids: the reference numbers clusters in a racy order)."""
+    exe = ROOT / "oracle" / "_ref" / "ref_gpu_basins"
+    if not exe.exists():
+        return None
+    w = BASINS
+    steps = n * n * sweep_steps_per_point(w)
+    args = (w["tMax"], n, w["h"], 3, w["initialConditions"], w["ranges"], w["indicesOfMutVars"], w["writableVar"],
+            w["maxValue"], w["transientTime"], w["values"], 3, 1, w["eps"])
+    with tempfile.TemporaryDirectory() as d:
+        try:
+            p = subprocess.run([str(exe), str(Path(d) / "ref"), str(n)], capture_output=True, text=True,
+                               timeout=600)
+        except subprocess.TimeoutExpired:
+            return {"value": None, "error": "timed out after 600 s"}
+        if p.returncode != 0:
+            return {"value": None, "error": f"exit {p.returncode}"}
+        s = json.loads(p.stdout.strip().splitlines()[-1])["seconds"]
+        ref_labels = np.array([int(float(c)) for c in _csv_matrix_cells(Path(d) / "ref")])
+        out = {"value": steps / s, "unit": UNIT, "seconds": s, "steps": float(steps), "grid": f"{n}x{n}",
+               "what": "the reference's unchanged basins sources (FP64, nvcc defaults) built for sm_103a with the "
+                       "Lorenz RK4 plug-in, timed around one call of Basins::basinsOfAttraction_2 incl. its "
+                       "host work and its host-driven clustering"}
+        C.set_system("lorenz")
+        # engine_fp64_grid_fma: the grid values rounded as the reference's stock build computes them
+        # (CHAOS_TUNE_GRID_FMA = 1); the default keeps the source's separate multiply and add
+        for prec, name, fma in ((C.FP64, "engine_fp64", 0), (C.FP64, "engine_fp64_grid_fma", 1),
+                                (C.FP32, "engine_fp32", 0)):
+            C.set_precision(prec)
+            C.set_tuning(C.TUNE_GRID_FMA, fma)
+            try:
+                C.Basins.basinsOfAttraction_2(*args[:1], 16, *args[2:], Path(d) / "warm")
+                t0 = time.perf_counter()
+                C.Basins.basinsOfAttraction_2(*args, Path(d) / "eng")
+                dt = time.perf_counter() - t0
+            finally:
+                C.set_tuning(C.TUNE_GRID_FMA, 0)
+            eng = np.array([int(float(c)) for c in _csv_matrix_cells(Path(d) / "eng")])
+            out[name] = {"value": steps / dt, "unit": UNIT, "seconds": dt, "speedup_vs_reference": s / dt,
+                         "label_agreement_vs_reference": label_agreement(eng, ref_labels, fixed=(0,))}
+        C.set_precision(C.FP64)
+    return out
 
 
 def bif2d_extras(C, prec, w):

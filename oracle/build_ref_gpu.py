@@ -10,6 +10,7 @@ for ``systems/systems.cuh``:
   oracle/_ref/ref_gpu_bif1d   Bifurcation::bifurcation1D with the Lorenz RK4 plug-in
   oracle/_ref/ref_gpu_bif2d   Bifurcation::bifurcation2D with the reference's own systems.cuh (Chameleon)
   oracle/_ref/ref_gpu_lle2d   LLE::LLE2D with the Rossler RK4 plug-in
+  oracle/_ref/ref_gpu_basins  Basins::basinsOfAttraction_2 with the Lorenz RK4 plug-in
 
 Nothing here is shipped or called by the engine; ``bench.py`` runs these
 binaries, when present, to time the reference beside the engine.
@@ -33,12 +34,14 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FILES = ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp",
          "Bifurcation/include/bifurcationCUDA.cuh", "Bifurcation/include/bifurcationHOST.h",
          "LLE/src/LLECUDA.cu", "LLE/src/LLEHost.cpp", "LLE/include/LLECUDA.cuh", "LLE/include/LLEHost.h",
-         "debri/cudaMacros.cu", "debri/cudaMacros.cuh", "systems/systems.cuh"]
+         "Basins/src/basinsCUDA.cu", "Basins/src/basinsHOST.cpp", "Basins/include/basinsCUDA.cuh",
+         "Basins/include/basinsHOST.h", "debri/cudaMacros.cu", "debri/cudaMacros.cuh", "systems/systems.cuh"]
 TARGETS = {
     "bif1d": ("lorenz", "REF_BIF1D", ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp"]),
     # the reference's own systems.cuh as shipped (its default plug-in, the Chameleon model)
     "bif2d": (None, "REF_BIF2D", ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp"]),
     "lle2d": ("rossler", "REF_LLE2D", ["LLE/src/LLECUDA.cu", "LLE/src/LLEHost.cpp"]),
+    "basins": ("lorenz", "REF_BASINS", ["Basins/src/basinsCUDA.cu", "Basins/src/basinsHOST.cpp"]),
 }
 
 
@@ -71,6 +74,7 @@ def _build_one(name: str, verbose: bool) -> Path:
     exe = binary(name)
     cmd = [NVCC, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-w", f"-D{macro}",
            f"-I{sysdir}", f"-I{STAGE / 'Bifurcation/include'}", f"-I{STAGE / 'LLE/include'}",
+           f"-I{STAGE / 'Basins/include'}",
            f"-I{STAGE / 'debri'}", "-x", "cu"] + [str(STAGE / s) for s in srcs] + \
           [str(STAGE / "debri/cudaMacros.cu"), str(HERE / "ref_gpu_main.cu"), "-o", str(exe)]
     if verbose:

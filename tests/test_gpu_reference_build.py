@@ -101,3 +101,57 @@ def test_lle_reference_twin_start_agrees_with_reference_gpu_build(engine, tmp_pa
     # measured on GB300: twin 1 -> 82.6 % of all points and 97.4 % of the regular ones within 1e-3
     assert within[1][0] >= 0.80 and within[1][1] >= 0.95
     assert within[1][0] > within[0][0]
+
+
+REF_BASINS = ROOT / "oracle" / "_ref" / "ref_gpu_basins"
+
+
+def _matrix_cells(path):
+    body = Path(path).read_text().split("\n", 2)[2]
+    return [c for c in body.replace("\n", "").split(", ") if c != ""]
+
+
+def _matched_agreement(a, b, fixed=(0,)):
+    """Share of points whose labels agree after the best one-to-one matching of
+    cluster ids (the reference numbers its clusters in a racy order)."""
+    from scipy.optimize import linear_sum_assignment
+
+    a, b = np.asarray(a), np.asarray(b)
+    same_fixed = sum(int(np.sum((a == f) & (b == f))) for f in fixed)
+    m = ~np.isin(a, fixed) & ~np.isin(b, fixed)
+    ua, ia = np.unique(a[m], return_inverse=True)
+    ub, ib = np.unique(b[m], return_inverse=True)
+    M = np.zeros((ua.size, ub.size), np.int64)
+    np.add.at(M, (ia, ib), 1)
+    r, c = linear_sum_assignment(-M)
+    return (same_fixed + int(M[r, c].sum())) / a.size
+
+
+def test_basins_agree_with_reference_gpu_build(engine, tmp_path):
+    """The basins map (Lorenz rho 24, the basins workload's ranges, 64^2)
+    through the engine's Basins::basinsOfAttraction_2 against the reference's
+    own GPU build: with CHAOS_TUNE_GRID_FMA = 1 (the contraction the stock
+    build applies to the grid values) the flag file is identical, the feature
+    files agree on at least 99.9 % of the cells and the basin labels on at
+    least 99.9 % of the points after matching cluster ids."""
+    pytest.importorskip("scipy")
+    _need(REF_BASINS)
+    n = 64
+    ref = tmp_path / "ref"
+    subprocess.run([str(REF_BASINS), str(ref), str(n)], check=True, capture_output=True, timeout=600)
+    engine.set_system("lorenz")
+    engine.set_precision("fp64")
+    engine.set_tuning(engine.TUNE_GRID_FMA, 1)
+    try:
+        engine.Basins.basinsOfAttraction_2(50.0, n, 0.01, 3, [0.0, 0.0, 27.0], [-30.0, 30.0, -30.0, 30.0], [0, 1], 0,
+                                           1e8, 200.0, [10.0, 24.0, 8 / 3], 3, 1, 0.05, str(tmp_path / "eng"))
+    finally:
+        engine.set_tuning(engine.TUNE_GRID_FMA, 0)
+    assert (tmp_path / "ref_3.csv").read_text() == (tmp_path / "eng_3.csv").read_text()
+    for k in (1, 2):
+        r, e = _matrix_cells(tmp_path / f"ref_{k}.csv"), _matrix_cells(tmp_path / f"eng_{k}.csv")
+        assert len(r) == len(e) == n * n
+        assert np.mean([x == y for x, y in zip(r, e)]) >= 0.999
+    lr = [int(c) for c in _matrix_cells(ref)]
+    le = [int(c) for c in _matrix_cells(tmp_path / "eng")]
+    assert _matched_agreement(le, lr) >= 0.999
