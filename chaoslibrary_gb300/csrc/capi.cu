@@ -676,8 +676,9 @@ int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridM
                        indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
         return rc;
     const bool fp32 = ex && ex->precision == CHAOS_FP32;
-    if (fp32 && !system_has_difference_form(system))
-        return set_error(CHAOS_E_UNSUPPORTED, "the FP32 spectrum needs a quadratic RK4 system (0-2); use CHAOS_FP64");
+    if (fp32 && !system_has_fp32_lle(system))
+        return set_error(CHAOS_E_UNSUPPORTED,
+                         "the FP32 spectrum needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     Call c;
     if ((rc = c.begin(ex))) return rc;
     if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);

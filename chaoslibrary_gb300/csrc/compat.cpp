@@ -230,11 +230,10 @@ static int legacy_bif1d(int gridMode, double tMax, int nPts, double h, int amoun
 }
 
 // The arithmetic of the LLE-type wrappers: FP32 only where the engine has it
-// (LLE: the RK4 systems and Chameleon; spectrum: the RK4 systems).
-static chaos_exec lle_exec(bool spectrum = false) {
+// (the RK4 systems and Chameleon).
+static chaos_exec lle_exec() {
     chaos_exec ex = active_exec();
-    const int last = spectrum ? CHAOS_SYS_CHEN_RK4 : CHAOS_SYS_CHAMELEON;
-    if (ex.precision == CHAOS_FP32 && active_system() > last) ex.precision = CHAOS_FP64;
+    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
     return ex;
 }
 
@@ -276,7 +275,7 @@ static int legacy_ls(int dim, double tMax, double NT, int nPts, double h, double
     const long long n = dim == 2 ? (long long)nPts * nPts : nPts;
     const int nx = amountOfInitialConditions;
     std::vector<double> sp((size_t)n * nx);
-    chaos_exec ex = lle_exec(true);
+    chaos_exec ex = lle_exec();
     int rc = chaos_lyapunov_spectrum(&ex, active_system(), dim, 0, tMax, NT, nPts, h, eps, initialConditions,
                                      amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
                                      amountOfValues, sp.data());

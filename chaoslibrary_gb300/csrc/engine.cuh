@@ -567,16 +567,14 @@ __device__ __forceinline__ void spectrum_point_full(const LleParams& L, long lon
     for (int j = 0; j < N; ++j) out[p * N + j] = sum[j] / L.tMax;
 }
 
-// The spectrum in FP32 for the quadratic RK4 systems: the twins carried as
-// exact differences e_j (rk4_step_multi), Gram-Schmidt in FP32, per block
-// log2(|b_j|^2/eps^2) on the SFU summed in FP32 groups of kLleGroup blocks
-// and added into FP64, as the FP32 LLE map does.
-template <class F>
-__device__ __forceinline__ void spectrum_point_twin(const LleParams& L, long long p, double* out) {
-    float x[3], a[3], e[3][3];
-    lle_load<3, 3>(L, p, x, a);
-    const RK4H<float> c((float)L.h);
-    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
+// The spectrum in FP32 for the quadratic RK4 systems and Chameleon: the twins
+// carried as exact differences e_j, Gram-Schmidt in FP32, per block
+// log2(|b_j|^2/eps^2) on the SFU summed in FP32 groups of kLleGroup blocks and
+// added into FP64, as the FP32 LLE map does. steps(e, n) advances the orbit
+// and the three differences by n steps.
+template <class Steps>
+__device__ __forceinline__ void spectrum_twin_blocks(const LleParams& L, long long p, double* out, Steps&& steps) {
+    float e[3][3];
     const float eps = (float)L.eps;
     const float inv_eps2 = (float)(1.0 / (L.eps * L.eps));
 #pragma unroll
@@ -589,7 +587,7 @@ __device__ __forceinline__ void spectrum_point_twin(const LleParams& L, long lon
         const int bn = min(kLleGroup, nb - b0);
         float part[3] = {0.f, 0.f, 0.f};
         for (int b = 0; b < bn; ++b) {
-            for (int s = 0; s < L.ntp; ++s) rk4_step_multi<F, 3>(x, e, a, c);
+            steps(e, L.ntp);
             float g[3][3];
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
@@ -618,6 +616,27 @@ __device__ __forceinline__ void spectrum_point_twin(const LleParams& L, long lon
     }
 #pragma unroll
     for (int j = 0; j < 3; ++j) out[p * 3 + j] = sum[j] * (0.5 * 0.69314718055994530942) / L.tMax;
+}
+
+template <class F>
+__device__ __forceinline__ void spectrum_point_twin(const LleParams& L, long long p, double* out) {
+    float x[3], a[3];
+    lle_load<3, 3>(L, p, x, a);
+    const RK4H<float> c((float)L.h);
+    for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
+    spectrum_twin_blocks(L, p, out, [&](float (*e)[3], int n) {
+        for (int s = 0; s < n; ++s) rk4_step_multi<F, 3>(x, e, a, c);
+    });
+}
+
+__device__ __forceinline__ void spectrum_point_twin_chameleon(const LleParams& L, long long p, double* out) {
+    float x[3], a[7];
+    lle_load<3, 7>(L, p, x, a);
+    const float h = (float)L.h;
+    for (int s = 0; s < L.trans; ++s) chameleon_step<float>(x, a, h);
+    spectrum_twin_blocks(L, p, out, [&](float (*e)[3], int n) {
+        for (int s = 0; s < n; ++s) chameleon_step_multi<float, 3>(x, e, a, h);
+    });
 }
 
 // ---------------------------------------------------------------------------

@@ -45,6 +45,12 @@ __global__ void __launch_bounds__(kBlock, MINB) lle_twin_kernel_f32(LleParams L,
     out[o] = lle_point_twin<F>(L, L.pBegin + o);
 }
 
+__global__ void __launch_bounds__(kBlock) spectrum_chameleon_kernel_f32(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    spectrum_point_twin_chameleon(L, L.pBegin + o, out);
+}
+
 __global__ void __launch_bounds__(kBlock) lle_chameleon_kernel_f32(LleParams L, double* out) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= L.nPoints) return;
@@ -335,6 +341,7 @@ cudaError_t launch_spectrum_f32(const LleParams& L, double* out, cudaStream_t st
         case SYS_LORENZ_RK4: spectrum_kernel_f32<Lorenz><<<g, kBlock, 0, st>>>(L, out); break;
         case SYS_ROSSLER_RK4: spectrum_kernel_f32<Rossler><<<g, kBlock, 0, st>>>(L, out); break;
         case SYS_CHEN_RK4: spectrum_kernel_f32<Chen><<<g, kBlock, 0, st>>>(L, out); break;
+        case SYS_CHAMELEON: spectrum_chameleon_kernel_f32<<<g, kBlock, 0, st>>>(L, out); break;
         default: return cudaErrorNotSupported;
     }
     note_launch();

@@ -317,32 +317,51 @@ template <class T> CHAOS_HD void chameleon_step(T* X, const T* a, T h) {
     X[0] = fmaT(h2, -a[6] * X[1], X[0]);
 }
 
-// The Chameleon step of a twin carried as the difference E = Q - X from the
-// orbit X (FP32 LLE map). Every update of the composition is linear in the
-// state except the cos term, whose difference is taken in product form,
-// cos(u + d) - cos(u) = -2 sin(u + d/2) sin(d/2) with u = a5*X1, d = a5*E1:
-// E keeps its full relative precision while |E| is far below the
-// resolution of X. X advances exactly as chameleon_step does.
-template <class T> CHAOS_HD void chameleon_step_twin(T* X, T* E, const T* a, T h) {
+// The Chameleon step of NE twins carried as differences E[q] = Q_q - X from
+// the orbit X (FP32 LLE map and spectrum). Every update of the composition is
+// linear in the state except the cos term, whose difference is taken in
+// product form, cos(u + d) - cos(u) = -2 sin(u + d/2) sin(d/2) with
+// u = a5*X1, d = a5*E1: each E keeps its full relative precision while |E| is
+// far below the resolution of X. X advances exactly as chameleon_step does.
+template <class T, int NE> CHAOS_HD void chameleon_step_multi(T* X, T (*E)[3], const T* a, T h) {
     const T h1 = a[0] * h;
     const T h2 = (T(1) - a[0]) * h;
     X[0] = fmaT(h1, -a[6] * X[1], X[0]);
-    E[0] = fmaT(h1, -a[6] * E[1], E[0]);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) E[q][0] = fmaT(h1, -a[6] * E[q][1], E[q][0]);
     X[1] = fmaT(h1, a[6] * X[0] + a[1] * X[2], X[1]);
-    E[1] = fmaT(h1, a[6] * E[0] + a[1] * E[2], E[1]);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) E[q][1] = fmaT(h1, a[6] * E[q][0] + a[1] * E[q][2], E[q][1]);
     const T u = a[5] * X[1];
-    const T half = T(0.5) * (a[5] * E[1]);
     const T cos_term = cosT(u);
-    const T dcos = T(-2) * sinT(u + half) * sinT(half);
+    T dcos[NE];
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) {
+        const T half = T(0.5) * (a[5] * E[q][1]);
+        dcos[q] = T(-2) * sinT(u + half) * sinT(half);
+    }
     X[2] = fmaT(h1, a[2] - a[3] * X[2] + a[4] * cos_term, X[2]);
-    E[2] = fmaT(h1, a[4] * dcos - a[3] * E[2], E[2]);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) E[q][2] = fmaT(h1, a[4] * dcos[q] - a[3] * E[q][2], E[q][2]);
     const T den = T(1) + a[3] * h2;
     X[2] = fmaT(h2, (a[2] + a[4] * cos_term), X[2]) / den;
-    E[2] = fmaT(h2, a[4] * dcos, E[2]) / den;
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) E[q][2] = fmaT(h2, a[4] * dcos[q], E[q][2]) / den;
     X[1] = fmaT(h2, (a[6] * X[0] + a[1] * X[2]), X[1]);
-    E[1] = fmaT(h2, (a[6] * E[0] + a[1] * E[2]), E[1]);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) E[q][1] = fmaT(h2, (a[6] * E[q][0] + a[1] * E[q][2]), E[q][1]);
     X[0] = fmaT(h2, -a[6] * X[1], X[0]);
-    E[0] = fmaT(h2, -a[6] * E[1], E[0]);
+CHAOS_UNROLL
+    for (int q = 0; q < NE; ++q) E[q][0] = fmaT(h2, -a[6] * E[q][1], E[q][0]);
+}
+
+// One twin (the LLE map).
+template <class T> CHAOS_HD void chameleon_step_twin(T* X, T* E, const T* a, T h) {
+    T Em[1][3] = {{E[0], E[1], E[2]}};
+    chameleon_step_multi<T, 1>(X, Em, a, h);
+    E[0] = Em[0][0];
+    E[1] = Em[0][1];
+    E[2] = Em[0][2];
 }
 
 // Rossler, "CD" composition (systems/systems.cuh:41-63).

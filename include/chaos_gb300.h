@@ -188,7 +188,7 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
  * sum of log(|b_j| / eps) / tMax over calcBlocks + 1 blocks (the LLE map's
  * count; exponent 0 estimates what chaos_lle_sweep estimates).
  * spectrum[p*SIZE_X + j], p and gridMode as in chaos_lle_sweep. Built-in systems; FP32
- * for the RK4 systems (exact-difference twins).
+ * for the RK4 systems and Chameleon (exact-difference twins).
  */
 int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
                             int nPts, double h, double eps, const double* initialConditions,

@@ -765,3 +765,33 @@ def test_chameleon_fp32_lle_within_the_maps_conditioning(engine):
     assert np.percentile(d32, 90) <= 2 * np.percentile(dself, 90) + 0.02
     cls = lambda v: (v > 0.01).astype(int)  # noqa: E731
     assert np.mean(cls(l32) == cls(l64)) >= np.mean(cls(l64b) == cls(l64)) - 0.05
+
+
+def test_chameleon_spectrum_sum_is_the_jacobian_volume(engine):
+    """Chameleon's step is volume-contracting by the constant factor
+    (1 - h1*a3) / (1 + a3*h2) (the only non-shear updates of its composition),
+    so the exponents of the spectrum sum to blocks * NT/h * log(factor) / tMax
+    at every grid point: checked in FP64 and in the FP32 difference-form twins.
+    (The twins span a parallelepiped of side eps = 1e-6, not an infinitesimal
+    one: with cos(18 x) in the field its volume follows the Jacobian's to
+    about 4e-4 of the sum.)"""
+    kw = dict(tMax=50.0, NT=0.5, nPts=8, h=0.01, eps=1e-6, initialConditions=[3.0, 3.0, 0.0], ranges=[0.5, 4.0],
+              indicesOfMutVars=[3], transientTime=100.0, values=[0.5, 3, 0, 2, 1, 18, 1])
+    a3 = np.array([0.5 + k * (3.5 / 7) for k in range(8)])
+    h = kw["h"]
+    h1, h2 = 0.5 * h, (1 - 0.5) * h
+    ntp = int(round(kw["NT"] / h))
+    blocks = int(round(kw["tMax"] / h)) // ntp + 2
+    expect = blocks * ntp * np.log((1 - h1 * a3) / (1 + a3 * h2)) / kw["tMax"]
+    for p, tol in ((engine.FP64, 1e-3), (engine.FP32, 2e-3)):
+        s = engine.lyapunov_spectrum("chameleon", 1, precision=p, **kw)
+        assert np.all(np.isfinite(s))
+        assert np.max(np.abs(s.sum(axis=1) - expect)) < tol, (p, s.sum(axis=1), expect)
+
+
+def test_chameleon_fp32_spectrum_short_horizon(engine):
+    kw = dict(tMax=2.0, NT=0.5, nPts=12, h=0.01, eps=1e-6, initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0],
+              indicesOfMutVars=[3], transientTime=1.0, values=[0.5, 3, 0, 2, 1, 18, 1])
+    s32 = engine.lyapunov_spectrum("chameleon", 1, precision=engine.FP32, **kw)
+    s64 = engine.lyapunov_spectrum("chameleon", 1, precision=engine.FP64, **kw)
+    assert np.max(np.abs(s32 - s64)) < 2e-3
