@@ -12,7 +12,8 @@
 // on the batch, chunk or block it ran in.
 //
 // Batches are FP32 (trajectories in FP32 registers, FP64 accumulation); the
-// LLE jobs use the packed two-points-per-thread path. A prepared batch is
+// jobs of the RK4 systems run two points per thread (packed FP32x2 lanes; for
+// basins the hybrid form), the others one. A prepared batch is
 // replayed from a captured CUDA graph (counter reset + the group kernels).
 #include <cuda_runtime.h>
 
@@ -31,13 +32,47 @@ namespace {
 
 constexpr int kBatchBlock = 128;
 
+template <int S> struct FieldOf;
+template <> struct FieldOf<SYS_LORENZ_RK4> { using F = Lorenz; };
+template <> struct FieldOf<SYS_ROSSLER_RK4> { using F = Rossler; };
+template <> struct FieldOf<SYS_CHEN_RK4> { using F = Chen; };
+
+// Bifurcation chunks: the RK4 systems two points per thread in packed FP32x2
+// lanes (chunks of two blocks' worth of points), the others one per thread.
 template <int S>
 __device__ __forceinline__ void run_bif(const JobDesc& J, long long b, int cnt) {
     __shared__ SweepParams sP;
     if (threadIdx.x == 0) sP = J.sp;
     __syncthreads();
+    if constexpr (S <= SYS_CHEN_RK4) {
 #pragma unroll 1
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) bif_point<S, float>(sP, J.bif, b + t, b + t);
+        for (int t = 2 * threadIdx.x; t < cnt; t += 2 * blockDim.x) {
+            const long long p = b + t;
+            const bool two = t + 1 < cnt;
+            bif_pair_point<typename FieldOf<S>::F>(sP, J.bif, p, two ? p + 1 : p, p, two ? p + 1 : p, two);
+        }
+    } else {
+#pragma unroll 1
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) bif_point<S, float>(sP, J.bif, b + t, b + t);
+    }
+}
+
+// Basins chunks: the RK4 systems as hybrid pairs (packed transient, recorded
+// part lane by lane), the others one point per thread.
+template <int S, bool PRE1>
+__device__ __forceinline__ void run_basins_as(const SweepParams& sP, const JobDesc& J, long long b, int cnt) {
+    if constexpr (S <= SYS_CHEN_RK4) {
+#pragma unroll 1
+        for (int t = 2 * threadIdx.x; t < cnt; t += 2 * blockDim.x) {
+            const long long p = b + t;
+            const bool two = t + 1 < cnt;
+            basins_hybrid_point<typename FieldOf<S>::F, PRE1>(sP, J.bas, p, two ? p + 1 : p, p, two ? p + 1 : p,
+                                                              two);
+        }
+    } else {
+#pragma unroll 1
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) basins_point<S, float, PRE1>(sP, J.bas, b + t, b + t);
+    }
 }
 
 template <int S>
@@ -45,13 +80,8 @@ __device__ __forceinline__ void run_basins(const JobDesc& J, long long b, int cn
     __shared__ SweepParams sP;
     if (threadIdx.x == 0) sP = J.sp;
     __syncthreads();
-    if (sP.preScaller == 1) {
-#pragma unroll 1
-        for (int t = threadIdx.x; t < cnt; t += blockDim.x) basins_point<S, float, true>(sP, J.bas, b + t, b + t);
-    } else {
-#pragma unroll 1
-        for (int t = threadIdx.x; t < cnt; t += blockDim.x) basins_point<S, float, false>(sP, J.bas, b + t, b + t);
-    }
+    if (sP.preScaller == 1) run_basins_as<S, true>(sP, J, b, cnt);
+    else run_basins_as<S, false>(sP, J, b, cnt);
 }
 
 // The job's parameter block is staged in shared memory for the chunk: read
@@ -70,11 +100,6 @@ __device__ __forceinline__ void run_lle(const JobDesc& J, long long b, int cnt) 
         lle_pair_twin<F>(L, p, two ? p + 1 : p, J.lle + p, two ? J.lle + p + 1 : nullptr);
     }
 }
-
-template <int S> struct FieldOf;
-template <> struct FieldOf<SYS_LORENZ_RK4> { using F = Lorenz; };
-template <> struct FieldOf<SYS_ROSSLER_RK4> { using F = Rossler; };
-template <> struct FieldOf<SYS_CHEN_RK4> { using F = Chen; };
 
 // Persistent kernel of one (kind, system) group: pulls chunks [0, count) of
 // the group's range from its counter until none is left. One kernel per

@@ -122,7 +122,8 @@ inline void make_chunks(const std::vector<JobDesc>& jobs, std::vector<Chunk>& ch
         const JobDesc& J = jobs[j];
         if (groups.empty() || groups.back().kind != J.kind || groups.back().system != J.system)
             groups.push_back(Group{J.kind, J.system, (int)chunks.size(), 0});
-        const int size = J.kind == CHAOS_JOB_LLE2D ? 2 * block : block;
+        // two points per thread for the RK4 systems (every LLE job is one)
+        const int size = (J.kind == CHAOS_JOB_LLE2D || J.system <= SYS_CHEN_RK4) ? 2 * block : block;
         for (long long b = 0; b < J.nPoints; b += size)
             chunks.push_back(Chunk{j, (int)std::min<long long>(size, J.nPoints - b), b});
         groups.back().count = (int)chunks.size() - groups.back().begin;
