@@ -12,8 +12,8 @@
 // on the batch, chunk or block it ran in.
 //
 // Batches are FP32 (trajectories in FP32 registers, FP64 accumulation); the
-// jobs of the RK4 systems run two points per thread (packed FP32x2 lanes; for
-// basins the hybrid form), the others one. A prepared batch is
+// jobs of the RK4 systems run two points per thread (packed FP32x2 lanes; the
+// bifurcation and basins jobs in the hybrid form), the others one. A prepared batch is
 // replayed from a captured CUDA graph (counter reset + the group kernels).
 #include <cuda_runtime.h>
 
@@ -37,8 +37,9 @@ template <> struct FieldOf<SYS_LORENZ_RK4> { using F = Lorenz; };
 template <> struct FieldOf<SYS_ROSSLER_RK4> { using F = Rossler; };
 template <> struct FieldOf<SYS_CHEN_RK4> { using F = Chen; };
 
-// Bifurcation chunks: the RK4 systems two points per thread in packed FP32x2
-// lanes (chunks of two blocks' worth of points), the others one per thread.
+// Bifurcation chunks: the RK4 systems as hybrid pairs (packed transient,
+// recorded part lane by lane; chunks of two blocks' worth of points), the
+// others one point per thread.
 template <int S>
 __device__ __forceinline__ void run_bif(const JobDesc& J, long long b, int cnt) {
     __shared__ SweepParams sP;
@@ -49,7 +50,7 @@ __device__ __forceinline__ void run_bif(const JobDesc& J, long long b, int cnt) 
         for (int t = 2 * threadIdx.x; t < cnt; t += 2 * blockDim.x) {
             const long long p = b + t;
             const bool two = t + 1 < cnt;
-            bif_pair_point<typename FieldOf<S>::F>(sP, J.bif, p, two ? p + 1 : p, p, two ? p + 1 : p, two);
+            bif_hybrid_point<typename FieldOf<S>::F>(sP, J.bif, p, two ? p + 1 : p, p, two ? p + 1 : p, two);
         }
     } else {
 #pragma unroll 1

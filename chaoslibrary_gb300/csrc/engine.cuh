@@ -200,6 +200,53 @@ template <int NX, class T> __device__ __forceinline__ bool basins_fixed(const T*
     return sqrt(fabs((double)s)) < 1e-9;
 }
 
+// The recorded part of a bifurcation point, from its state x after a
+// transient that ended bounded and not fixed: nB samples through the
+// streaming peak detector (intervals in units hI), divergence and fixed-point
+// tests; writes flags/counts/first and the first `cap` kept peaks/intervals
+// of row o.
+template <int S, class T>
+__device__ __forceinline__ void bif_record(const SweepParams& P, const BifOut& O, T* x, const T* a,
+                                           const StepCtx<T>& c, int nB, double hI, long long o) {
+    constexpr int NX = Traits<S>::NX;
+    T xp[NX];
+    const int wv = P.wv;
+    int flag = 1;
+    PeakStream<T> ps;
+    ps.init();
+    const double first = (double)pick<NX>(x, wv);
+    double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
+    double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
+    T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
+#pragma unroll
+    for (int j = 0; j < NX; ++j) xp[j] = x[j];
+    for (int i = 0; i < nB; ++i) {
+#pragma unroll
+        for (int j = 0; j < NX; ++j) xp[j] = x[j];
+        T val;
+        int t;
+        if (ps.push(v, val, t)) {
+            if (ps.n >= 1) {
+                const int q = ps.n - 1;
+                if (q < O.cap) {
+                    if (pk) pk[q] = (double)val;
+                    if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), hI);
+                }
+            }
+            ps.tprev = t;
+            ++ps.n;
+        }
+        step<S>(x, a, c);
+        v = pick<NX>(x, wv);
+        if (bif_diverged(v, P)) { flag = 0; break; }
+    }
+    if (flag == 1 && nB > 0 && bif_fixed<NX>(x, xp)) flag = -1;
+    const int kept = ps.n > 1 ? ps.n - 1 : 0;
+    O.flags[o] = flag;
+    O.counts[o] = flag == 1 ? kept : (flag == -1 ? -1 : 0);
+    if (O.first) O.first[o] = first;
+}
+
 // ---------------------------------------------------------------------------
 // Bifurcation point (reference kernels calculateTransTimeCUDA +
 // calculateDiscreteModelCUDA + peakFinderCUDA, bifurcationCUDA.cu:258-371),
@@ -229,43 +276,13 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
         }
         if (flag == 1 && bif_fixed<NX>(x, xp)) flag = -1;
     }
-    double first = 0.0;
-    int kept = 0;
     if (flag == 1) {
-        PeakStream<T> ps;
-        ps.init();
-        first = (double)pick<NX>(x, wv);
-        double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
-        double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
-        T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
-        for (int i = 0; i < nB; ++i) {
-#pragma unroll
-            for (int j = 0; j < NX; ++j) xp[j] = x[j];
-            T val;
-            int t;
-            if (ps.push(v, val, t)) {
-                if (ps.n >= 1) {
-                    const int q = ps.n - 1;
-                    if (q < O.cap) {
-                        if (pk) pk[q] = (double)val;
-                        if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), hI);
-                    }
-                }
-                ps.tprev = t;
-                ++ps.n;
-            }
-            step<S>(x, a, c);
-            v = pick<NX>(x, wv);
-            if (bif_diverged(v, P)) { flag = 0; break; }
-        }
-        if (flag == 1 && nB > 0 && bif_fixed<NX>(x, xp)) flag = -1;
-        kept = ps.n > 1 ? ps.n - 1 : 0;
-    } else {
-        flag = 0;  // a transient that ended diverged or fixed is reported as diverged
+        bif_record<S, T>(P, O, x, a, c, nB, hI, o);
+    } else {  // a transient that ended diverged or fixed is reported as diverged
+        O.flags[o] = 0;
+        O.counts[o] = 0;
+        if (O.first) O.first[o] = 0.0;
     }
-    O.flags[o] = flag;
-    O.counts[o] = flag == 1 ? kept : (flag == -1 ? -1 : 0);
-    if (O.first) O.first[o] = first;
 }
 
 // Sums over the kept peaks of a basins point: peak values and intervals.
@@ -926,6 +943,51 @@ __device__ __forceinline__ void basins_hybrid_point(const SweepParams& P, const 
             as[k] = lane(a[k], l);
         }
         basins_record<SysOf<F>::S, float, PRE1>(P, O, xs, as, cs, l ? o1 : o0);
+    }
+}
+
+// Two bifurcation points per thread, hybrid: the transient packed (per-lane
+// divergence and fixed-point tests, as bif_pair_point), the recorded part lane
+// by lane with the scalar loop (bif_record). Bit-identical to bif_point.
+template <class F>
+__device__ __forceinline__ void bif_hybrid_point(const SweepParams& P, const BifOut& O, long long p0, long long p1,
+                                                 long long o0, long long o1, bool two) {
+    P2 x[3], a[3], xp[3];
+    load_pair<F>(P, p0, p1, x, a);
+    const int wv = P.wv;
+    int flag[2] = {1, two ? 1 : 0};
+    if (P.S > 0) {
+        const RK4H<P2> c((float)P.h);
+        for (int s = 0; s < P.S; ++s) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+            rk4_step<F>(x, a, c);
+            const P2 v = pick2<3>(x, wv);
+            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
+            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
+            if (flag[0] != 1 && flag[1] != 1) break;
+        }
+#pragma unroll
+        for (int l = 0; l < 2; ++l)
+            if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+    }
+    const StepCtx<float> cs((float)P.h);
+#pragma unroll 1
+    for (int l = 0; l < (two ? 2 : 1); ++l) {
+        const long long o = l ? o1 : o0;
+        if (flag[l] != 1) {  // diverged or fixed in the transient: reported as diverged
+            O.flags[o] = 0;
+            O.counts[o] = 0;
+            if (O.first) O.first[o] = 0.0;
+            continue;
+        }
+        float xs[3], as[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            xs[k] = lane(x[k], l);
+            as[k] = lane(a[k], l);
+        }
+        bif_record<SysOf<F>::S, float>(P, O, xs, as, cs, P.B, P.hInterval, o);
     }
 }
 

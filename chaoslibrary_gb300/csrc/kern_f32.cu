@@ -89,6 +89,14 @@ __global__ void __launch_bounds__(kMaxBlock) basins_pair_kernel_f32(SweepParams 
     basins_pair_point<F, PRE1>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
 }
 
+template <class F>
+__global__ void __launch_bounds__(kMaxBlock) bif_hybrid_kernel_f32(SweepParams P, BifOut O) {
+    const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (o >= P.nPoints) return;
+    const bool two = o + 1 < P.nPoints;
+    bif_hybrid_point<F>(P, O, P.pBegin + o, P.pBegin + (two ? o + 1 : o), o, two ? o + 1 : o, two);
+}
+
 template <class F, bool PRE1>
 __global__ void __launch_bounds__(kMaxBlock) basins_hybrid_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -140,13 +148,13 @@ bool lle_variant_forced() { return g_lle_variant.load(std::memory_order_relaxed)
 std::atomic<int> g_sweep_pairs{-1};
 
 // Paired (two points per thread) FP32 sweeps for the RK4 systems. Mode 1
-// (default): sweeps of at least 4 x SMs x 1024 points run paired --
-// bifurcation fully packed (measured on GB300: +1..3 % there, slower below),
-// basins as hybrid pairs (packed transient, recorded part lane by lane:
-// 150.9 ms for the 2048^2 Lorenz map against 159.6 ms one point per thread
-// and 154.7 ms fully packed); 2: always fully packed; 0: never; 3: basins
-// always hybrid, bifurcation as 1. Set with chaos_set_tuning or
-// CHAOS_SWEEP_PAIRS.
+// (default): sweeps of at least 4 x SMs x 1024 points run as hybrid pairs
+// (packed transient, recorded part lane by lane), smaller ones one point per
+// thread (pairs halve the threads of a latency-bound sweep). Measured on
+// GB300: the 2048^2 Lorenz basins map 150.9 ms hybrid, 154.7 ms fully packed,
+// 159.6 ms one point per thread; a 1.6 M-point Lorenz 1-D bifurcation 65.9 /
+// 69.3 / 69.8 ms, Rossler 59.7 / 60.3 / 64.0 ms. 2: always fully packed;
+// 0: never; 3: always hybrid. Set with chaos_set_tuning or CHAOS_SWEEP_PAIRS.
 int sweep_pairs() {
     const int v = g_sweep_pairs.load(std::memory_order_relaxed);
     if (v >= 0) return v;
@@ -204,12 +212,12 @@ Launch sweep_launch(const SweepParams& P, bool basins) {
     const bool big = P.nPoints >= pair_threshold();
     if (mode == 0) return {1, block};
     if (mode == 2) return {2, block};
-    if (mode == 3 && basins) return {3, block};
+    if (mode == 3) return {3, block};
     if (shape) {
         const int form = shape / 1024;
-        return {form == 3 && !basins ? 1 : (form >= 2 && !big ? 1 : form), block};
+        return {form >= 2 && !big ? 1 : form, block};
     }
-    return {big ? (basins ? 3 : 2) : 1, kBlock};
+    return {big ? 3 : 1, kBlock};
 }
 
 template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, int block, cudaStream_t st) {
@@ -221,6 +229,11 @@ template <class F> void launch_basins_pairs(const SweepParams& P, const BasinsOu
     const unsigned g = grid_of((P.nPoints + 1) / 2, block);
     if (P.preScaller == 1) basins_pair_kernel_f32<F, true><<<g, block, 0, st>>>(P, O);
     else basins_pair_kernel_f32<F, false><<<g, block, 0, st>>>(P, O);
+    note_launch();
+}
+
+template <class F> void launch_bif_hybrid(const SweepParams& P, const BifOut& O, int block, cudaStream_t st) {
+    bif_hybrid_kernel_f32<F><<<grid_of((P.nPoints + 1) / 2, block), block, 0, st>>>(P, O);
     note_launch();
 }
 
@@ -238,6 +251,12 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
         if (P.system == SYS_LORENZ_RK4) launch_bif_pairs<Lorenz>(P, O, l.block, st);
         else if (P.system == SYS_ROSSLER_RK4) launch_bif_pairs<Rossler>(P, O, l.block, st);
         else launch_bif_pairs<Chen>(P, O, l.block, st);
+        return cudaGetLastError();
+    }
+    if (l.form == 3) {
+        if (P.system == SYS_LORENZ_RK4) launch_bif_hybrid<Lorenz>(P, O, l.block, st);
+        else if (P.system == SYS_ROSSLER_RK4) launch_bif_hybrid<Rossler>(P, O, l.block, st);
+        else launch_bif_hybrid<Chen>(P, O, l.block, st);
         return cudaGetLastError();
     }
 #define CALL(S) (bif_kernel_f32<S><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O), note_launch())

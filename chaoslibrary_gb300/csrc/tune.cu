@@ -42,7 +42,7 @@ std::vector<int> candidates(int kind) {
         c.push_back(1 * 1024 + block);
         c.push_back(2 * 1024 + block);
     }
-    if (kind == 1)  // basins: also the hybrid (packed transient, recorded part lane by lane)
+    if (kind <= 1)  // bifurcation and basins: also the hybrid (packed transient, recorded part lane by lane)
         for (int block : {64, 128, 256}) c.push_back(3 * 1024 + block);
     if (kind == 2) {  // the LLE map: one point per thread exists only as the 12 / 16 register shapes
         c.erase(std::remove_if(c.begin(), c.end(), [](int s) { return s / 1024 == 1; }), c.end());

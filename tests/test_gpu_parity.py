@@ -533,7 +533,7 @@ def test_paired_sweeps_identical(engine, system, values, ic, mi, rng, maxv):
               indicesOfMutVars=[0, 1], writableVar=0, maxValue=maxv * 2, transientTime=3.0, values=values)
     res = {}
     try:
-        for v in (0, 2, 3):  # one point per thread, fully packed, hybrid basins (packed transient)
+        for v in (0, 2, 3):  # one point per thread, fully packed, hybrid (packed transient)
             engine.set_tuning(knob, v)
             res[v] = (engine.bifurcation1d(system, precision=engine.FP32, peakCapacity=40, **kw),
                       engine.basins_features(system, precision=engine.FP32, preScaller=2, **bk),
@@ -544,6 +544,14 @@ def test_paired_sweeps_identical(engine, system, values, ic, mi, rng, maxv):
         assert np.array_equal(res[0][1][k], res[3][1][k]), k
         assert np.array_equal(res[0][2][k], res[3][2][k]), k
         assert np.array_equal(res[0][2][k], res[2][2][k]), k
+    b3 = res[3][0]
+    for k in ("flags", "counts", "first"):
+        assert np.array_equal(res[0][0][k], b3[k]), k
+    for r, c in enumerate(res[0][0]["counts"]):
+        m = min(int(c), 40)
+        if m > 0:
+            assert np.array_equal(res[0][0]["peaks"][r, :m], b3["peaks"][r, :m])
+            assert np.array_equal(res[0][0]["intervals"][r, :m], b3["intervals"][r, :m])
     (b0, f0, _), (b1, f1, _) = res[0], res[2]
     assert np.array_equal(b0["flags"], b1["flags"]) and np.array_equal(b0["counts"], b1["counts"])
     assert np.array_equal(b0["first"], b1["first"])
