@@ -419,47 +419,57 @@ __global__ void core_kernel(Sorted S, const int* cellOf, long long n, const unsi
     list_append(take, (int)i, sparse, nSparse);
 }
 
-// warp per listed point: neighbours within eps counted 32 at a time, whole
-// safe cells counted or skipped by their bounding boxes, early exit at minPts
+// block per listed point: neighbours within eps counted blockDim at a time
+// (__syncthreads_count), whole safe cells counted or skipped by their
+// bounding boxes, early exit at minPts. A point at the edge of a dense cell
+// (the basin maps put up to 225,000 points in one cell) may have to test
+// every point of it: a block spreads that scan over 8 warps. The cells whose
+// box the ball contains are counted before any cell is scanned.
 __global__ void core_sparse_kernel(Feat F, Sorted S, const int* cellOf, const int* sparse, int nSparse,
                                    const int* nbStart, const int* nbList, const unsigned char* unsafeCell,
                                    const double* boxLo, const double* boxHi, double eps, int minPts,
                                    unsigned char* core) {
-    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x;
     if (w >= nSparse) return;
     const int i = sparse[w];
     const int c = cellOf[i];
     double me[3] = {0, 0, 0};
     for (int d = 0; d < F.D; ++d) me[d] = F.f[d][i];
     const double eps2 = eps * eps;
-    int cnt = 0;  // the same in every lane
-    auto count_cell = [&](int cell) {
-        if (!unsafeCell[cell]) {
-            double near2, far2;
-            box_dist2(me, boxLo + 3 * (long long)cell, boxHi + 3 * (long long)cell, S.D, near2, far2);
-            if (near2 > eps2 * kBoxOut) return;
-            if (far2 < eps2 * kBoxIn) {
-                cnt += S.start[cell + 1] - S.start[cell];
-                return;
-            }
-        }
+    // box test of a safe cell: 0 skip, 1 count whole, 2 scan
+    auto classify = [&](int cell) {
+        if (unsafeCell[cell]) return 2;
+        double near2, far2;
+        box_dist2(me, boxLo + 3 * (long long)cell, boxHi + 3 * (long long)cell, S.D, near2, far2);
+        if (near2 > eps2 * kBoxOut) return 0;
+        if (far2 < eps2 * kBoxIn) return 1;
+        return 2;
+    };
+    int cnt = 0;  // the same in every thread
+    if (!unsafeCell[c]) cnt = S.start[c + 1] - S.start[c];  // one cell is within eps of itself
+    for (int e = nbStart[c]; e < nbStart[c + 1] && cnt < minPts; ++e) {
+        const int cell = nbList[e];
+        if (classify(cell) == 1) cnt += S.start[cell + 1] - S.start[cell];
+    }
+    auto scan_cell = [&](int cell) {
         const int end = S.start[cell + 1];
-        for (int p0 = S.start[cell]; p0 < end && cnt < minPts; p0 += 32) {
-            const int p = p0 + lane;
+        for (int p0 = S.start[cell]; p0 < end && cnt < minPts; p0 += blockDim.x) {
+            const int p = p0 + threadIdx.x;
             bool hit = false;
             if (p < end) {
                 double v[3];
                 S.load(p, v);
                 hit = sqrt(dist2(me, v, S.D)) <= eps;
             }
-            cnt += __popc(__ballot_sync(0xffffffffu, hit));
+            cnt += __syncthreads_count(hit);
         }
     };
-    if (!unsafeCell[c]) cnt = S.start[c + 1] - S.start[c];  // one cell is within eps of itself
-    else count_cell(c);
-    for (int e = nbStart[c]; e < nbStart[c + 1] && cnt < minPts; ++e) count_cell(nbList[e]);
-    if (lane == 0) core[i] = cnt >= minPts ? 1 : 0;
+    if (unsafeCell[c] && cnt < minPts) scan_cell(c);
+    for (int e = nbStart[c]; e < nbStart[c + 1] && cnt < minPts; ++e) {
+        const int cell = nbList[e];
+        if (classify(cell) == 2) scan_cell(cell);
+    }
+    if (threadIdx.x == 0) core[i] = cnt >= minPts ? 1 : 0;
 }
 
 // rep[c] = smallest core index of cell c (or -1); every core point of a safe
@@ -882,7 +892,7 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
         CK(cudaMemcpyAsync(&hSparse, nSparse, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         if (hSparse > 0) {
-            core_sparse_kernel<<<blocks((long long)hSparse * 32), kTPB, 0, st>>>(
+            core_sparse_kernel<<<hSparse, kTPB, 0, st>>>(
                 F, S, cellOf, sparse, hSparse, nbStart, nbList, unsafeCell, boxLo, boxHi, eps, minPts, core);
             note_launch();
         }
