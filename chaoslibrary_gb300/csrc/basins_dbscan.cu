@@ -58,19 +58,27 @@ __global__ void minmax_kernel(BasinsOut O, long long n, unsigned long long* mm, 
     }
 }
 
+// v = (f - lo) * (1 / (hi - lo)) per feature: the three reciprocals once per
+// block (a divide per point and feature would keep the FP64 pipe busy for
+// most of the kernel).
 __global__ void normalise_kernel(BasinsOut O, long long n, const unsigned long long* mm, double* F) {
+    __shared__ double slo[3], sinv[3];
+    __shared__ int sok[3];
+    if (threadIdx.x < 3) {
+        const int d = threadIdx.x;
+        const bool any = mm[d] != ~0ull;
+        const double lo = any ? ounkey(mm[d]) : 0.0, hi = any ? ounkey(mm[3 + d]) : 0.0;
+        slo[d] = lo;
+        sok[d] = any && hi > lo;
+        sinv[d] = sok[d] ? 1.0 / (hi - lo) : 0.0;
+    }
+    __syncthreads();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double f[3];
     raw_features(O, i, f);
-    for (int d = 0; d < 3; ++d) {
-        double v = 0.0;
-        if (O.flags[i] != 0 && mm[d] != ~0ull) {
-            const double lo = ounkey(mm[d]), hi = ounkey(mm[3 + d]);
-            v = hi > lo ? (f[d] - lo) / (hi - lo) : 0.0;
-        }
-        F[i * 3 + d] = v;
-    }
+    const bool in = O.flags[i] != 0;
+    for (int d = 0; d < 3; ++d) F[i * 3 + d] = in && sok[d] ? (f[d] - slo[d]) * sinv[d] : 0.0;
 }
 
 }  // namespace

@@ -2,7 +2,7 @@
 //
 // Both clusterings share one pipeline over points in a D-dimensional feature
 // space (D = 1..3), all integer/FP64 and bound by memory traffic:
-//   1. cell of every point: floor(f / side) per dimension, side = eps/sqrt(D)
+//   1. cell of every point: floor(f * (1/side)) per dimension, side = eps/sqrt(D)
 //      shrunk by 1e-9, so two points of one cell are always within eps and a
 //      neighbour within eps is at most R = 2 cells away per dimension;
 //   2. an open-addressing hash table of the occupied cells (64-bit packed
@@ -138,7 +138,11 @@ __global__ void add_offsets_kernel(int* out, const int* offsets, long long n) {
 inline unsigned blocks(long long n, int tpb = kTPB) { return (unsigned)((n + tpb - 1) / tpb); }
 
 // ---- grid construction -----------------------------------------------------
-__global__ void cell_key_kernel(Feat F, const int* include, long long n, double side, unsigned long long* key,
+// q = f * (1/side): the rounding of the product (|q| < 2^19: below 1e-10 of a
+// cell) stays far inside the 1e-9 by which the side is shrunk, so two points
+// of one cell are still within eps (a division here would cost the FP64 pipe
+// three divides per point for the same guarantee).
+__global__ void cell_key_kernel(Feat F, const int* include, long long n, double invSide, unsigned long long* key,
                                 unsigned char* unsafe) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -146,7 +150,7 @@ __global__ void cell_key_kernel(Feat F, const int* include, long long n, double 
     long long c[3] = {0, 0, 0};
     bool bad = false;
     for (int d = 0; d < F.D; ++d) {
-        const double q = F.f[d][i] / side;
+        const double q = F.f[d][i] * invSide;
         if (q != q) { c[0] = kLim + 5; c[1] = kLim + 5; c[2] = kLim + 5; bad = true; break; }
         long long v;
         if (q >= (double)kLim) { v = kLim; bad = true; }
@@ -158,19 +162,28 @@ __global__ void cell_key_kernel(Feat F, const int* include, long long n, double 
     unsafe[i] = bad ? 1 : 0;
 }
 
+// The lanes of a warp that carry the same cell key are served by one lane
+// (__match_any_sync): a basin map puts up to 225,000 points in one cell, and
+// neighbouring grid points mostly share theirs, so the hot cells' table slot,
+// counter and cursor see one access per warp instead of one per point.
 __global__ void hash_insert_kernel(const unsigned long long* key, long long n, unsigned long long* tab,
                                    unsigned long long mask, long long* slot) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned long long k = key[i];
-    if (k == kEmpty) { slot[i] = -1; return; }
-    unsigned long long h = mix(k) & mask;
-    for (unsigned long long probe = 0; probe <= mask; ++probe) {
-        const unsigned long long prev = atomicCAS(&tab[h], kEmpty, k);
-        if (prev == kEmpty || prev == k) { slot[i] = (long long)h; return; }
-        h = (h + 1) & mask;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long k = i < n ? key[i] : kEmpty;
+    const unsigned grp = __match_any_sync(0xffffffffu, k);
+    const int leader = __ffs(grp) - 1;
+    long long h = -1;
+    if (k != kEmpty && lane == leader) {
+        unsigned long long g = mix(k) & mask;
+        for (unsigned long long probe = 0; probe <= mask; ++probe) {
+            const unsigned long long prev = atomicCAS(&tab[g], kEmpty, k);
+            if (prev == kEmpty || prev == k) { h = (long long)g; break; }
+            g = (g + 1) & mask;
+        }  // the table has twice as many slots as points: a free slot is always found
     }
-    slot[i] = -1;  // unreachable: the table has twice as many slots as points
+    h = __shfl_sync(0xffffffffu, h, leader);
+    if (i < n) slot[i] = k == kEmpty ? -1 : h;
 }
 
 __global__ void occupied_kernel(const unsigned long long* tab, long long cap, int* occ) {
@@ -192,20 +205,26 @@ __global__ void cell_ids_kernel(const unsigned long long* tab, long long cap, co
 
 __global__ void point_cell_kernel(const long long* slot, long long n, const int* slotCell, int* cellOf, int* cnt) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (slot[i] < 0) { cellOf[i] = -1; return; }
-    const int c = slotCell[slot[i]];
-    cellOf[i] = c;
-    atomicAdd(&cnt[c], 1);
+    const int lane = threadIdx.x & 31;
+    const long long sl = i < n ? slot[i] : -1;
+    const int c = sl >= 0 ? slotCell[sl] : -1;
+    if (i < n) cellOf[i] = c;
+    const unsigned grp = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && lane == __ffs(grp) - 1) atomicAdd(&cnt[c], __popc(grp));
 }
 
 __global__ void scatter_kernel(Feat F, long long n, const int* cellOf, const int* start, int* cursor, int* order,
                                double* s0, double* s1, double* s2) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int c = cellOf[i];
+    const int lane = threadIdx.x & 31;
+    const int c = i < n ? cellOf[i] : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (c >= 0 && lane == leader) base = atomicAdd(&cursor[c], __popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
     if (c < 0) return;
-    const int pos = start[c] + atomicAdd(&cursor[c], 1);
+    const int pos = start[c] + base + __popc(grp & ((1u << lane) - 1u));
     order[pos] = (int)i;
     s0[pos] = F.f[0][i];
     if (F.D > 1) s1[pos] = F.f[1][i];
@@ -799,7 +818,7 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     NEED(!c.failed);
     include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include);
     note_launch();
-    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, side, key, unsafePt);
+    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, 1.0 / side, key, unsafePt);
     note_launch();
     CK(cudaMemsetAsync(tab, 0xff, cap * sizeof(unsigned long long), st));
     hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot);

@@ -232,8 +232,8 @@ def basins_features(system: int, tMax, nPts, h, ic, ranges, mut, wv, maxValue, t
 
 def basin_feature_matrix(feat: dict):
     """(amplitude, kept peak count, mean interval) per point -- the mean peak,
-    or the last sample without peaks -- min-max scaled over flag != 0 points;
-    returns (features n x 3, mask)."""
+    or the last sample without peaks -- min-max scaled over flag != 0 points,
+    (f - lo) * (1 / (hi - lo)); returns (features n x 3, mask)."""
     c = feat["counts"]
     f = np.stack([np.where(c > 0, feat["avg_peaks"], feat["last"]), c.astype(np.float64),
                   np.where(c > 0, feat["avg_intervals"], 0.0)], axis=1)
@@ -244,7 +244,7 @@ def basin_feature_matrix(feat: dict):
         hi = f[mask == 1].max(axis=0)
         for d in range(3):
             if hi[d] > lo[d]:
-                out[:, d] = np.where(mask == 1, (f[:, d] - lo[d]) / (hi[d] - lo[d]), 0.0)
+                out[:, d] = np.where(mask == 1, (f[:, d] - lo[d]) * (1.0 / (hi[d] - lo[d])), 0.0)
     return out, mask
 
 
