@@ -240,25 +240,45 @@ class Clocks:
 
 # ---- CPU leg (the oracle restatement of the reference algorithm) --------------------------
 def cpu_sample_lle(w, target_s=10.0):
+    """The LLE map on the host cores over a bounded sample of its points: the
+    reference's own per-thread code (its calculateSystem and step loop,
+    compiled for the host by oracle/build_ref.py, OpenMP over points) where
+    that build exists, else the oracle's C++ restatement."""
     from oracle import oracle as O
 
     nthreads = os.cpu_count() or 1
     n_all = w["nPts"] * w["nPts"]
-    args = (w["sysid"], w["tMax"], w["NT"], w["nPts"], w["h"], w["eps"], w["initialConditions"], w["ranges"],
-            w["indicesOfMutVars"], w["transientTime"], w["values"])
+    kind = "port"
+    try:
+        ref = O.RefLib(w["system"])
+        args = (w["tMax"], w["NT"], w["nPts"], w["h"], w["eps"], w["initialConditions"], w["ranges"],
+                w["indicesOfMutVars"], w["transientTime"], w["values"])
+
+        def run(b, e):
+            ref.lle_range(*args, b, e, nthreads=nthreads)
+        kind = "reference"
+    except (OSError, AttributeError):
+        args = (w["sysid"], w["tMax"], w["NT"], w["nPts"], w["h"], w["eps"], w["initialConditions"], w["ranges"],
+                w["indicesOfMutVars"], w["transientTime"], w["values"])
+
+        def run(b, e):
+            O.lle2d(*args, p_begin=b, p_end=e, nthreads=nthreads)
     probe = 2 * nthreads
     t = time.perf_counter()
-    O.lle2d(*args, p_begin=n_all // 2, p_end=n_all // 2 + probe, nthreads=nthreads)
+    run(n_all // 2, n_all // 2 + probe)
     dt = time.perf_counter() - t
     n = int(min(n_all, max(probe, probe * target_s / max(dt, 1e-3))))
     begin = n_all // 2 - n // 2
     t = time.perf_counter()
-    O.lle2d(*args, p_begin=begin, p_end=begin + n, nthreads=nthreads)
+    run(begin, begin + n)
     dt = time.perf_counter() - t
     steps = n * lle_steps_per_point(w)
-    return {"value": steps / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+    what = ("the reference's own calculateSystem and step loop (LLE/src/LLECUDA.cu) compiled for the host, "
+            "its transient by its loopCalculateDiscreteModel, twin at x + eps*e_x" if kind == "reference"
+            else "the oracle's C++ restatement")
+    return {"value": steps / dt, "unit": UNIT, "cores": nthreads, "kind": kind,
             "sample": f"{n} contiguous grid points from the middle of the 1024x1024 map, full 105,040 steps each, "
-                      f"FP64, {dt:.1f} s"}
+                      f"FP64, {dt:.1f} s; {what}"}
 
 
 def cpu_sample_spectrum(w, target_s=10.0):

@@ -5,7 +5,10 @@ functions named below verbatim into ``oracle/_ref/*.inc`` (git-ignored), and
 compile them with ``oracle/ref_harness.cpp`` and the CUDA host shim in
 ``oracle/ref_shim/`` into one shared library per plug-in system,
 ``oracle/_ref/libref_<system>.so``. Nothing here is shipped or called by the
-engine; the tests use these libraries to pin the oracle to the reference.
+engine; the tests use these libraries to pin the oracle to the reference, and
+``bench.py``'s CPU baseline times the reference's own LLE code through them.
+Where the reference checkout is absent (the benchmark machine), the recipe
+compiles the extracted files and headers already under ``oracle/_ref``.
 
 The reference's host drivers (which allocate device memory and launch
 kernels) and its cuRAND-seeded LLE transient are not built.
@@ -111,8 +114,8 @@ def write_inc(src: Path, namespace: str, funcs: list[str], shared: str | None, d
     text = src.read_text(encoding="utf-8", errors="replace")
     parts = [f"// extracted verbatim from {src} by oracle/build_ref.py", f"namespace {namespace} {{",
              extract_constants(text)]
-    if shared:
-        parts.append(f"double {shared}[4096];")
+    if shared:  # the kernel's shared memory: one array per replaying host thread
+        parts.append(f"thread_local double {shared}[4096];")
     for f in funcs:
         parts.append(extract_function(text, f))
     parts.append("}")
@@ -131,27 +134,50 @@ def system_header(name: str) -> str:
             f"// the {macro} block of {REF / 'systems' / 'systems.cuh'}\n" + m.group(1) + "\n")
 
 
-def available() -> bool:
+STAGED = OUT / "gpu_src"  # the reference's headers, staged by oracle/build_ref_gpu.py
+
+
+def _checkout() -> bool:
     return (REF / "Bifurcation" / "src" / "bifurcationCUDA.cu").is_file()
+
+
+def _staged() -> bool:
+    """The extracted functions, the system headers and the reference's headers
+    are already under oracle/_ref (they travel with the tree to a machine
+    without the reference checkout, where this recipe then compiles them)."""
+    return all((OUT / f).is_file() for f in ("ref_bif.inc", "ref_basins.inc", "ref_lle.inc")) and \
+        (STAGED / "Bifurcation/include").is_dir()
+
+
+def available() -> bool:
+    return _checkout() or _staged()
 
 
 def build(systems: list[str] | None = None, verbose: bool = False) -> list[Path]:
     if not available():
         raise FileNotFoundError(f"reference sources not found under {REF}")
     OUT.mkdir(exist_ok=True)
-    write_inc(REF / "Bifurcation/src/bifurcationCUDA.cu", "Bifurcation_constants", BIF_FUNCS, "s", OUT / "ref_bif.inc")
-    write_inc(REF / "Basins/src/basinsCUDA.cu", "basinsGPU", BASINS_FUNCS, None, OUT / "ref_basins.inc")
-    write_inc(REF / "LLE/src/LLECUDA.cu", "LLE_constants", LLE_FUNCS, "sh_mem", OUT / "ref_lle.inc")
+    fresh = _checkout()
+    inc_root = REF if fresh else STAGED
+    if fresh:
+        write_inc(REF / "Bifurcation/src/bifurcationCUDA.cu", "Bifurcation_constants", BIF_FUNCS, "s",
+                  OUT / "ref_bif.inc")
+        write_inc(REF / "Basins/src/basinsCUDA.cu", "basinsGPU", BASINS_FUNCS, None, OUT / "ref_basins.inc")
+        write_inc(REF / "LLE/src/LLECUDA.cu", "LLE_constants", LLE_FUNCS, "sh_mem", OUT / "ref_lle.inc")
     built = []
     for name in systems or list(PLUGINS) + list(REF_SYSTEMS):
         sysdir = OUT / f"sys_{name}"
         sysdir.mkdir(exist_ok=True)
-        (sysdir / "systems.cuh").write_text(system_header(name))
+        if fresh or name in PLUGINS:
+            (sysdir / "systems.cuh").write_text(system_header(name))
+        elif not (sysdir / "systems.cuh").is_file():
+            continue
         lib = OUT / f"libref_{name}.so"
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-w",
                f"-I{HERE / 'ref_shim'}", f"-I{sysdir}", f"-I{OUT}",
-               f"-I{REF / 'Bifurcation/include'}", f"-I{REF / 'Basins/include'}", f"-I{REF / 'LLE/include'}",
-               f"-I{REF / 'debri'}", str(HERE / "ref_harness.cpp"), "-o", str(lib)]
+               f"-I{inc_root / 'Bifurcation/include'}", f"-I{inc_root / 'Basins/include'}",
+               f"-I{inc_root / 'LLE/include'}", f"-I{inc_root / 'debri'}", str(HERE / "ref_harness.cpp"),
+               "-o", str(lib)]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)

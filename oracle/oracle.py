@@ -295,6 +295,8 @@ class RefLib:
         L.refh_basins_dbscan.argtypes = [_dp, _dp, _ip, _ip, C.c_int, C.c_double]
         L.refh_lle.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _ip,
                                C.c_double, _dp, C.c_int, _dp]
+        L.refh_lle_range.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp,
+                                     _ip, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _dp, C.c_int]
 
     def steps(self, x0, a, h, n):
         x = _d(x0).copy()
@@ -349,6 +351,16 @@ class RefLib:
         labels = np.zeros(ap.size, np.int32)
         self.L.refh_basins_dbscan(ap, ai, labels, fl, ap.size, eps)
         return labels
+
+    def lle_range(self, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values, p_begin, p_end,
+                  nthreads=0):
+        """LLE2D points [p_begin, p_end) (p = b*nPts + a) by the reference's own
+        per-thread code, spread over nthreads host threads."""
+        ic, values = _d(ic), _d(values)
+        out = np.zeros(p_end - p_begin)
+        self.L.refh_lle_range(tMax, NT, nPts, h, eps, ic.size, ic, _d(ranges), _i(mut), transientTime, values,
+                              values.size, p_begin, p_end, out, nthreads)
+        return out
 
     def lle(self, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values):
         ic, values = _d(ic), _d(values)

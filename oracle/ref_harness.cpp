@@ -25,10 +25,13 @@
 #include <LLECUDA.cuh>
 #include <systems.cuh>
 
+#include <omp.h>
+
 #include <cstring>
+#include <memory>
 #include <vector>
 
-dim3 threadIdx, blockIdx, blockDim;
+thread_local dim3 threadIdx, blockIdx, blockDim;
 
 #include "ref_bif.inc"
 #include "ref_basins.inc"
@@ -214,6 +217,53 @@ void refh_lle(double tMax, double NT, int nPts, double h, double eps, int nIC, c
         }
     for (int a = 0; a < nPts; ++a)
         for (int b = 0; b < nPts; ++b) out[(size_t)b * nPts + a] = rows[a][b];
+    delete[] linA;
+    delete[] linB;
+}
+
+// The same LLE2D points [pBegin, pEnd) (p = b*nPts + a, the CSV layout) with
+// the replayed threads spread over nthreads host threads (OpenMP; the launch
+// indices and the shared-memory array are thread-local): the reference's own
+// per-thread code as a CPU baseline. out[p - pBegin].
+void refh_lle_range(double tMax, double NT, int nPts, double h, double eps, int nIC, const double* ic,
+                    const double* ranges, const int* mut, double transientTime, const double* values, int nValues,
+                    long long pBegin, long long pEnd, double* out, int nthreads) {
+    using namespace LLE_constants;
+    int ntp = static_cast<int>(NT / h);
+    int trans = static_cast<int>(transientTime / h);
+    int all = static_cast<int>(tMax / h);
+    int calcBlocks = static_cast<int>(all / ntp) + 1;
+    double* linA = linspace(ranges[0], ranges[1], nPts);
+    double* linB = linspace(ranges[2], ranges[3], nPts);
+    d_idxParamA = mut[0]; d_idxParamB = mut[1]; d_size_linspace_A = nPts; d_size_linspace_B = nPts;
+    d_h = h; d_transTime = transientTime; d_tMax = tMax; d_Nt_steps = ntp; d_paramsSize = nValues;
+    d_XSize = nIC; d_amountOfNTPoints = ntp; d_amountOfTransPoints = trans; d_amountOfAllpoints = all;
+    d_amountOfCalcBlocks = calcBlocks; d_eps = eps;
+    const int per = 2 * nIC + nValues;
+    // whole-map index space, touched only at the sampled points (no zero fill)
+    std::unique_ptr<double[]> semi(new double[(size_t)nPts * nPts * per]);
+    std::unique_ptr<double[]> store(new double[(size_t)nPts * nPts]);
+    std::vector<double*> rows(nPts);
+    for (int a = 0; a < nPts; ++a) rows[a] = store.get() + (size_t)a * nPts;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long p = pBegin; p < pEnd; ++p) {
+        const int a = (int)(p % nPts), b = (int)(p / nPts);
+        rows[a][b] = 0.0;
+        double* r = semi.get() + ((size_t)a * nPts + b) * per;
+        for (int i = 0; i < nIC; ++i) r[i] = ic[i];
+        for (int i = 0; i < nValues; ++i) r[nIC + i] = values[i];
+        r[nIC + mut[0]] = linA[a];
+        r[nIC + mut[1]] = linB[b];
+        loopCalculateDiscreteModel(r, r + nIC, trans);
+        for (int i = 0; i < nIC; ++i) r[nIC + nValues + i] = r[i];
+        r[nIC + nValues] = r[0] + eps;
+        threadIdx = dim3{0, 0, 0};
+        blockDim = dim3{1, 1, 1};
+        blockIdx = dim3{(unsigned)a, (unsigned)b, 0};
+        calculateSystem(nullptr, nullptr, linA, linB, semi.get(), rows.data());
+        out[p - pBegin] = rows[a][b];
+    }
     delete[] linA;
     delete[] linB;
 }

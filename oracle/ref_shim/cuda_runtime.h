@@ -1,7 +1,7 @@
 // Host shim used ONLY to compile the reference's per-thread CUDA functions as
 // plain host functions for the checker (see oracle/build_ref.py). It maps the
-// CUDA qualifiers to nothing, a launch index to three globals the harness
-// sets before each "thread", and the few device intrinsics the extracted code
+// CUDA qualifiers to nothing, a launch index to three thread-local globals the
+// harness sets before each "thread", and the few device intrinsics the extracted code
 // uses to their host equivalents (same IEEE rounding for the _rn forms; the
 // fast __logf becomes the accurate logf).
 #pragma once
@@ -21,7 +21,7 @@
 struct dim3 {
     unsigned x, y, z;
 };
-extern dim3 threadIdx, blockIdx, blockDim;
+extern thread_local dim3 threadIdx, blockIdx, blockDim;  // per host thread (OpenMP replays)
 typedef int cudaError_t;
 
 inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
