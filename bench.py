@@ -302,21 +302,35 @@ def cpu_sample_spectrum(w, target_s=10.0):
 
 
 def cpu_sample_sweep(w, kind, target_s=10.0):
+    """A sweep on the host cores over a bounded sample of its points: the
+    reference's own per-thread kernels (transient, recorded loop, peak finder
+    or peak averages; compiled for the host by oracle/build_ref.py, replayed
+    through its own chunking, OpenMP over points) where that build exists,
+    else the oracle's C++ restatement."""
     from oracle import oracle as O
 
     nthreads = os.cpu_count() or 1
     dim = 1 if kind == "bif1d" else 2
     n_all = w["nPts"] ** dim
     probe = 2 * nthreads
+    args = (w["tMax"], w["nPts"], w["h"], w["initialConditions"], w["ranges"], w["indicesOfMutVars"],
+            w["writableVar"], w["maxValue"], w["transientTime"], w["values"])
+    impl = "port"
+    try:
+        ref = O.RefLib(w["system"])
+        impl = "reference"
+    except (OSError, AttributeError):
+        ref = None
+
     def run(b, e):
-        if kind == "bif1d":
-            O.bifurcation(w["sysid"], 1, w["tMax"], w["nPts"], w["h"], w["initialConditions"], w["ranges"],
-                          w["indicesOfMutVars"], w["writableVar"], w["maxValue"], w["transientTime"], w["values"],
-                          cap=64, p_begin=b, p_end=e, nthreads=nthreads)
+        if ref is not None and kind in ("bif1d", "bif2d"):
+            ref.bifurcation_range(dim, *args, b, e, nthreads=nthreads)
+        elif ref is not None:
+            ref.basins_range(*args, b, e, nthreads=nthreads)
+        elif kind in ("bif1d", "bif2d"):
+            O.bifurcation(w["sysid"], dim, *args, cap=64, p_begin=b, p_end=e, nthreads=nthreads)
         else:
-            O.basins_features(w["sysid"], w["tMax"], w["nPts"], w["h"], w["initialConditions"], w["ranges"],
-                              w["indicesOfMutVars"], w["writableVar"], w["maxValue"], w["transientTime"], w["values"],
-                              p_begin=b, p_end=e, nthreads=nthreads)
+            O.basins_features(w["sysid"], *args, p_begin=b, p_end=e, nthreads=nthreads)
     t = time.perf_counter()
     run(0, probe)
     dt = time.perf_counter() - t
@@ -325,10 +339,14 @@ def cpu_sample_sweep(w, kind, target_s=10.0):
     t = time.perf_counter()
     run(b, b + n)
     dt = time.perf_counter() - t
-    return {"value": n * sweep_steps_per_point(w) / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n} of {n_all} grid points, full horizon, FP64, {dt:.1f} s"
+    what = ("the reference's own per-thread kernels compiled for the host" if impl == "reference"
+            else "the oracle's C++ restatement")
+    return {"value": n * sweep_steps_per_point(w) / dt, "unit": UNIT, "cores": nthreads, "kind": impl,
+            "sample": f"{n} of {n_all} grid points, full horizon, FP64, {dt:.1f} s; {what}"
                       + ("; per-point integration and features (the clustering needs the whole map and is not "
-                         "in the sample)" if kind == "basins" else "")}
+                         "in the sample)" if kind == "basins" else "")
+                      + ("; per-point integration and peaks (the per-point clustering is not in the sample)"
+                         if kind == "bif2d" else "")}
 
 
 def reference_arm(args, ws, rank):

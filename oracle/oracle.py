@@ -295,6 +295,12 @@ class RefLib:
         L.refh_basins_dbscan.argtypes = [_dp, _dp, _ip, _ip, C.c_int, C.c_double]
         L.refh_lle.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp, _ip,
                                C.c_double, _dp, C.c_int, _dp]
+        L.refh_bifurcation_range.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip,
+                                             C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_int, C.c_longlong,
+                                             C.c_longlong, _ip, C.c_int]
+        L.refh_basins_range.argtypes = [C.c_double, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, C.c_int,
+                                        C.c_double, C.c_double, _dp, C.c_int, C.c_int, C.c_longlong, C.c_longlong,
+                                        _ip, _dp, _dp, C.c_int]
         L.refh_lle_range.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, _dp, _dp,
                                      _ip, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _dp, C.c_int]
 
@@ -351,6 +357,28 @@ class RefLib:
         labels = np.zeros(ap.size, np.int32)
         self.L.refh_basins_dbscan(ap, ai, labels, fl, ap.size, eps)
         return labels
+
+    def bifurcation_range(self, dim, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values,
+                          p_begin, p_end, preScaller=1, nthreads=0):
+        """Kept-peak counts of points [p_begin, p_end) by the reference's own
+        per-thread code (its chunking), spread over nthreads host threads."""
+        ic, values = _d(ic), _d(values)
+        counts = np.zeros(p_end - p_begin, np.int32)
+        self.L.refh_bifurcation_range(dim, tMax, nPts, h, ic.size, ic, _d(ranges), _i(mut), wv, maxValue,
+                                      transientTime, values, values.size, preScaller, p_begin, p_end, counts,
+                                      nthreads)
+        return counts
+
+    def basins_range(self, tMax, nPts, h, ic, ranges, mut, wv, maxValue, transientTime, values, p_begin, p_end,
+                     preScaller=1, nthreads=0):
+        """Flags and features of points [p_begin, p_end) by the reference's own
+        per-thread code (its chunking), spread over nthreads host threads."""
+        ic, values = _d(ic), _d(values)
+        n = p_end - p_begin
+        flags, ap, ai = np.zeros(n, np.int32), np.zeros(n), np.zeros(n)
+        self.L.refh_basins_range(tMax, nPts, h, ic.size, ic, _d(ranges), _i(mut), wv, maxValue, transientTime,
+                                 values, values.size, preScaller, p_begin, p_end, flags, ap, ai, nthreads)
+        return dict(flags=flags, avg_peaks=ap, avg_intervals=ai)
 
     def lle_range(self, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime, values, p_begin, p_end,
                   nthreads=0):

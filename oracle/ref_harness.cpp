@@ -27,6 +27,7 @@
 
 #include <omp.h>
 
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -219,6 +220,78 @@ void refh_lle(double tMax, double NT, int nPts, double h, double eps, int nIC, c
         for (int b = 0; b < nPts; ++b) out[(size_t)b * nPts + a] = rows[a][b];
     delete[] linA;
     delete[] linB;
+}
+
+// bifurcation1D / bifurcation2D points [pBegin, pEnd) through the reference's
+// own chunking (d_amountOfCalculatedPoints, d_nPtsLimiter), chunks of up to
+// 4096 points, the replayed threads of a chunk spread over nthreads host
+// threads (OpenMP; launch indices and shared memory are thread-local): the
+// transient, recorded and peak-finder kernels of each point in turn.
+// counts[p - pBegin] = the point's amountOfPeaks after peakFinderCUDA.
+void refh_bifurcation_range(int dim, double tMax, int nPts, double h, int nIC, const double* ic,
+                            const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
+                            const double* values, int nValues, int preScaller, long long pBegin, long long pEnd,
+                            int* counts, int nthreads) {
+    using namespace Bifurcation_constants;
+    const int B = tMax / h / preScaller;
+    const int S = transientTime / h;
+    const long long N = dim == 1 ? (long long)nPts : (long long)nPts * nPts;
+    const long long chunk = 4096;
+    d_tMax = tMax; d_nPts = nPts; d_h = h; d_amountOfInitialConditions = nIC; d_writableVar = wv;
+    d_maxValue = maxValue; d_transientTime = transientTime; d_amountOfValues = nValues;
+    d_preScaller = preScaller; d_amountOfPointsInBlock = B; d_originalNPtsLimiter = (int)std::min(chunk, N);
+    d_amountOfPointsForSkip = S; d_dimension = dim;
+    std::unique_ptr<double[]> data(new double[(size_t)chunk * B]), intervals(new double[(size_t)chunk * B]);
+    std::unique_ptr<double[]> semi(new double[(size_t)chunk * (nIC + nValues)]);
+    std::unique_ptr<int[]> amount(new int[chunk]);
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    for (long long c0 = pBegin; c0 < pEnd; c0 += chunk) {
+        const long long cnt = std::min(chunk, pEnd - c0);
+        d_nPtsLimiter = (int)cnt;
+        d_amountOfCalculatedPoints = (int)c0;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long long i = 0; i < cnt; ++i) {
+            as_thread(i);
+            calculateTransTimeCUDA((double*)ranges, (int*)mut, (double*)ic, values, semi.get(), amount.get());
+            calculateDiscreteModelCUDA((double*)ranges, (int*)mut, (double*)ic, values, data.get(), semi.get(),
+                                       amount.get());
+            peakFinderCUDA(data.get(), amount.get(), data.get(), intervals.get(), h * (double)preScaller);
+            counts[c0 - pBegin + i] = amount[i];
+        }
+    }
+}
+
+// basinsOfAttraction_2's per-point kernels for points [pBegin, pEnd) of the
+// nPts^2 grid, chunked and replayed as refh_bifurcation_range: flags and
+// features into helpful / avgPeaks / avgIntervals[p - pBegin].
+void refh_basins_range(double tMax, int nPts, double h, int nIC, const double* ic, const double* ranges,
+                       const int* mut, int wv, double maxValue, double transientTime, const double* values,
+                       int nValues, int preScaller, long long pBegin, long long pEnd, int* helpful,
+                       double* avgPeaks, double* avgIntervals, int nthreads) {
+    using namespace basinsGPU;
+    const int B = tMax / h / preScaller;
+    const int S = transientTime / h;
+    const long long chunk = 4096;
+    d_h = h; d_tMax = tMax; d_nPts = nPts; d_amountOfIterations = 1; d_amountOfInitialConditions = nIC;
+    d_amountOfValues = nValues; d_amountOfPointsInBlock = B; d_amountOfPointsForSkip = S; d_writableVar = wv;
+    d_maxValue = maxValue; d_preScaller = preScaller; d_dimension = 2;
+    std::unique_ptr<double[]> data(new double[(size_t)chunk * B]), intervals(new double[(size_t)chunk * B]);
+    std::unique_ptr<double[]> semi(new double[(size_t)chunk * (nIC + nValues)]);
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    for (long long c0 = pBegin; c0 < pEnd; c0 += chunk) {
+        const long long cnt = std::min(chunk, pEnd - c0);
+        d_nPtsLimiter = (int)cnt;
+        d_amountOfCalculatedPoints = (int)c0;
+        int* hf = helpful + (c0 - pBegin);
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long long i = 0; i < cnt; ++i) {
+            as_thread(i);
+            calculateTransTimeCUDA((double*)ranges, (int*)mut, (double*)ic, values, semi.get(), hf);
+            calculateDiscreteModelCUDA((double*)ranges, (int*)mut, (double*)ic, values, data.get(), semi.get(), hf);
+            avgPeakFinderCUDA(data.get(), B, (int)cnt, avgPeaks + (c0 - pBegin), avgIntervals + (c0 - pBegin),
+                              data.get(), intervals.get(), hf, h * preScaller);
+        }
+    }
 }
 
 // The same LLE2D points [pBegin, pEnd) (p = b*nPts + a, the CSV layout) with
