@@ -121,3 +121,18 @@ def test_dbscan_compat_grid_equals_bfs(oracle):
         a = oracle.dbscan_compat(ap, ai, flags, 0.02, "grid")
         b = oracle.dbscan_compat(ap, ai, flags, 0.02, "bfs")
         assert np.array_equal(a, b)
+
+
+def test_threaded_range_replays_equal_the_full_replays(refs):
+    """The chunked, multi-threaded replays of the reference's kernels (the CPU
+    baselines of bench.py) give the sequential full replay's results."""
+    R = refs["lorenz"]
+    kw = (10.0, 50, 0.01, [0.1, 0.1, 0.1], [20.0, 200.0], [1], 0, 1e4, 5.0, [10.0, 28.0, 8.0 / 3.0])
+    assert np.array_equal(R.bifurcation(1, *kw)["counts"][7:43], R.bifurcation_range(1, *kw, 7, 43, nthreads=4))
+    kb = (4.0, 24, 0.01, [0.0, 0.0, 27.0], [-30.0, 30.0, -30.0, 30.0], [0, 1], 0, 1e8, 5.0, [10.0, 24.0, 8.0 / 3.0])
+    full, part = R.basins(*kb), R.basins_range(*kb, 100, 576, nthreads=4)
+    for k in ("flags", "avg_peaks", "avg_intervals"):
+        assert np.array_equal(np.asarray(full[k])[100:576], part[k]), k
+    kl = (20.0, 0.1, 12, 0.01, 1e-8, [1.0, 1.0, 1.0], [0.1, 0.4, 2.0, 10.0], [0, 2], 5.0, [0.2, 0.2, 5.7])
+    Rr = refs["rossler"]
+    assert np.array_equal(Rr.lle(*kl)[5:130], Rr.lle_range(*kl, 5, 130, nthreads=4))
