@@ -10,6 +10,8 @@
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -70,6 +72,54 @@ template <class T, class F> void write_matrix(std::ofstream& o, const T* v, long
     }
 }
 
+// Runs a C-ABI body and turns a failed host allocation (or any other C++
+// exception) into a status: nothing thrown here crosses the C boundary.
+template <class F> int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return chaos::set_error(CHAOS_E_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return chaos::set_error(CHAOS_E_IO, "%s", e.what());
+    }
+}
+
+// Every kept peak of a 1-D sweep: a first pass with at most 1024 rows per
+// point, then, only when some point kept more, a second pass with rows for the
+// largest count. Host memory follows the peaks that exist, not B/2 rows per
+// point (B can be 1e7 for a long sweep at a small step).
+struct Bif1dRows {
+    std::vector<int> counts, flags;
+    std::vector<double> first, peaks, intervals;
+    int cap = 1;
+};
+
+int bif1d_rows(int gridMode, double tMax, int nPts, double h, int amountOfInitialConditions,
+               const double* initialConditions, const double* ranges, const int* indicesOfMutVars, int writableVar,
+               double maxValue, double transientTime, const double* values, int amountOfValues, int preScaller,
+               int capFull, Bif1dRows& r) {
+    chaos_exec ex = active_exec();
+    int cap = std::max(1, std::min(capFull, 1024));
+    for (int pass = 0; pass < 2; ++pass) {
+        r.counts.assign(nPts, 0);
+        r.flags.assign(nPts, 0);
+        r.first.assign(nPts, 0.0);
+        r.peaks.assign((size_t)nPts * cap, 0.0);
+        r.intervals.assign((size_t)nPts * cap, 0.0);
+        int rc = chaos_bifurcation_sweep(&ex, active_system(), 1, gridMode, tMax, nPts, h, amountOfInitialConditions,
+                                         initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
+                                         transientTime, values, amountOfValues, preScaller, 0.0, cap,
+                                         r.counts.data(), r.flags.data(), r.first.data(), r.peaks.data(),
+                                         r.intervals.data(), nullptr);
+        if (rc) return rc;
+        const int mx = *std::max_element(r.counts.begin(), r.counts.end());
+        r.cap = cap;
+        if (mx <= cap) return CHAOS_OK;
+        cap = mx;
+    }
+    return CHAOS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -93,73 +143,76 @@ int chaos_compat_bifurcation1D(double tMax, int nPts, double h, int amountOfInit
                                const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
                                int writableVar, double maxValue, double transientTime, const double* values,
                                int amountOfValues, int preScaller, const char* OUT_FILE_PATH) {
-    if (nPts < 2 || !(h > 0) || preScaller < 1) return chaos::set_error(CHAOS_E_ARGS, "bad sweep arguments");
-    const int B = (int)(tMax / h / preScaller);
-    const int cap = B / 2 > 0 ? B / 2 : 1;
-    std::vector<int> counts(nPts), flags(nPts);
-    std::vector<double> first(nPts), peaks((size_t)nPts * cap), intervals((size_t)nPts * cap);
-    chaos_exec ex = active_exec();
-    int rc = chaos_bifurcation1d(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions,
-                                 ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values,
-                                 amountOfValues, preScaller, cap, counts.data(), flags.data(), first.data(),
-                                 peaks.data(), intervals.data());
-    if (rc) return rc;
-    std::ofstream o(OUT_FILE_PATH);
-    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
-    o << ranges[0] << " " << ranges[1] << "\n";
-    o << std::setprecision(12);
-    for (int k = 0; k < nPts; ++k) {
-        const double p = host_grid_value(k, nPts, ranges[0], ranges[1]);
-        if (counts[k] == -1) {
-            o << p << ", " << first[k] << ", " << 0 << '\n';
-        } else {
-            for (int j = 0; j < counts[k]; ++j)
-                o << p << ", " << peaks[(size_t)k * cap + j] << ", " << intervals[(size_t)k * cap + j] << '\n';
+    return guarded([&]() -> int {
+        if (nPts < 2 || !(h > 0) || preScaller < 1) return chaos::set_error(CHAOS_E_ARGS, "bad sweep arguments");
+        const int B = (int)(tMax / h / preScaller);
+        Bif1dRows r;
+        int rc = bif1d_rows(0, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                            indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
+                            preScaller, B / 2 > 0 ? B / 2 : 1, r);
+        if (rc) return rc;
+        std::ofstream o(OUT_FILE_PATH);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+        o << ranges[0] << " " << ranges[1] << "\n";
+        o << std::setprecision(12);
+        for (int k = 0; k < nPts; ++k) {
+            const double p = host_grid_value(k, nPts, ranges[0], ranges[1]);
+            if (r.counts[k] == -1) {
+                o << p << ", " << r.first[k] << ", " << 0 << '\n';
+            } else {
+                for (int j = 0; j < r.counts[k]; ++j)
+                    o << p << ", " << r.peaks[(size_t)k * r.cap + j] << ", " << r.intervals[(size_t)k * r.cap + j]
+                      << '\n';
+            }
         }
-    }
-    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+        return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_bifurcation2D(double tMax, int nPts, double h, int amountOfInitialConditions,
                                const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
                                int writableVar, double maxValue, double transientTime, const double* values,
                                int amountOfValues, int preScaller, double eps, const char* OUT_FILE_PATH) {
-    if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
-    const long long n = (long long)nPts * nPts;
-    std::vector<int> labels(n);
-    chaos_exec ex = active_exec();
-    int rc = chaos_bifurcation2d(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions,
-                                 ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values,
-                                 amountOfValues, preScaller, eps, labels.data(), nullptr);
-    if (rc) return rc;
-    std::ofstream o(OUT_FILE_PATH);
-    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
-    o << ranges[0] << " " << ranges[1] << "\n";
-    o << ranges[2] << " " << ranges[3] << "\n";
-    o << std::setprecision(12);
-    write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
-    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+        const long long n = (long long)nPts * nPts;
+        std::vector<int> labels(n);
+        chaos_exec ex = active_exec();
+        int rc = chaos_bifurcation2d(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions,
+                                     ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                     amountOfValues, preScaller, eps, labels.data(), nullptr);
+        if (rc) return rc;
+        std::ofstream o(OUT_FILE_PATH);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+        o << ranges[0] << " " << ranges[1] << "\n";
+        o << ranges[2] << " " << ranges[3] << "\n";
+        o << std::setprecision(12);
+        write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+        return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_LLE2D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
                        int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                        int writableVar, double maxValue, double transientTime, const double* values,
                        int amountOfValues, const char* OUT_FILE_PATH) {
-    if (nPts < 1) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 1");
-    const long long n = (long long)nPts * nPts;
-    std::vector<double> lle(n);
-    chaos_exec ex = active_exec();
-    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
-    std::ofstream o(OUT_FILE_PATH);
-    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
-    o << ranges[0] << " " << ranges[1] << "\n";
-    o << ranges[2] << " " << ranges[3] << "\n";
-    int rc = chaos_lle2d(&ex, active_system(), tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
-                         ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
-                         lle.data());
-    if (rc) return rc;
-    write_matrix(o, lle.data(), n, nPts, [](std::ofstream& s, double v) { s << (std::isnan(v) ? 0 : v); });
-    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        if (nPts < 1) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 1");
+        const long long n = (long long)nPts * nPts;
+        std::vector<double> lle(n);
+        chaos_exec ex = active_exec();
+        if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
+        std::ofstream o(OUT_FILE_PATH);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+        o << ranges[0] << " " << ranges[1] << "\n";
+        o << ranges[2] << " " << ranges[3] << "\n";
+        int rc = chaos_lle2d(&ex, active_system(), tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
+                             ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues,
+                             lle.data());
+        if (rc) return rc;
+        write_matrix(o, lle.data(), n, nPts, [](std::ofstream& s, double v) { s << (std::isnan(v) ? 0 : v); });
+        return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_basinsOfAttraction_2(double tMax, int nPts, double h, int amountOfInitialConditions,
@@ -167,30 +220,32 @@ int chaos_compat_basinsOfAttraction_2(double tMax, int nPts, double h, int amoun
                                       const int* indicesOfMutVars, int writableVar, double maxValue,
                                       double transientTime, const double* values, int amountOfValues,
                                       int preScaller, double eps, const char* OUT_FILE_PATH) {
-    if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
-    const long long n = (long long)nPts * nPts;
-    std::vector<int> labels(n), flags(n);
-    std::vector<double> ap(n), ai(n);
-    chaos_exec ex = active_exec();
-    int rc = chaos_basins(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
-                          indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
-                          eps, labels.data(), ap.data(), ai.data(), flags.data());
-    if (rc) return rc;
-    const std::string base(OUT_FILE_PATH);
-    const std::string paths[4] = {base, base + "_1.csv", base + "_2.csv", base + "_3.csv"};
-    for (int f = 0; f < 4; ++f) {
-        std::ofstream o(paths[f]);
-        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", paths[f].c_str());
-        o << std::setprecision(15);
-        o << ranges[0] << " " << ranges[1] << "\n";
-        o << ranges[2] << " " << ranges[3] << "\n";
-        if (f == 0) write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
-        if (f == 1) write_matrix(o, ap.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
-        if (f == 2) write_matrix(o, ai.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
-        if (f == 3) write_matrix(o, flags.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
-        if (!o.good()) return chaos::set_error(CHAOS_E_IO, "write failed: %s", paths[f].c_str());
-    }
-    return CHAOS_OK;
+    return guarded([&]() -> int {
+        if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+        const long long n = (long long)nPts * nPts;
+        std::vector<int> labels(n), flags(n);
+        std::vector<double> ap(n), ai(n);
+        chaos_exec ex = active_exec();
+        int rc = chaos_basins(&ex, active_system(), tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                              indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                              eps, labels.data(), ap.data(), ai.data(), flags.data());
+        if (rc) return rc;
+        const std::string base(OUT_FILE_PATH);
+        const std::string paths[4] = {base, base + "_1.csv", base + "_2.csv", base + "_3.csv"};
+        for (int f = 0; f < 4; ++f) {
+            std::ofstream o(paths[f]);
+            if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", paths[f].c_str());
+            o << std::setprecision(15);
+            o << ranges[0] << " " << ranges[1] << "\n";
+            o << ranges[2] << " " << ranges[3] << "\n";
+            if (f == 0) write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+            if (f == 1) write_matrix(o, ap.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
+            if (f == 2) write_matrix(o, ai.data(), n, nPts, [](std::ofstream& s, double v) { s << v; });
+            if (f == 3) write_matrix(o, flags.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+            if (!o.good()) return chaos::set_error(CHAOS_E_IO, "write failed: %s", paths[f].c_str());
+        }
+        return CHAOS_OK;
+    });
 }
 
 // ---- the legacy library's analyses (namespace old_library, debri/hostLibrary.cuh) ----
@@ -210,21 +265,17 @@ static int legacy_bif1d(int gridMode, double tMax, int nPts, double h, int amoun
     const double hMin = stepAxis ? std::min(ranges[0], ranges[1]) * (1.0 - 1e-9) : h;
     if (!(hMin > 0)) return chaos::set_error(CHAOS_E_ARGS, "need a positive step");
     const int B = (int)(tMax / hMin / preScaller);
-    const int cap = B / 2 > 0 ? B / 2 : 1;
-    std::vector<int> counts(nPts), flags(nPts);
-    std::vector<double> peaks((size_t)nPts * cap);
-    chaos_exec ex = active_exec();
-    int rc = chaos_bifurcation_sweep(&ex, active_system(), 1, gridMode, tMax, nPts, h, amountOfInitialConditions,
-                                     initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
-                                     transientTime, values, amountOfValues, preScaller, 0.0, cap, counts.data(),
-                                     flags.data(), nullptr, peaks.data(), nullptr, nullptr);
+    Bif1dRows r;
+    int rc = bif1d_rows(gridMode, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                        B / 2 > 0 ? B / 2 : 1, r);
     if (rc) return rc;
     std::ofstream o(OUT_FILE_PATH);
     if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
     o << std::setprecision(12);
     for (int k = 0; k < nPts; ++k) {
         const double p = host_grid_value(k, nPts, ranges[0], ranges[1]);
-        for (int j = 0; j < counts[k] && j < cap; ++j) o << p << ", " << peaks[(size_t)k * cap + j] << '\n';
+        for (int j = 0; j < r.counts[k]; ++j) o << p << ", " << r.peaks[(size_t)k * r.cap + j] << '\n';
     }
     return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
 }
@@ -308,19 +359,23 @@ int chaos_compat_bifurcation1DIC(double tMax, int nPts, double h, int amountOfIn
                                  const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
                                  int writableVar, double maxValue, double transientTime, const double* values,
                                  int amountOfValues, int preScaller, const char* OUT_FILE_PATH) {
-    return legacy_bif1d(CHAOS_GRID_STATE, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
-                        indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
-                        OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        return legacy_bif1d(CHAOS_GRID_STATE, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                            indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
+                            OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_bifurcation1DForH(double tMax, int nPts, int amountOfInitialConditions,
                                    const double* initialConditions, const double* ranges, int writableVar,
                                    double maxValue, double transientTime, const double* values, int amountOfValues,
                                    int preScaller, const char* OUT_FILE_PATH) {
-    const int mut[1] = {CHAOS_MUT_STEP};
-    return legacy_bif1d(CHAOS_GRID_LOG0 | CHAOS_GRID_LOG_F32, tMax, nPts, 0.0, amountOfInitialConditions,
-                        initialConditions, ranges, mut, writableVar, maxValue, transientTime, values, amountOfValues,
-                        preScaller, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        const int mut[1] = {CHAOS_MUT_STEP};
+        return legacy_bif1d(CHAOS_GRID_LOG0 | CHAOS_GRID_LOG_F32, tMax, nPts, 0.0, amountOfInitialConditions,
+                            initialConditions, ranges, mut, writableVar, maxValue, transientTime, values, amountOfValues,
+                            preScaller, OUT_FILE_PATH);
+    });
 }
 
 // bifurcation2DIC writes bifurcation2D's file (debri/hostLibrary.cu:2932-2936, 3058-3076).
@@ -328,72 +383,84 @@ int chaos_compat_bifurcation2DIC(double tMax, int nPts, double h, int amountOfIn
                                  const double* initialConditions, const double* ranges, const int* indicesOfMutVars,
                                  int writableVar, double maxValue, double transientTime, const double* values,
                                  int amountOfValues, int preScaller, double eps, const char* OUT_FILE_PATH) {
-    if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
-    const long long n = (long long)nPts * nPts;
-    std::vector<int> labels(n);
-    chaos_exec ex = active_exec();
-    int rc = chaos_bifurcation_sweep(&ex, active_system(), 2, CHAOS_GRID_STATE, tMax, nPts, h,
-                                     amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
-                                     writableVar, maxValue, transientTime, values, amountOfValues, preScaller, eps, 0,
-                                     nullptr, nullptr, nullptr, nullptr, nullptr, labels.data());
-    if (rc) return rc;
-    std::ofstream o(OUT_FILE_PATH);
-    if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
-    o << ranges[0] << " " << ranges[1] << "\n";
-    o << ranges[2] << " " << ranges[3] << "\n";
-    o << std::setprecision(12);
-    write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
-    return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        if (nPts < 2) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 2");
+        const long long n = (long long)nPts * nPts;
+        std::vector<int> labels(n);
+        chaos_exec ex = active_exec();
+        int rc = chaos_bifurcation_sweep(&ex, active_system(), 2, CHAOS_GRID_STATE, tMax, nPts, h,
+                                         amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
+                                         writableVar, maxValue, transientTime, values, amountOfValues, preScaller, eps, 0,
+                                         nullptr, nullptr, nullptr, nullptr, nullptr, labels.data());
+        if (rc) return rc;
+        std::ofstream o(OUT_FILE_PATH);
+        if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
+        o << ranges[0] << " " << ranges[1] << "\n";
+        o << ranges[2] << " " << ranges[3] << "\n";
+        o << std::setprecision(12);
+        write_matrix(o, labels.data(), n, nPts, [](std::ofstream& s, int v) { s << v; });
+        return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_LLE1D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
                        int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                        int writableVar, double maxValue, double transientTime, const double* values,
                        int amountOfValues, const char* OUT_FILE_PATH) {
-    (void)writableVar;
-    (void)maxValue;
-    return legacy_lle(1, 0, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                      indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        (void)writableVar;
+        (void)maxValue;
+        return legacy_lle(1, 0, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                          indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_LLE1DIC(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
                          int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                          int writableVar, double maxValue, double transientTime, const double* values,
                          int amountOfValues, const char* OUT_FILE_PATH) {
-    (void)writableVar;
-    (void)maxValue;
-    return legacy_lle(1, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
-                      ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        (void)writableVar;
+        (void)maxValue;
+        return legacy_lle(1, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
+                          ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_LLE2DIC(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
                          int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                          int writableVar, double maxValue, double transientTime, const double* values,
                          int amountOfValues, const char* OUT_FILE_PATH) {
-    (void)writableVar;
-    (void)maxValue;
-    return legacy_lle(2, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
-                      ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        (void)writableVar;
+        (void)maxValue;
+        return legacy_lle(2, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
+                          ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_LS1D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
                       int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                       int writableVar, double maxValue, double transientTime, const double* values,
                       int amountOfValues, const char* OUT_FILE_PATH) {
-    (void)writableVar;
-    (void)maxValue;
-    return legacy_ls(1, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                     indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        (void)writableVar;
+        (void)maxValue;
+        return legacy_ls(1, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                         indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    });
 }
 
 int chaos_compat_LS2D(double tMax, double NT, int nPts, double h, double eps, const double* initialConditions,
                       int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                       int writableVar, double maxValue, double transientTime, const double* values,
                       int amountOfValues, const char* OUT_FILE_PATH) {
-    (void)writableVar;
-    (void)maxValue;
-    return legacy_ls(2, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                     indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        (void)writableVar;
+        (void)maxValue;
+        return legacy_ls(2, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                         indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+    });
 }
 
 // The legacy basins map (debri/hostLibrary.cu:4115-4556) writes the four files
@@ -404,9 +471,11 @@ int chaos_compat_basinsOfAttraction(double tMax, int nPts, double h, int amountO
                                     const int* indicesOfMutVars, int writableVar, double maxValue,
                                     double transientTime, const double* values, int amountOfValues, int preScaller,
                                     double eps, const char* OUT_FILE_PATH) {
-    return chaos_compat_basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
-                                             indicesOfMutVars, writableVar, maxValue, transientTime, values,
-                                             amountOfValues, preScaller, eps, OUT_FILE_PATH);
+    return guarded([&]() -> int {
+        return chaos_compat_basinsOfAttraction_2(tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                                                 indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                                 amountOfValues, preScaller, eps, OUT_FILE_PATH);
+    });
 }
 
 }  // extern "C"
