@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -256,7 +257,11 @@ static int upload_log_axes(Call& c, int gridMode, int dim, int nPts, const doubl
     for (int d = 0; d < dim; ++d) {
         if (!(gridMode & (d ? CHAOS_GRID_LOG1 : CHAOS_GRID_LOG0))) continue;
         std::vector<double> v;
-        log_axis_values(ranges[2 * d], ranges[2 * d + 1], nPts, (gridMode & CHAOS_GRID_LOG_F32) != 0, v);
+        try {
+            log_axis_values(ranges[2 * d], ranges[2 * d + 1], nPts, (gridMode & CHAOS_GRID_LOG_F32) != 0, v);
+        } catch (const std::bad_alloc&) {
+            return set_error(CHAOS_E_NOMEM, "host allocation of a log-scale axis failed");
+        }
         double* dv = (double*)c.alloc(v.size() * sizeof(double));
         if (c.failed) return CHAOS_E_NOMEM;
         cudaError_t e = cudaMemcpyAsync(dv, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream);
