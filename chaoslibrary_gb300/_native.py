@@ -63,6 +63,7 @@ _SIGS = {
     "chaos_lle2d": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _I, _D, _D, _P, _I, _P], _I),
     "chaos_bifurcation_sweep": ([_P, _I, _I, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _I, _P, _P, _P,
                                  _P, _P, _P], _I),
+    "chaos_compact_peaks": ([_P, _P, _P, _P, C.c_longlong, _I, _P, _P, _P, _P, C.c_longlong, _P], _I),
     "chaos_lle_sweep": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lyapunov_spectrum": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
@@ -521,6 +522,26 @@ def bifurcation_sweep(system, dim, gridMode, tMax, nPts, h, initialConditions, r
         writableVar, maxValue, transientTime, A.d(vals), vals.size, preScaller, eps, 0, _out_ptr(out.get("counts")),
         None, None, None, None, _out_ptr(out["labels"])))
     return out
+
+
+def compact_peaks(counts, peaks, intervals):
+    """Dense peak list of a 1-D sweep's rows (chaos_compact_peaks): returns
+    offsets[n + 1], peaks, intervals and the point of every kept peak."""
+    A = _Args()
+    cnt = np.ascontiguousarray(counts, np.int32)
+    pk = np.ascontiguousarray(peaks, np.float64)
+    iv = np.ascontiguousarray(intervals, np.float64)
+    n, cap = pk.shape
+    ex = _exec(FP64, {}, None)
+    total = C.c_longlong(0)
+    offsets = np.zeros(n + 1, np.int64)
+    _check(lib().chaos_compact_peaks(C.byref(ex), A.i(cnt), None, None, n, cap, offsets.ctypes.data, None, None,
+                                     None, 0, C.byref(total)))
+    m = int(total.value)
+    dp, di, dw = np.zeros(m), np.zeros(m), np.zeros(m, np.int32)
+    _check(lib().chaos_compact_peaks(C.byref(ex), A.i(cnt), A.d(pk), A.d(iv), n, cap, offsets.ctypes.data,
+                                     _out_ptr(dp), _out_ptr(di), _out_ptr(dw), m, C.byref(total)))
+    return dict(offsets=offsets, peaks=dp, intervals=di, point=dw)
 
 
 def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime, values,

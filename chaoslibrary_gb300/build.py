@@ -33,6 +33,7 @@ SOURCES = [
     ("server.cu", []),
     ("probe.cu", []),
     ("noalloc.cu", []),
+    ("peaks_compact.cu", []),
     ("compat.cpp", []),
 ]
 

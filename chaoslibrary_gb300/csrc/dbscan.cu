@@ -93,35 +93,36 @@ __device__ __forceinline__ double dist2(const double* a, const double* b, int D)
 // ---- prefix sum ------------------------------------------------------------
 constexpr int kScanItems = 4096;  // 1024 threads x 4
 
-__global__ void __launch_bounds__(1024) scan_block_kernel(const int* in, int* out, int* blockSums, long long n) {
-    __shared__ int warpSums[32];
+template <class T>
+__global__ void __launch_bounds__(1024) scan_block_kernel(const T* in, T* out, T* blockSums, long long n) {
+    __shared__ T warpSums[32];
     const long long base = (long long)blockIdx.x * kScanItems + threadIdx.x * 4;
-    int v[4], s = 0;
+    T v[4], s = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         v[j] = base + j < n ? in[base + j] : 0;
         s += v[j];
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int x = s;
+    T x = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        const T y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
     if (lane == 31) warpSums[w] = x;
     __syncthreads();
     if (w == 0) {
-        int ws = warpSums[lane];
+        T ws = warpSums[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, ws, o);
+            const T y = __shfl_up_sync(0xffffffffu, ws, o);
             if (lane >= o) ws += y;
         }
         warpSums[lane] = ws;
     }
     __syncthreads();
-    int prefix = (w > 0 ? warpSums[w - 1] : 0) + x - s;
+    T prefix = (w > 0 ? warpSums[w - 1] : 0) + x - s;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (base + j < n) out[base + j] = prefix;
@@ -130,7 +131,8 @@ __global__ void __launch_bounds__(1024) scan_block_kernel(const int* in, int* ou
     if (threadIdx.x == 1023) blockSums[blockIdx.x] = warpSums[31];
 }
 
-__global__ void add_offsets_kernel(int* out, const int* offsets, long long n) {
+template <class T>
+__global__ void add_offsets_kernel(T* out, const T* offsets, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] += offsets[i / kScanItems];
 }
@@ -978,28 +980,37 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
 
 }  // namespace
 
-int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total) {
+template <class T>
+static int exclusive_scan_t(Call& c, const T* in, T* out, long long n, T* total) {
     if (n <= 0) {
         if (total) *total = 0;
         return CHAOS_OK;
     }
     const long long nb = (n + kScanItems - 1) / kScanItems;
-    int* sums = (int*)c.alloc((size_t)(nb + 1) * sizeof(int));
+    T* sums = (T*)c.alloc((size_t)(nb + 1) * sizeof(T));
     if (!sums) return CHAOS_E_NOMEM;
-    scan_block_kernel<<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n);
+    scan_block_kernel<T><<<(unsigned)nb, 1024, 0, c.stream>>>(in, out, sums, n);
     note_launch();
     CK(cudaGetLastError());
     if (nb > 1) {
-        int rc = exclusive_scan(c, sums, sums, nb, total);
+        int rc = exclusive_scan_t<T>(c, sums, sums, nb, total);
         if (rc) return rc;
-        add_offsets_kernel<<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n);
+        add_offsets_kernel<T><<<blocks(n), kTPB, 0, c.stream>>>(out, sums, n);
         note_launch();
         CK(cudaGetLastError());
     } else if (total) {
-        CK(cudaMemcpyAsync(total, sums, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaMemcpyAsync(total, sums, sizeof(T), cudaMemcpyDeviceToHost, c.stream));
         CK(cudaStreamSynchronize(c.stream));
     }
     return CHAOS_OK;
+}
+
+int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total) {
+    return exclusive_scan_t<int>(c, in, out, n, total);
+}
+
+int exclusive_scan64(Call& c, const long long* in, long long* out, long long n, long long* total) {
+    return exclusive_scan_t<long long>(c, in, out, n, total);
 }
 
 int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgIntervals, const int* flags, long long n,

@@ -14,7 +14,9 @@ int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgInter
 int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,
                   int* labels);
 
-// Exclusive prefix sum of n ints (device arrays; in == out allowed).
+// Exclusive prefix sum of n ints / 64-bit ints (device arrays; in == out
+// allowed); *total (host) receives the sum.
 int exclusive_scan(Call& c, const int* in, int* out, long long n, int* total);
+int exclusive_scan64(Call& c, const long long* in, long long* out, long long n, long long* total);
 
 }  // namespace chaos

@@ -148,6 +148,22 @@ int chaos_bifurcation_sweep(const chaos_exec* ex, int system, int dim, int gridM
                             double* peaks, double* intervals, int* labels);
 
 /*
+ * Dense peak list of a 1-D sweep's rows (chaos_bifurcation1d /
+ * chaos_bifurcation_sweep outputs): the kept peaks of point k, min(max(counts[k],
+ * 0), peakCapacity) of them, move from row k to positions offsets[k] ..
+ * offsets[k+1]-1 of densePeaks / denseIntervals (densePoint receives k there):
+ * the reference CSV's row order without the empty rows. Prefix sums of the
+ * counts on the device, then a warp per point. offsets (n + 1 entries) and the
+ * dense arrays may be NULL; *total (host memory) always receives the number of
+ * kept peaks, so a first call with NULL dense arrays sizes them. When
+ * denseCapacity < *total the first denseCapacity entries are written and the
+ * call returns CHAOS_E_ARGS.
+ */
+int chaos_compact_peaks(const chaos_exec* ex, const int* counts, const double* peaks, const double* intervals,
+                        long long n, int peakCapacity, long long* offsets, double* densePeaks,
+                        double* denseIntervals, int* densePoint, long long denseCapacity, long long* total);
+
+/*
  * Largest-Lyapunov-exponent map. Replaces LLE::LLE2D (LLE/include/LLEHost.h:25-41,
  * LLE/src/LLECUDA.cu:205-428). lle[j*nPts + i] is the value at
  * values[indicesOfMutVars[0]] = linspace(ranges[0], ranges[1])[i] and

@@ -239,3 +239,35 @@ def test_perf_cli_tables(engine, tmp_path):
         assert len(t) == 5 and all(re.fullmatch(rf"(Resolution|ModelingTime),\d+,{lib},\d+", ln) for ln in t[1:])
     assert (tmp_path / "bif2d_res_test_24.csv").read_text().startswith("0 5\n0 20\n")
     assert (tmp_path / "lle_tt_test_200.csv").exists() and (tmp_path / "basins_res_test_16.csv_3.csv").exists()
+
+
+def test_compact_peaks_dense_list(engine):
+    """chaos_compact_peaks: the kept peaks of every row, in row order, clamped
+    to the rows (a point keeping more peaks than its row holds contributes the
+    row), none for fixed or diverged points; a too-small capacity is refused
+    with the total reported."""
+    kw = dict(tMax=15.0, nPts=301, h=0.01, initialConditions=[0.1, 0.1, 0.1], ranges=[20.0, 200.0],
+              indicesOfMutVars=[1], writableVar=0, maxValue=40.0, transientTime=5.0, values=LORENZ)
+    cap = 20  # the rows keep 16-24 peaks: some rows overflow, some do not
+    r = engine.bifurcation1d("lorenz", precision=engine.FP32, peakCapacity=cap, **kw)
+    assert (r["counts"] > cap).any() and (r["counts"] <= 0).any() and ((r["counts"] > 0) & (r["counts"] <= cap)).any()
+    d = engine.compact_peaks(r["counts"], r["peaks"], r["intervals"])
+    kept = np.clip(r["counts"], 0, cap)
+    assert np.array_equal(d["offsets"], np.concatenate([[0], np.cumsum(kept)]))
+    exp_p = np.concatenate([r["peaks"][k, :kept[k]] for k in range(len(kept))])
+    exp_i = np.concatenate([r["intervals"][k, :kept[k]] for k in range(len(kept))])
+    exp_w = np.concatenate([np.full(kept[k], k) for k in range(len(kept))])
+    assert np.array_equal(d["peaks"], exp_p) and np.array_equal(d["intervals"], exp_i)
+    assert np.array_equal(d["point"], exp_w)
+    import ctypes as C
+
+    L = engine.lib()
+    ex = engine._native._exec(engine.FP64, {}, None)
+    total = C.c_longlong(0)
+    small = np.zeros(5)
+    cnt = np.ascontiguousarray(r["counts"], np.int32)
+    pk = np.ascontiguousarray(r["peaks"])
+    rc = L.chaos_compact_peaks(C.byref(ex), cnt.ctypes.data, pk.ctypes.data, None, len(cnt), cap, None,
+                               small.ctypes.data, None, None, 5, C.byref(total))
+    assert rc == -1 and total.value == int(kept.sum())
+    assert np.array_equal(small, exp_p[:5])

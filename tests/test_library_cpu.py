@@ -122,6 +122,20 @@ def test_grid_mode_argument_errors(native):
                          [10.0, 28.0, 8 / 3], gridMode=native.GRID_LOG1)
 
 
+def test_compact_peaks_argument_errors(native):
+    import ctypes as C
+
+    L = native.lib()
+    total = C.c_longlong(0)
+    cnt = np.zeros(4, np.int32)
+    assert L.chaos_compact_peaks(None, cnt.ctypes.data, None, None, 4, 0, None, None, None, None, 0,
+                                 C.byref(total)) == -1
+    assert L.chaos_compact_peaks(None, None, None, None, 4, 8, None, None, None, None, 0, C.byref(total)) == -1
+    out = np.zeros(4)
+    assert L.chaos_compact_peaks(None, cnt.ctypes.data, None, None, 4, 8, None, out.ctypes.data, None, None, 4,
+                                 C.byref(total)) == -1  # dense peaks without the peak rows
+
+
 def test_compat_system_selection(native):
     L = native.lib()
     assert L.chaos_compat_set_system(99) == -1
