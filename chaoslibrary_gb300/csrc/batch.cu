@@ -102,6 +102,16 @@ __device__ __forceinline__ void run_lle(const JobDesc& J, long long b, int cnt) 
     }
 }
 
+// Chameleon LLE chunks: one point per thread, the twin as the difference of
+// chameleon_step_twin (lle_point_twin_chameleon, as the single-sweep kernel).
+__device__ __forceinline__ void run_lle_chameleon(const JobDesc& J, long long b, int cnt) {
+    __shared__ LleParams sL;
+    if (threadIdx.x == 0) sL = J.lp;
+    __syncthreads();
+#pragma unroll 1
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) J.lle[b + t] = lle_point_twin_chameleon(sL, b + t);
+}
+
 // Persistent kernel of one (kind, system) group: pulls chunks [0, count) of
 // the group's range from its counter until none is left. One kernel per
 // group keeps each code path's register allocation as small as the
@@ -123,6 +133,7 @@ __global__ void __launch_bounds__(kBatchBlock) group_kernel(const JobDesc* __res
         if (KIND == CHAOS_JOB_BIF1D) run_bif<S>(J, ch.begin, ch.count);
         else if (KIND == CHAOS_JOB_BASINS) run_basins<S>(J, ch.begin, ch.count);
         else if constexpr (S <= SYS_CHEN_RK4) run_lle<typename FieldOf<S>::F>(J, ch.begin, ch.count);
+        else if constexpr (S == SYS_CHAMELEON) run_lle_chameleon(J, ch.begin, ch.count);
     }
 }
 
@@ -138,7 +149,7 @@ GroupKernel kernel_for_system(int s) {
         case SYS_LORENZ_RK4: return group_kernel<KIND, SYS_LORENZ_RK4>;
         case SYS_ROSSLER_RK4: return group_kernel<KIND, SYS_ROSSLER_RK4>;
         case SYS_CHEN_RK4: return group_kernel<KIND, SYS_CHEN_RK4>;
-        case SYS_CHAMELEON: return KIND == CHAOS_JOB_LLE2D ? nullptr : group_kernel<KIND, SYS_CHAMELEON>;
+        case SYS_CHAMELEON: return group_kernel<KIND, SYS_CHAMELEON>;
         case SYS_ROSSLER_CD: return KIND == CHAOS_JOB_LLE2D ? nullptr : group_kernel<KIND, SYS_ROSSLER_CD>;
         case SYS_SIN3: return KIND == CHAOS_JOB_LLE2D ? nullptr : group_kernel<KIND, SYS_SIN3>;
         case SYS_SIN2: return KIND == CHAOS_JOB_LLE2D ? nullptr : group_kernel<KIND, SYS_SIN2>;

@@ -85,8 +85,8 @@ int prepare_job(const chaos_job& j, int memory, JobDesc& J, std::vector<HostOut>
             rc = fill_lle(J.lp, j.system, j.tMax, j.NT, j.nPts, j.h, j.eps, j.initialConditions, nx, j.ranges,
                           j.indicesOfMutVars, j.transientTime, j.values, na);
             if (rc) return rc;
-            if (!system_has_difference_form(j.system))
-                return set_error(CHAOS_E_UNSUPPORTED, "batched LLE jobs need a quadratic RK4 system (0-2)");
+            if (!system_has_fp32_lle(j.system))
+                return set_error(CHAOS_E_UNSUPPORTED, "batched LLE jobs need a quadratic RK4 system (0-2) or Chameleon");
             if (J.lp.twin != 0)
                 return set_error(CHAOS_E_UNSUPPORTED, "batched LLE jobs are FP32: the reference twin start is FP64 only");
             if (!j.lle) return set_error(CHAOS_E_ARGS, "LLE job needs lle");
@@ -122,8 +122,8 @@ inline void make_chunks(const std::vector<JobDesc>& jobs, std::vector<Chunk>& ch
         const JobDesc& J = jobs[j];
         if (groups.empty() || groups.back().kind != J.kind || groups.back().system != J.system)
             groups.push_back(Group{J.kind, J.system, (int)chunks.size(), 0});
-        // two points per thread for the RK4 systems (every LLE job is one)
-        const int size = (J.kind == CHAOS_JOB_LLE2D || J.system <= SYS_CHEN_RK4) ? 2 * block : block;
+        // two points per thread for the RK4 systems
+        const int size = J.system <= SYS_CHEN_RK4 ? 2 * block : block;
         for (long long b = 0; b < J.nPoints; b += size)
             chunks.push_back(Chunk{j, (int)std::min<long long>(size, J.nPoints - b), b});
         groups.back().count = (int)chunks.size() - groups.back().begin;

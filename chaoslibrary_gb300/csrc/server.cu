@@ -442,8 +442,8 @@ int chaos_server_submit(chaos_server* S, const chaos_job* job, long long* reques
     r->bytes = bytes;
     r->perPoint = work_per_point(r->desc);
     r->steps = r->perPoint * r->nPoints;
-    // two points per thread for the RK4 systems (every LLE job is one), as in batches
-    r->chunk = ((job->kind == CHAOS_JOB_LLE2D || job->system <= SYS_CHEN_RK4) ? 2 : 1) * batch_block_size();
+    // two points per thread for the RK4 systems, as in batches
+    r->chunk = (job->system <= SYS_CHEN_RK4 ? 2 : 1) * batch_block_size();
     std::lock_guard<std::mutex> lk(S->mu);
     if (S->stop) return set_error(CHAOS_E_BUSY, "server is shutting down");
     if (!S->started) {

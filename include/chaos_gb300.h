@@ -323,7 +323,7 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
  * single-job entry points; outputs are host or device arrays per ex->memory.
  */
 #define CHAOS_JOB_BIF1D 1  /* chaos_bifurcation1d: counts, flags, first?, peaks?, intervals? */
-#define CHAOS_JOB_LLE2D 2  /* chaos_lle2d (RK4 systems): lle */
+#define CHAOS_JOB_LLE2D 2  /* chaos_lle2d (RK4 systems and Chameleon): lle */
 #define CHAOS_JOB_BASINS 3 /* chaos_basins_features: flags, avgPeaks, avgIntervals, counts? */
 
 typedef struct chaos_job {

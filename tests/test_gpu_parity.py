@@ -321,6 +321,9 @@ def _batch_jobs():
         ("bif", "chameleon", dict(tMax=10.0, nPts=77, h=0.01, initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0],
                                   indicesOfMutVars=[3], writableVar=0, maxValue=1e4, transientTime=5.0,
                                   values=[0.5, 3, 0, 2, 1, 18, 1])),
+        ("lle", "chameleon", dict(tMax=10.0, NT=0.5, nPts=19, h=0.01, eps=1e-6, initialConditions=[3.0, 3.0, 0.0],
+                                  ranges=[0.0, 5.0, 0.0, 20.0], indicesOfMutVars=[3, 5], transientTime=5.0,
+                                  values=[0.5, 3, 0, 2, 1, 18, 1])),
     ]
 
 
