@@ -711,8 +711,8 @@ int chaos_lle2d_checked(const chaos_exec* ex, int system, double tMax, double NT
     if ((rc = fill_lle(Lc, system, fullCheck ? tMax : checkTMax, NT, nPts, h, eps, initialConditions,
                        amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values, amountOfValues)))
         return rc;
-    if (!system_has_difference_form(system))
-        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2)");
+    if (system == SYS_USER || !system_has_fp32_lle(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon");
     if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
     if (L.nPoints > 0x7fffffffLL) return set_error(CHAOS_E_ARGS, "nPts^2 must be < 2^31");
     Call c;

@@ -214,7 +214,7 @@ int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridM
 /*
  * LLE map in FP32 with an FP64 sign re-check (no reference counterpart: the
  * reference computes in FP64 only). Arguments as chaos_lle2d (RK4 systems
- * 0-2; ex->precision is ignored). The map is computed as chaos_lle2d with
+ * 0-2 and Chameleon; ex->precision is ignored). The map is computed as chaos_lle2d with
  * CHAOS_FP32; every point whose FP32 value v has |v| <= band or is not finite
  * is integrated again in FP64 over a short horizon of checkTMax time units
  * (same transient, NT and eps). Where the check's class (positive,

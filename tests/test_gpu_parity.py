@@ -592,29 +592,40 @@ def test_launch_count(engine):
     b.close()
 
 
-def test_lle_sign_recheck(engine):
+CHAM_LLE = dict(NT=0.5, h=0.01, eps=1e-6, initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0, 0.0, 20.0],
+                indicesOfMutVars=[3, 5], values=[0.5, 3, 0, 2, 1, 18, 1])
+
+
+@pytest.mark.parametrize("system", ["rossler", "chameleon"])
+def test_lle_sign_recheck(engine, system):
     """FP32 LLE map with the FP64 sign re-check: points outside the band keep
     their FP32 value; exactly the checked points whose short FP64 check
     disagrees in class (positive / non-positive / not finite) are replaced,
     by the FP64 map's value bit for bit; with a full-horizon check the
     replaced points are those whose FP32 and FP64 classes differ."""
-    kw = dict(tMax=60.0, NT=0.1, nPts=40, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
-              ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=10.0, values=[0.2, 0.2, 5.7])
+    if system == "rossler":
+        kw = dict(tMax=60.0, NT=0.1, nPts=40, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+                  ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=10.0,
+                  values=[0.2, 0.2, 5.7])
+    else:
+        kw = dict(tMax=60.0, NT=0.5, nPts=32, h=0.01, eps=1e-6, **{k: v for k, v in CHAM_LLE.items()
+                                                                   if k not in ("NT", "h", "eps")},
+                  transientTime=20.0)
     band, ct = 0.02, 15.0
-    v32 = engine.lle2d("rossler", precision=engine.FP32, **kw)
-    v64 = engine.lle2d("rossler", precision=engine.FP64, **kw)
-    vs = engine.lle2d("rossler", precision=engine.FP64, **dict(kw, tMax=ct))
+    v32 = engine.lle2d(system, precision=engine.FP32, **kw)
+    v64 = engine.lle2d(system, precision=engine.FP64, **kw)
+    vs = engine.lle2d(system, precision=engine.FP64, **dict(kw, tMax=ct))
 
     def cls(v):
         return np.where(~np.isfinite(v), -1, (v > 0).astype(int))
 
     checked = ~(np.abs(v32) > band)
-    got, nc, nr = engine.lle2d_checked("rossler", band=band, checkTMax=ct, **kw)
+    got, nc, nr = engine.lle2d_checked(system, band=band, checkTMax=ct, **kw)
     flip = checked & (cls(v32) != cls(vs))
     assert nc == int(checked.sum()) and nr == int(flip.sum())
     assert np.array_equal(got[~flip], v32[~flip], equal_nan=True)
     assert np.array_equal(got[flip], v64[flip], equal_nan=True)
-    got2, nc2, nr2 = engine.lle2d_checked("rossler", band=band, checkTMax=kw["tMax"], **kw)
+    got2, nc2, nr2 = engine.lle2d_checked(system, band=band, checkTMax=kw["tMax"], **kw)
     flip2 = checked & (cls(v32) != cls(v64))
     assert nc2 == nc and nr2 == int(flip2.sum())
     assert np.array_equal(got2[flip2], v64[flip2], equal_nan=True)
@@ -745,9 +756,6 @@ def test_spectrum_lorenz_physics_fp32_and_fp64(engine):
         assert np.all(np.abs(s[:, 2] + 14.57) < 0.15), s
         assert np.all(np.abs(s.sum(axis=1) + (10 + 1 + 8 / 3) * span) < 0.02), s
 
-
-CHAM_LLE = dict(NT=0.5, h=0.01, eps=1e-6, initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0, 0.0, 20.0],
-                indicesOfMutVars=[3, 5], values=[0.5, 3, 0, 2, 1, 18, 1])
 
 
 def test_chameleon_fp32_lle_short_horizon(engine):
