@@ -116,30 +116,31 @@ template <class T> struct PeakStream {
     T p1;          // d[k-1]
     bool rise;     // d[k-1] - d[k-2] > 1e-13
     int k;         // index of the next sample
-    int cand;      // scan mode: next candidate index; plateau mode: -1
+    int wait;      // samples before the next candidate is judged (2, 1 or 0); -1: in a plateau
     int i0;        // plateau: index of the candidate that opened it
     int n;         // peaks detected so far (the dropped first one included)
     int tprev;     // time index of the previous detected peak
 
-    __device__ __forceinline__ void init() { k = 0; cand = 1; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false; }
+    __device__ __forceinline__ void init() { k = 0; wait = 2; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false; }
 
     // Pushes d[k] = v; returns true and sets (val, t) when a peak was detected.
+    // Candidate k-1 is judged when wait == 0 (d[k-2], d[k-1] and d[k] known);
+    // a judged candidate that is no peak makes k the next one (wait 0), a
+    // found peak or a plateau left upwards skips one sample (wait 1).
     __device__ __forceinline__ bool push(T v, T& val, int& t) {
         const DiffTest c = diff_test(v, p1);
         bool hit = false;
-        if (k >= 2) {
-            if (cand < 0) {  // plateau, j = k-1
-                if (c.up) cand = k + 1;
-                else if (c.below) { hit = true; val = p1; t = (i0 + k - 1) >> 1; cand = k + 1; }
-            } else if (cand == k - 1) {
-                if (rise && c.ge) {
-                    i0 = k - 1;
-                    if (c.below) { hit = true; val = p1; t = k - 1; cand = k + 1; }
-                    else cand = -1;
-                } else {
-                    cand = k;
-                }
+        if (wait < 0) {  // plateau, j = k-1
+            if (c.up) wait = 1;
+            else if (c.below) { hit = true; val = p1; t = (i0 + k - 1) >> 1; wait = 1; }
+        } else if (wait == 0) {
+            if (rise && c.ge) {
+                i0 = k - 1;
+                if (c.below) { hit = true; val = p1; t = k - 1; wait = 1; }
+                else wait = -1;
             }
+        } else {
+            --wait;
         }
         rise = c.above;
         p1 = v;
