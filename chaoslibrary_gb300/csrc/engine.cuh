@@ -115,32 +115,43 @@ __device__ __forceinline__ DiffTest diff_test(float v, float p1) {
 template <class T> struct PeakStream {
     T p1;          // d[k-1]
     bool rise;     // d[k-1] - d[k-2] > 1e-13
+    bool plateau;  // a plateau is open: it started at candidate i0 and runs to j = k-1
     int k;         // index of the next sample
-    int wait;      // samples before the next candidate is judged (2, 1 or 0); -1: in a plateau
+    int nc;        // candidate k-1 is judged when k > nc (outside a plateau)
     int i0;        // plateau: index of the candidate that opened it
     int n;         // peaks detected so far (the dropped first one included)
     int tprev;     // time index of the previous detected peak
 
-    __device__ __forceinline__ void init() { k = 0; wait = 2; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false; }
+    __device__ __forceinline__ void init() {
+        k = 0; nc = 1; plateau = false; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false;
+    }
 
     // Pushes d[k] = v; returns true and sets (val, t) when a peak was detected.
-    // Candidate k-1 is judged when wait == 0 (d[k-2], d[k-1] and d[k] known);
-    // a judged candidate that is no peak makes k the next one (wait 0), a
-    // found peak or a plateau left upwards skips one sample (wait 1).
+    // Outside a plateau, candidate k-1 (d[k-2], d[k-1] and d[k] known) is
+    // judged when k > nc; the first judged candidate is 1 (nc = 1), and after
+    // a plateau ends at j = k-1 the scan resumes at candidate j+2 = k+1
+    // (nc = k+1). A judged candidate that is no peak leaves nc as it is, so the
+    // common sample costs one compare of k with nc besides the sample tests.
     __device__ __forceinline__ bool push(T v, T& val, int& t) {
         const DiffTest c = diff_test(v, p1);
         bool hit = false;
-        if (wait < 0) {  // plateau, j = k-1
-            if (c.up) wait = 1;
-            else if (c.below) { hit = true; val = p1; t = (i0 + k - 1) >> 1; wait = 1; }
-        } else if (wait == 0) {
-            if (rise && c.ge) {
-                i0 = k - 1;
-                if (c.below) { hit = true; val = p1; t = k - 1; wait = 1; }
-                else wait = -1;
+        if (plateau) {  // j = k-1
+            if (c.up) {
+                plateau = false;
+                nc = k + 1;
+            } else if (c.below) {
+                hit = true; val = p1; t = (i0 + k - 1) >> 1;
+                plateau = false;
+                nc = k + 1;
             }
-        } else {
-            --wait;
+        } else if (k > nc && rise && c.ge) {
+            i0 = k - 1;
+            if (c.below) {
+                hit = true; val = p1; t = k - 1;
+                nc = k + 1;
+            } else {
+                plateau = true;
+            }
         }
         rise = c.above;
         p1 = v;
@@ -823,7 +834,8 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
             for (int l = 0; l < 2; ++l) {
                 float val;
                 int t;
-                if (rec[l] && ps[l].push(lane(v, l), val, t)) {
+                const bool hit = ps[l].push(lane(v, l), val, t);  // a lane that stopped keeps stepping its detector
+                if (rec[l] && hit) {
                     if (ps[l].n >= 1) {
                         const int q = ps[l].n - 1;
                         if (q < O.cap) {
