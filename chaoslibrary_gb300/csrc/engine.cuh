@@ -60,10 +60,14 @@ template <> __device__ __forceinline__ bool bif_diverged<double>(double v, const
     if (b >= 0x4340000000000000ull) return true;  // |v| >= 2^53, infinite or NaN
     return P.checkMax && max_exceeded(b, P);
 }
-// The same test for a float v (float compares): |v| > maxValue <=> |v| > maxValueF.
+// The same test for a float v, as one compare against a limit that does not
+// change in the loop: !(|v| < 2^53) || (checkMax && |v| > maxValueF) holds
+// exactly when !(|v| <= lim), lim = min(maxValueF, 2^53 - 2^29) with checkMax,
+// else 2^53 - 2^29 (the largest float below 2^53); NaN fails every compare.
 template <> __device__ __forceinline__ bool bif_diverged<float>(float v, const SweepParams& P) {
-    const float av = fabsf(v);
-    return !(av < 9007199254740992.0f) || (P.checkMax && av > P.maxValueF);
+    constexpr float kBelow2p53 = 9007198717870080.0f;
+    const float lim = P.checkMax ? fminf(P.maxValueF, kBelow2p53) : kBelow2p53;
+    return !(fabsf(v) <= lim);
 }
 // Divergence test of the basins loop (basinsCUDA.cu:350-361): isnan || isinf, then maxValue.
 template <class T> __device__ __forceinline__ bool basins_diverged(T v, const SweepParams& P);
@@ -280,13 +284,19 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
     const int wv = P.wv;
     int flag = 1;
     if (nS > 0) {
-        for (int s = 0; s < nS; ++s) {
-#pragma unroll
-            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+        // the state before the last step is kept for the fixed-point test:
+        // the last step is peeled off the loop, so the others copy nothing
+        for (int s = 0; s < nS - 1; ++s) {
             step<S>(x, a, c);
             if (bif_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
         }
-        if (flag == 1 && bif_fixed<NX>(x, xp)) flag = -1;
+        if (flag == 1) {
+#pragma unroll
+            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+            step<S>(x, a, c);
+            if (bif_diverged(pick<NX>(x, wv), P)) flag = 0;
+            else if (bif_fixed<NX>(x, xp)) flag = -1;
+        }
     }
     if (flag == 1) {
         bif_record<S, T>(P, O, x, a, c, nB, hI, o);
@@ -797,18 +807,24 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
     const int wv = P.wv;
     int flag[2] = {1, two ? 1 : 0};
     if (P.S > 0) {
-        for (int s = 0; s < P.S; ++s) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+        for (int s = 0; s < P.S - 1; ++s) {  // the last step peeled off, as in bif_point
             rk4_step<F>(x, a, c);
             const P2 v = pick2<3>(x, wv);
             if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
             if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
             if (flag[0] != 1 && flag[1] != 1) break;
         }
+        if (flag[0] == 1 || flag[1] == 1) {
 #pragma unroll
-        for (int l = 0; l < 2; ++l)
-            if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+            rk4_step<F>(x, a, c);
+            const P2 v = pick2<3>(x, wv);
+            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
+            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
+#pragma unroll
+            for (int l = 0; l < 2; ++l)
+                if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+        }
     }
     bool rec[2];
     double first[2] = {0.0, 0.0};  // stays 0 for a lane that does not record (as the scalar path)
@@ -971,18 +987,24 @@ __device__ __forceinline__ void bif_hybrid_point(const SweepParams& P, const Bif
     int flag[2] = {1, two ? 1 : 0};
     if (P.S > 0) {
         const RK4H<P2> c((float)P.h);
-        for (int s = 0; s < P.S; ++s) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+        for (int s = 0; s < P.S - 1; ++s) {  // the last step peeled off, as in bif_point
             rk4_step<F>(x, a, c);
             const P2 v = pick2<3>(x, wv);
             if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
             if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
             if (flag[0] != 1 && flag[1] != 1) break;
         }
+        if (flag[0] == 1 || flag[1] == 1) {
 #pragma unroll
-        for (int l = 0; l < 2; ++l)
-            if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+            for (int j = 0; j < 3; ++j) xp[j] = x[j];
+            rk4_step<F>(x, a, c);
+            const P2 v = pick2<3>(x, wv);
+            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
+            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
+#pragma unroll
+            for (int l = 0; l < 2; ++l)
+                if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
+        }
     }
     const StepCtx<float> cs((float)P.h);
 #pragma unroll 1
