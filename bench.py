@@ -796,7 +796,7 @@ def engine_arm(args, ws, rank, local):
                 line["cpu_baseline"] = cpu_sample_spectrum(w, args.cpu_seconds)
             else:
                 line["cpu_baseline"] = cpu_sample_sweep(w, args.workload, args.cpu_seconds)
-        except Exception as e:  # the checker is optional at run time
+        except Exception as e:  # the oracle is optional at run time
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -191,7 +191,7 @@ static void sizes_of(int system, int* nx, int* na) {
 
 static int check_system(int system, int nIC, int nValues) {
     if (system == SYS_USER && !user_system_available())
-        return set_error(CHAOS_E_UNSUPPORTED, "this build has no user plug-in (CHAOS_USER_SYSTEMS at build time)");
+        return set_error(CHAOS_E_UNSUPPORTED, "the library was built without a user plug-in (CHAOS_USER_SYSTEMS at build time)");
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
     int nx, na;
     sizes_of(system, &nx, &na);
@@ -419,7 +419,7 @@ int chaos_launch_count(long long* count) {
 
 int chaos_system_info(int system, int* sizeX, int* sizeA) {
     if (system == SYS_USER && !user_system_available())
-        return set_error(CHAOS_E_UNSUPPORTED, "this build has no user plug-in");
+        return set_error(CHAOS_E_UNSUPPORTED, "the library was built without a user plug-in");
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
     int nx, na;
     sizes_of(system, &nx, &na);
@@ -967,7 +967,7 @@ int chaos_get_tuning(int knob) {
 int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const double* x0, const double* a, double h,
                      int nSteps, double* out) {
     if (system == SYS_USER && !user_system_available())
-        return set_error(CHAOS_E_UNSUPPORTED, "this build has no user plug-in");
+        return set_error(CHAOS_E_UNSUPPORTED, "the library was built without a user plug-in");
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
     if (nTraj < 0 || nSteps < 0 || !(h == h) || (nTraj > 0 && (!x0 || !a || !out)))
         return set_error(CHAOS_E_ARGS, "bad trajectory arguments");

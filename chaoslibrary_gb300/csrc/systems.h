@@ -453,7 +453,7 @@ template <class T> CHAOS_HD void memristor_step(T* X, const T* a, T h) {
 }
 
 #if defined(CHAOS_USER_SYSTEM)
-// The step of a reference-format plug-in header compiled into this build
+// The step of a reference-format plug-in header compiled into the library
 // (kern_user.cu): CALC_DISCRETE_MODEL(X, a, h) on doubles.
 template <class T> __device__ void user_step(T* x, const T* a, T h);
 #endif

@@ -1,6 +1,6 @@
 // CPU oracle for the bifurcation / LLE / basins path.
 //
-// TEST INFRASTRUCTURE ONLY. This file is the checker the parity tests, the
+// TEST INFRASTRUCTURE ONLY. This file is the oracle the parity tests, the
 // smoke check and the CPU-baseline leg of the benchmark compare the CUDA
 // engine against; the engine never calls it and never falls back to it.
 //

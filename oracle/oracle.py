@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (and of the host build of the reference).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
-the CPU-baseline leg of ``bench.py`` as the checker. The engine package never
+the CPU-baseline leg of ``bench.py`` as the reference result. The engine package never
 imports it.
 """
 from __future__ import annotations

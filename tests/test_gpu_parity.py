@@ -287,7 +287,7 @@ def test_lle_fp32_variants_identical(engine, system, values, ranges, mut):
 
 @pytest.mark.parametrize("precision", ["fp64"])
 def test_basins_dbscan_vs_oracle(engine, oracle, precision):
-    """BASELINE-mode basins (normalised features, DBSCAN eps/minPts) bit for bit
+    """Basins with normalised features and DBSCAN (eps, minPts) bit for bit
     against the oracle's features and DBSCAN on a small Lorenz rho=24 grid."""
     kw = dict(tMax=10.0, nPts=40, h=0.01, initialConditions=[0.0, 0.0, 27.0], ranges=[-30.0, 30.0, -30.0, 30.0],
               indicesOfMutVars=[0, 1], writableVar=0, maxValue=1e8, transientTime=20.0, values=[10.0, 24.0, 8 / 3])
