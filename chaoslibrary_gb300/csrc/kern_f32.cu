@@ -298,9 +298,15 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
     return cudaGetLastError();
 }
 
-// Two points per thread in packed FP32x2 lanes.
+// Two points per thread in packed FP32x2 lanes. Registers capped at 56 (three
+// resident blocks of 384 threads): nine blocks of 128 per SM instead of eight
+// at the 62 the kernel takes unbounded. The cap costs a few bytes of spills
+// outside the step loop; the 1024^2 Rössler map went from 133.7 to 128.6 ms
+// (from 3.37 waves of resident blocks to 2.99) and the Lorenz map from 39.1
+// to 36.2 ms, results unchanged. Blocks of 64, 128 and 256 (the tuner's
+// choices) all launch under the bound.
 template <class F>
-__global__ void __launch_bounds__(kMaxBlock) lle_pair_kernel_f32(LleParams L, double* out) {
+__global__ void __launch_bounds__(384, 3) lle_pair_kernel_f32(LleParams L, double* out) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (o >= L.nPoints) return;
     const bool two = o + 1 < L.nPoints;
