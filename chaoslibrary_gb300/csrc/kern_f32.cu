@@ -14,18 +14,20 @@ namespace {
 constexpr int kBlock = 128;     // default block
 constexpr int kMaxBlock = 256;  // largest block a tuned launch may use
 
-template <int S>
+// Sel: the peak detector as selects (sweeps within one wave of resident
+// threads, where each warp waits on its own trajectory) or with branches.
+template <int S, bool Sel>
 __global__ void __launch_bounds__(kMaxBlock) bif_kernel_f32(SweepParams P, BifOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
-    bif_point<S, float>(P, O, P.pBegin + o, o);
+    bif_point<S, float, Sel>(P, O, P.pBegin + o, o);
 }
 
 template <int S>
 __global__ void __launch_bounds__(kBlock) bif_list_kernel_f32(SweepParams P, BifOut O, const int* list, int count) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
-    bif_point<S, float>(P, O, list[k], k);
+    bif_point<S, float, true>(P, O, list[k], k);
 }
 
 template <int S, bool PRE1>
@@ -196,6 +198,19 @@ long long pair_threshold() {
     return threshold;
 }
 
+// Threads of one wave at 1024 resident threads per SM: below it a
+// one-point-per-thread sweep is latency-bound (every warp waits on its own
+// dependent chain).
+long long one_wave_threads() {
+    static long long threads = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return (long long)std::max(sms, 1) * 1024;
+    }();
+    return threads;
+}
+
 struct Launch {
     int form;  // 1 one point per thread, 2 packed pairs, 3 hybrid pairs (basins)
     int block;
@@ -259,7 +274,11 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
         else launch_bif_hybrid<Chen>(P, O, l.block, st);
         return cudaGetLastError();
     }
-#define CALL(S) (bif_kernel_f32<S><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O), note_launch())
+    const bool sel = P.nPoints <= one_wave_threads();
+#define CALL(S)                                                                           \
+    (sel ? bif_kernel_f32<S, true><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O) \
+         : bif_kernel_f32<S, false><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O), \
+     note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
