@@ -369,7 +369,7 @@ template <> struct PeakSums<float> {
 // sweep has preScaller == 1 (one step per sample, no inner loop).
 // The recorded part of a basins point, from its state x after the transient:
 // peak detector, divergence and fixed-point tests, features into row o.
-template <int S, class T, bool PRE1>
+template <int S, class T, bool PRE1, bool Sel = false>
 __device__ __forceinline__ void basins_record(const SweepParams& P, const BasinsOut& O, T* x, const T* a,
                                               const StepCtx<T>& c, long long o) {
     constexpr int NX = Traits<S>::NX;
@@ -377,7 +377,7 @@ __device__ __forceinline__ void basins_record(const SweepParams& P, const Basins
     const int wv = P.wv;
 #pragma unroll
     for (int j = 0; j < NX; ++j) xp[j] = x[j];
-    PeakStream<T> ps;
+    PeakStream<T, Sel> ps;
     ps.init();
     int flag = 1;
     PeakSums<T> sums;
@@ -415,14 +415,14 @@ __device__ __forceinline__ void basins_record(const SweepParams& P, const Basins
     if (O.last) O.last[o] = last;
 }
 
-template <int S, class T, bool PRE1 = false>
+template <int S, class T, bool PRE1 = false, bool Sel = false>
 __device__ __forceinline__ void basins_point(const SweepParams& P, const BasinsOut& O, long long p, long long o) {
     constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
     T x[NX], a[NA];
     load_point<S, T>(P, p, x, a);
     const StepCtx<T> c((T)P.h);
     for (int s = 0; s < P.S; ++s) step<S>(x, a, c);
-    basins_record<S, T, PRE1>(P, O, x, a, c, o);
+    basins_record<S, T, PRE1, Sel>(P, O, x, a, c, o);
 }
 
 // ---------------------------------------------------------------------------

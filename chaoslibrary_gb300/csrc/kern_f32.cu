@@ -30,11 +30,11 @@ __global__ void __launch_bounds__(kBlock) bif_list_kernel_f32(SweepParams P, Bif
     bif_point<S, float, true>(P, O, list[k], k);
 }
 
-template <int S, bool PRE1>
+template <int S, bool PRE1, bool Sel>
 __global__ void __launch_bounds__(kMaxBlock) basins_kernel_f32(SweepParams P, BasinsOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
-    basins_point<S, float, PRE1>(P, O, P.pBegin + o, o);
+    basins_point<S, float, PRE1, Sel>(P, O, P.pBegin + o, o);
 }
 
 // MINB = resident blocks per SM the register allocation is shaped for:
@@ -308,9 +308,12 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
         return cudaGetLastError();
     }
     const unsigned g = grid_of(P.nPoints, l.block);
-#define CALL(S)                                                                \
-    (P.preScaller == 1 ? basins_kernel_f32<S, true><<<g, l.block, 0, st>>>(P, O) \
-                       : basins_kernel_f32<S, false><<<g, l.block, 0, st>>>(P, O), \
+    const bool sel = P.nPoints <= one_wave_threads();  // the detector as selects, as in the 1-D sweeps
+#define CALL(S)                                                                               \
+    (P.preScaller == 1 ? (sel ? basins_kernel_f32<S, true, true><<<g, l.block, 0, st>>>(P, O)    \
+                              : basins_kernel_f32<S, true, false><<<g, l.block, 0, st>>>(P, O))  \
+                       : (sel ? basins_kernel_f32<S, false, true><<<g, l.block, 0, st>>>(P, O)   \
+                              : basins_kernel_f32<S, false, false><<<g, l.block, 0, st>>>(P, O)), \
      note_launch())
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
