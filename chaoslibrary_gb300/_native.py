@@ -75,6 +75,7 @@ _SIGS = {
     "chaos_peak_finder": ([_P, _P, _L, _I, _D, _I, _P, _P, _P], _I),
     "chaos_point_dbscan": ([_P, _P, _P, _L, _I, _D, _P], _I),
     "chaos_fma_probe": ([_P, _L, _P, _P], _I),
+    "chaos_device_code_version": ([_I, _P, _P], _I),
     "chaos_launch_count": ([_P], _I),
     "chaos_autotune": ([_P, _P, _I], _I),
     "chaos_trajectory": ([_P, _I, _L, _P, _P, _D, _I, _P], _I),
@@ -194,6 +195,14 @@ def fma_probe(iters: int = 200000, device=None) -> float:
     sec, fl = C.c_double(), C.c_double()
     _check(lib().chaos_fma_probe(C.byref(ex), iters, C.byref(sec), C.byref(fl)))
     return fl.value / sec.value
+
+
+def device_code_version(device: int = -1) -> tuple[int, int]:
+    """(binaryVersion, ptxVersion) of the library's device code on `device`
+    (cudaFuncGetAttributes of one of its kernels): (103, 103) for sm_103a."""
+    b, p = C.c_int(), C.c_int()
+    _check(lib().chaos_device_code_version(int(device), C.byref(b), C.byref(p)))
+    return b.value, p.value
 
 
 def autotune(device=None) -> list[dict]:

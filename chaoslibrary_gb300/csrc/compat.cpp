@@ -31,7 +31,9 @@ int parse_system(const char* s) {
     if (strcmp(s, "user") == 0) return CHAOS_SYS_USER;
     char* end = nullptr;
     long v = strtol(s, &end, 10);
-    return (end && *end == 0) ? (int)v : CHAOS_SYS_CHAMELEON;
+    // an unknown name is an error, never a silent choice of another system:
+    // -1 makes every entry point return CHAOS_E_ARGS ("unknown system -1")
+    return (*s && end && *end == 0) ? (int)v : -1;
 }
 
 int active_system() {

@@ -169,8 +169,8 @@ __global__ void point_dbscan_kernel(const double* __restrict__ intervals, const 
         if (lane == 0) outBase[oi] = INT_MIN;
         return;
     }
-    if (P <= 1) {
-        if (lane == 0) outBase[oi] = P == -1 ? -1 : (P == 0 ? 0 : 1);
+    if (P <= 1) {  // dbscanCUDA: -1 passes through; dbscan returns 0 for P <= 0 and 1 for P == 1
+        if (lane == 0) outBase[oi] = P == -1 ? -1 : (P == 1 ? 1 : 0);
         return;
     }
     const double* iv = intervals + w * (long long)stride;

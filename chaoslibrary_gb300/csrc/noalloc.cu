@@ -2,14 +2,13 @@
 // bifurcation (the kernel behind chaos_point_dbscan) with its scratch rows in
 // a fixed array compiled into the library instead of memory allocated per call.
 //
-// Who needs it: code that must not allocate device memory while it runs --
-// work recorded into a CUDA graph (a cudaMalloc inside a stream capture
-// breaks the capture), latency-critical loops where cudaMalloc/cudaFree would
-// synchronise the device, and host applications that reserve device memory
-// through their own allocator and budget (a framework's caching allocator, an
-// MPS client with a memory limit), where a library-side cudaMalloc can fail or
-// break the host's accounting. The caller provides every input and output in
-// device memory; this call allocates nothing.
+// Who needs it: callers that cannot call cudaMalloc while they run -- hosts
+// that reserve all device memory up front through their own allocator and
+// budget (a framework's caching allocator, an MPS client with a memory limit),
+// where a library-side cudaMalloc can fail or break the host's accounting, and
+// latency-critical loops where cudaMalloc / cudaFree would synchronise the
+// device. The caller provides every input and output in device memory; this
+// call allocates nothing.
 //
 // The scratch array costs kNoAllocMaxEntries * 2 * 4 bytes = 8 MiB on every
 // GPU that loads the library, held until the process exits. All calls share
@@ -18,8 +17,6 @@
 // The kernel clears each row it uses before reading it, so the contents left
 // by a previous call do not matter.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/chaos_gb300.h"
 #include "capi_internal.h"
@@ -31,22 +28,15 @@ constexpr long long kNoAllocMaxEntries = 1LL << 20;  // n * stride limit: label 
 
 static __device__ __align__(256) int g_noalloc_scratch[2 * kNoAllocMaxEntries];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-int* g_scratch[kMaxDevices];  // device address of g_noalloc_scratch, per device
-
-// Device address of the scratch array on the current device, looked up once
-// per device (the array's host-side name is not a device address).
-int scratch_address(int dev, int** out) {
-    if (dev < 0 || dev >= kMaxDevices) return chaos::set_error(CHAOS_E_ARGS, "device %d not supported", dev);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return chaos::cuda_error(e, "scratch address");
-        g_scratch[dev] = static_cast<int*>(p);
-    }
-    *out = g_scratch[dev];
+// Device address of the scratch array in the current device's context. The
+// array's host-side name is only a stand-in, not a device address, so the
+// address is looked up on every call (the lookup allocates nothing): a cached
+// address would dangle after a cudaDeviceReset, which reloads the module.
+int scratch_address(int** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return chaos::cuda_error(e, "scratch address");
+    *out = static_cast<int*>(p);
     return CHAOS_OK;
 }
 
@@ -71,7 +61,7 @@ extern "C" int chaos_point_dbscan_noalloc(const chaos_exec* ex, const double* in
     const int dev = ex->device >= 0 ? ex->device : prev;
     if (dev != prev && (e = cudaSetDevice(dev)) != cudaSuccess) return cuda_error(e, "set device");
     int* scratch = nullptr;
-    int rc = scratch_address(dev, &scratch);
+    int rc = scratch_address(&scratch);
     if (rc == CHAOS_OK) {
         // NULL selects the legacy default stream here: this entry creates no stream of its own
         cudaStream_t st = ex->stream ? (cudaStream_t)ex->stream : cudaStreamLegacy;

@@ -56,7 +56,9 @@ int parse_system(const char* s) {
     static const char* names[] = {"lorenz", "rossler", "chen", "chameleon", "rossler_cd", "sin3", "sin2", "memristor"};
     for (int i = 0; i < 8; ++i)
         if (std::strcmp(s, names[i]) == 0) return i;
-    return std::atoi(s);
+    char* end = nullptr;
+    const long v = std::strtol(s, &end, 10);
+    return (*s && end && *end == 0) ? (int)v : -1;  // -1: unknown (rejected by the caller)
 }
 
 void usage() {
@@ -222,6 +224,10 @@ int main(int argc, char** argv) {
             ++i;
         } else if (a == "--basins-system" && v) {
             o.basinsSystem = parse_system(v);
+            if (o.basinsSystem < 0) {
+                std::cerr << "chaos_perf: unknown system '" << v << "'\n";
+                return 2;
+            }
             ++i;
         } else {
             usage();

@@ -53,3 +53,20 @@ extern "C" int chaos_fma_probe(const chaos_exec* ex, long long iters, double* se
     *flops = (double)grid * 256.0 * (double)iters * 16.0;
     return c.finish(CHAOS_OK);
 }
+
+extern "C" int chaos_device_code_version(int device, int* binaryVersion, int* ptxVersion) {
+    using namespace chaos;
+    if (!binaryVersion || !ptxVersion) return set_error(CHAOS_E_ARGS, "bad version arguments");
+    int prev = 0;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e != cudaSuccess) return cuda_error(e, "get device");
+    const int dev = device >= 0 ? device : prev;
+    if (dev != prev && (e = cudaSetDevice(dev)) != cudaSuccess) return cuda_error(e, "set device");
+    cudaFuncAttributes fa{};
+    e = cudaFuncGetAttributes(&fa, fma_probe_kernel);
+    if (dev != prev) cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_error(e, "function attributes");
+    *binaryVersion = fa.binaryVersion;
+    *ptxVersion = fa.ptxVersion;
+    return CHAOS_OK;
+}

@@ -409,16 +409,18 @@ int chaos_server_destroy(chaos_server* server);
 
 /*
  * chaos_point_dbscan without any allocation. No counterpart in the reference:
- * for callers that must not allocate device memory during the call (work
- * captured into a CUDA graph, latency-critical loops, hosts that reserve
- * device memory through their own allocator). Every array is a device
- * pointer (ex->memory must be CHAOS_MEM_DEVICE); ex->stream NULL means the
- * legacy default stream; the call is asynchronous. The scratch rows live in
- * one fixed array compiled into the library (8 MiB per GPU that loads it, kept
- * until exit), so n * stride is limited to 1,048,576 (larger sizes return
- * CHAOS_E_ARGS). All calls share that array: calls whose kernels overlap on the
- * GPU race and must be serialised by the caller. The first call on a device
- * looks up the array's device address; make it before any stream capture.
+ * for callers that cannot call cudaMalloc during the call (hosts that reserve
+ * all device memory through their own allocator and budget, latency-critical
+ * loops where cudaMalloc / cudaFree would synchronise the device). Every array
+ * is a device pointer (ex->memory must be CHAOS_MEM_DEVICE); ex->stream NULL
+ * means the legacy default stream; the call is asynchronous. The scratch rows
+ * live in one fixed array compiled into the library (8 MiB per GPU that loads
+ * it, kept until exit), so n * stride is limited to 1,048,576 (larger sizes
+ * return CHAOS_E_ARGS). All calls share that array: calls whose kernels
+ * overlap on the GPU race and must be serialised by the caller. Every call
+ * looks up the array's device address in the current context (a lookup, no
+ * allocation); the first call on a device also loads the library's device
+ * code there, so make it before any stream capture.
  */
 int chaos_point_dbscan_noalloc(const chaos_exec* ex, const double* intervals, const int* counts, long long n,
                                int stride, double eps, int* labels);
@@ -495,6 +497,13 @@ int chaos_autotune(const chaos_exec* ex, double* table, int nTable);
  * integration kernels' roofline.
  */
 int chaos_fma_probe(const chaos_exec* ex, long long iters, double* seconds, double* flops);
+
+/*
+ * Architecture of the device code the library loaded on `device` (-1 = the
+ * current one): cudaFuncAttributes.binaryVersion and .ptxVersion of one of
+ * its kernels (103 for an sm_103a build). No reference counterpart.
+ */
+int chaos_device_code_version(int device, int* binaryVersion, int* ptxVersion);
 
 #ifdef __cplusplus
 }

@@ -24,7 +24,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 OUT = HERE / "_ref"
-REF = Path(os.environ.get("CHAOS_REFERENCE_DIR", "/root/reference"))
+# The reference checkout: CHAOS_REFERENCE_DIR, else a directory named
+# "reference" beside this repository.
+REF = Path(os.environ.get("CHAOS_REFERENCE_DIR") or (REPO.parent / "reference"))
 
 BIF_FUNCS = ["calculateTransTimeCUDA", "calculateDiscreteModelCUDA", "peakFinderCUDA", "dbscanCUDA",
              "getValueByIdx", "loopCalculateDiscreteModel_int", "peakFinder", "dbscan", "distance"]

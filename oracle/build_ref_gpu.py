@@ -28,7 +28,9 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 OUT = HERE / "_ref"
 STAGE = OUT / "gpu_src"
-REF = Path(os.environ.get("CHAOS_REFERENCE_DIR", "/root/reference"))
+# The reference checkout: CHAOS_REFERENCE_DIR, else a directory named
+# "reference" beside this repository.
+REF = Path(os.environ.get("CHAOS_REFERENCE_DIR") or (REPO.parent / "reference"))
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
 FILES = ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp",

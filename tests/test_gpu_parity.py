@@ -21,6 +21,12 @@ def eng_kw(kw):
                 transientTime=kw["transientTime"], values=kw["values"])
 
 
+def test_device_code_is_sm_103a(engine):
+    """The kernels that run were built for sm_103a (cudaFuncGetAttributes)."""
+    binary, ptx = engine.device_code_version(0)
+    assert binary == 103, (binary, ptx)
+
+
 @pytest.mark.parametrize("name", ["peaks_crafted", "peaks_random"])
 def test_peak_finder_golden(engine, name):
     g = golden(name)

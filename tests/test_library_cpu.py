@@ -50,11 +50,10 @@ def test_every_declared_symbol_is_exported(native):
         assert cxx in out, cxx
 
 
-def test_kernels_built_for_sm_103a(native):
-    out = subprocess.run(["cuobjdump", "--list-elf", str(native.lib_path())], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+def test_build_targets_sm_103a_only():
+    from chaoslibrary_gb300 import build as B
+
+    assert B.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def test_abi_version_and_system_info(native):
@@ -144,6 +143,34 @@ def test_compat_system_selection(native):
     assert L.chaos_compat_set_system(3) == 0
 
 
+def test_compat_unknown_system_name_is_an_error(native, tmp_path):
+    """CHAOS_SYSTEM with a name the library does not know makes the
+    reference-signature wrappers fail with CHAOS_E_ARGS instead of running
+    another system (fresh process: the selection is read once)."""
+    code = (
+        "import ctypes as C\n"
+        f"L = C.CDLL({str(native.lib_path())!r})\n"
+        "L.chaos_last_error.restype = C.c_char_p\n"
+        "assert L.chaos_compat_get_system() == -1\n"
+        "D = C.c_double * 3\n"
+        "f = L.chaos_compat_bifurcation1D\n"
+        "f.argtypes = [C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,\n"
+        "              C.c_double, C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_char_p]\n"
+        "ic, rg, v = D(0.1, 0.1, 0.1), D(20.0, 200.0, 0.0), D(10.0, 28.0, 8.0 / 3.0)\n"
+        "mv = (C.c_int * 1)(1)\n"
+        f"rc = f(1.0, 8, 0.01, 3, ic, rg, mv, 0, 1e4, 1.0, v, 3, 1, {str(tmp_path / 'out.csv')!r}.encode())\n"
+        "assert rc == -1, rc\n"
+        "assert b'unknown system' in L.chaos_last_error(), L.chaos_last_error()\n"
+    )
+    import os
+    import sys
+
+    env = {**os.environ, "CHAOS_SYSTEM": "lorenzz"}
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env)
+    assert out.returncode == 0, out.stderr
+    assert not (tmp_path / "out.csv").exists()
+
+
 def test_no_cpu_fallback(monkeypatch, tmp_path):
     """Without the built library the package raises instead of computing."""
     from chaoslibrary_gb300 import _native as N
@@ -163,3 +190,5 @@ def test_perf_cli_builds_and_parses(native, tmp_path):
     assert out.returncode == 0 and "--suite" in out.stdout
     bad = subprocess.run([str(cli), "--suite", "nothing"], capture_output=True, text=True)
     assert bad.returncode == 2
+    bad = subprocess.run([str(cli), "--basins-system", "sin33"], capture_output=True, text=True)
+    assert bad.returncode == 2 and "unknown system" in bad.stderr

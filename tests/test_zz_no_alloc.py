@@ -1,10 +1,12 @@
 """chaos_point_dbscan_noalloc: the per-point interval clustering of the 2-D
-bifurcation for callers that cannot allocate device memory during the call
-(graph capture, latency-critical loops, hosts that own all device memory
-through their own allocator). Its scratch is a fixed array inside the
-library, so the test calls it twice in a row through the C ABI and checks
-each result against the allocating entry point, chaos_point_dbscan, exactly
-(integer labels). Collected last on purpose: it runs alone or after the rest."""
+bifurcation for callers that cannot call cudaMalloc during the call (hosts
+that own all device memory through their own allocator and budget,
+latency-critical loops where an allocation would synchronise the device).
+Its scratch is a fixed array inside the library, so the test calls it twice
+in a row through the C ABI and checks each result against the allocating
+entry point, chaos_point_dbscan, exactly (integer labels). Counts below -1
+(accepted from callers) must give 0, as the reference's dbscan does for any
+count <= 0. Collected last on purpose: it runs alone or after the rest."""
 import ctypes as C
 
 import numpy as np
@@ -28,6 +30,7 @@ def _cases():
     rng = np.random.default_rng(99)
     iv = np.round(rng.uniform(0.3, 1.7, size=(500, 96)), 2)
     counts = rng.integers(-1, 97, size=500).astype(np.int32)
+    counts[:4] = [-2, -7, -1, 0]  # below -1: 0, as dbscan (bifurcationCUDA.cu:520-521) returns for P <= 0
     yield iv, counts, 0.02
 
 
@@ -50,6 +53,8 @@ def test_point_dbscan_noalloc_matches_allocating_entry(engine):
             assert rc == 0, engine.lib().chaos_last_error()
             torch.cuda.synchronize()
             assert np.array_equal(out.cpu().numpy(), expected), f"call {call}"
+        if counts[0] == -2:
+            assert list(expected[:4]) == [0, 0, -1, 0]
 
 
 def test_point_dbscan_noalloc_rejects_oversize(engine):
