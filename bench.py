@@ -7,17 +7,21 @@ a in [0.1, 0.4] x c in [2, 10] on a 1024 x 1024 grid, b = 0.2, x0 = (1,1,1),
 5,000 transient steps, then 5,002 Benettin blocks of 10 steps of the orbit
 and of its twin (offset 1e-8 along x): 105,040 trajectory-steps per grid
 point, 1.101e11 per map. One bench step = one full map. The engine arm runs
-the FP32 kernel (exact-difference twin, FP64 log-stretch sum); the line also
-carries the plain FP64 kernel's rate and the FP32 map's error against FP64.
+the float-float kernel (CHAOS_FF32: the orbit in two FP32 words, ~48 bits,
+on the FP32 pipe; the twin as an exact FP32 difference; exact log-stretch
+sum), whose map agrees with the plain FP64 map as closely as the FP64 map
+agrees with itself started 1e-13 away. The line also carries, on the same
+1024^2 map, the plain FP64 kernel's rate, the FP32 kernel's rate and
+roofline, and every map's error against FP64.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
                   [--workload lle|bif1d|bif2d|basins|spectrum|batch|serve]
-                  [--precision fp32|fp64]
+                  [--precision auto|ff32|fp32|fp64]
 
---impl reference times the CPU path of the reference algorithm (the oracle's
-C++ restatement, OpenMP over all host cores) on a bounded sample of the same
-workload; the reference itself has no CPU implementation and its GPU code
-cannot be built or run on the benchmark machine.
+--impl reference times the reference's own per-thread code for the path,
+compiled for the host (FP64, OpenMP over all host cores), on a bounded sample
+of the same workload (the reference has no CPU implementation of its own; its
+GPU build is timed separately as reference_gpu).
 """
 from __future__ import annotations
 
@@ -368,7 +372,7 @@ def reference_arm(args, ws, rank):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_of(args), "cpu_baseline": {**last, "value": v},
+            "config": {**config_of(args), "precision": "fp64"}, "cpu_baseline": {**last, "value": v},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -380,8 +384,15 @@ def config_of(args):
         return {"workload": "LLE map, Rossler RK4 h=0.01, a in [0.1,0.4] x c in [2,10], 1024x1024, b=0.2, "
                             "x0=(1,1,1), 5000 transient + 5002 blocks x 10 steps x 2 trajectories",
                 "grid_points": 1048576, "steps_per_point": lle_steps_per_point(LLE), "eps": 1e-8,
-                "precision": args.precision, "l2": "256 MB buffer written between timed steps; the map's state "
-                                                  "lives in registers (inputs: 88 B of parameters)"}
+                "precision": args.precision,
+                "arithmetic": {"ff32": "float-float orbit (two FP32 words, ~48 bits, FP32 pipe), twin as an "
+                                       "exact FP32 difference, exact power-of-two renormalisation, FP64 log",
+                               "fp32": "FP32 orbit, twin as an exact FP32 difference, exact power-of-two "
+                                       "renormalisation, FP64 log",
+                               "fp64": "FP64 orbit and twin, the reference's per-block FP64 norm and log"
+                               }.get(args.precision),
+                "l2": "256 MB buffer written between timed steps; the map's state "
+                      "lives in registers (inputs: 88 B of parameters)"}
     if args.workload == "spectrum":
         return {"workload": "Lyapunov spectrum (Gram-Schmidt per block), Lorenz RK4 h=0.01, rho in [20,200] x "
                             "sigma in [5,15], 1024x1024, beta=8/3, x0=(1,1,1), 2000 transient steps + 1002 blocks "
@@ -414,6 +425,21 @@ def traffic_from_profiles(kernel_tag: str):
         return None
     for line in p.read_text().splitlines():
         if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def pipe_busy_from_profiles(kernel_tag: str):
+    """FMA-pipe busy fraction recorded in profiles/<kernel_tag>.md (a line
+    'fp32_pipe_busy: F'), or None."""
+    p = ROOT / "profiles" / f"{kernel_tag}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("fp32_pipe_busy:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -637,7 +663,7 @@ def engine_arm(args, ws, rank, local):
     torch.cuda.set_device(dev)
     if args.lle_variant:
         C.set_tuning(C.TUNE_LLE_F32_VARIANT, args.lle_variant)
-    prec = C.FP32 if args.precision == "fp32" else C.FP64
+    prec = {"fp32": C.FP32, "fp64": C.FP64, "ff32": C.FF32}[args.precision]
     w = {"lle": LLE, "bif1d": BIF1D, "bif2d": BIF2D, "basins": BASINS, "spectrum": SPECTRUM}[args.workload]
     n_points = w["nPts"] ** (1 if args.workload == "bif1d" else 2)
     if args.workload == "spectrum":
@@ -664,7 +690,7 @@ def engine_arm(args, ws, rank, local):
             return C.lle2d(w["system"], precision=prec, **kw)
         d2h = n_points * 8
         tag = f"lle_{args.precision}_rossler_1024"
-        line_extra = {"lle_variant": C.get_tuning(C.TUNE_LLE_F32_VARIANT)}
+        line_extra = {"lle_variant": C.get_tuning(C.TUNE_LLE_F32_VARIANT)} if prec == C.FP32 else {}
     elif args.workload == "bif1d":
         steps_pp = sweep_steps_per_point(w)
         cap = 64
@@ -739,7 +765,7 @@ def engine_arm(args, ws, rank, local):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == C.FP32 else "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": {C.FP32: "f32", C.FP64: "f64", C.FF32: "ff32"}[prec],
             "data": "synthetic (deterministic parameter / initial-condition grids)",
             "config": config_of(args), "clocks": clocks, "wall_s_timed_region": wall, "gpu_launches": launches}
     if args.workload == "lle":
@@ -753,13 +779,19 @@ def engine_arm(args, ws, rank, local):
         mean_s = statistics.mean(ms) / 1e3
         algo = w["flops"] * steps_per_call
         achieved = algo / mean_s / 1e12
-        peak = C.fma_probe() / 1e12 if prec == C.FP32 else None
-        line["roofline"] = {"bound": "fp32_fma" if prec == C.FP32 else "fp64_fma", "achieved": achieved,
+        peak = C.fma_probe() / 1e12 if prec in (C.FP32, C.FF32) else None
+        line["roofline"] = {"bound": "fp64_fma" if prec == C.FP64 else "fp32_fma", "achieved": achieved,
                             "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
                             "traffic": traffic_from_profiles(tag) if tag else None,
                             "algorithmic": f"{w['flops']} flops per RK4 step x {steps_per_call:.4g} steps per launch",
                             "peak_source": "measured in this run: FP32 fmaf-chain probe (chaos_fma_probe), "
                                            "2048 threads/SM; MEASURED_PEAKS.json has only HBM and bf16 tensor peaks"}
+        if prec == C.FF32:
+            line["roofline"]["note"] = (
+                "float-float arithmetic issues ~7 FP32 operations per algorithmic flop, so the algorithmic "
+                "fraction is low by construction; fp32_pipe_busy is the FMA pipe's busy fraction in the ncu "
+                "capture of this kernel")
+            line["roofline"]["fp32_pipe_busy"] = pipe_busy_from_profiles(tag)
 
     # e2e through the public API with host buffers (copies inside the timed region)
     t_e2e = []
@@ -784,8 +816,10 @@ def engine_arm(args, ws, rank, local):
             line["reference_gpu"] = ref
     if rank == 0 and ws == 1 and args.workload == "bif2d" and not args.no_extras:
         line.update(bif2d_extras(C, prec, w))
-    if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras:
-        line.update(lle_precision_report(C, prec, dev))
+    if rank == 0 and ws == 1 and args.workload == "lle" and not args.no_extras and not args.npts \
+            and not args.tmax:
+        line.update(lle_precision_report(C, prec, dev, w, out.cpu().numpy(), statistics.mean(ms) / 1e3,
+                                         line.get("roofline", {}).get("peak")))
     if rank == 0 and ws == 1 and args.workload == "basins" and not args.no_extras:
         line.update(basins_extras(C, prec, dev, w))
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -976,61 +1010,100 @@ def basins_extras(C, prec, dev, w):
     return out
 
 
-def lle_precision_report(C, prec, dev):
-    """Plain FP64 kernel rate and the FP32 map's error against it, on the
-    512x512 map over the same parameter ranges (262,144 points)."""
+REGULAR = 0.005  # a point is "regular" (periodic orbit or fixed point) when its FP64 LLE is below this
+
+
+def lle_error_stats(v, a):
+    """|v - a| over the points finite in both maps (a = the plain FP64 map):
+    quantiles, the fraction within 1e-3, the same over the regular points,
+    agreement of the chaotic class (LLE > 0.01) and the points finite in one
+    map and not the other."""
+    fin = np.isfinite(a) & np.isfinite(v)
+    d = np.abs(v[fin] - a[fin])
+    reg = a[fin] < REGULAR
+    return {"points": int(fin.sum()), "p50": float(np.median(d)), "p90": float(np.percentile(d, 90)),
+            "p99": float(np.percentile(d, 99)), "max": float(d.max()), "frac_le_1e-3": float(np.mean(d <= 1e-3)),
+            "regular_points": int(reg.sum()), "regular_frac_le_1e-3": float(np.mean(d[reg] <= 1e-3)),
+            "regular_max": float(d[reg].max()) if reg.any() else None,
+            "chaotic_class_agreement": float(np.mean((a[fin] > 0.01) == (v[fin] > 0.01))),
+            "nonfinite_mismatch": int(np.sum(np.isfinite(a) != np.isfinite(v)))}
+
+
+def lle_precision_report(C, prec, dev, w, head_map, head_s, fma_peak):
+    """Everything on the benchmark's own 1024x1024 map: the plain FP64
+    kernel's rate (one timed launch) and map; the FP64 map started 1e-13
+    away in x (the finite-time LLE's own sensitivity: the self-spread every
+    other arithmetic is measured against); the float-float map of the timed
+    region; the FP32 kernel's rate and roofline under its three stretch
+    measurements (CHAOS_TUNE_LLE_RENORM 0/1/2: exact power-of-two, per-block
+    FP32 log, per-block FP64 norm and log); each map's error against FP64;
+    and the FP32 map with the FP64 sign re-check."""
     import torch
 
-    w = dict(LLE)
-    w["nPts"] = 512
     kw = kw_of(w)
-    n = 512 * 512
-    o64 = torch.empty(n, dtype=torch.float64, device=dev)
-    o32 = torch.empty(n, dtype=torch.float64, device=dev)
-    C.lle2d("rossler", precision=C.FP64, out=o64, **dict(kw, nPts=64))  # warm-up
-    torch.cuda.synchronize()
+    n = w["nPts"] ** 2
+    steps = n * lle_steps_per_point(w)
+    buf = torch.empty(n, dtype=torch.float64, device=dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    C.lle2d("rossler", precision=C.FP64, out=o64, **kw)
-    e1.record()
-    torch.cuda.synchronize()
-    t64 = e0.elapsed_time(e1) / 1e3
-    e0.record()
-    C.lle2d("rossler", precision=C.FP32, out=o32, **kw)
-    e1.record()
-    torch.cuda.synchronize()
-    t32 = e0.elapsed_time(e1) / 1e3
+
+    def run(p, **over):
+        e0.record()
+        C.lle2d(w["system"], precision=p, out=buf, **dict(kw, **over))
+        e1.record()
+        torch.cuda.synchronize()
+        return buf.cpu().numpy().copy(), e0.elapsed_time(e1) / 1e3
+
+    run(C.FP64, nPts=64)  # warm-up launch
+    a, t64 = run(C.FP64)
+    ic = list(w["initialConditions"])
+    p13, _ = run(C.FP64, initialConditions=[ic[0] + 1e-13] + ic[1:])
+    self_spread = lle_error_stats(p13, a)
+    out = {"fp64_plain": {"value": steps / t64, "unit": UNIT, "seconds": t64,
+                          "map": f"{w['nPts']}x{w['nPts']} (the benchmark's map), one launch"}}
+    errs = {"fp64_started_1e-13_away": self_spread}
+
+    def vs_self(st):
+        return {**st, "p50_vs_self_spread": st["p50"] / self_spread["p50"],
+                "p90_vs_self_spread": st["p90"] / self_spread["p90"]}
+    if prec == C.FF32:
+        errs["ff32"] = vs_self(lle_error_stats(head_map, a))
+        out["speedup_vs_fp64_plain"] = {"ff32": t64 / head_s}
+    fp32 = {}
+    old = C.get_tuning(C.TUNE_LLE_RENORM)
+    for mode, name in ((0, "pow2_exact"), (1, "fp32_log_per_block"), (2, "fp64_norm_log_per_block")):
+        C.set_tuning(C.TUNE_LLE_RENORM, mode)
+        run(C.FP32, nPts=64)
+        v, t32 = run(C.FP32)
+        fp32[name] = {"value": steps / t32, "unit": UNIT, "seconds": t32,
+                      "error_vs_fp64": vs_self(lle_error_stats(v, a))}
+        if mode == 0:
+            achieved = w["flops"] * steps / t32 / 1e12
+            fp32[name]["roofline"] = {"bound": "fp32_fma", "achieved": achieved, "peak": fma_peak,
+                                      "unit": "TFLOP/s", "frac": achieved / fma_peak if fma_peak else None}
+            errs["fp32"] = fp32[name]["error_vs_fp64"]
+            out.setdefault("speedup_vs_fp64_plain", {})["fp32"] = t64 / t32
+    C.set_tuning(C.TUNE_LLE_RENORM, old)
+    out["fp32"] = {"renorm_ablation": fp32,
+                   "note": "the FP32 map's error does not depend on how the stretch is measured: it comes from "
+                           "the FP32 orbit (rounded at 2^-24 every step), which the float-float orbit removes"}
+    out["lle_error_vs_fp64"] = {**errs, "regular": f"FP64 LLE < {REGULAR}"}
     # FP32 map with the FP64 sign re-check of the points within 0.01 of zero
-    # (short check over tMax / 10 time units)
-    C.lle2d_checked("rossler", **dict(kw, nPts=64))
+    C.lle2d_checked(w["system"], **dict(kw, nPts=64))
     e0.record()
-    oc, n_checked, n_replaced = C.lle2d_checked("rossler", band=0.01, checkTMax=w["tMax"] / 10, **kw)
+    oc, n_checked, n_replaced = C.lle2d_checked(w["system"], band=0.01, checkTMax=w["tMax"] / 10, **kw)
     e1.record()
     torch.cuda.synchronize()
     tc = e0.elapsed_time(e1) / 1e3
-    a, b = o64.cpu().numpy(), o32.cpu().numpy()
 
     def cls(v):
         return np.where(~np.isfinite(v), -1, (v > 0).astype(int))
-    recheck = {"band": 0.01, "check_tmax": w["tMax"] / 10, "points_checked": n_checked,
-               "points_replaced": n_replaced, "value": n * lle_steps_per_point(w) / tc, "unit": UNIT,
-               "time_vs_fp32": tc / t32,
-               "sign_class_agreement_with_fp64": {"fp32": float(np.mean(cls(b) == cls(a))),
-                                                  "fp32_rechecked": float(np.mean(cls(oc) == cls(a)))}}
-    fin = np.isfinite(a) & np.isfinite(b)
-    d = np.abs(a[fin] - b[fin])
-    reg = a[fin] < 0.005
-    steps = n * lle_steps_per_point(w)
-    return {"fp64_plain": {"value": steps / t64, "unit": UNIT, "map": "512x512 (same ranges)",
-                           "fp32_same_map": steps / t32, "speedup_fp32_vs_fp64": t64 / t32},
-            "lle_error_vs_fp64": {"points": int(fin.sum()), "p50": float(np.median(d)),
-                                  "p90": float(np.percentile(d, 90)), "p99": float(np.percentile(d, 99)),
-                                  "max": float(d.max()), "frac_le_1e-3": float(np.mean(d <= 1e-3)),
-                                  "regular_points": int(reg.sum()),
-                                  "regular_max": float(d[reg].max()) if reg.any() else None,
-                                  "chaotic_class_agreement": float(np.mean((a[fin] > 0.01) == (b[fin] > 0.01))),
-                                  "nonfinite_mismatch": int(np.sum(np.isfinite(a) != np.isfinite(b)))},
-            "fp64_sign_recheck": recheck}
+    out["fp64_sign_recheck"] = {
+        "band": 0.01, "check_tmax": w["tMax"] / 10, "points_checked": n_checked, "points_replaced": n_replaced,
+        "value": steps / tc, "unit": UNIT,
+        "sign_class_agreement_with_fp64": {"fp32_rechecked": float(np.mean(cls(oc) == cls(a))),
+                                           "ff32": float(np.mean(cls(head_map) == cls(a)))
+                                           if prec == C.FF32 else None}}
+    return out
 
 
 def main():
@@ -1045,13 +1118,17 @@ def main():
     ap.add_argument("--rate", type=float, default=100.0, help="served stream arrival rate (requests/s)")
     ap.add_argument("--hbm-budget-gb", type=int, default=64)
     ap.add_argument("--iteration-steps", type=float, default=2e10)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "ff32", "fp32", "fp64"],
+                    help="auto: ff32 for the LLE map (the arithmetic that meets the FP64 map's own spread), "
+                         "fp32 for the other workloads")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--lle-variant", type=int, default=0, help="FP32 LLE kernel variant (0 default, 2, 12, 16)")
     ap.add_argument("--npts", type=int, default=None, help="grid resolution override (profiling runs only)")
     ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()
+    if args.precision == "auto":
+        args.precision = "ff32" if args.workload == "lle" and args.impl == "engine" else "fp32"
     for w in (LLE, BIF1D, BIF2D, BASINS, SPECTRUM):
         if args.npts:
             w["nPts"] = args.npts

@@ -9,7 +9,7 @@ from types import SimpleNamespace
 import numpy as np
 
 _PKG = Path(__file__).resolve().parent
-FP64, FP32 = 0, 1
+FP64, FP32, FF32 = 0, 1, 2  # CHAOS_FP64, CHAOS_FP32, CHAOS_FF32
 CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
 MEM_HOST, MEM_DEVICE = 0, 1
 SYSTEMS = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3, "rossler_cd": 4, "sin3": 5, "sin2": 6,
@@ -137,9 +137,15 @@ def _sys(system) -> int:
     return SYSTEMS[system] if isinstance(system, str) else int(system)
 
 
+_PREC_NAMES = {"fp64": FP64, "f64": FP64, "float64": FP64, "fp32": FP32, "f32": FP32, "float32": FP32,
+               "ff32": FF32, "float-float": FF32}
+
+
 def _prec(precision) -> int:
     if isinstance(precision, str):
-        return FP32 if precision.lower() in ("fp32", "f32", "float32") else FP64
+        if precision.lower() not in _PREC_NAMES:
+            raise ChaosError(-1, f"unknown precision {precision!r} (fp64, fp32 or ff32)")
+        return _PREC_NAMES[precision.lower()]
     return int(precision)
 
 
@@ -247,6 +253,8 @@ TUNE_GRID_FMA = 3
 TUNE_LLE_TWIN = 4
 TUNE_BIF2D_CAP = 5
 TUNE_SHAPES = 6
+TUNE_LLE_RENORM = 7
+TUNE_FF_PAIRS = 8
 
 
 def set_tuning(knob: int, value: int) -> None:

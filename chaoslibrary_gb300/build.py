@@ -25,6 +25,7 @@ SOURCES = [
     ("kern_f64.cu", ["--fmad=false"]),
     ("tune.cu", []),
     ("kern_f32.cu", []),
+    ("kern_ff.cu", ["--fmad=false"]),
     ("dbscan.cu", ["--fmad=false", "--extended-lambda"]),
     ("basins_dbscan.cu", ["--fmad=false"]),
     ("capi.cu", []),

@@ -110,8 +110,8 @@ int aux_streams(int dev, std::vector<cudaStream_t>& out) {
 
 int Call::begin(const chaos_exec* e) {
     ex = e ? *e : chaos_exec{CHAOS_FP64, CHAOS_MEM_HOST, nullptr, -1};
-    if (ex.precision != CHAOS_FP64 && ex.precision != CHAOS_FP32)
-        return set_error(CHAOS_E_ARGS, "precision must be CHAOS_FP64 or CHAOS_FP32");
+    if (ex.precision != CHAOS_FP64 && ex.precision != CHAOS_FP32 && ex.precision != CHAOS_FF32)
+        return set_error(CHAOS_E_ARGS, "precision must be CHAOS_FP64, CHAOS_FP32 or CHAOS_FF32");
     if (ex.memory != CHAOS_MEM_HOST && ex.memory != CHAOS_MEM_DEVICE)
         return set_error(CHAOS_E_ARGS, "memory must be CHAOS_MEM_HOST or CHAOS_MEM_DEVICE");
     cudaError_t err = cudaGetDevice(&prevDevice);
@@ -204,6 +204,24 @@ static int check_system(int system, int nIC, int nValues) {
     return CHAOS_OK;
 }
 
+// CHAOS_FF32 is implemented for the LLE maps and trajectories of the RK4
+// systems; the other sweeps refuse it instead of running another precision.
+static int no_ff32(const chaos_exec* ex, const char* what) {
+    if (ex && ex->precision == CHAOS_FF32)
+        return set_error(CHAOS_E_UNSUPPORTED, "CHAOS_FF32 runs the LLE maps (chaos_lle2d, chaos_lle_sweep) and "
+                                              "chaos_trajectory of the RK4 systems; %s takes CHAOS_FP64 or CHAOS_FP32",
+                         what);
+    return CHAOS_OK;
+}
+// CHAOS_FF32 LLE: the RK4 systems (the twin as an exact difference) with the twin at x + eps e_x.
+static int check_ff32_lle(const chaos_exec* ex, int system, const LleParams& L) {
+    if (!ex || ex->precision != CHAOS_FF32) return CHAOS_OK;
+    if (system == SYS_USER || !system_has_difference_form(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "CHAOS_FF32 LLE needs an RK4 system (0-2); use CHAOS_FP64");
+    if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+    return CHAOS_OK;
+}
+
 // precision / plug-in dispatch of the sweep kernels
 static cudaError_t run_bif(int prec, const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_bif_user(P, O, st);
@@ -218,7 +236,8 @@ static cudaError_t run_basins(int prec, const SweepParams& P, const BasinsOut& O
     return prec == CHAOS_FP32 ? launch_basins_f32(P, O, st) : launch_basins_f64(P, O, st);
 }
 static cudaError_t run_lle(int prec, const LleParams& L, double* out, cudaStream_t st) {
-    if (L.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_lle_user(L, out, st);
+    if (L.system == SYS_USER) return prec != CHAOS_FP64 ? cudaErrorNotSupported : launch_lle_user(L, out, st);
+    if (prec == CHAOS_FF32) return launch_lle_ff(L, out, st);
     return prec == CHAOS_FP32 ? launch_lle_f32(L, out, st) : launch_lle_f64(L, out, st);
 }
 
@@ -447,6 +466,7 @@ static int bif1d_run(const chaos_exec* ex, SweepParams P, int gridMode, const do
     if (!counts || !flags) return set_error(CHAOS_E_ARGS, "counts and flags are required");
     if (peakCapacity < 0 || ((peaks || intervals) && peakCapacity == 0))
         return set_error(CHAOS_E_ARGS, "peakCapacity must be > 0 when peaks or intervals are requested");
+    if ((rc = no_ff32(ex, "the bifurcation sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     if ((rc = upload_log_axes(c, gridMode, P.dim, (int)P.grid.nPts, ranges, P.grid.table))) return c.finish(rc);
@@ -475,6 +495,7 @@ static int bif2d_run(const chaos_exec* ex, SweepParams P, int gridMode, const do
                      int* labels, int* counts) {
     int rc = CHAOS_OK;
     if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
+    if ((rc = no_ff32(ex, "the bifurcation sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     if ((rc = upload_log_axes(c, gridMode, P.dim, (int)P.grid.nPts, ranges, P.grid.table))) return c.finish(rc);
@@ -634,6 +655,7 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
         return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+    if ((rc = check_ff32_lle(ex, system, L))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
@@ -658,6 +680,7 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
         return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+    if ((rc = check_ff32_lle(ex, system, L))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);
@@ -680,6 +703,7 @@ int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridM
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
                        indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
         return rc;
+    if ((rc = no_ff32(ex, "the Lyapunov spectrum"))) return rc;
     const bool fp32 = ex && ex->precision == CHAOS_FP32;
     if (fp32 && !system_has_fp32_lle(system))
         return set_error(CHAOS_E_UNSUPPORTED,
@@ -762,6 +786,7 @@ int chaos_basins_features(const chaos_exec* ex, int system, double tMax, int nPt
                         true);
     if (rc) return rc;
     if (!flags || !avgPeaks || !avgIntervals) return set_error(CHAOS_E_ARGS, "flags, avgPeaks and avgIntervals are required");
+    if ((rc = no_ff32(ex, "the basins sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     const long long n = P.nPoints;
@@ -792,6 +817,7 @@ int chaos_basins(const chaos_exec* ex, int system, double tMax, int nPts, double
     if (rc) return rc;
     if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
     if (!(eps >= 0)) return set_error(CHAOS_E_ARGS, "eps must be >= 0");
+    if ((rc = no_ff32(ex, "the basins sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     const long long n = P.nPoints;
@@ -825,6 +851,7 @@ int chaos_basins_dbscan(const chaos_exec* ex, int system, double tMax, int nPts,
     if (rc) return rc;
     if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
     if (!(eps > 0) || minPts < 1) return set_error(CHAOS_E_ARGS, "need eps > 0 and minPts >= 1");
+    if ((rc = no_ff32(ex, "the basins sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     const long long n = P.nPoints;
@@ -936,6 +963,11 @@ int chaos_set_tuning(int knob, int value) {
         return set_lle_variant(value) == 0 ? CHAOS_OK : set_error(CHAOS_E_ARGS, "LLE variant must be 0, 2, 12 or 16");
     if (knob == CHAOS_TUNE_SWEEP_PAIRS)
         return set_sweep_pairs(value) ? set_error(CHAOS_E_ARGS, "sweep-pairs mode %d (0, 1, 2 or 3)", value) : CHAOS_OK;
+    if (knob == CHAOS_TUNE_LLE_RENORM)
+        return set_lle_renorm(value) ? set_error(CHAOS_E_ARGS, "LLE renormalisation mode %d (0, 1 or 2)", value)
+                                     : CHAOS_OK;
+    if (knob == CHAOS_TUNE_FF_PAIRS)
+        return set_ff_pairs(value) ? set_error(CHAOS_E_ARGS, "float-float pairs mode %d (0 or 1)", value) : CHAOS_OK;
     if (knob == CHAOS_TUNE_SHAPES) {
         if (value != 0) return set_error(CHAOS_E_ARGS, "CHAOS_TUNE_SHAPES takes 0 (forget tuned shapes)");
         for (int k = 0; k < 3; ++k)
@@ -961,6 +993,8 @@ int chaos_get_tuning(int knob) {
     if (knob == CHAOS_TUNE_GRID_FMA) return g_grid_fma.load();
     if (knob == CHAOS_TUNE_LLE_TWIN) return g_lle_twin.load();
     if (knob == CHAOS_TUNE_BIF2D_CAP) return g_bif2d_cap.load();
+    if (knob == CHAOS_TUNE_LLE_RENORM) return get_lle_renorm();
+    if (knob == CHAOS_TUNE_FF_PAIRS) return get_ff_pairs();
     return set_error(CHAOS_E_ARGS, "unknown tuning knob %d", knob);
 }
 
@@ -971,6 +1005,8 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
     if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
     if (nTraj < 0 || nSteps < 0 || !(h == h) || (nTraj > 0 && (!x0 || !a || !out)))
         return set_error(CHAOS_E_ARGS, "bad trajectory arguments");
+    if (ex && ex->precision == CHAOS_FF32 && !system_has_difference_form(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "CHAOS_FF32 trajectories need an RK4 system (0-2)");
     Call c;
     int rc = c.begin(ex);
     if (rc) return rc;
@@ -984,8 +1020,10 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e;
     if (system == SYS_USER)
-        e = c.ex.precision == CHAOS_FP32 ? cudaErrorNotSupported
+        e = c.ex.precision != CHAOS_FP64 ? cudaErrorNotSupported
                                          : launch_trajectory_user(dX, dA, h, nSteps, dO, nTraj, c.stream);
+    else if (c.ex.precision == CHAOS_FF32)
+        e = launch_trajectory_ff(system, dX, dA, h, nSteps, dO, nTraj, c.stream);
     else
         e = c.ex.precision == CHAOS_FP32 ? launch_trajectory_f32(system, dX, dA, h, nSteps, dO, nTraj, c.stream)
                                          : launch_trajectory_f64(system, dX, dA, h, nSteps, dO, nTraj, c.stream);

@@ -42,13 +42,35 @@ int active_system() {
     return s ? parse_system(s) : CHAOS_SYS_CHAMELEON;
 }
 
-chaos_exec active_exec() {
+// The arithmetic chosen by chaos_compat_set_precision or CHAOS_PRECISION
+// (fp64 / fp32 / ff32).
+chaos_exec chosen_exec() {
     int prec = g_precision;
     if (prec < 0) {
         const char* s = getenv("CHAOS_PRECISION");
-        prec = (s && (strcmp(s, "fp32") == 0 || strcmp(s, "1") == 0)) ? CHAOS_FP32 : CHAOS_FP64;
+        prec = (s && (strcmp(s, "fp32") == 0 || strcmp(s, "1") == 0))   ? CHAOS_FP32
+               : (s && (strcmp(s, "ff32") == 0 || strcmp(s, "2") == 0)) ? CHAOS_FF32
+                                                                       : CHAOS_FP64;
     }
     return chaos_exec{prec, CHAOS_MEM_HOST, nullptr, -1};
+}
+
+// The bifurcation and basins wrappers: float-float is an LLE arithmetic, so
+// CHAOS_FF32 runs these sweeps in FP64.
+chaos_exec active_exec() {
+    chaos_exec ex = chosen_exec();
+    if (ex.precision == CHAOS_FF32) ex.precision = CHAOS_FP64;
+    return ex;
+}
+
+// The LLE wrappers: FP32 where the engine has it (the RK4 systems and
+// Chameleon), float-float for the RK4 systems; FP64 otherwise.
+chaos_exec lle_exec() {
+    chaos_exec ex = chosen_exec();
+    const int sys = active_system();
+    if (ex.precision == CHAOS_FP32 && sys > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
+    if (ex.precision == CHAOS_FF32 && sys > CHAOS_SYS_CHEN_RK4) ex.precision = CHAOS_FP64;
+    return ex;
 }
 
 // getValueByIdx as the reference's host code evaluates it for the CSV
@@ -134,7 +156,8 @@ int chaos_compat_set_system(int system) {
 }
 
 int chaos_compat_set_precision(int precision) {
-    if (precision != CHAOS_FP64 && precision != CHAOS_FP32) return chaos::set_error(CHAOS_E_ARGS, "bad precision");
+    if (precision != CHAOS_FP64 && precision != CHAOS_FP32 && precision != CHAOS_FF32)
+        return chaos::set_error(CHAOS_E_ARGS, "bad precision");
     g_precision = precision;
     return CHAOS_OK;
 }
@@ -202,8 +225,7 @@ int chaos_compat_LLE2D(double tMax, double NT, int nPts, double h, double eps, c
         if (nPts < 1) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 1");
         const long long n = (long long)nPts * nPts;
         std::vector<double> lle(n);
-        chaos_exec ex = active_exec();
-        if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
+        chaos_exec ex = lle_exec();
         std::ofstream o(OUT_FILE_PATH);
         if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
         o << ranges[0] << " " << ranges[1] << "\n";
@@ -282,13 +304,6 @@ static int legacy_bif1d(int gridMode, double tMax, int nPts, double h, int amoun
     return o.good() ? CHAOS_OK : chaos::set_error(CHAOS_E_IO, "write failed: %s", OUT_FILE_PATH);
 }
 
-// The arithmetic of the LLE-type wrappers: FP32 only where the engine has it
-// (the RK4 systems and Chameleon).
-static chaos_exec lle_exec() {
-    chaos_exec ex = active_exec();
-    if (ex.precision == CHAOS_FP32 && active_system() > CHAOS_SYS_CHAMELEON) ex.precision = CHAOS_FP64;
-    return ex;
-}
 
 // LLE1D / LLE1DIC: rows "value, lle" at precision 12, no header
 // (debri/hostLibrary.cu:3291-3300, 3508-3517); LLE2DIC: the matrix rule at the
@@ -329,6 +344,7 @@ static int legacy_ls(int dim, double tMax, double NT, int nPts, double h, double
     const int nx = amountOfInitialConditions;
     std::vector<double> sp((size_t)n * nx);
     chaos_exec ex = lle_exec();
+    if (ex.precision == CHAOS_FF32) ex.precision = CHAOS_FP64;  // the spectrum has no float-float kernel
     int rc = chaos_lyapunov_spectrum(&ex, active_system(), dim, 0, tMax, NT, nPts, h, eps, initialConditions,
                                      amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
                                      amountOfValues, sp.data());

@@ -16,6 +16,7 @@
 #include "launch.h"
 #include "peaks.h"
 #include "systems.h"
+#include "ff.h"
 
 namespace chaos {
 
@@ -398,12 +399,91 @@ __device__ __forceinline__ double lle_point_full(const LleParams& L, long long p
 
 // LLE point with the twin carried as the exact difference e = q - x (only for
 // the quadratic RK4 systems): x and e in FP32 registers. Same block count and
-// division by tMax as above. Per block the stretch is measured as
-// log2(|e|^2 / eps^2) with the SFU (__log2f) and e is rescaled to length eps
-// with rsqrtf; the per-block logs are summed in FP32 over groups of
-// kLleGroup blocks and every group sum is added to an FP64 accumulator, so the
-// FP64 pipe (1/64 of the FP32 rate on this GPU) sees one add per group.
+// division by tMax as above. How the stretch of every block is measured and
+// the twin renormalised is the Stretch mode:
+//   kRenormPow2 (default): e is scaled by a power of two 2^-k that brings |e|
+//     back to within a factor sqrt(2) of eps -- exact in FP32 -- and k is
+//     summed as an integer, so the sum of the blocks' log-stretches telescopes
+//     exactly to k ln 2 + log(|e_final| / eps), taken once in FP64 from the
+//     FP64 norm of the final e (ff.h);
+//   kRenormF32Log: log2(|e|^2 / eps^2) per block on the SFU (__log2f), e
+//     rescaled to length eps with rsqrtf, the logs summed in FP32 over groups
+//     of kLleGroup blocks and the group sums in FP64;
+//   kRenormF64: the reference's arithmetic (LLE/src/LLECUDA.cu:146-162):
+//     dist = sqrt(sum (x - p)^2) / eps in FP64, sum += log(dist), e /= dist.
+enum LleRenorm { kRenormPow2 = 0, kRenormF32Log = 1, kRenormF64 = 2 };
 constexpr int kLleGroup = 16;
+
+__device__ __forceinline__ double nan_if_not_finite(double v) {
+    return isfinite(v) ? v : __longlong_as_double(0x7ff8000000000000LL);
+}
+
+template <int RN> struct Stretch;
+template <> struct Stretch<kRenormPow2> {
+    float e0;
+    int eps2Exp, k = 0;
+    double v = 0.0;
+    __device__ __forceinline__ explicit Stretch(float eps) : e0(eps) {
+        eps2Exp = (int)((__float_as_uint(eps * eps) >> 23) & 0xff) - 126;
+    }
+    __device__ __forceinline__ float renorm(float e0_, float e1, float e2) {
+        const int j = pow2_rescale_exponent(fmaf(e0_, e0_, fmaf(e1, e1, e2 * e2)), eps2Exp);
+        k += j;
+        return pow2_scale(j);
+    }
+    __device__ __forceinline__ void last(float e0_, float e1, float e2) {
+        const double n2 = (double)e0_ * e0_ + (double)e1 * e1 + (double)e2 * e2;
+        v = pow2_log_stretch(k, n2, (double)e0);
+    }
+    __device__ __forceinline__ double result(double tMax) const { return nan_if_not_finite(v / tMax); }
+};
+template <> struct Stretch<kRenormF32Log> {
+    float eps, inv_eps2, part = 0.f;
+    int cnt = 0;
+    double sum = 0.0;  // sum of log2(d^2)
+    __device__ __forceinline__ Stretch(float eps_, double epsd) : eps(eps_), inv_eps2((float)(1.0 / (epsd * epsd))) {}
+    __device__ __forceinline__ float add(float n2) {
+        part += __log2f(n2 * inv_eps2);
+        if (++cnt == kLleGroup) {
+            sum += (double)part;
+            part = 0.f;
+            cnt = 0;
+        }
+        return n2;
+    }
+    __device__ __forceinline__ float renorm(float e0, float e1, float e2) {
+        const float n2 = add(fmaf(e0, e0, fmaf(e1, e1, e2 * e2)));
+        return eps * rsqrtf(n2);
+    }
+    __device__ __forceinline__ void last(float e0, float e1, float e2) { add(fmaf(e0, e0, fmaf(e1, e1, e2 * e2))); }
+    __device__ __forceinline__ double result(double tMax) const {
+        return (sum + (double)part) * (0.5 * 0.69314718055994530942) / tMax;  // log2(d^2) -> ln(d)
+    }
+};
+template <> struct Stretch<kRenormF64> {
+    double eps, sum = 0.0;
+    __device__ __forceinline__ explicit Stretch(double eps_) : eps(eps_) {}
+    __device__ __forceinline__ double dist(float e0, float e1, float e2) const {
+        return sqrt((double)e0 * e0 + (double)e1 * e1 + (double)e2 * e2) / eps;
+    }
+    __device__ __forceinline__ float renorm(float e0, float e1, float e2) {
+        const double d = dist(e0, e1, e2);
+        sum += log(d);
+        return (float)(1.0 / d);
+    }
+    __device__ __forceinline__ void last(float e0, float e1, float e2) { sum += log(dist(e0, e1, e2)); }
+    __device__ __forceinline__ double result(double tMax) const { return sum / tMax; }
+};
+template <int RN> __device__ __forceinline__ Stretch<RN> make_stretch(const LleParams& L);
+template <> __device__ __forceinline__ Stretch<kRenormPow2> make_stretch<kRenormPow2>(const LleParams& L) {
+    return Stretch<kRenormPow2>((float)L.eps);
+}
+template <> __device__ __forceinline__ Stretch<kRenormF32Log> make_stretch<kRenormF32Log>(const LleParams& L) {
+    return Stretch<kRenormF32Log>((float)L.eps, L.eps);
+}
+template <> __device__ __forceinline__ Stretch<kRenormF64> make_stretch<kRenormF64>(const LleParams& L) {
+    return Stretch<kRenormF64>(L.eps);
+}
 
 template <class F, class T>
 __device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>& c, int n) {  // n steps, 2 per trip
@@ -417,29 +497,23 @@ __device__ __forceinline__ void twin_steps(T* x, T* e, const T* a, const RK4H<T>
 
 // The Benettin blocks of an FP32 twin carried as a difference e (three state
 // components): steps(e, n) advances the orbit and e by n steps.
-template <class Steps>
+template <int RN = kRenormPow2, class Steps>
 __device__ __forceinline__ double lle_twin_blocks(const LleParams& L, Steps&& steps) {
-    using T = float;
-    const T eps = (T)L.eps;
-    const T inv_eps2 = (T)(1.0 / (L.eps * L.eps));
-    T e[3] = {eps, T(0), T(0)};
-    double sum = 0.0;  // sum of log2(d^2)
+    Stretch<RN> st = make_stretch<RN>(L);
+    float e[3] = {(float)L.eps, 0.f, 0.f};
     const int nb = L.calcBlocks + 1;
-    for (int b0 = 0; b0 < nb; b0 += kLleGroup) {
-        const int bn = min(kLleGroup, nb - b0);
-        T part = T(0);
-        for (int b = 0; b < bn; ++b) {
-            steps(e, L.ntp);
-            const T n2 = fmaf(e[0], e[0], fmaf(e[1], e[1], e[2] * e[2]));
-            part += __log2f(n2 * inv_eps2);
-            const T r = eps * rsqrtf(n2);
+    for (int b = 0; b < nb; ++b) {
+        steps(e, L.ntp);
+        if (b + 1 < nb) {
+            const float r = st.renorm(e[0], e[1], e[2]);
             e[0] *= r;
             e[1] *= r;
             e[2] *= r;
+        } else {
+            st.last(e[0], e[1], e[2]);
         }
-        sum += (double)part;
     }
-    return sum * (0.5 * 0.69314718055994530942) / L.tMax;  // log2(d^2) -> ln(d)
+    return st.result(L.tMax);
 }
 
 template <class F>
@@ -619,6 +693,14 @@ __device__ __forceinline__ P2 operator*(P2 a, P2 b) { return mk(__fmul2_rn(a.v, 
 __device__ __forceinline__ P2& operator*=(P2& a, P2 b) { a = a * b; return a; }
 __device__ __forceinline__ P2 fmaT(P2 a, P2 b, P2 c) { return mk(__ffma2_rn(a.v, b.v, c.v)); }
 __device__ __forceinline__ P2 addR(P2 a, P2 b) { return a + b; }
+// Word operations of float-float pairs of packed lanes (ff.h): each one
+// paired instruction, rounded per lane exactly as the scalar operation;
+// a - b as fma(b, -1, a), which is RN(a - b) in one instruction.
+__device__ __forceinline__ P2 w_add(P2 a, P2 b) { return mk(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ P2 w_sub(P2 a, P2 b) { return mk(__ffma2_rn(b.v, make_float2(-1.f, -1.f), a.v)); }
+__device__ __forceinline__ P2 w_mul(P2 a, P2 b) { return mk(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ P2 w_fma(P2 a, P2 b, P2 c) { return mk(__ffma2_rn(a.v, b.v, c.v)); }
+__device__ __forceinline__ P2 w_neg(P2 a) { return mk(make_float2(-a.v.x, -a.v.y)); }
 
 // Step constants of a packed pair: rounded exactly as RK4H<float> rounds them.
 template <> struct RK4H<P2> {
@@ -628,9 +710,9 @@ template <> struct RK4H<P2> {
 };
 
 // Two LLE points per thread (indices p and q), lanes of P2. Same arithmetic
-// per lane as lle_point_twin with T = float; the per-block log and rescale
-// run per lane on the SFU.
-template <class F>
+// per lane as lle_point_twin with T = float; the per-block stretch and
+// renormalisation (Stretch mode RN) run per lane.
+template <class F, int RN = kRenormPow2>
 __device__ __forceinline__ void lle_pair_twin(const LleParams& L, long long p, long long q, double* outp,
                                               double* outq) {
     P2 x[3], e[3], a[3];
@@ -645,30 +727,25 @@ __device__ __forceinline__ void lle_pair_twin(const LleParams& L, long long p, l
     const RK4H<P2> c((float)L.h);
     for (int s = 0; s < L.trans; ++s) rk4_step<F>(x, a, c);
     const float eps = (float)L.eps;
-    const float inv_eps2 = (float)(1.0 / (L.eps * L.eps));
     e[0] = P2((double)eps);
     e[1] = P2(0.0);
     e[2] = P2(0.0);
-    double sum0 = 0.0, sum1 = 0.0;
+    Stretch<RN> s0 = make_stretch<RN>(L), s1 = make_stretch<RN>(L);
     const int nb = L.calcBlocks + 1;
-    for (int b0 = 0; b0 < nb; b0 += kLleGroup) {
-        const int bn = min(kLleGroup, nb - b0);
-        float part0 = 0.f, part1 = 0.f;
-        for (int b = 0; b < bn; ++b) {
-            twin_steps<F>(x, e, a, c, L.ntp);
-            const P2 n2 = fmaT(e[0], e[0], fmaT(e[1], e[1], e[2] * e[2]));
-            part0 += __log2f(n2.v.x * inv_eps2);
-            part1 += __log2f(n2.v.y * inv_eps2);
-            const P2 r(eps * rsqrtf(n2.v.x), eps * rsqrtf(n2.v.y));
+    for (int b = 0; b < nb; ++b) {
+        twin_steps<F>(x, e, a, c, L.ntp);
+        if (b + 1 < nb) {
+            const P2 r(s0.renorm(e[0].v.x, e[1].v.x, e[2].v.x), s1.renorm(e[0].v.y, e[1].v.y, e[2].v.y));
             e[0] *= r;
             e[1] *= r;
             e[2] *= r;
+        } else {
+            s0.last(e[0].v.x, e[1].v.x, e[2].v.x);
+            s1.last(e[0].v.y, e[1].v.y, e[2].v.y);
         }
-        sum0 += (double)part0;
-        sum1 += (double)part1;
     }
-    *outp = sum0 * (0.5 * 0.69314718055994530942) / L.tMax;
-    if (outq) *outq = sum1 * (0.5 * 0.69314718055994530942) / L.tMax;
+    *outp = s0.result(L.tMax);
+    if (outq) *outq = s1.result(L.tMax);
 }
 
 // ---------------------------------------------------------------------------

@@ -327,17 +327,27 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
 // (from 3.37 waves of resident blocks to 2.99) and the Lorenz map from 39.1
 // to 36.2 ms, results unchanged. Blocks of 64, 128 and 256 (the tuner's
 // choices) all launch under the bound.
-template <class F>
+template <class F, int RN = kRenormPow2>
 __global__ void __launch_bounds__(384, 3) lle_pair_kernel_f32(LleParams L, double* out) {
     const long long o = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (o >= L.nPoints) return;
     const bool two = o + 1 < L.nPoints;
-    lle_pair_twin<F>(L, L.pBegin + o, L.pBegin + (two ? o + 1 : o), out + o, two ? out + o + 1 : nullptr);
+    lle_pair_twin<F, RN>(L, L.pBegin + o, L.pBegin + (two ? o + 1 : o), out + o, two ? out + o + 1 : nullptr);
 }
+
+// Stretch mode of the FP32 LLE maps of the RK4 systems (LleRenorm): 0 the
+// exact power-of-two renormalisation (default); 1 and 2 run the pair kernel
+// with the per-block FP32 log or the per-block FP64 norm and log instead.
+std::atomic<int> g_lle_renorm{0};
 
 template <class F>
 static void launch_twin(const LleParams& L, double* out, cudaStream_t st, int minb, int block) {
-    if (minb == 2) lle_pair_kernel_f32<F><<<grid_of((L.nPoints + 1) / 2, block), block, 0, st>>>(L, out);
+    const int rn = g_lle_renorm.load(std::memory_order_relaxed);
+    const unsigned gp = grid_of((L.nPoints + 1) / 2, minb == 2 ? block : kBlock);
+    const int bp = minb == 2 ? block : kBlock;
+    if (rn == kRenormF32Log) lle_pair_kernel_f32<F, kRenormF32Log><<<gp, bp, 0, st>>>(L, out);
+    else if (rn == kRenormF64) lle_pair_kernel_f32<F, kRenormF64><<<gp, bp, 0, st>>>(L, out);
+    else if (minb == 2) lle_pair_kernel_f32<F><<<gp, bp, 0, st>>>(L, out);
     else if (minb >= 16) lle_twin_kernel_f32<F, 16><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
     else lle_twin_kernel_f32<F, 12><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out);
     note_launch();
@@ -358,6 +368,13 @@ int set_lle_variant(int v) {
     return 0;
 }
 int get_lle_variant() { return lle_occupancy_variant(0); }
+
+int set_lle_renorm(int v) {
+    if (v < kRenormPow2 || v > kRenormF64) return -1;
+    g_lle_renorm.store(v);
+    return 0;
+}
+int get_lle_renorm() { return g_lle_renorm.load(); }
 
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;

@@ -99,6 +99,10 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
+// float-float base trajectory, FP32 twin difference (kern_ff.cu; RK4 systems)
+cudaError_t launch_lle_ff(const LleParams& L, double* out, cudaStream_t st);
+int set_ff_pairs(int v);  // 1: two points per thread (default), 0: one
+int get_ff_pairs();
 // Lyapunov spectrum, out[p*SIZE_X + j] (FP64: every built-in system; FP32: the RK4 systems)
 cudaError_t launch_spectrum_f64(const LleParams& L, double* out, cudaStream_t st);
 cudaError_t launch_spectrum_f32(const LleParams& L, double* out, cudaStream_t st);
@@ -125,6 +129,8 @@ cudaError_t launch_trajectory_f64(int system, const double* x0, const double* a0
                                   double* out, long long n, cudaStream_t st);
 cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0, double h, int nSteps,
                                   double* out, long long n, cudaStream_t st);
+cudaError_t launch_trajectory_ff(int system, const double* x0, const double* a0, double h, int nSteps,
+                                 double* out, long long n, cudaStream_t st);
 
 // Basin features in normalised form (basins_dbscan.cu): per point (amplitude,
 // peak count, mean interval), min-max scaled over the points with flag != 0.
@@ -135,6 +141,8 @@ cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double*
 // thread (packed FP32x2), 12 / 16 = one point per thread at that occupancy.
 int set_lle_variant(int v);
 int get_lle_variant();
+int set_lle_renorm(int v);  // LleRenorm mode of the FP32 LLE maps of the RK4 systems
+int get_lle_renorm();
 // Paired FP32 bifurcation / basins kernels for the RK4 systems (kern_f32.cu).
 int sweep_pairs();
 // launch shapes found by the tuner (kern_f32.cu): kind 0 bifurcation, 1 basins,

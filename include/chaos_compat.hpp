@@ -9,7 +9,9 @@
 // variable CHAOS_SYSTEM (a CHAOS_SYS_* number or a name: lorenz, rossler,
 // chen, chameleon, rossler_cd, sin3, sin2, memristor); the default is
 // Chameleon, the reference's default. The arithmetic is FP64 unless
-// chaos_compat_set_precision(CHAOS_FP32) or CHAOS_PRECISION=fp32.
+// chaos_compat_set_precision(CHAOS_FP32) or CHAOS_PRECISION=fp32; with
+// CHAOS_FF32 (CHAOS_PRECISION=ff32) the LLE wrappers of the RK4 systems run
+// float-float and every other wrapper FP64.
 #ifndef CHAOS_COMPAT_HPP
 #define CHAOS_COMPAT_HPP
 

@@ -39,6 +39,13 @@ extern "C" {
 /* arithmetic of the trajectories */
 #define CHAOS_FP64 0 /* the reference's FP64 arithmetic; bit-identical to the CPU oracle */
 #define CHAOS_FP32 1 /* FP32 state, FP64 accumulation (peak times, means, log-stretch sums) */
+/* Float-float state: the base trajectory as the unevaluated sum of two FP32
+   words (about 48 significant bits, every operation on the FP32 pipe), the LLE
+   twin as an exact FP32 difference, the log-stretch exact (power-of-two
+   renormalisation) with one FP64 log. The LLE maps (chaos_lle2d,
+   chaos_lle_sweep) and chaos_trajectory of the RK4 systems 0-2; other calls
+   return CHAOS_E_UNSUPPORTED. */
+#define CHAOS_FF32 2
 
 /* where the caller's arrays live */
 #define CHAOS_MEM_HOST 0   /* results are copied back and the call returns when they are there */
@@ -472,6 +479,18 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
 /* CHAOS_TUNE_SHAPES: 0 forgets the launch shapes chaos_autotune installed
    (the built-in rules apply again). */
 #define CHAOS_TUNE_SHAPES 6
+/* CHAOS_TUNE_LLE_RENORM: how the FP32 LLE maps of the RK4 systems
+   (chaos_lle2d, chaos_lle_sweep) measure each Benettin block's stretch.
+   0 (default): the twin is rescaled by an exact power of two and the
+   stretch summed exactly (an integer count of octaves plus one FP64 log of
+   the final FP64 norm); 1: log2 of the FP32 norm per block on the SFU,
+   summed in FP32 groups of 16 blocks added in FP64; 2: the reference's
+   arithmetic, FP64 norm and FP64 log per block (LLE/src/LLECUDA.cu:146-162).
+   Modes 1 and 2 run the two-points-per-thread kernel; process-wide. */
+#define CHAOS_TUNE_LLE_RENORM 7
+/* CHAOS_TUNE_FF_PAIRS: CHAOS_FF32 LLE maps run two points per thread in
+   packed FP32x2 words (1, default) or one (0); results are identical. */
+#define CHAOS_TUNE_FF_PAIRS 8
 int chaos_set_tuning(int knob, int value);
 int chaos_get_tuning(int knob);
 

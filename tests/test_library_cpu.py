@@ -99,6 +99,27 @@ def test_lle_argument_errors(native):
     assert e.value.code == -6  # FP32 LLE needs a quadratic RK4 system or Chameleon
 
 
+def test_ff32_refused_where_not_implemented(native):
+    """CHAOS_FF32 runs the LLE maps and trajectories of the RK4 systems; every
+    other call refuses it (CHAOS_E_UNSUPPORTED) before touching a device,
+    instead of running another precision."""
+    with pytest.raises(native.ChaosError) as e:
+        native.lle2d("chameleon", precision=native.FF32, tMax=1.0, NT=0.1, nPts=4, h=0.01, eps=1e-6,
+                     initialConditions=[3.0, 3.0, 0.0], ranges=[0.0, 5.0, 0.0, 20.0], indicesOfMutVars=[3, 5],
+                     transientTime=1.0, values=[0.5, 3, 0, 2, 1, 18, 1])
+    assert e.value.code == -6
+    with pytest.raises(native.ChaosError) as e:
+        native.bifurcation1d("lorenz", precision=native.FF32, **BIF)
+    assert e.value.code == -6 and "CHAOS_FF32" in str(e.value)
+    with pytest.raises(native.ChaosError) as e:
+        native.trajectory("sin3", [[0.1, 0.1, 0.1]], [[1, 1, 1, 1, 1]], 0.01, 3, precision=native.FF32)
+    assert e.value.code == -6
+    with pytest.raises(native.ChaosError, match="unknown precision"):
+        native.lle2d("rossler", precision="fp16", tMax=1.0, NT=0.1, nPts=4, h=0.01, eps=1e-8,
+                     initialConditions=[1.0, 1.0, 1.0], ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2],
+                     transientTime=1.0, values=[0.2, 0.2, 5.7])
+
+
 def test_dbscan_argument_errors(native):
     with pytest.raises(native.ChaosError, match="dims"):
         native.dbscan(np.zeros((4, 5)), 0.1, 2)
