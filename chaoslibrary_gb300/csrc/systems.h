@@ -109,6 +109,23 @@ CHAOS_HD double addR(double a, double b) {
 }
 CHAOS_HD float addR(float a, float b) { return a + b; }
 
+// a*b + c as each arithmetic's kernels round it: FP64 as written, a product
+// and a sum (the FP64 translation units and the host checker compile without
+// contraction); FP32 one fused multiply-add, written out so that every FP32
+// kernel -- single sweep, batch, server -- rounds it the same way instead of
+// leaving the choice of which product to fuse to the compiler.
+CHAOS_HD double madd(double a, double b, double c) { return a * b + c; }
+CHAOS_HD float madd(float a, float b, float c) { return fmaf(a, b, c); }
+// a + b that no compiler may merge with a neighbouring product (FP32).
+CHAOS_HD double add_rn(double a, double b) { return a + b; }
+CHAOS_HD float add_rn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+
 // ---- vector fields of the RK4 systems ---------------------------------------
 struct Lorenz {
     template <class T> static CHAOS_HD void f(const T* x, const T* a, T* k) {
@@ -321,16 +338,19 @@ CHAOS_UNROLL
 
 // ---- the reference's own plug-in systems, restated --------------------------
 // Chameleon, semi-implicit two-stage composition (systems/systems.cuh:11-39).
+// The sums of products are written with madd: in FP64 they round exactly as
+// the reference's expressions (a6*X0 + a1*X2, a2 - a3*X2 + a4*cos, 1 + a3*h2,
+// a2 + a4*cos); in FP32 each is a fixed fused form.
 template <class T> CHAOS_HD void chameleon_step(T* X, const T* a, T h) {
     T h1 = a[0] * h;
     T h2 = (T(1) - a[0]) * h;
     X[0] = fmaT(h1, -a[6] * X[1], X[0]);
-    X[1] = fmaT(h1, a[6] * X[0] + a[1] * X[2], X[1]);
+    X[1] = fmaT(h1, madd(a[6], X[0], a[1] * X[2]), X[1]);
     T cos_term = cosT(a[5] * X[1]);
-    X[2] = fmaT(h1, a[2] - a[3] * X[2] + a[4] * cos_term, X[2]);
-    const T den = T(1) + a[3] * h2;
-    X[2] = div_by(fmaT(h2, (a[2] + a[4] * cos_term), X[2]), den, T(1) / den);
-    X[1] = fmaT(h2, (a[6] * X[0] + a[1] * X[2]), X[1]);
+    X[2] = fmaT(h1, madd(a[4], cos_term, madd(-a[3], X[2], a[2])), X[2]);
+    const T den = madd(a[3], h2, T(1));
+    X[2] = div_by(fmaT(h2, madd(a[4], cos_term, a[2]), X[2]), den, T(1) / den);
+    X[1] = fmaT(h2, madd(a[6], X[0], a[1] * X[2]), X[1]);
     X[0] = fmaT(h2, -a[6] * X[1], X[0]);
 }
 
@@ -346,28 +366,28 @@ template <class T, int NE> CHAOS_HD void chameleon_step_multi(T* X, T (*E)[3], c
     X[0] = fmaT(h1, -a[6] * X[1], X[0]);
 CHAOS_UNROLL
     for (int q = 0; q < NE; ++q) E[q][0] = fmaT(h1, -a[6] * E[q][1], E[q][0]);
-    X[1] = fmaT(h1, a[6] * X[0] + a[1] * X[2], X[1]);
+    X[1] = fmaT(h1, madd(a[6], X[0], a[1] * X[2]), X[1]);
 CHAOS_UNROLL
-    for (int q = 0; q < NE; ++q) E[q][1] = fmaT(h1, a[6] * E[q][0] + a[1] * E[q][2], E[q][1]);
+    for (int q = 0; q < NE; ++q) E[q][1] = fmaT(h1, madd(a[6], E[q][0], a[1] * E[q][2]), E[q][1]);
     const T u = a[5] * X[1];
     const T cos_term = cosT(u);
     T dcos[NE];
 CHAOS_UNROLL
     for (int q = 0; q < NE; ++q) {
         const T half = T(0.5) * (a[5] * E[q][1]);
-        dcos[q] = T(-2) * sinT(u + half) * sinT(half);
+        dcos[q] = T(-2) * sinT(add_rn(u, half)) * sinT(half);
     }
-    X[2] = fmaT(h1, a[2] - a[3] * X[2] + a[4] * cos_term, X[2]);
+    X[2] = fmaT(h1, madd(a[4], cos_term, madd(-a[3], X[2], a[2])), X[2]);
 CHAOS_UNROLL
-    for (int q = 0; q < NE; ++q) E[q][2] = fmaT(h1, a[4] * dcos[q] - a[3] * E[q][2], E[q][2]);
-    const T den = T(1) + a[3] * h2;
+    for (int q = 0; q < NE; ++q) E[q][2] = fmaT(h1, madd(a[4], dcos[q], -(a[3] * E[q][2])), E[q][2]);
+    const T den = madd(a[3], h2, T(1));
     const T rden = T(1) / den;
-    X[2] = div_by(fmaT(h2, (a[2] + a[4] * cos_term), X[2]), den, rden);
+    X[2] = div_by(fmaT(h2, madd(a[4], cos_term, a[2]), X[2]), den, rden);
 CHAOS_UNROLL
     for (int q = 0; q < NE; ++q) E[q][2] = div_by(fmaT(h2, a[4] * dcos[q], E[q][2]), den, rden);
-    X[1] = fmaT(h2, (a[6] * X[0] + a[1] * X[2]), X[1]);
+    X[1] = fmaT(h2, madd(a[6], X[0], a[1] * X[2]), X[1]);
 CHAOS_UNROLL
-    for (int q = 0; q < NE; ++q) E[q][1] = fmaT(h2, (a[6] * E[q][0] + a[1] * E[q][2]), E[q][1]);
+    for (int q = 0; q < NE; ++q) E[q][1] = fmaT(h2, madd(a[6], E[q][0], a[1] * E[q][2]), E[q][1]);
     X[0] = fmaT(h2, -a[6] * X[1], X[0]);
 CHAOS_UNROLL
     for (int q = 0; q < NE; ++q) E[q][0] = fmaT(h2, -a[6] * E[q][1], E[q][0]);
