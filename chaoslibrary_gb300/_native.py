@@ -64,6 +64,7 @@ _SIGS = {
     "chaos_bifurcation_sweep": ([_P, _I, _I, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _D, _I, _P, _P, _P,
                                  _P, _P, _P], _I),
     "chaos_compact_peaks": ([_P, _P, _P, _P, C.c_longlong, _I, _P, _P, _P, _P, C.c_longlong, _P], _I),
+    "chaos_lle_from_states": ([_P, _I, C.c_longlong, _P, _D, _D, _D, _D, _P], _I),
     "chaos_lle_sweep": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lyapunov_spectrum": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
@@ -573,6 +574,20 @@ def lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMu
     _check(lib().chaos_lle2d(C.byref(ex), _sys(system), tMax, NT, nPts, h, eps, A.d(ic), ic.size, A.d(ranges),
                              A.i(indicesOfMutVars), writableVar, maxValue, transientTime, A.d(vals), vals.size,
                              _out_ptr(out)))
+    return out
+
+
+def lle_from_states(system, states, tMax, NT, h, eps, precision=FP64, out=None, stream=None):
+    """Benettin stage of the LLE map from starting states (chaos_lle_from_states):
+    states[n, 2*SIZE_X + SIZE_A] = (orbit after the transient, parameters,
+    twin start) per point, the reference's semi_result rows."""
+    A = _Args()
+    st = np.ascontiguousarray(np.atleast_2d(states), np.float64)
+    n = st.shape[0]
+    if out is None:
+        out = np.zeros(n)
+    ex = _exec(precision, {"lle": out}, stream)
+    _check(lib().chaos_lle_from_states(C.byref(ex), _sys(system), n, A.d(st), tMax, NT, h, eps, _out_ptr(out)))
     return out
 
 

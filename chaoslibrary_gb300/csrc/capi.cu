@@ -692,6 +692,45 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
     return c.finish(rc);
 }
 
+int chaos_lle_from_states(const chaos_exec* ex, int system, long long n, const double* states, double tMax,
+                          double NT, double h, double eps, double* lle) {
+    if (system == SYS_USER) return set_error(CHAOS_E_UNSUPPORTED, "starting states run on the built-in systems");
+    if (!system_supported(system)) return set_error(CHAOS_E_ARGS, "unknown system %d", system);
+    if (n < 0 || (n > 0 && (!states || !lle))) return set_error(CHAOS_E_ARGS, "bad starting-state arguments");
+    if (!(h > 0) || !(tMax > 0) || !(NT > 0) || !(eps > 0)) return set_error(CHAOS_E_ARGS, "need h, tMax, NT, eps > 0");
+    if (NT / h > 2.0e9 || tMax / h > 2.0e9) return set_error(CHAOS_E_ARGS, "step counts must fit in int");
+    const int prec = ex ? ex->precision : CHAOS_FP64;
+    if (prec == CHAOS_FP32)
+        return set_error(CHAOS_E_UNSUPPORTED, "starting states run in CHAOS_FP64 or CHAOS_FF32");
+    if (prec == CHAOS_FF32 && !system_has_difference_form(system))
+        return set_error(CHAOS_E_UNSUPPORTED, "CHAOS_FF32 LLE needs an RK4 system (0-2)");
+    LleParams L;
+    memset(&L, 0, sizeof L);
+    L.system = system;
+    L.ntp = static_cast<int>(NT / h);
+    if (L.ntp < 1) return set_error(CHAOS_E_ARGS, "NT / h must be >= 1");
+    L.calcBlocks = static_cast<int>(tMax / h) / L.ntp + 1;
+    L.h = h;
+    L.eps = eps;
+    L.tMax = tMax;
+    L.nPoints = n;
+    int nx, na;
+    sizes_of(system, &nx, &na);
+    const size_t rowBytes = (size_t)(2 * nx + na) * sizeof(double);
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    if (n == 0) return c.finish(CHAOS_OK);
+    const double* dStates = (const double*)c.input(states, (size_t)n * rowBytes);
+    double* dOut = (double*)c.output(lle, (size_t)n * sizeof(double));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = prec == CHAOS_FF32 ? launch_lle_states_ff(L, dStates, dOut, c.stream)
+                                       : launch_lle_states_f64(L, dStates, dOut, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "LLE kernel"));
+    rc = c.to_host(lle, dOut, (size_t)n * sizeof(double));
+    return c.finish(rc);
+}
+
 int chaos_lyapunov_spectrum(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
                             int nPts, double h, double eps, const double* initialConditions,
                             int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,

@@ -361,6 +361,32 @@ __device__ __forceinline__ void lle_load(const LleParams& L, long long p, T* x, 
     }
 }
 
+// The Benettin blocks of the reference's calculateSystem (LLE/src/LLECUDA.cu:
+// 146-162) from an orbit x and a full twin trajectory q: calcBlocks + 1
+// blocks of ntp steps of each, dist = sqrt(sum (x - q)^2) / eps, sum +=
+// log(dist), q = x - (x - q) / dist; the sum over tMax.
+template <int S, class T>
+__device__ __forceinline__ double lle_benettin_full(const LleParams& L, T* x, T* q, const T* a) {
+    constexpr int NX = Traits<S>::NX;
+    const StepCtx<T> c((T)L.h);
+    double sum = 0.0;
+    for (int b = 0; b <= L.calcBlocks; ++b) {
+        for (int s = 0; s < L.ntp; ++s) step<S>(x, a, c);
+        for (int s = 0; s < L.ntp; ++s) step<S>(q, a, c);
+        double dist = 0.0;
+#pragma unroll
+        for (int k = 0; k < NX; ++k) {
+            const double df = (double)x[k] - (double)q[k];
+            dist = dist + df * df;
+        }
+        dist = sqrt(dist) / L.eps;
+        sum = sum + log(dist);
+#pragma unroll
+        for (int k = 0; k < NX; ++k) q[k] = (T)((double)x[k] - (((double)x[k] - (double)q[k]) / dist));
+    }
+    return sum / L.tMax;
+}
+
 template <int S, class T>
 __device__ __forceinline__ double lle_point_full(const LleParams& L, long long p) {
     constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
@@ -379,22 +405,7 @@ __device__ __forceinline__ double lle_point_full(const LleParams& L, long long p
     } else {
         q[0] = x[0] + (T)L.eps;
     }
-    double sum = 0.0;
-    for (int b = 0; b <= L.calcBlocks; ++b) {
-        for (int s = 0; s < L.ntp; ++s) step<S>(x, a, c);
-        for (int s = 0; s < L.ntp; ++s) step<S>(q, a, c);
-        double dist = 0.0;
-#pragma unroll
-        for (int k = 0; k < NX; ++k) {
-            const double df = (double)x[k] - (double)q[k];
-            dist = dist + df * df;
-        }
-        dist = sqrt(dist) / L.eps;
-        sum = sum + log(dist);
-#pragma unroll
-        for (int k = 0; k < NX; ++k) q[k] = (T)((double)x[k] - (((double)x[k] - (double)q[k]) / dist));
-    }
-    return sum / L.tMax;
+    return lle_benettin_full<S>(L, x, q, a);
 }
 
 // LLE point with the twin carried as the exact difference e = q - x (only for
@@ -420,11 +431,12 @@ __device__ __forceinline__ double nan_if_not_finite(double v) {
 
 template <int RN> struct Stretch;
 template <> struct Stretch<kRenormPow2> {
-    float e0;
+    double eps;  // the stretch of every block is measured against eps, as the reference measures it
     int eps2Exp, k = 0;
     double v = 0.0;
-    __device__ __forceinline__ explicit Stretch(float eps) : e0(eps) {
-        eps2Exp = (int)((__float_as_uint(eps * eps) >> 23) & 0xff) - 126;
+    __device__ __forceinline__ explicit Stretch(double eps_) : eps(eps_) {
+        const float e0 = (float)eps_;
+        eps2Exp = (int)((__float_as_uint(e0 * e0) >> 23) & 0xff) - 126;
     }
     __device__ __forceinline__ float renorm(float e0_, float e1, float e2) {
         const int j = pow2_rescale_exponent(fmaf(e0_, e0_, fmaf(e1, e1, e2 * e2)), eps2Exp);
@@ -433,7 +445,7 @@ template <> struct Stretch<kRenormPow2> {
     }
     __device__ __forceinline__ void last(float e0_, float e1, float e2) {
         const double n2 = (double)e0_ * e0_ + (double)e1 * e1 + (double)e2 * e2;
-        v = pow2_log_stretch(k, n2, (double)e0);
+        v = pow2_log_stretch(k, n2, eps);
     }
     __device__ __forceinline__ double result(double tMax) const { return nan_if_not_finite(v / tMax); }
 };
@@ -476,7 +488,7 @@ template <> struct Stretch<kRenormF64> {
 };
 template <int RN> __device__ __forceinline__ Stretch<RN> make_stretch(const LleParams& L);
 template <> __device__ __forceinline__ Stretch<kRenormPow2> make_stretch<kRenormPow2>(const LleParams& L) {
-    return Stretch<kRenormPow2>((float)L.eps);
+    return Stretch<kRenormPow2>(L.eps);
 }
 template <> __device__ __forceinline__ Stretch<kRenormF32Log> make_stretch<kRenormF32Log>(const LleParams& L) {
     return Stretch<kRenormF32Log>((float)L.eps, L.eps);

@@ -42,6 +42,26 @@ __global__ void __launch_bounds__(kBlock) lle_kernel(LleParams L, double* out) {
     out[o] = lle_point_full<S, double>(L, L.pBegin + o);
 }
 
+// Benettin blocks from caller-supplied starting states (the reference's
+// semi_result layout, LLE/src/LLECUDA.cu:102-111): point k's row of 2*NX + NA
+// values holds the orbit after the transient, the parameters and the twin.
+template <int S>
+__global__ void __launch_bounds__(kBlock) lle_states_kernel(LleParams L, const double* states, double* out) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA, W = 2 * NX + NA;
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L.nPoints) return;
+    const double* r = states + k * W;
+    double x[NX], q[NX], a[NA];
+#pragma unroll
+    for (int i = 0; i < NX; ++i) {
+        x[i] = r[i];
+        q[i] = r[NX + NA + i];
+    }
+#pragma unroll
+    for (int i = 0; i < NA; ++i) a[i] = r[NX + i];
+    out[k] = lle_benettin_full<S>(L, x, q, a);
+}
+
 // Lyapunov spectrum, out[p*SIZE_X + j]
 template <int S>
 __global__ void __launch_bounds__(kBlock) spectrum_kernel(LleParams L, double* out) {
@@ -243,6 +263,14 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
 #define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
+    CHAOS_SYSTEM_SWITCH(L.system, CALL)
+#undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_states_f64(const LleParams& L, const double* states, double* out, cudaStream_t st) {
+    if (L.nPoints <= 0) return cudaSuccess;
+#define CALL(S) (lle_states_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, states, out), note_launch())
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
     return cudaGetLastError();

@@ -30,27 +30,13 @@ __device__ __forceinline__ int exp_of(float v) { return (int)((__float_as_uint(v
 
 __device__ __forceinline__ double finite_or_nan(double v) { return isfinite(v) ? v : __longlong_as_double(0x7ff8000000000000LL); }
 
+// The Benettin blocks of an FF orbit x with the FP32 twin difference e
+// (started where the caller put it), renormalised by powers of two; the
+// stretch of the blocks relative to eps, as the reference measures it.
 template <class F>
-__device__ __forceinline__ double lle_point_ff(const LleParams& L, long long p) {
-    double xd[3], ad[3];
-    lle_load<3, 3>(L, p, xd, ad);
-    FF<float> x[3], a[3];
-    float af[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        x[k] = ff_from_double(xd[k]);
-        a[k] = ff_from_double(ad[k]);
-        af[k] = (float)ad[k];
-    }
-    FFH<float> c;
-    c.hh = ff_from_double(L.h * 0.5);
-    c.h = ff_from_double(L.h);
-    c.h6 = ff_from_double(L.h / 6.0);
-    const RK4H<float> cf((float)L.h);
-    for (int s = 0; s < L.trans; ++s) ff_rk4_step<F, false>(x, (float*)nullptr, a, af, c, cf);
-    const float e0 = (float)L.eps;
-    const int eps2Exp = exp_of(e0 * e0);
-    float e[3] = {e0, 0.f, 0.f};
+__device__ __forceinline__ double ff_benettin(const LleParams& L, FF<float>* x, float* e, const FF<float>* a,
+                                              const float* af, const FFH<float>& c, const RK4H<float>& cf) {
+    const int eps2Exp = exp_of((float)L.eps * (float)L.eps);
     int ktot = 0;
     const int nb = L.calcBlocks + 1;
     for (int b = 0; b < nb; ++b) {
@@ -66,7 +52,54 @@ __device__ __forceinline__ double lle_point_ff(const LleParams& L, long long p) 
         }
     }
     const double n2 = (double)e[0] * e[0] + (double)e[1] * e[1] + (double)e[2] * e[2];
-    return finite_or_nan(pow2_log_stretch(ktot, n2, (double)e0) / L.tMax);
+    return finite_or_nan(pow2_log_stretch(ktot, n2, L.eps) / L.tMax);
+}
+
+__device__ __forceinline__ FFH<float> ff_consts(double h) {
+    FFH<float> c;
+    c.hh = ff_from_double(h * 0.5);
+    c.h = ff_from_double(h);
+    c.h6 = ff_from_double(h / 6.0);
+    return c;
+}
+
+template <class F>
+__device__ __forceinline__ double lle_point_ff(const LleParams& L, long long p) {
+    double xd[3], ad[3];
+    lle_load<3, 3>(L, p, xd, ad);
+    FF<float> x[3], a[3];
+    float af[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        x[k] = ff_from_double(xd[k]);
+        a[k] = ff_from_double(ad[k]);
+        af[k] = (float)ad[k];
+    }
+    const FFH<float> c = ff_consts(L.h);
+    const RK4H<float> cf((float)L.h);
+    for (int s = 0; s < L.trans; ++s) ff_rk4_step<F, false>(x, (float*)nullptr, a, af, c, cf);
+    float e[3] = {(float)L.eps, 0.f, 0.f};
+    return ff_benettin<F>(L, x, e, a, af, c, cf);
+}
+
+// From caller-supplied starting states (the reference's semi_result layout:
+// orbit, parameters, twin): the twin difference is q - x, exact in FP64 for
+// a twin this close to its orbit, then rounded to FP32.
+template <class F>
+__global__ void __launch_bounds__(kBlock) lle_ff_states_kernel(LleParams L, const double* states, double* out) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L.nPoints) return;
+    const double* r = states + k * 9;
+    FF<float> x[3], a[3];
+    float af[3], e[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        x[i] = ff_from_double(r[i]);
+        a[i] = ff_from_double(r[3 + i]);
+        af[i] = (float)r[3 + i];
+        e[i] = (float)(r[6 + i] - r[i]);
+    }
+    out[k] = ff_benettin<F>(L, x, e, a, af, ff_consts(L.h), RK4H<float>((float)L.h));
 }
 
 // Two points per thread: FF words are packed pairs (one paired FP32
@@ -115,8 +148,8 @@ __device__ __forceinline__ void lle_pair_ff(const LleParams& L, long long p, lon
     }
     const double n0 = (double)e[0].v.x * e[0].v.x + (double)e[1].v.x * e[1].v.x + (double)e[2].v.x * e[2].v.x;
     const double n1 = (double)e[0].v.y * e[0].v.y + (double)e[1].v.y * e[1].v.y + (double)e[2].v.y * e[2].v.y;
-    *outp = finite_or_nan(pow2_log_stretch(k0, n0, (double)e0) / L.tMax);
-    if (outq) *outq = finite_or_nan(pow2_log_stretch(k1, n1, (double)e0) / L.tMax);
+    *outp = finite_or_nan(pow2_log_stretch(k0, n0, L.eps) / L.tMax);
+    if (outq) *outq = finite_or_nan(pow2_log_stretch(k1, n1, L.eps) / L.tMax);
 }
 
 template <class F>
@@ -192,6 +225,19 @@ cudaError_t launch_lle_ff(const LleParams& L, double* out, cudaStream_t st) {
         case SYS_CHEN_RK4: launch_ff<Chen>(L, out, st); break;
         default: return cudaErrorNotSupported;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lle_states_ff(const LleParams& L, const double* states, double* out, cudaStream_t st) {
+    if (L.nPoints <= 0) return cudaSuccess;
+    const unsigned g = blocks_for(L.nPoints);
+    switch (L.system) {
+        case SYS_LORENZ_RK4: lle_ff_states_kernel<Lorenz><<<g, kBlock, 0, st>>>(L, states, out); break;
+        case SYS_ROSSLER_RK4: lle_ff_states_kernel<Rossler><<<g, kBlock, 0, st>>>(L, states, out); break;
+        case SYS_CHEN_RK4: lle_ff_states_kernel<Chen><<<g, kBlock, 0, st>>>(L, states, out); break;
+        default: return cudaErrorNotSupported;
+    }
+    note_launch();
     return cudaGetLastError();
 }
 

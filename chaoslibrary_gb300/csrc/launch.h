@@ -101,6 +101,10 @@ cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
 // float-float base trajectory, FP32 twin difference (kern_ff.cu; RK4 systems)
 cudaError_t launch_lle_ff(const LleParams& L, double* out, cudaStream_t st);
+// Benettin blocks from caller-supplied states, rows of 2*SIZE_X + SIZE_A (orbit, parameters,
+// twin; kern_f64.cu / kern_ff.cu)
+cudaError_t launch_lle_states_f64(const LleParams& L, const double* states, double* out, cudaStream_t st);
+cudaError_t launch_lle_states_ff(const LleParams& L, const double* states, double* out, cudaStream_t st);
 int set_ff_pairs(int v);  // 1: two points per thread (default), 0: one
 int get_ff_pairs();
 // Lyapunov spectrum, out[p*SIZE_X + j] (FP64: every built-in system; FP32: the RK4 systems)

@@ -188,6 +188,22 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
                 const double* values, int amountOfValues, double* lle);
 
 /*
+ * The Benettin stage of the LLE map on caller-supplied starting states:
+ * replaces the reference's calculateSystem kernel (LLE/src/LLECUDA.cu:114-166),
+ * which reads the semi_result rows its transient kernel wrote
+ * (LLECUDA.cu:56-112). states holds n rows of 2*SIZE_X + SIZE_A values:
+ * the orbit after the transient, the point's parameters, the twin's start
+ * (the reference's row layout). lle[k] = sum over calcBlocks + 1 blocks of
+ * NT/h steps of log(|x - p| / eps), over tMax, with the reference's
+ * renormalisation (CHAOS_FP64), or with the orbit in float-float and the twin
+ * as the FP32 difference p - x (CHAOS_FF32, RK4 systems). No transient is
+ * run: a caller can hand over the reference's own randomised twin starts
+ * (its cuRAND draw, LLECUDA.cu:88-101) and compare on identical inputs.
+ */
+int chaos_lle_from_states(const chaos_exec* ex, int system, long long n, const double* states, double tMax,
+                          double NT, double h, double eps, double* lle);
+
+/*
  * LLE over a 1-D or 2-D grid of parameters (gridMode 0) or of initial
  * conditions (gridMode CHAOS_GRID_STATE), linear or log-scale axes
  * (CHAOS_GRID_LOG0 / LOG1 / LOG_F32): the legacy library's LLE1D, LLE1DIC,

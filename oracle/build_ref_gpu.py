@@ -44,7 +44,11 @@ TARGETS = {
     "bif2d": (None, "REF_BIF2D", ["Bifurcation/src/bifurcationCUDA.cu", "Bifurcation/src/bifurcationHOST.cpp"]),
     "lle2d": ("rossler", "REF_LLE2D", ["LLE/src/LLECUDA.cu", "LLE/src/LLEHost.cpp"]),
     "basins": ("lorenz", "REF_BASINS", ["Basins/src/basinsCUDA.cu", "Basins/src/basinsHOST.cpp"]),
+    # the reference's LLE kernels on their own, dumping their starting states (ref_gpu_lle_states.cu
+    # includes LLE/src/LLECUDA.cu itself)
+    "lle_states": ("rossler", "REF_LLE_STATES", []),
 }
+MAINS = {"lle_states": "ref_gpu_lle_states.cu"}
 
 
 def binary(name: str) -> Path:
@@ -77,8 +81,8 @@ def _build_one(name: str, verbose: bool) -> Path:
     cmd = [NVCC, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-w", f"-D{macro}",
            f"-I{sysdir}", f"-I{STAGE / 'Bifurcation/include'}", f"-I{STAGE / 'LLE/include'}",
            f"-I{STAGE / 'Basins/include'}",
-           f"-I{STAGE / 'debri'}", "-x", "cu"] + [str(STAGE / s) for s in srcs] + \
-          [str(STAGE / "debri/cudaMacros.cu"), str(HERE / "ref_gpu_main.cu"), "-o", str(exe)]
+           f"-I{STAGE / 'debri'}", f"-I{STAGE / 'LLE/src'}", "-x", "cu"] + [str(STAGE / s) for s in srcs] + \
+          [str(STAGE / "debri/cudaMacros.cu"), str(HERE / MAINS.get(name, "ref_gpu_main.cu")), "-o", str(exe)]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True, capture_output=not verbose)

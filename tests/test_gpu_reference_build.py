@@ -103,6 +103,50 @@ def test_lle_reference_twin_start_agrees_with_reference_gpu_build(engine, tmp_pa
     assert within[1][0] > within[0][0]
 
 
+REF_STATES = ROOT / "oracle" / "_ref" / "ref_gpu_lle_states"
+
+
+def _ref_states(tmp_path, n, tmax):
+    """The reference's semi_result rows (orbit after its transient, parameters,
+    its cuRAND twin start) and its map from them, indexed ia * n + ib."""
+    out = tmp_path / "states.bin"
+    subprocess.run([str(REF_STATES), str(out), str(n), str(tmax)], check=True, capture_output=True, timeout=600)
+    raw = out.read_bytes()
+    nP, W = (int(v) for v in np.frombuffer(raw[:8], np.int32))
+    body = np.frombuffer(raw[8:], np.float64)
+    return body[: nP * nP * W].reshape(nP * nP, W), body[nP * nP * W:]
+
+
+def test_lle_on_reference_twin_starts_matches_reference_gpu_build(engine, tmp_path):
+    """Parity on identical inputs. The reference starts each point's twin from
+    a cuRAND draw rounded through FP32 (LLE/src/LLECUDA.cu:88-101); handed
+    those starting states (its own semi_result rows), the engine's FP64
+    Benettin stage reproduces the reference's map within 1e-3 on >= 99.9 %
+    of a 128^2 map of the benchmark's Rossler ranges (only the per-block log
+    differs: the reference takes it in FP32, __logf). The float-float stage
+    on the same states keeps every regular point within 1e-3. The engine's
+    own FP64 transient from the reference's parameters lands on the
+    reference's post-transient orbit bit for bit."""
+    _need(REF_STATES)
+    n, tmax = 128, 500.0
+    semi, ref = _ref_states(tmp_path, n, tmax)
+    assert semi.shape == (n * n, 9)
+    fin = np.isfinite(ref)
+    l64 = engine.lle_from_states("rossler", semi, tmax, 0.1, 0.01, 1e-8, precision=engine.FP64)
+    d64 = np.abs(l64 - ref)[fin & np.isfinite(l64)]
+    assert np.mean(d64 <= 1e-3) >= 0.999, np.mean(d64 <= 1e-3)
+    assert np.median(d64) < 1e-5
+    lff = engine.lle_from_states("rossler", semi, tmax, 0.1, 0.01, 1e-8, precision=engine.FF32)
+    ok = fin & np.isfinite(lff)
+    reg = ok & (ref < 0.005)
+    assert np.mean(np.abs(lff - ref)[reg] <= 1e-3) >= 0.999
+    # the transient: 5,000 FP64 steps from (1, 1, 1) with the reference's parameters
+    rows = np.random.default_rng(5).choice(n * n, 256, replace=False)
+    t = engine.trajectory("rossler", np.tile([1.0, 1.0, 1.0], (256, 1)), semi[rows, 3:6], 0.01, 5000,
+                          precision=engine.FP64)
+    assert np.array_equal(t[:, -1, :], semi[rows, 0:3])
+
+
 REF_BASINS = ROOT / "oracle" / "_ref" / "ref_gpu_basins"
 
 

@@ -120,6 +120,18 @@ def test_ff32_refused_where_not_implemented(native):
                      transientTime=1.0, values=[0.2, 0.2, 5.7])
 
 
+def test_lle_from_states_argument_errors(native):
+    st = np.zeros((4, 9))
+    with pytest.raises(native.ChaosError) as e:
+        native.lle_from_states("rossler", st, 10.0, 0.1, 0.01, 1e-8, precision=native.FP32)
+    assert e.value.code == -6
+    with pytest.raises(native.ChaosError) as e:
+        native.lle_from_states("chameleon", np.zeros((4, 13)), 10.0, 0.1, 0.01, 1e-8, precision=native.FF32)
+    assert e.value.code == -6
+    with pytest.raises(native.ChaosError, match="NT / h"):
+        native.lle_from_states("rossler", st, 10.0, 0.001, 0.01, 1e-8)
+
+
 def test_dbscan_argument_errors(native):
     with pytest.raises(native.ChaosError, match="dims"):
         native.dbscan(np.zeros((4, 5)), 0.1, 2)
