@@ -28,7 +28,7 @@ class Exec(C.Structure):
     _fields_ = [("precision", C.c_int), ("memory", C.c_int), ("stream", C.c_void_p), ("device", C.c_int)]
 
 
-JOB_BIF1D, JOB_LLE2D, JOB_BASINS = 1, 2, 3
+JOB_BIF1D, JOB_LLE2D, JOB_BASINS, JOB_LLE2D_FF32 = 1, 2, 3, 4
 
 
 class Job(C.Structure):
@@ -315,8 +315,11 @@ class Batch:
         return out
 
     def add_lle2d(self, system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars, transientTime,
-                  values):
-        j = self._common(JOB_LLE2D, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, 0, 0.0,
+                  values, precision=FP32):
+        """An LLE map job: FP32 (CHAOS_JOB_LLE2D) or float-float (precision
+        FF32: CHAOS_JOB_LLE2D_FF32, RK4 systems)."""
+        kind = JOB_LLE2D_FF32 if _prec(precision) == FF32 else JOB_LLE2D
+        j = self._common(kind, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, 0, 0.0,
                          transientTime, values, 1)
         j.NT, j.eps = NT, eps
         out = dict(lle=self._alloc(nPts * nPts, np.float64))
@@ -412,10 +415,10 @@ class Server:
         return self._submit(b.jobs[0], b, out), out
 
     def submit_lle2d(self, system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
-                     transientTime, values):
+                     transientTime, values, precision=FP32):
         b = Batch()
         out = b.add_lle2d(system, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
-                          transientTime, values)
+                          transientTime, values, precision)
         return self._submit(b.jobs[0], b, out), out
 
     def submit_basins(self, system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar,

@@ -11,7 +11,9 @@
 // device function as the single-sweep kernels, so its result does not depend
 // on the batch, chunk or block it ran in.
 //
-// Batches are FP32 (trajectories in FP32 registers, FP64 accumulation); the
+// Batches are FP32 (trajectories in FP32 registers, FP64 accumulation) but
+// for the float-float LLE jobs, whose group kernel lives with the other FF
+// kernels (kern_ff.cu, compiled without contraction); the
 // jobs of the RK4 systems run two points per thread (packed FP32x2 lanes; the
 // bifurcation and basins jobs in the hybrid form), the others one. A prepared batch is
 // replayed from a captured CUDA graph (counter reset + the group kernels).
@@ -172,6 +174,7 @@ GroupKernel group_kernel_for(int kind, int system) {
 int batch_block_size() { return kBatchBlock; }
 
 int group_resident_blocks(int kind, int system, int device) {
+    if (kind == CHAOS_JOB_LLE2D_FF32) return group_ff_resident_blocks(system, device);
     GroupKernel k = group_kernel_for(kind, system);
     if (!k) return 0;
     int perSm = 0, sms = 0;
@@ -188,6 +191,7 @@ cudaError_t reset_counters(int* counters, int n, cudaStream_t st) {
 
 cudaError_t launch_group(int kind, int system, const JobDesc* jobs, const Chunk* chunks, int count, int* counter,
                          int gridBlocks, cudaStream_t st) {
+    if (kind == CHAOS_JOB_LLE2D_FF32) return launch_group_ff(system, jobs, chunks, count, counter, gridBlocks, st);
     GroupKernel k = group_kernel_for(kind, system);
     if (!k) return cudaErrorInvalidValue;
     if (count <= 0) return cudaSuccess;

@@ -33,5 +33,9 @@ int group_resident_blocks(int kind, int system, int device);
 cudaError_t reset_counters(int* counters, int n, cudaStream_t st);  // n <= 32
 cudaError_t launch_group(int kind, int system, const JobDesc* jobs, const Chunk* chunks, int count, int* counter,
                          int gridBlocks, cudaStream_t st);
+// the float-float LLE group (CHAOS_JOB_LLE2D_FF32; kern_ff.cu): resident blocks and launch
+int group_ff_resident_blocks(int system, int device);
+cudaError_t launch_group_ff(int system, const JobDesc* jobs, const Chunk* chunks, int count, int* counter,
+                            int gridBlocks, cudaStream_t st);
 
 }  // namespace chaos

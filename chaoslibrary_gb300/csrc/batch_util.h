@@ -24,7 +24,8 @@ struct HostOut {  // a device output of one job and where it goes on the host
 
 // Work per point of a job (trajectory-steps), the key of the longest-first order.
 inline long long work_per_point(const JobDesc& J) {
-    if (J.kind == CHAOS_JOB_LLE2D) return J.lp.trans + 2LL * J.lp.ntp * (J.lp.calcBlocks + 1);
+    if (J.kind == CHAOS_JOB_LLE2D || J.kind == CHAOS_JOB_LLE2D_FF32)
+        return J.lp.trans + 2LL * J.lp.ntp * (J.lp.calcBlocks + 1);
     return (long long)J.sp.S + (long long)J.sp.B * J.sp.preScaller;
 }
 
@@ -81,10 +82,13 @@ int prepare_job(const chaos_job& j, int memory, JobDesc& J, std::vector<HostOut>
             J.bas.last = nullptr;
             break;
         }
-        case CHAOS_JOB_LLE2D: {
+        case CHAOS_JOB_LLE2D:
+        case CHAOS_JOB_LLE2D_FF32: {
             rc = fill_lle(J.lp, j.system, j.tMax, j.NT, j.nPts, j.h, j.eps, j.initialConditions, nx, j.ranges,
                           j.indicesOfMutVars, j.transientTime, j.values, na);
             if (rc) return rc;
+            if (j.kind == CHAOS_JOB_LLE2D_FF32 && !system_has_difference_form(j.system))
+                return set_error(CHAOS_E_UNSUPPORTED, "float-float LLE jobs need an RK4 system (0-2)");
             if (!system_has_fp32_lle(j.system))
                 return set_error(CHAOS_E_UNSUPPORTED, "batched LLE jobs need a quadratic RK4 system (0-2) or Chameleon");
             if (J.lp.twin != 0)

@@ -18,6 +18,7 @@
 // error-free transformations.
 #include <atomic>
 
+#include "batch.h"
 #include "engine.cuh"
 
 namespace chaos {
@@ -196,6 +197,44 @@ __global__ void __launch_bounds__(kBlock) trajectory_kernel_ff(const double* x0,
     }
 }
 
+// Persistent kernel of a batch's float-float LLE jobs of one system
+// (CHAOS_JOB_LLE2D_FF32): pulls chunks of two blocks' worth of points from
+// its counter; every point runs lle_pair_ff, the single-sweep kernel's device
+// function, with the job's parameters staged in shared memory.
+template <class F>
+__global__ void __launch_bounds__(kBlock) group_ff_kernel(const JobDesc* __restrict__ jobs,
+                                                          const Chunk* __restrict__ chunks, int count, int* counter) {
+    __shared__ int slot;
+    __shared__ LleParams sL;
+    for (;;) {
+        if (threadIdx.x == 0) slot = atomicAdd(counter, 1);
+        __syncthreads();
+        const int c = slot;
+        __syncthreads();
+        if (c >= count) return;
+        const Chunk ch = chunks[c];
+        const JobDesc& J = jobs[ch.job];
+        if (threadIdx.x == 0) sL = J.lp;
+        __syncthreads();
+#pragma unroll 1
+        for (int t = 2 * threadIdx.x; t < ch.count; t += 2 * blockDim.x) {
+            const long long p = ch.begin + t;
+            const bool two = t + 1 < ch.count;
+            lle_pair_ff<F>(sL, p, two ? p + 1 : p, J.lle + p, two ? J.lle + p + 1 : nullptr);
+        }
+    }
+}
+
+using GroupFF = void (*)(const JobDesc*, const Chunk*, int, int*);
+GroupFF group_ff_for(int system) {
+    switch (system) {
+        case SYS_LORENZ_RK4: return group_ff_kernel<Lorenz>;
+        case SYS_ROSSLER_RK4: return group_ff_kernel<Rossler>;
+        case SYS_CHEN_RK4: return group_ff_kernel<Chen>;
+        default: return nullptr;
+    }
+}
+
 unsigned blocks_for(long long threads) { return (unsigned)((threads + kBlock - 1) / kBlock); }
 
 // 1 (default): two points per thread in packed words; 0: one point per thread.
@@ -225,6 +264,25 @@ cudaError_t launch_lle_ff(const LleParams& L, double* out, cudaStream_t st) {
         case SYS_CHEN_RK4: launch_ff<Chen>(L, out, st); break;
         default: return cudaErrorNotSupported;
     }
+    return cudaGetLastError();
+}
+
+int group_ff_resident_blocks(int system, int device) {
+    GroupFF k = group_ff_for(system);
+    if (!k) return 0;
+    int perSm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k, kBlock, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    return (perSm > 1 ? perSm : 1) * (sms > 1 ? sms : 1);
+}
+
+cudaError_t launch_group_ff(int system, const JobDesc* jobs, const Chunk* chunks, int count, int* counter,
+                            int gridBlocks, cudaStream_t st) {
+    GroupFF k = group_ff_for(system);
+    if (!k) return cudaErrorInvalidValue;
+    if (count <= 0) return cudaSuccess;
+    k<<<gridBlocks, kBlock, 0, st>>>(jobs, chunks, count, counter);
+    note_launch();
     return cudaGetLastError();
 }
 

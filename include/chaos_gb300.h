@@ -341,13 +341,16 @@ int chaos_point_dbscan(const chaos_exec* ex, const double* intervals, const int*
  * in and runs one sweep per call). Many independent jobs of different kinds,
  * systems, sizes and transients run in ONE persistent launch that pulls
  * chunks of points from a device work queue. FP32 trajectories with FP64
- * accumulation (ex->precision is ignored); a point's result is bit-identical
- * to the single-job FP32 call's. Arguments mean what they mean in the
+ * accumulation, or float-float for CHAOS_JOB_LLE2D_FF32 jobs (ex->precision
+ * is ignored); a point's result is bit-identical to the single-job call's in
+ * that arithmetic. Arguments mean what they mean in the
  * single-job entry points; outputs are host or device arrays per ex->memory.
  */
 #define CHAOS_JOB_BIF1D 1  /* chaos_bifurcation1d: counts, flags, first?, peaks?, intervals? */
 #define CHAOS_JOB_LLE2D 2  /* chaos_lle2d (RK4 systems and Chameleon): lle */
 #define CHAOS_JOB_BASINS 3 /* chaos_basins_features: flags, avgPeaks, avgIntervals, counts? */
+#define CHAOS_JOB_LLE2D_FF32 4 /* chaos_lle2d with CHAOS_FF32 (RK4 systems 0-2): lle; bit-identical to
+                                  the single-sweep CHAOS_FF32 call */
 
 typedef struct chaos_job {
     int kind;

@@ -330,6 +330,12 @@ def _batch_jobs():
         ("lle", "chameleon", dict(tMax=10.0, NT=0.5, nPts=19, h=0.01, eps=1e-6, initialConditions=[3.0, 3.0, 0.0],
                                   ranges=[0.0, 5.0, 0.0, 20.0], indicesOfMutVars=[3, 5], transientTime=5.0,
                                   values=[0.5, 3, 0, 2, 1, 18, 1])),
+        ("lleff", "rossler", dict(tMax=20.0, NT=0.1, nPts=21, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0],
+                                  ranges=[0.1, 0.4, 2.0, 10.0], indicesOfMutVars=[0, 2], transientTime=10.0,
+                                  values=[0.2, 0.2, 5.7])),
+        ("lleff", "chen", dict(tMax=5.0, NT=0.1, nPts=12, h=0.01, eps=1e-8, initialConditions=[-10.0, 0.0, 37.0],
+                               ranges=[20.0, 30.0, 30.0, 40.0], indicesOfMutVars=[2, 0], transientTime=2.0,
+                               values=[35.0, 3.0, 28.0])),
     ]
 
 
@@ -345,6 +351,8 @@ def test_batch_equals_single_jobs(engine, mode):
             outs.append(b.add_bifurcation1d(system, peakCapacity=32, **kw))
         elif kind == "lle":
             outs.append(b.add_lle2d(system, **kw))
+        elif kind == "lleff":
+            outs.append(b.add_lle2d(system, precision=engine.FF32, **kw))
         else:
             outs.append(b.add_basins(system, **kw))
     runs = 2 if mode.endswith("graph") else 1
@@ -366,13 +374,75 @@ def test_batch_equals_single_jobs(engine, mode):
                     m = min(int(c), 32)
                     assert np.array_equal(got["peaks"][r, :m], ref["peaks"][r, :m])
                     assert np.array_equal(got["intervals"][r, :m], ref["intervals"][r, :m])
-            elif kind == "lle":
-                ref = engine.lle2d(system, precision=engine.FP32, **kw)
-                assert np.array_equal(got["lle"], ref, equal_nan=True), system
+            elif kind in ("lle", "lleff"):
+                p = engine.FF32 if kind == "lleff" else engine.FP32
+                ref = engine.lle2d(system, precision=p, **kw)
+                assert np.array_equal(got["lle"], ref, equal_nan=True), (kind, system)
             else:
                 ref = engine.basins_features(system, precision=engine.FP32, **kw)
                 for k in ("flags", "avg_peaks", "avg_intervals", "counts"):
                     assert np.array_equal(got[k], ref[k]), k
+    b.close()
+
+
+SYSID = {"lorenz": 0, "rossler": 1, "chen": 2, "chameleon": 3}
+
+
+def test_batch_jobs_match_fp64_oracle(engine, oracle):
+    """Every job of the mixed batch against the CPU oracle (FP64, the
+    reference's algorithm, pinned to its own code), at the stated tolerances
+    of each arithmetic over these short horizons. Chaotic orbits in FP32
+    leave the FP64 orbit within a few time units, so for them the bars are on
+    distributions, per point only where the arithmetic holds the orbit:
+    * bifurcation (FP32): flags equal on >= 99 % of points; the peak-count
+      distribution's deciles within 1 and its mean within 2 %;
+    * basins features (FP32): flags equal on >= 99 %, kept-peak counts on
+      >= 95 %, median relative deviation of the mean peak amplitude <= 1e-3;
+    * LLE in FP32: Rossler within 2e-4 everywhere, Chameleon median within
+      1e-3, Lorenz (10 time units of a chaotic orbit) median within 3e-2;
+    * LLE in float-float: Rossler within 2e-5, Chen within 5e-4 everywhere
+      (the FP64 twin's own cancellation noise is of that order)."""
+    b = engine.Batch()
+    jobs = _batch_jobs()
+    outs = []
+    for kind, system, kw in jobs:
+        if kind == "bif":
+            outs.append(b.add_bifurcation1d(system, peakCapacity=32, **kw))
+        elif kind in ("lle", "lleff"):
+            outs.append(b.add_lle2d(system, precision=engine.FF32 if kind == "lleff" else engine.FP32, **kw))
+        else:
+            outs.append(b.add_basins(system, **kw))
+    b.run()
+    lle_max = {("lle", "rossler"): 2e-4, ("lleff", "rossler"): 2e-5, ("lleff", "chen"): 5e-4}
+    lle_median = {("lle", "chameleon"): 1e-3, ("lle", "lorenz"): 3e-2}
+    for (kind, system, kw), got in zip(jobs, outs):
+        s = SYSID[system]
+        if kind == "bif":
+            o = oracle.bifurcation(s, 1, kw["tMax"], kw["nPts"], kw["h"], kw["initialConditions"], kw["ranges"],
+                                   kw["indicesOfMutVars"], kw["writableVar"], kw["maxValue"], kw["transientTime"],
+                                   kw["values"], cap=32)
+            assert np.mean(got["flags"] == o["flags"]) >= 0.99, system
+            dec = [abs(np.percentile(got["counts"], q) - np.percentile(o["counts"], q)) for q in range(10, 100, 10)]
+            assert max(dec) <= 1, (system, dec)
+            assert abs(got["counts"].mean() - o["counts"].mean()) <= 0.02 * o["counts"].mean(), system
+        elif kind in ("lle", "lleff"):
+            o = oracle.lle2d(s, kw["tMax"], kw["NT"], kw["nPts"], kw["h"], kw["eps"], kw["initialConditions"],
+                             kw["ranges"], kw["indicesOfMutVars"], kw["transientTime"], kw["values"])
+            fin = np.isfinite(o) & np.isfinite(got["lle"])
+            assert fin.mean() > 0.95
+            d = np.abs(got["lle"] - o)[fin]
+            if (kind, system) in lle_max:
+                assert d.max() < lle_max[(kind, system)], (kind, system, d.max())
+            else:
+                assert np.median(d) < lle_median[(kind, system)], (kind, system, np.median(d))
+        else:
+            o = oracle.basins_features(s, kw["tMax"], kw["nPts"], kw["h"], kw["initialConditions"], kw["ranges"],
+                                       kw["indicesOfMutVars"], kw["writableVar"], kw["maxValue"],
+                                       kw["transientTime"], kw["values"])
+            assert np.mean(got["flags"] == o["flags"]) >= 0.99
+            assert np.mean(got["counts"] == o["counts"]) >= 0.95
+            ap, oa = got["avg_peaks"], o["avg_peaks"]
+            assert np.median(np.abs(ap - oa) / np.maximum(1.0, np.abs(oa))) <= 1e-3
     b.close()
 
 
@@ -387,8 +457,8 @@ def test_server_results_equal_alone(engine):
     for i, (kind, system, kw) in enumerate(_batch_jobs() * 2):
         if kind == "bif":
             rid, out = srv.submit_bifurcation1d(system, peakCapacity=32, **kw)
-        elif kind == "lle":
-            rid, out = srv.submit_lle2d(system, **kw)
+        elif kind in ("lle", "lleff"):
+            rid, out = srv.submit_lle2d(system, precision=engine.FF32 if kind == "lleff" else engine.FP32, **kw)
         else:
             rid, out = srv.submit_basins(system, eps=0.05, **kw)
         reqs.append((rid, kind, system, kw, out))
@@ -406,8 +476,8 @@ def test_server_results_equal_alone(engine):
             for r, c in enumerate(ref["counts"]):
                 m = min(int(c), 32)
                 assert np.array_equal(got["peaks"][r, :m], ref["peaks"][r, :m])
-        elif kind == "lle":
-            ref = engine.lle2d(system, precision=engine.FP32, **kw)
+        elif kind in ("lle", "lleff"):
+            ref = engine.lle2d(system, precision=engine.FF32 if kind == "lleff" else engine.FP32, **kw)
             assert np.array_equal(got["lle"], ref, equal_nan=True)
         else:
             ref = engine.basins(system, precision=engine.FP32, eps=0.05, **kw)
