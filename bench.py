@@ -104,11 +104,14 @@ def batch_jobs(seed: int = 2024, n_jobs: int = 256):
     return jobs
 
 
-def serve_requests(seed: int = 7, n: int = 2000):
+def serve_requests(seed: int = 7, n: int = 10000):
     """The served stream: n requests, 40 % 1-D bifurcation, 40 % LLE maps,
-    20 % basins maps (features + reference clustering), systems uniform over
-    Lorenz / Rossler / Chen, grid sizes log-uniform in [1e3, 4e6] points,
-    2000 transient steps and 2000 recorded (or 202 Benettin blocks of 10)."""
+    20 % basins maps (features + the reference clustering), systems uniform
+    over Lorenz / Rossler / Chen, grid sizes log-uniform in [1e3, 4e6] points,
+    with the horizons of the single-workload configurations: bifurcation
+    10,000 transient + 10,000 recorded steps, LLE 5,000 transient + 5,002
+    blocks of 10 steps of orbit and twin, basins 20,000 transient + 5,000
+    recorded steps (h = 0.01)."""
     rng = np.random.default_rng(seed)
     reqs = []
     for _ in range(n):
@@ -121,20 +124,20 @@ def serve_requests(seed: int = 7, n: int = 2000):
         ic = {"lorenz": [0.1, 0.1, 0.1], "rossler": [1.0, 1.0, 1.0], "chen": [-10.0, 0.0, 37.0]}[system]
         if kind == "bif":
             mut, rg = {"lorenz": ([1], [20.0, 200.0]), "rossler": ([2], [2.0, 10.0]), "chen": ([2], [20.0, 30.0])}[system]
-            reqs.append((kind, system, dict(tMax=20.0, nPts=N, h=0.01, initialConditions=ic, ranges=rg,
-                                            indicesOfMutVars=mut, writableVar=0, maxValue=1e4, transientTime=20.0,
+            reqs.append((kind, system, dict(tMax=100.0, nPts=N, h=0.01, initialConditions=ic, ranges=rg,
+                                            indicesOfMutVars=mut, writableVar=0, maxValue=1e4, transientTime=100.0,
                                             values=vals)))
         elif kind == "lle":
             mut, rg = {"lorenz": ([1, 0], [20.0, 200.0, 5.0, 15.0]), "rossler": ([0, 2], [0.1, 0.4, 2.0, 10.0]),
                        "chen": ([2, 0], [20.0, 30.0, 30.0, 40.0])}[system]
-            reqs.append((kind, system, dict(tMax=20.0, NT=0.1, nPts=m, h=0.01, eps=1e-8, initialConditions=ic,
-                                            ranges=rg, indicesOfMutVars=mut, transientTime=20.0, values=vals)))
+            reqs.append((kind, system, dict(tMax=500.0, NT=0.1, nPts=m, h=0.01, eps=1e-8, initialConditions=ic,
+                                            ranges=rg, indicesOfMutVars=mut, transientTime=50.0, values=vals)))
         else:
             icb = {"lorenz": [0.0, 0.0, 27.0], "rossler": [0.0, 0.0, 0.5], "chen": [0.0, 0.0, 20.0]}[system]
             vb = {"lorenz": [10.0, 24.0, 8 / 3], "rossler": [0.2, 0.2, 5.7], "chen": [35.0, 3.0, 28.0]}[system]
-            reqs.append((kind, system, dict(tMax=20.0, nPts=m, h=0.01, initialConditions=icb,
+            reqs.append((kind, system, dict(tMax=50.0, nPts=m, h=0.01, initialConditions=icb,
                                             ranges=[-30.0, 30.0, -30.0, 30.0], indicesOfMutVars=[0, 1],
-                                            writableVar=0, maxValue=1e8, transientTime=20.0, values=vb)))
+                                            writableVar=0, maxValue=1e8, transientTime=200.0, values=vb)))
     return reqs
 
 
@@ -450,50 +453,67 @@ def pipe_busy_from_profiles(kernel_tag: str):
 # ---- engine arm ----------------------------------------------------------------------------
 def batch_arm(args, ws, rank, local):
     """The heterogeneous batch as one prepared submission (CUDA graph of the
-    grouped persistent kernels), against the same jobs run one by one."""
+    grouped persistent kernels), against the same jobs run one by one. The
+    LLE jobs run float-float (--precision ff32, the default: the arithmetic
+    whose maps match FP64 to the FP64 map's own spread) or FP32; the line
+    carries the other batch's rate too, and the sampled jobs' FP64 rate and
+    LLE error."""
     import torch
 
     import chaoslibrary_gb300 as C
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    lle_prec = C.FP32 if args.precision == "fp32" else C.FF32
     jobs = batch_jobs()
     total_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in jobs)
     flops = sum(SYS_FLOPS[s_] * float(np.prod(job_points_steps(k, kw))) for k, s_, kw in jobs)
-    b = C.Batch(device=True)
-    for kind, system, kw in jobs:
-        if kind == "bif":
-            b.add_bifurcation1d(system, peakCapacity=64, **kw)
-        else:
-            b.add_lle2d(system, **kw)
+
+    def make(prec, device=True):
+        b = C.Batch(device=device)
+        outs = []
+        for kind, system, kw in jobs:
+            if kind == "bif":
+                outs.append(b.add_bifurcation1d(system, peakCapacity=64, **kw))
+            else:
+                outs.append(b.add_lle2d(system, precision=prec, **kw))
+        return b, outs
+
+    def timed(b, steps, flush, stream):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            b.replay()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(c) for a, c in ev]
+
+    b, outs = make(lle_prec)
     b.prepare()
     for _ in range(args.warmup):
         b.replay()
     torch.cuda.synchronize()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with Clocks([local] if ws == 1 else list(range(ws))) as clk:
         barrier(ws)
         torch.cuda.synchronize()
         l0 = C.launch_count()
-        for k in range(args.steps):
-            flush.fill_(k & 0xff)
-            ev[k][0].record(stream)
-            b.replay()
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
+        ms = timed(b, args.steps, flush, stream)
         launches = C.launch_count() - l0
         barrier(ws)
-    ms = [a.elapsed_time(c) for a, c in ev]
     t_total = max_over_ranks(ws, sum(ms) / 1e3)
     value = ws * total_steps * args.steps / t_total
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded job list)",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (bifurcation) / ff32 (LLE)" if lle_prec == C.FF32 else "f32",
+            "data": "synthetic (seeded job list)",
             "config": {"workload": "256 heterogeneous jobs (seed 2024): N log-uniform 1e3..1e6, systems "
                                    "Lorenz/Rossler/Chen, transients 2000..20000 steps, half 1-D bifurcation "
                                    "(10000 recorded steps), half LLE maps (tMax 100, NT 0.1)",
+                       "lle_precision": "ff32" if lle_prec == C.FF32 else "fp32",
                        "total_steps": float(total_steps), "jobs": len(jobs),
                        "l2": "256 MB buffer written between timed steps"},
             "clocks": clk.summary(), "gpu_launches": launches}
@@ -505,92 +525,98 @@ def batch_arm(args, ws, rank, local):
                             "algorithmic": "71/63/79 flops per Lorenz/Rossler/Chen RK4 step",
                             "peak_source": "measured in this run: chaos_fma_probe"}
     # e2e: one-shot host-memory submission (descriptor upload, launch, results copied back)
-    bh = C.Batch(device=False)
-    for kind, system, kw in jobs:
-        if kind == "bif":
-            bh.add_bifurcation1d(system, peakCapacity=64, **kw)
-        else:
-            bh.add_lle2d(system, **kw)
+    bh, _ = make(lle_prec, device=False)
     bh.run()
     t0 = time.perf_counter()
     bh.run()
     e2e_s = max_over_ranks(ws, time.perf_counter() - t0)
     d2h = sum(sum(v.nbytes for v in o.values()) for o in bh.outputs)
+    bh.close()
     line["e2e"] = {"value": ws * total_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": d2h}
     if rank == 0 and not args.no_extras:
-        # the same jobs one at a time through the single-sweep FP32 entry points (device outputs)
-        outs = []
+        # the other LLE arithmetic, same jobs, same timing
+        other = C.FP32 if lle_prec == C.FF32 else C.FF32
+        b2, _ = make(other)
+        b2.prepare()
+        b2.replay()
+        torch.cuda.synchronize()
+        ms2 = timed(b2, max(2, min(args.steps, 5)), flush, stream)
+        b2.close()
+        line["other_lle_precision"] = {"lle_precision": "fp32" if other == C.FP32 else "ff32",
+                                       "value": total_steps / (statistics.mean(ms2) / 1e3), "unit": UNIT}
+        # the same jobs one at a time through the single-sweep entry points (device outputs)
+        single = []
         for kind, system, kw in jobs:
             n, _ = job_points_steps(kind, kw)
             if kind == "bif":
-                outs.append(dict(counts=torch.empty(n, dtype=torch.int32, device=dev),
-                                 flags=torch.empty(n, dtype=torch.int32, device=dev),
-                                 first=torch.empty(n, dtype=torch.float64, device=dev),
-                                 peaks=torch.empty(n * 64, dtype=torch.float64, device=dev),
-                                 intervals=torch.empty(n * 64, dtype=torch.float64, device=dev)))
+                single.append(dict(counts=torch.empty(n, dtype=torch.int32, device=dev),
+                                   flags=torch.empty(n, dtype=torch.int32, device=dev),
+                                   first=torch.empty(n, dtype=torch.float64, device=dev),
+                                   peaks=torch.empty(n * 64, dtype=torch.float64, device=dev),
+                                   intervals=torch.empty(n * 64, dtype=torch.float64, device=dev)))
             else:
-                outs.append(torch.empty(n, dtype=torch.float64, device=dev))
+                single.append(torch.empty(n, dtype=torch.float64, device=dev))
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        for (kind, system, kw), o in zip(jobs, outs):
+        for (kind, system, kw), o in zip(jobs, single):
             if kind == "bif":
                 C.bifurcation1d(system, precision=C.FP32, peakCapacity=64, out=o, **kw)
             else:
-                C.lle2d(system, precision=C.FP32, out=o, **kw)
+                C.lle2d(system, precision=lle_prec, out=o, **kw)
         e1.record()
         torch.cuda.synchronize()
         t_seq = e0.elapsed_time(e1) / 1e3
-        # plain FP64 single-sweep kernel on every 16th job
-        sample = jobs[::16]
-        s_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in sample)
-        e0.record()
-        for kind, system, kw in sample:
+        # plain FP64 single-sweep kernel on every 15th job (both kinds), and the
+        # batch's LLE maps of those jobs against their FP64 maps
+        sample = list(range(0, len(jobs), 15))
+        s_steps = sum(np.prod(job_points_steps(*jobs[k][::2])) for k in sample)
+        errs = []
+        t64 = 0.0
+        for k in sample:
+            kind, system, kw = jobs[k]
+            e0.record()
             if kind == "bif":
                 C.bifurcation1d(system, precision=C.FP64, peakCapacity=64, **kw)
             else:
-                C.lle2d(system, precision=C.FP64, **kw)
-        e1.record()
-        torch.cuda.synchronize()
-        t64 = e0.elapsed_time(e1) / 1e3
-        line["one_by_one_fp32"] = {"value": total_steps / t_seq, "unit": UNIT,
-                                   "batched_speedup": t_seq / (statistics.mean(ms) / 1e3)}
-        line["fp64_plain"] = {"value": s_steps / t64, "unit": UNIT, "sample": "every 16th job, one by one",
-                              "batched_fp32_speedup": value / (s_steps / t64)}
+                a = C.lle2d(system, precision=C.FP64, **kw)
+            e1.record()
+            torch.cuda.synchronize()
+            t64 += e0.elapsed_time(e1) / 1e3
+            if kind != "bif":
+                v = outs[k]["lle"].cpu().numpy()
+                fin = np.isfinite(a) & np.isfinite(v)
+                errs.append(np.abs(v - a)[fin])
+        d = np.concatenate(errs) if errs else np.zeros(1)
+        line["one_by_one"] = {"value": total_steps / t_seq, "unit": UNIT,
+                              "batched_speedup": t_seq / (statistics.mean(ms) / 1e3)}
+        line["fp64_plain"] = {"value": s_steps / t64, "unit": UNIT, "sample": "every 15th job, one by one",
+                              "batched_speedup": value / (s_steps / t64)}
+        line["lle_error_vs_fp64"] = {"jobs": len(errs), "points": int(d.size), "p50": float(np.median(d)),
+                                     "p90": float(np.percentile(d, 90)), "max": float(d.max()),
+                                     "frac_le_1e-3": float(np.mean(d <= 1e-3)),
+                                     "note": "tMax 100: a chaotic orbit's finite-time LLE over 100 time units "
+                                             "differs between FP64 runs started 1e-13 apart by about this much"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     b.close()
 
 
-def serve_arm(args, ws, rank, local):
-    """Poisson arrivals of the served stream into the request loop; reports
-    p50/p99 latency and aggregate throughput."""
+def serve_stream(C, args, seed, lle_prec, local):
+    """One served stream: Poisson arrivals of serve_requests(seed) into the
+    request loop. Returns its line fields and the outputs of the small LLE
+    requests kept for the precision check."""
     import threading
 
-    import chaoslibrary_gb300 as C
-
-    reqs = serve_requests(n=args.requests)
-    rng = np.random.default_rng(11)
+    reqs = serve_requests(seed=seed, n=args.requests)
+    rng = np.random.default_rng(seed + 1000)
     gaps = rng.exponential(1.0 / args.rate, size=len(reqs))
+    keep = {k for k, (kind, _, kw) in enumerate(reqs) if kind == "lle" and kw["nPts"] ** 2 <= 16384}
+    keep = set(sorted(keep)[:12])
     srv = C.Server(hbm_budget_bytes=args.hbm_budget_gb << 30, max_active=256, iteration_steps=args.iteration_steps)
-    # warm-up: a small request of each kind and system (kernel loading), not counted
-    w = []
-    for kind, system, kw in serve_requests(n=60):
-        kw = dict(kw, nPts=min(kw["nPts"], 1000 if kind == "bif" else 32))
-        if kind == "bif":
-            w.append(srv.submit_bifurcation1d(system, peakCapacity=4, **kw))
-        elif kind == "lle":
-            w.append(srv.submit_lle2d(system, **kw))
-        else:
-            w.append(srv.submit_basins(system, eps=0.05, **kw))
-    for rid, _ in w:
-        srv.wait(rid)
-    srv.close()
-    srv = C.Server(hbm_budget_bytes=args.hbm_budget_gb << 30, max_active=256, iteration_steps=args.iteration_steps)
-    ids = []
+    ids, kept, done_lat = [], {}, []
     lock = threading.Lock()
-    done_lat = []
 
     def waiter():
         k = 0
@@ -608,6 +634,8 @@ def serve_arm(args, ws, rank, local):
             srv.wait(rid, timeout=3600)
             done_lat.append(srv.latency(rid))
             with lock:
+                if k in keep:
+                    kept[k] = ids[k][1]["lle"].copy()
                 ids[k] = (rid, None)  # drop the output arrays
             k += 1
 
@@ -625,7 +653,7 @@ def serve_arm(args, ws, rank, local):
             if kind == "bif":
                 rid, out = srv.submit_bifurcation1d(system, peakCapacity=4, **kw)
             elif kind == "lle":
-                rid, out = srv.submit_lle2d(system, **kw)
+                rid, out = srv.submit_lle2d(system, precision=lle_prec, **kw)
             else:
                 rid, out = srv.submit_basins(system, eps=0.05, **kw)
             with lock:
@@ -637,20 +665,69 @@ def serve_arm(args, ws, rank, local):
     srv.close()
     total_steps = sum(np.prod(job_points_steps(k, kw)) for k, _, kw in reqs)
     lat = np.array(done_lat)
-    line = {"metric": METRIC, "value": total_steps / wall, "unit": UNIT, "n_gpus": 1, "steps": len(reqs),
-            "warmup": 1, "ms_per_step": 1e3 * wall / len(reqs), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded request stream)",
-            "config": {"workload": f"served stream: {len(reqs)} Poisson requests at {args.rate}/s, 40% 1-D "
-                                   "bifurcation, 40% LLE, 20% basins (+clustering), Lorenz/Rossler/Chen, "
-                                   "1e3..4e6 points, 2000 transient + 2000 recorded steps",
-                       "rate_per_s": args.rate, "requests": len(reqs), "hbm_budget_gb": args.hbm_budget_gb,
-                       "iteration_steps": args.iteration_steps},
+    return {"seed": seed, "value": total_steps / wall, "wall_s": wall, "total_steps": float(total_steps),
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "mean": float(lat.mean()), "max": float(lat.max())},
-            "server": st, "clocks": clk.summary(), "total_steps": float(total_steps), "wall_s": wall,
-            "gpu_launches": launches,
-            "e2e": {"value": total_steps / wall, "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": None}}
+            "server": st, "clocks": clk.summary(), "gpu_launches": launches}, reqs, kept
+
+
+def serve_arm(args, ws, rank, local):
+    """Poisson arrivals of the served stream into the request loop, repeated
+    over --repeats seeds; reports p50/p99 latency per stream and their
+    spread, aggregate throughput, and the served LLE maps' error against the
+    plain FP64 maps of the same requests (the small ones, <= 128^2 points)."""
+    import chaoslibrary_gb300 as C
+
+    lle_prec = C.FF32 if args.precision == "ff32" else C.FP32
+    srv = C.Server(hbm_budget_bytes=args.hbm_budget_gb << 30, max_active=256, iteration_steps=args.iteration_steps)
+    # warm-up: a small request of each kind and system (kernel loading), not counted
+    w = []
+    for kind, system, kw in serve_requests(n=60):
+        kw = dict(kw, nPts=min(kw["nPts"], 1000 if kind == "bif" else 32), tMax=min(kw["tMax"], 5.0))
+        if kind == "bif":
+            w.append(srv.submit_bifurcation1d(system, peakCapacity=4, **kw))
+        elif kind == "lle":
+            w.append(srv.submit_lle2d(system, precision=lle_prec, **kw))
+        else:
+            w.append(srv.submit_basins(system, eps=0.05, **kw))
+    for rid, _ in w:
+        srv.wait(rid)
+    srv.close()
+    runs, errs = [], []
+    for r in range(args.repeats):
+        run, reqs, kept = serve_stream(C, args, 7 + r, lle_prec, local)
+        runs.append(run)
+        for k, v in kept.items():
+            _, system, kw = reqs[k]
+            a = C.lle2d(system, precision=C.FP64, **kw)
+            fin = np.isfinite(a) & np.isfinite(v)
+            errs.append((np.abs(v - a)[fin], (a < 0.005)[fin]))
+    first = runs[0]
+    d = np.concatenate([e for e, _ in errs]) if errs else np.zeros(0)
+    reg = np.concatenate([g for _, g in errs]) if errs else np.zeros(0, bool)
+    p50s, p99s = [x["latency_s"]["p50"] for x in runs], [x["latency_s"]["p99"] for x in runs]
+    line = {"metric": METRIC, "value": first["value"], "unit": UNIT, "n_gpus": 1, "steps": args.requests,
+            "warmup": 1, "ms_per_step": 1e3 * first["wall_s"] / args.requests, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "ff32 (LLE requests) / f32" if lle_prec == C.FF32
+            else "f32", "data": "synthetic (seeded request streams)",
+            "config": {"workload": f"served stream: {args.requests} Poisson requests at {args.rate}/s, 40% 1-D "
+                                   "bifurcation (10,000 + 10,000 steps), 40% LLE maps (5,000 + 5,002 x 10 x 2 "
+                                   "steps), 20% basins (20,000 + 5,000 steps, + the reference clustering), "
+                                   "Lorenz/Rossler/Chen, 1e3..4e6 points",
+                       "lle_precision": "ff32" if lle_prec == C.FF32 else "fp32", "rate_per_s": args.rate,
+                       "requests": args.requests, "repeats": args.repeats, "hbm_budget_gb": args.hbm_budget_gb,
+                       "iteration_steps": args.iteration_steps},
+            "latency_s": first["latency_s"], "server": first["server"], "clocks": first["clocks"],
+            "total_steps": first["total_steps"], "wall_s": first["wall_s"], "gpu_launches": first["gpu_launches"],
+            "repeats": [{k: x[k] for k in ("seed", "value", "wall_s", "latency_s")} for x in runs],
+            "latency_spread_s": {"p50_min": min(p50s), "p50_max": max(p50s), "p99_min": min(p99s),
+                                 "p99_max": max(p99s)},
+            "lle_error_vs_fp64": None if d.size == 0 else {
+                "requests": len(errs), "points": int(d.size), "p50": float(np.median(d)),
+                "p90": float(np.percentile(d, 90)), "max": float(d.max()), "frac_le_1e-3": float(np.mean(d <= 1e-3)),
+                "regular_points": int(reg.sum()),
+                "regular_frac_le_1e-3": float(np.mean(d[reg] <= 1e-3)) if reg.any() else None},
+            "e2e": {"value": first["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": None}}
     print(json.dumps(line), flush=True)
 
 
@@ -726,7 +803,6 @@ def engine_arm(args, ws, rank, local):
         # min-max normalised, textbook DBSCAN eps=0.05, minPts=8
         steps_pp = sweep_steps_per_point(w)
         outs = dict(labels=torch.empty(n_points, dtype=torch.int32, device=dev),
-                    features=torch.empty((n_points, 3), dtype=torch.float64, device=dev),
                     flags=torch.empty(n_points, dtype=torch.int32, device=dev))
         kw = kw_of(w)
 
@@ -734,8 +810,8 @@ def engine_arm(args, ws, rank, local):
             return C.basins_dbscan(w["system"], precision=prec, out=outs, **kw)
 
         def step_host():
-            return C.basins_dbscan(w["system"], precision=prec, **kw)
-        d2h = n_points * (4 + 24 + 4)
+            return C.basins_dbscan(w["system"], precision=prec, with_features=False, **kw)
+        d2h = n_points * (4 + 4)
         tag = "basins_lorenz_2048" if args.precision == "fp32" else None
     steps_per_call = n_points * steps_pp
     for _ in range(args.warmup):
@@ -1114,8 +1190,9 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="lle",
                     choices=["lle", "bif1d", "bif2d", "basins", "spectrum", "batch", "serve"])
-    ap.add_argument("--requests", type=int, default=2000, help="served stream length")
-    ap.add_argument("--rate", type=float, default=100.0, help="served stream arrival rate (requests/s)")
+    ap.add_argument("--requests", type=int, default=10000, help="served stream length")
+    ap.add_argument("--rate", type=float, default=16.0, help="served stream arrival rate (requests/s)")
+    ap.add_argument("--repeats", type=int, default=1, help="served streams (seeds 7, 8, ...)")
     ap.add_argument("--hbm-budget-gb", type=int, default=64)
     ap.add_argument("--iteration-steps", type=float, default=2e10)
     ap.add_argument("--precision", default="auto", choices=["auto", "ff32", "fp32", "fp64"],
@@ -1127,8 +1204,8 @@ def main():
     ap.add_argument("--npts", type=int, default=None, help="grid resolution override (profiling runs only)")
     ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()
-    if args.precision == "auto":
-        args.precision = "ff32" if args.workload == "lle" and args.impl == "engine" else "fp32"
+    if args.precision == "auto":  # the LLE arithmetic that matches FP64 to the FP64 map's own spread
+        args.precision = "ff32" if args.workload in ("lle", "batch") and args.impl == "engine" else "fp32"
     for w in (LLE, BIF1D, BIF2D, BASINS, SPECTRUM):
         if args.npts:
             w["nPts"] = args.npts

@@ -686,13 +686,17 @@ def basins(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, w
 
 
 def basins_dbscan(system, tMax, nPts, h, initialConditions, ranges, indicesOfMutVars, writableVar, maxValue,
-                  transientTime, values, preScaller=1, eps=0.05, minPts=8, precision=FP64, out=None, stream=None):
+                  transientTime, values, preScaller=1, eps=0.05, minPts=8, precision=FP64, out=None, stream=None,
+                  with_features=True):
     """Basins with normalised (amplitude, peak count, interval) features and
-    textbook DBSCAN; labels 0.. clusters, -1 noise, -2 diverged."""
+    textbook DBSCAN; labels 0.. clusters, -1 noise, -2 diverged. The n x 3
+    feature matrix is returned when with_features (or when out holds it)."""
     A = _Args()
     n = nPts * nPts
     if out is None:
-        out = dict(labels=np.zeros(n, np.int32), features=np.zeros((n, 3)), flags=np.zeros(n, np.int32))
+        out = dict(labels=np.zeros(n, np.int32), flags=np.zeros(n, np.int32))
+        if with_features:
+            out["features"] = np.zeros((n, 3))
     ex = _exec(precision, out, stream)
     ic = np.asarray(initialConditions, np.float64)
     vals = np.asarray(values, np.float64)

@@ -900,16 +900,19 @@ int chaos_basins_dbscan(const chaos_exec* ex, int system, double tMax, int nPts,
     O.avgIntervals = (double*)c.alloc(n * sizeof(double));
     O.counts = (int*)c.alloc(n * sizeof(int));
     O.last = (double*)c.alloc(n * sizeof(double));
-    double* F = features ? (double*)c.output(features, (size_t)n * 3 * sizeof(double))
-                         : (double*)c.alloc((size_t)n * 3 * sizeof(double));
+    // the clustering reads the features as three columns; the row-major
+    // matrix is written only when the caller asks for it
+    double* F = features ? (double*)c.output(features, (size_t)n * 3 * sizeof(double)) : nullptr;
+    double* cols[3];
+    for (auto& col : cols) col = (double*)c.alloc(n * sizeof(double));
     int* mask = (int*)c.alloc(n * sizeof(int));
     double* minmax = (double*)c.alloc(6 * sizeof(double));
     int* dLabels = (int*)c.output(labels, n * sizeof(int));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e = run_basins(c.ex.precision, P, O, c.stream);
-    if (e == cudaSuccess) e = launch_basin_feature_matrix(O, n, minmax, F, mask, c.stream);
+    if (e == cudaSuccess) e = launch_basin_feature_matrix(O, n, minmax, F, cols, mask, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "basins feature kernels"));
-    rc = dbscan_device(c, F, n, 3, eps, minPts, mask, dLabels);
+    rc = dbscan_device_soa(c, cols, n, 3, eps, minPts, mask, dLabels);
     if (!rc) rc = c.to_host(labels, dLabels, n * sizeof(int));
     if (!rc && features) rc = c.to_host(features, F, (size_t)n * 3 * sizeof(double));
     if (!rc && flags) rc = c.to_host(flags, O.flags, n * sizeof(int));

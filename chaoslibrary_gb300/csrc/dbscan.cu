@@ -29,6 +29,8 @@
 // exact pair tests.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 
@@ -144,24 +146,51 @@ inline unsigned blocks(long long n, int tpb = kTPB) { return (unsigned)((n + tpb
 // cell) stays far inside the 1e-9 by which the side is shrunk, so two points
 // of one cell are still within eps (a division here would cost the FP64 pipe
 // three divides per point for the same guarantee).
+// The kernel also reduces the extent of the cell coordinates of its ordinary
+// points (ext[d] = -min, ext[3 + d] = max, per dimension) and counts the
+// clamped or NaN ones (ext[6]): the number of occupied cells is at most the
+// product of the extents plus that count, which sizes the hash table (a
+// basin map's normalised features occupy at most ~35^3 cells of its 4.2 M
+// points). One atomic per warp and quantity.
 __global__ void cell_key_kernel(Feat F, const int* include, long long n, double invSide, unsigned long long* key,
-                                unsigned char* unsafe) {
+                                unsigned char* unsafe, long long* ext) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (!include[i]) { key[i] = kEmpty; unsafe[i] = 0; return; }
     long long c[3] = {0, 0, 0};
-    bool bad = false;
-    for (int d = 0; d < F.D; ++d) {
-        const double q = F.f[d][i] * invSide;
-        if (q != q) { c[0] = kLim + 5; c[1] = kLim + 5; c[2] = kLim + 5; bad = true; break; }
-        long long v;
-        if (q >= (double)kLim) { v = kLim; bad = true; }
-        else if (q < -(double)kLim) { v = -kLim; bad = true; }
-        else v = (long long)floor(q);
-        c[d] = v;
+    bool bad = false, ok = false;
+    if (i < n) {
+        if (!include[i]) {
+            key[i] = kEmpty;
+            unsafe[i] = 0;
+        } else {
+            for (int d = 0; d < F.D; ++d) {
+                const double q = F.f[d][i] * invSide;
+                if (q != q) { c[0] = kLim + 5; c[1] = kLim + 5; c[2] = kLim + 5; bad = true; break; }
+                long long v;
+                if (q >= (double)kLim) { v = kLim; bad = true; }
+                else if (q < -(double)kLim) { v = -kLim; bad = true; }
+                else v = (long long)floor(q);
+                c[d] = v;
+            }
+            key[i] = pack(c, F.D);
+            unsafe[i] = bad ? 1 : 0;
+            ok = !bad;
+        }
     }
-    key[i] = pack(c, F.D);
-    unsafe[i] = bad ? 1 : 0;
+    const int lane = threadIdx.x & 31;
+    const unsigned nbad = __popc(__ballot_sync(0xffffffffu, bad));
+    if (lane == 0 && nbad) atomicAdd((unsigned long long*)&ext[6], (unsigned long long)nbad);
+    if (!__any_sync(0xffffffffu, ok)) return;
+    for (int d = 0; d < F.D; ++d) {
+        long long lo = ok ? -c[d] : LLONG_MIN, hi = ok ? c[d] : LLONG_MIN;  // max of -c and of c
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = max(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            atomicMax(&ext[d], lo);
+            atomicMax(&ext[3 + d], hi);
+        }
+    }
 }
 
 // The lanes of a warp that carry the same cell key are served by one lane
@@ -182,7 +211,7 @@ __global__ void hash_insert_kernel(const unsigned long long* key, long long n, u
             const unsigned long long prev = atomicCAS(&tab[g], kEmpty, k);
             if (prev == kEmpty || prev == k) { h = (long long)g; break; }
             g = (g + 1) & mask;
-        }  // the table has twice as many slots as points: a free slot is always found
+        }  // the table has at least twice as many slots as occupied cells: a free slot is always found
     }
     h = __shfl_sync(0xffffffffu, h, leader);
     if (i < n) slot[i] = k == kEmpty ? -1 : h;
@@ -812,16 +841,33 @@ int grid_cluster(Call& c, Feat F, long long n, double eps, int minPts, bool comp
     unsigned long long* key = (unsigned long long*)c.alloc(n * sizeof(unsigned long long));
     unsigned char* unsafePt = (unsigned char*)c.alloc(n);
     long long* slot = (long long*)c.alloc(n * sizeof(long long));
-    unsigned long long cap = 1;
-    while (cap < (unsigned long long)(2 * n + 2)) cap <<= 1;
+    long long* ext = (long long*)c.alloc(8 * sizeof(long long));
+    NEED(!c.failed);
+    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include);
+    note_launch();
+    {
+        const long long init[8] = {LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN, 0, 0};
+        CK(cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, st));
+    }
+    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, 1.0 / side, key, unsafePt, ext);
+    note_launch();
+    // table capacity: a power of two >= twice a bound on the occupied cells
+    long long hx[8];
+    CK(cudaMemcpyAsync(hx, ext, sizeof hx, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double bound = (double)hx[6];
+    if (hx[3] != LLONG_MIN) {  // some ordinary point
+        double prod = 1.0;
+        for (int d = 0; d < D; ++d) prod *= (double)(hx[3 + d] + hx[d] + 1);
+        bound += prod;
+    }
+    bound = std::min(bound, (double)n);
+    unsigned long long cap = 1024;
+    while ((double)cap < 2.0 * bound + 2.0) cap <<= 1;
     unsigned long long* tab = (unsigned long long*)c.alloc(cap * sizeof(unsigned long long));
     int* occ = (int*)c.alloc(cap * sizeof(int));
     int* slotCell = (int*)c.alloc(cap * sizeof(int));
     NEED(!c.failed);
-    include_kernel<<<blocks(n), kTPB, 0, st>>>(flags, mask, n, compat ? 1 : 0, include);
-    note_launch();
-    cell_key_kernel<<<blocks(n), kTPB, 0, st>>>(F, include, n, 1.0 / side, key, unsafePt);
-    note_launch();
     CK(cudaMemsetAsync(tab, 0xff, cap * sizeof(unsigned long long), st));
     hash_insert_kernel<<<blocks(n), kTPB, 0, st>>>(key, n, tab, cap - 1, slot);
     note_launch();
@@ -1021,6 +1067,14 @@ int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgInter
     F.f[2] = avgIntervals;
     F.D = 2;
     return grid_cluster(c, F, n, eps, 1, true, flags, nullptr, labels);
+}
+
+int dbscan_device_soa(Call& c, const double* const* columns, long long n, int dims, double eps, int minPts,
+                      const int* mask, int* labels) {
+    Feat F;
+    for (int d = 0; d < 3; ++d) F.f[d] = columns[d < dims ? d : dims - 1];
+    F.D = dims;
+    return grid_cluster(c, F, n, eps, minPts, false, nullptr, mask, labels);
 }
 
 int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,

@@ -10,6 +10,10 @@ namespace chaos {
 int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgIntervals, const int* flags, long long n,
                          double eps, int* labels);
 
+// The same on dims device columns of n values (one array per feature).
+int dbscan_device_soa(Call& c, const double* const* columns, long long n, int dims, double eps, int minPts,
+                      const int* mask, int* labels);
+
 // DBSCAN with scikit-learn semantics on a row-major n x dims device matrix.
 int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,
                   int* labels);

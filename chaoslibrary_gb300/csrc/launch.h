@@ -139,7 +139,7 @@ cudaError_t launch_trajectory_ff(int system, const double* x0, const double* a0,
 // Basin features in normalised form (basins_dbscan.cu): per point (amplitude,
 // peak count, mean interval), min-max scaled over the points with flag != 0.
 cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double* minmax, double* features,
-                                        int* mask, cudaStream_t st);
+                                        double* const* columns, int* mask, cudaStream_t st);
 
 // FP32 LLE kernel variant (kern_f32.cu): 0 = default, 2 = two points per
 // thread (packed FP32x2), 12 / 16 = one point per thread at that occupancy.

@@ -35,6 +35,8 @@ BASINS_FUNCS = ["getValueByIdx", "calculateDiscreteModel", "calculateTransTimeCU
                 "CUDA_dbscan_search_clear_points_kernel", "CUDA_dbscan_search_fixed_points_kernel",
                 "CUDA_dbscan_kernel"]
 LLE_FUNCS = ["loopCalculateDiscreteModel", "calculateDiscreteModel", "calculateSystem", "linspace"]
+# the legacy library's helpers behind the engine's legacy analyses (debri/cudaLibrary.cu)
+LEGACY_FUNCS = ["getValueByIdx", "getValueByIdxLog", "peakFinder", "projectionOperator", "gramSchmidtProcess"]
 
 # plug-in systems: name -> (header text of a systems.cuh stand-in)
 PLUGINS = {
@@ -166,7 +168,16 @@ def build(systems: list[str] | None = None, verbose: bool = False) -> list[Path]
                   OUT / "ref_bif.inc")
         write_inc(REF / "Basins/src/basinsCUDA.cu", "basinsGPU", BASINS_FUNCS, None, OUT / "ref_basins.inc")
         write_inc(REF / "LLE/src/LLECUDA.cu", "LLE_constants", LLE_FUNCS, "sh_mem", OUT / "ref_lle.inc")
+        write_inc(REF / "debri/cudaLibrary.cu", "legacy", LEGACY_FUNCS, None, OUT / "ref_legacy.inc")
     built = []
+    if (OUT / "ref_legacy.inc").is_file():
+        lib = OUT / "libref_legacy.so"
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", f"-I{HERE / 'ref_shim'}",
+               f"-I{OUT}", str(HERE / "ref_legacy_harness.cpp"), "-o", str(lib)]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+        built.append(lib)
     for name in systems or list(PLUGINS) + list(REF_SYSTEMS):
         sysdir = OUT / f"sys_{name}"
         sysdir.mkdir(exist_ok=True)

@@ -398,6 +398,49 @@ class RefLib:
         return out
 
 
+class LegacyLib:
+    """Host build of the reference's legacy helpers (debri/cudaLibrary.cu:
+    getValueByIdx, getValueByIdxLog, peakFinder, projectionOperator,
+    gramSchmidtProcess, extracted unchanged) with a host replay of the legacy
+    spectrum's block loop around them (oracle/ref_legacy_harness.cpp)."""
+
+    def __init__(self):
+        path = REF_DIR / "libref_legacy.so"
+        if not path.exists():
+            raise FileNotFoundError(path)
+        L = self.L = C.CDLL(str(path))
+        L.leg_value.argtypes = L.leg_value_log.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
+        L.leg_value.restype = L.leg_value_log.restype = C.c_double
+        L.leg_peak_finder.argtypes = [_dp, C.c_int, _dp, _dp, C.c_double]
+        L.leg_peak_finder.restype = C.c_int
+        L.leg_gram_schmidt.argtypes = [_dp, _dp, C.c_int, _dp]
+        L.leg_ls_replay.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
+                                    C.c_double, _dp, _dp]
+
+    def value_log(self, idx, nPts, start, finish, dim=0):
+        return self.L.leg_value_log(idx, nPts, start, finish, dim)
+
+    def value(self, idx, nPts, start, finish, dim=0):
+        return self.L.leg_value(idx, nPts, start, finish, dim)
+
+    def peak_finder(self, data, h):
+        d = _d(data).copy()
+        pk, tm = np.zeros(d.size), np.zeros(d.size)
+        c = self.L.leg_peak_finder(d, d.size, pk, tm, h)
+        return c, pk[:max(c, 0)], tm[:max(c, 0)]
+
+    def ls_replay(self, system, x0, a, h, trans, ntp, nblocks, eps, tmax, directions):
+        n = len(x0)
+        out = np.zeros(n)
+        self.L.leg_ls_replay(system, _d(x0), _d(a), h, trans, ntp, nblocks, eps, tmax,
+                             _d(np.asarray(directions, np.float64).ravel()), out)
+        return out
+
+
+def legacy_available() -> bool:
+    return (REF_DIR / "libref_legacy.so").exists()
+
+
 def ref_available(name: str = "lorenz") -> bool:
     return (REF_DIR / f"libref_{name}.so").exists()
 
