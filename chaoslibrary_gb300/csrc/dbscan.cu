@@ -151,9 +151,13 @@ inline unsigned blocks(long long n, int tpb = kTPB) { return (unsigned)((n + tpb
 // clamped or NaN ones (ext[6]): the number of occupied cells is at most the
 // product of the extents plus that count, which sizes the hash table (a
 // basin map's normalised features occupy at most ~35^3 cells of its 4.2 M
-// points). One atomic per warp and quantity.
+// points). Warps reduce with shuffles into shared memory, one global atomic
+// per block and quantity.
 __global__ void cell_key_kernel(Feat F, const int* include, long long n, double invSide, unsigned long long* key,
                                 unsigned char* unsafe, long long* ext) {
+    __shared__ long long sext[7];
+    if (threadIdx.x < 7) sext[threadIdx.x] = threadIdx.x < 6 ? LLONG_MIN : 0;
+    __syncthreads();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long c[3] = {0, 0, 0};
     bool bad = false, ok = false;
@@ -178,19 +182,23 @@ __global__ void cell_key_kernel(Feat F, const int* include, long long n, double 
     }
     const int lane = threadIdx.x & 31;
     const unsigned nbad = __popc(__ballot_sync(0xffffffffu, bad));
-    if (lane == 0 && nbad) atomicAdd((unsigned long long*)&ext[6], (unsigned long long)nbad);
-    if (!__any_sync(0xffffffffu, ok)) return;
-    for (int d = 0; d < F.D; ++d) {
-        long long lo = ok ? -c[d] : LLONG_MIN, hi = ok ? c[d] : LLONG_MIN;  // max of -c and of c
-        for (int o = 16; o > 0; o >>= 1) {
-            lo = max(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        }
-        if (lane == 0) {
-            atomicMax(&ext[d], lo);
-            atomicMax(&ext[3 + d], hi);
+    if (lane == 0 && nbad) atomicAdd((unsigned long long*)&sext[6], (unsigned long long)nbad);
+    if (__any_sync(0xffffffffu, ok)) {
+        for (int d = 0; d < F.D; ++d) {
+            long long lo = ok ? -c[d] : LLONG_MIN, hi = ok ? c[d] : LLONG_MIN;  // max of -c and of c
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = max(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            if (lane == 0) {
+                atomicMax(&sext[d], lo);
+                atomicMax(&sext[3 + d], hi);
+            }
         }
     }
+    __syncthreads();
+    if (threadIdx.x < 6 && sext[threadIdx.x] != LLONG_MIN) atomicMax(&ext[threadIdx.x], sext[threadIdx.x]);
+    if (threadIdx.x == 6 && sext[6]) atomicAdd((unsigned long long*)&ext[6], (unsigned long long)sext[6]);
 }
 
 // The lanes of a warp that carry the same cell key are served by one lane
