@@ -15,7 +15,7 @@
 // for the float-float LLE jobs, whose group kernel lives with the other FF
 // kernels (kern_ff.cu, compiled without contraction); the
 // jobs of the RK4 systems run two points per thread (packed FP32x2 lanes; the
-// bifurcation and basins jobs in the hybrid form), the others one. A prepared batch is
+// bifurcation jobs in the hybrid form), the others one. A prepared batch is
 // replayed from a captured CUDA graph (counter reset + the group kernels).
 #include <cuda_runtime.h>
 
@@ -60,8 +60,8 @@ __device__ __forceinline__ void run_bif(const JobDesc& J, long long b, int cnt) 
     }
 }
 
-// Basins chunks: the RK4 systems as hybrid pairs (packed transient, recorded
-// part lane by lane), the others one point per thread.
+// Basins chunks: the RK4 systems as packed pairs (the single sweep's default
+// form for large maps), the others one point per thread.
 template <int S, bool PRE1>
 __device__ __forceinline__ void run_basins_as(const SweepParams& sP, const JobDesc& J, long long b, int cnt) {
     if constexpr (S <= SYS_CHEN_RK4) {
@@ -69,8 +69,8 @@ __device__ __forceinline__ void run_basins_as(const SweepParams& sP, const JobDe
         for (int t = 2 * threadIdx.x; t < cnt; t += 2 * blockDim.x) {
             const long long p = b + t;
             const bool two = t + 1 < cnt;
-            basins_hybrid_point<typename FieldOf<S>::F, PRE1>(sP, J.bas, p, two ? p + 1 : p, p, two ? p + 1 : p,
-                                                              two);
+            basins_pair_point<typename FieldOf<S>::F, PRE1>(sP, J.bas, p, two ? p + 1 : p, p, two ? p + 1 : p,
+                                                            two);
         }
     } else {
 #pragma unroll 1

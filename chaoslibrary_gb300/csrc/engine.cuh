@@ -138,11 +138,31 @@ template <int NX, class T> __device__ __forceinline__ bool basins_fixed(const T*
     return sqrt(fabs((double)s)) < 1e-9;
 }
 
+// Samples per block of the recorded loops' block form: the steps of a block
+// run back to back, then the gate judges its samples together.
+constexpr int kRecordBlock = 4;
+// Steps per block of the bifurcation transients' block form.
+constexpr int kTransientBlock = 8;
+
+// The block form runs for the float detector (the branching form behind its
+// gate) on the built-in systems; a user system keeps the one-step loop (its
+// equations are not stepped past a divergence).
+template <int S, class T, bool Sel> struct RecordBlocks {
+    static constexpr bool value = PeakStream<T, Sel>::Gate && S != SYS_USER;
+};
+
 // The recorded part of a bifurcation point, from its state x after a
 // transient that ended bounded and not fixed: nB samples through the
 // streaming peak detector (intervals in units hI), divergence and fixed-point
 // tests; writes flags/counts/first and the first `cap` kept peaks/intervals
 // of row o.
+//
+// Block form: kRecordBlock steps without a branch, their divergence tests
+// or-ed together, then the samples through PeakStream::push_block. A block in
+// which the orbit diverged pushes its samples up to the divergent one, as the
+// one-step loop does, and ends the loop (the steps after the divergent one
+// change nothing that is reported). The last step, whose starting state the
+// fixed-point test keeps, always runs in the one-step loop.
 template <int S, class T, bool Sel = false>
 __device__ __forceinline__ void bif_record(const SweepParams& P, const BifOut& O, T* x, const T* a,
                                            const StepCtx<T>& c, int nB, double hI, long long o) {
@@ -155,29 +175,60 @@ __device__ __forceinline__ void bif_record(const SweepParams& P, const BifOut& O
     const double first = (double)pick<NX>(x, wv);
     double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
     double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
+    auto on_peak = [&](T val, int t) {
+        if (ps.n >= 1) {
+            const int q = ps.n - 1;
+            if (q < O.cap) {
+                if (pk) pk[q] = (double)val;
+                if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), hI);
+            }
+        }
+        ps.tprev = t;
+        ++ps.n;
+    };
     T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
 #pragma unroll
     for (int j = 0; j < NX; ++j) xp[j] = x[j];
-    for (int i = 0; i < nB; ++i) {
+    int i = 0;
+    if constexpr (RecordBlocks<S, T, Sel>::value) {
+        constexpr int K = kRecordBlock;
+        for (; i + K < nB; i += K) {
+            T s[K + 1];
+            s[0] = v;
+            bool dv = false;
 #pragma unroll
-        for (int j = 0; j < NX; ++j) xp[j] = x[j];
-        T val;
-        int t;
-        if (ps.push(v, val, t)) {
-            if (ps.n >= 1) {
-                const int q = ps.n - 1;
-                if (q < O.cap) {
-                    if (pk) pk[q] = (double)val;
-                    if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), hI);
-                }
+            for (int j = 1; j <= K; ++j) {
+                step<S>(x, a, c);
+                s[j] = pick<NX>(x, wv);
+                dv |= bif_diverged(s[j], P);
             }
-            ps.tprev = t;
-            ++ps.n;
+            if (__builtin_expect(!dv, 1)) {
+                ps.template push_block<K>(s, on_peak);
+                v = s[K];
+                continue;
+            }
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                T val;
+                int t;
+                if (ps.push(s[j], val, t)) on_peak(val, t);
+                if (bif_diverged(s[j + 1], P)) break;
+            }
+            flag = 0;
+            break;
         }
-        step<S>(x, a, c);
-        v = pick<NX>(x, wv);
-        if (bif_diverged(v, P)) { flag = 0; break; }
     }
+    if (flag == 1)
+        for (; i < nB; ++i) {
+#pragma unroll
+            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+            T val;
+            int t;
+            if (ps.push(v, val, t)) on_peak(val, t);
+            step<S>(x, a, c);
+            v = pick<NX>(x, wv);
+            if (bif_diverged(v, P)) { flag = 0; break; }
+        }
     if (flag == 1 && nB > 0 && bif_fixed<NX>(x, xp)) flag = -1;
     const int kept = ps.n > 1 ? ps.n - 1 : 0;
     O.flags[o] = flag;
@@ -208,10 +259,29 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
     if (nS > 0) {
         // the state before the last step is kept for the fixed-point test:
         // the last step is peeled off the loop, so the others copy nothing
-        for (int s = 0; s < nS - 1; ++s) {
-            step<S>(x, a, c);
-            if (bif_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+        int s = 0;
+        if constexpr (S != SYS_USER && !Sel) {
+            // blocks of kTransientBlock steps, one divergence branch a block:
+            // a point's flags do not depend on the step at which it diverged
+            // (the steps after it on an unbounded state report nothing). The
+            // select form (one-wave sweeps, one latency-bound orbit a warp)
+            // keeps the one-step loop and its registers.
+            constexpr int K = kTransientBlock;
+            for (; s + K <= nS - 1; s += K) {
+                bool dv = false;
+#pragma unroll
+                for (int j = 0; j < K; ++j) {
+                    step<S>(x, a, c);
+                    dv |= bif_diverged(pick<NX>(x, wv), P);
+                }
+                if (dv) { flag = 0; break; }
+            }
         }
+        if (flag == 1)
+            for (; s < nS - 1; ++s) {
+                step<S>(x, a, c);
+                if (bif_diverged(pick<NX>(x, wv), P)) { flag = 0; break; }
+            }
         if (flag == 1) {
 #pragma unroll
             for (int j = 0; j < NX; ++j) xp[j] = x[j];
@@ -280,24 +350,59 @@ __device__ __forceinline__ void basins_record(const SweepParams& P, const Basins
     int flag = 1;
     PeakSums<T> sums;
     T lastT = T(0);  // widened once after the loop (a per-step FP64 convert costs FP64-pipe time)
+    auto on_peak = [&](T val, int t) {
+        if (ps.n >= 1) sums.add(val, t - ps.tprev, P.hInterval);
+        ps.tprev = t;
+        ++ps.n;
+    };
     T v = pick<NX>(x, wv);  // the recorded sample, carried from one step to the next
-    for (int i = 0; i < P.B; ++i) {
+    int i = 0;
+    if constexpr (RecordBlocks<S, T, Sel>::value) {  // the block form of bif_record
+        constexpr int K = kRecordBlock;
+        for (; i + K < P.B; i += K) {
+            T s[K + 1];
+            s[0] = v;
+            bool dv = false;
 #pragma unroll
-        for (int j = 0; j < NX; ++j) xp[j] = x[j];
-        lastT = v;
-        T val;
-        int t;
-        if (ps.push(v, val, t)) {
-            if (ps.n >= 1) sums.add(val, t - ps.tprev, P.hInterval);
-            ps.tprev = t;
-            ++ps.n;
+            for (int j = 1; j <= K; ++j) {
+                if (PRE1) step<S>(x, a, c);
+                else
+                    for (int r = 0; r < P.preScaller; ++r) step<S>(x, a, c);
+                s[j] = pick<NX>(x, wv);
+                dv |= basins_diverged(s[j], P);
+            }
+            if (__builtin_expect(!dv, 1)) {
+                ps.template push_block<K>(s, on_peak);
+                lastT = s[K - 1];
+                v = s[K];
+                continue;
+            }
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                lastT = s[j];
+                T val;
+                int t;
+                if (ps.push(s[j], val, t)) on_peak(val, t);
+                if (basins_diverged(s[j + 1], P)) break;
+            }
+            flag = 0;
+            break;
         }
-        if (PRE1) step<S>(x, a, c);
-        else
-            for (int r = 0; r < P.preScaller; ++r) step<S>(x, a, c);
-        v = pick<NX>(x, wv);
-        if (basins_diverged(v, P)) { flag = 0; break; }
     }
+    if (flag == 1)
+        for (; i < P.B; ++i) {
+#pragma unroll
+            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+            lastT = v;
+            T val;
+            int t;
+            if (ps.push(v, val, t)) on_peak(val, t);
+            if (PRE1) step<S>(x, a, c);
+            else
+                for (int r = 0; r < P.preScaller; ++r) step<S>(x, a, c);
+            v = pick<NX>(x, wv);
+            if (basins_diverged(v, P)) { flag = 0; break; }
+        }
     if (flag == 1 && P.B > 0 && basins_fixed<NX>(x, xp)) flag = -1;
     const double last = (double)lastT;
     const int kept = ps.n > 1 ? ps.n - 1 : 0;
@@ -808,22 +913,41 @@ __device__ __forceinline__ void load_pair(const SweepParams& P, long long p0, lo
     }
 }
 
+// The transient of two bifurcation points in packed FP32x2 lanes, the last
+// step peeled off for the fixed-point test; flag[l] (1 on entry for a lane in
+// use, 0 otherwise) ends 1, 0 (diverged) or -1 (fixed), as bif_point's.
+// Blocks of kTransientBlock steps with one test a block, as in bif_point.
 template <class F>
-__device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOut& O, long long p0, long long p1,
-                                               long long o0, long long o1, bool two) {
-    P2 x[3], a[3], xp[3];
-    load_pair<F>(P, p0, p1, x, a);
-    const RK4H<P2> c((float)P.h);
+__device__ __forceinline__ void bif_pair_transient(const SweepParams& P, P2* x, const P2* a, int* flag) {
+    P2 xp[3];
     const int wv = P.wv;
-    int flag[2] = {1, two ? 1 : 0};
     if (P.S > 0) {
-        for (int s = 0; s < P.S - 1; ++s) {  // the last step peeled off, as in bif_point
-            rk4_step<F>(x, a, c);
-            const P2 v = pick2<3>(x, wv);
-            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
-            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
-            if (flag[0] != 1 && flag[1] != 1) break;
+        const RK4H<P2> c((float)P.h);
+        int s = 0;
+        {  // blocks of kTransientBlock steps with one test a block, as in bif_point
+            constexpr int K = kTransientBlock;
+            for (; s + K <= P.S - 1; s += K) {
+                bool d0 = false, d1 = false;
+#pragma unroll
+                for (int j = 0; j < K; ++j) {
+                    rk4_step<F>(x, a, c);
+                    const P2 v = pick2<3>(x, wv);
+                    d0 |= bif_diverged(v.v.x, P);
+                    d1 |= bif_diverged(v.v.y, P);
+                }
+                if (d0) flag[0] = 0;
+                if (d1) flag[1] = 0;
+                if (flag[0] != 1 && flag[1] != 1) break;
+            }
         }
+        if (flag[0] == 1 || flag[1] == 1)
+            for (; s < P.S - 1; ++s) {  // the last step peeled off, as in bif_point
+                rk4_step<F>(x, a, c);
+                const P2 v = pick2<3>(x, wv);
+                if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
+                if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
+                if (flag[0] != 1 && flag[1] != 1) break;
+            }
         if (flag[0] == 1 || flag[1] == 1) {
 #pragma unroll
             for (int j = 0; j < 3; ++j) xp[j] = x[j];
@@ -836,6 +960,17 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
                 if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
         }
     }
+}
+
+template <class F>
+__device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOut& O, long long p0, long long p1,
+                                               long long o0, long long o1, bool two) {
+    P2 x[3], a[3], xp[3];
+    load_pair<F>(P, p0, p1, x, a);
+    const RK4H<P2> c((float)P.h);
+    const int wv = P.wv;
+    int flag[2] = {1, two ? 1 : 0};
+    bif_pair_transient<F>(P, x, a, flag);
     bool rec[2];
     double first[2] = {0.0, 0.0};  // stays 0 for a lane that does not record (as the scalar path)
     PeakStream<float> ps[2];
@@ -853,7 +988,57 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
             if (rec[1]) first[1] = (double)v.v.y;
         }
         P2 v = pick2<3>(x, wv);  // carried from one step to the next
-        for (int i = 0; i < P.B; ++i) {
+        auto on_peak = [&](int l, float val, int t) {
+            if (ps[l].n >= 1) {
+                const int q = ps[l].n - 1;
+                if (q < O.cap) {
+                    if (O.peaks) O.peaks[oo[l] * O.cap + q] = (double)val;
+                    if (O.intervals)
+                        O.intervals[oo[l] * O.cap + q] = __dmul_rn((double)(t - ps[l].tprev), P.hInterval);
+                }
+            }
+            ps[l].tprev = t;
+            ++ps[l].n;
+        };
+        int i = 0;
+        {  // the block form of bif_record, per lane (a lane that stopped skips its detector)
+            constexpr int K = kRecordBlock;
+            for (; i + K < P.B; i += K) {
+                float s[2][K + 1];
+                s[0][0] = v.v.x;
+                s[1][0] = v.v.y;
+                bool dv[2] = {false, false};
+#pragma unroll
+                for (int j = 1; j <= K; ++j) {
+                    rk4_step<F>(x, a, c);
+                    const P2 w = pick2<3>(x, wv);
+                    s[0][j] = w.v.x;
+                    s[1][j] = w.v.y;
+                    dv[0] |= bif_diverged(w.v.x, P);
+                    dv[1] |= bif_diverged(w.v.y, P);
+                }
+#pragma unroll
+                for (int l = 0; l < 2; ++l) {
+                    if (!rec[l]) continue;
+                    if (__builtin_expect(!dv[l], 1)) {
+                        ps[l].template push_block<K>(s[l], [&](float val, int t) { on_peak(l, val, t); });
+                        continue;
+                    }
+#pragma unroll
+                    for (int j = 0; j < K; ++j) {
+                        float val;
+                        int t;
+                        if (ps[l].push(s[l][j], val, t)) on_peak(l, val, t);
+                        if (bif_diverged(s[l][j + 1], P)) break;
+                    }
+                    rec[l] = false;
+                    flag[l] = 0;
+                }
+                v = P2(s[0][K], s[1][K]);
+                if (!rec[0] && !rec[1]) break;
+            }
+        }
+        for (; i < P.B && (rec[0] || rec[1]); ++i) {
 #pragma unroll
             for (int j = 0; j < 3; ++j) xp[j] = x[j];
 #pragma unroll
@@ -861,18 +1046,7 @@ __device__ __forceinline__ void bif_pair_point(const SweepParams& P, const BifOu
                 float val;
                 int t;
                 const bool hit = ps[l].push(lane(v, l), val, t);  // a lane that stopped keeps stepping its detector
-                if (rec[l] && hit) {
-                    if (ps[l].n >= 1) {
-                        const int q = ps[l].n - 1;
-                        if (q < O.cap) {
-                            if (O.peaks) O.peaks[oo[l] * O.cap + q] = (double)val;
-                            if (O.intervals)
-                                O.intervals[oo[l] * O.cap + q] = __dmul_rn((double)(t - ps[l].tprev), P.hInterval);
-                        }
-                    }
-                    ps[l].tprev = t;
-                    ++ps[l].n;
-                }
+                if (rec[l] && hit) on_peak(l, val, t);
             }
             rk4_step<F>(x, a, c);
             v = pick2<3>(x, wv);
@@ -911,7 +1085,54 @@ __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const Ba
     ps[0].init();
     ps[1].init();
     P2 v = pick2<3>(x, wv);  // carried from one step to the next
-    for (int i = 0; i < P.B; ++i) {
+    auto on_peak = [&](int l, float val, int t) {
+        if (ps[l].n >= 1) sums[l].add(val, t - ps[l].tprev, P.hInterval);
+        ps[l].tprev = t;
+        ++ps[l].n;
+    };
+    int i = 0;
+    {  // the block form of basins_record, per lane
+        constexpr int K = kRecordBlock;
+        for (; i + K < P.B; i += K) {
+            float s[2][K + 1];
+            s[0][0] = v.v.x;
+            s[1][0] = v.v.y;
+            bool dv[2] = {false, false};
+#pragma unroll
+            for (int j = 1; j <= K; ++j) {
+                if (PRE1) rk4_step<F>(x, a, c);
+                else
+                    for (int r = 0; r < P.preScaller; ++r) rk4_step<F>(x, a, c);
+                const P2 w = pick2<3>(x, wv);
+                s[0][j] = w.v.x;
+                s[1][j] = w.v.y;
+                dv[0] |= basins_diverged(w.v.x, P);
+                dv[1] |= basins_diverged(w.v.y, P);
+            }
+#pragma unroll
+            for (int l = 0; l < 2; ++l) {
+                if (!rec[l]) continue;
+                if (__builtin_expect(!dv[l], 1)) {
+                    ps[l].template push_block<K>(s[l], [&](float val, int t) { on_peak(l, val, t); });
+                    lastF[l] = s[l][K - 1];
+                    continue;
+                }
+#pragma unroll
+                for (int j = 0; j < K; ++j) {
+                    lastF[l] = s[l][j];
+                    float val;
+                    int t;
+                    if (ps[l].push(s[l][j], val, t)) on_peak(l, val, t);
+                    if (basins_diverged(s[l][j + 1], P)) break;
+                }
+                rec[l] = false;
+                flag[l] = 0;
+            }
+            v = P2(s[0][K], s[1][K]);
+            if (!rec[0] && !rec[1]) break;
+        }
+    }
+    for (; i < P.B && (rec[0] || rec[1]); ++i) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) xp[j] = x[j];
 #pragma unroll
@@ -920,11 +1141,7 @@ __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const Ba
             lastF[l] = lane(v, l);
             float val;
             int t;
-            if (ps[l].push(lane(v, l), val, t)) {
-                if (ps[l].n >= 1) sums[l].add(val, t - ps[l].tprev, P.hInterval);
-                ps[l].tprev = t;
-                ++ps[l].n;
-            }
+            if (ps[l].push(lane(v, l), val, t)) on_peak(l, val, t);
         }
         if (PRE1) rk4_step<F>(x, a, c);
         else
@@ -991,31 +1208,10 @@ __device__ __forceinline__ void basins_hybrid_point(const SweepParams& P, const 
 template <class F>
 __device__ __forceinline__ void bif_hybrid_point(const SweepParams& P, const BifOut& O, long long p0, long long p1,
                                                  long long o0, long long o1, bool two) {
-    P2 x[3], a[3], xp[3];
+    P2 x[3], a[3];
     load_pair<F>(P, p0, p1, x, a);
-    const int wv = P.wv;
     int flag[2] = {1, two ? 1 : 0};
-    if (P.S > 0) {
-        const RK4H<P2> c((float)P.h);
-        for (int s = 0; s < P.S - 1; ++s) {  // the last step peeled off, as in bif_point
-            rk4_step<F>(x, a, c);
-            const P2 v = pick2<3>(x, wv);
-            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
-            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
-            if (flag[0] != 1 && flag[1] != 1) break;
-        }
-        if (flag[0] == 1 || flag[1] == 1) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j) xp[j] = x[j];
-            rk4_step<F>(x, a, c);
-            const P2 v = pick2<3>(x, wv);
-            if (flag[0] == 1 && bif_diverged(v.v.x, P)) flag[0] = 0;
-            if (flag[1] == 1 && bif_diverged(v.v.y, P)) flag[1] = 0;
-#pragma unroll
-            for (int l = 0; l < 2; ++l)
-                if (flag[l] == 1 && bif_fixed_lane<3>(x, xp, l)) flag[l] = -1;
-        }
-    }
+    bif_pair_transient<F>(P, x, a, flag);
     const StepCtx<float> cs((float)P.h);
 #pragma unroll 1
     for (int l = 0; l < (two ? 2 : 1); ++l) {

@@ -150,13 +150,16 @@ bool lle_variant_forced() { return g_lle_variant.load(std::memory_order_relaxed)
 std::atomic<int> g_sweep_pairs{-1};
 
 // Paired (two points per thread) FP32 sweeps for the RK4 systems. Mode 1
-// (default): sweeps of at least 4 x SMs x 1024 points run as hybrid pairs
-// (packed transient, recorded part lane by lane), smaller ones one point per
-// thread (pairs halve the threads of a latency-bound sweep). Measured on
-// GB300: the 2048^2 Lorenz basins map 150.9 ms hybrid, 154.7 ms fully packed,
-// 159.6 ms one point per thread; a 1.6 M-point Lorenz 1-D bifurcation 65.9 /
-// 69.3 / 69.8 ms, Rossler 59.7 / 60.3 / 64.0 ms. 2: always fully packed;
-// 0: never; 3: always hybrid. Set with chaos_set_tuning or CHAOS_SWEEP_PAIRS.
+// (default): sweeps of at least 4 x SMs x 1024 points run as pairs -- 1-D
+// bifurcations as hybrid pairs (packed transient, recorded part lane by lane),
+// basins maps fully packed -- and smaller ones one point per thread (pairs
+// halve the threads of a latency-bound sweep). Measured on GB300 with the
+// recorded loops' block form: a 1.6 M-point Lorenz 1-D bifurcation 53.4 ms
+// hybrid, 57.5 ms fully packed (Rossler 45.5 / 45.3 ms); the 2048^2 Lorenz
+// basins map 145.9 ms fully packed, 147.7 ms hybrid, and at 1024^2 the
+// packed form ahead by 1.3 / 1.7 / 2.0 % on Lorenz / Rossler / Chen.
+// 2: always fully packed; 0: never; 3: always hybrid. Set with
+// chaos_set_tuning or CHAOS_SWEEP_PAIRS.
 int sweep_pairs() {
     const int v = g_sweep_pairs.load(std::memory_order_relaxed);
     if (v >= 0) return v;
@@ -212,7 +215,7 @@ long long one_wave_threads() {
 }
 
 struct Launch {
-    int form;  // 1 one point per thread, 2 packed pairs, 3 hybrid pairs (basins)
+    int form;  // 1 one point per thread, 2 packed pairs, 3 hybrid pairs
     int block;
 };
 
@@ -232,7 +235,7 @@ Launch sweep_launch(const SweepParams& P, bool basins) {
         const int form = shape / 1024;
         return {form >= 2 && !big ? 1 : form, block};
     }
-    return {big ? 3 : 1, kBlock};
+    return {big ? (basins ? 2 : 3) : 1, kBlock};
 }
 
 template <class F> void launch_bif_pairs(const SweepParams& P, const BifOut& O, int block, cudaStream_t st) {

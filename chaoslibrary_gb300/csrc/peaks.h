@@ -58,6 +58,14 @@ CHAOS_HD DiffTest diff_test(float v, float p1) {
 // One subtraction per sample (diff_test): the next sample's rise test
 // "d[k] - d[k-1] > 1e-13" is taken when d[k] arrives and kept as a flag.
 template <class T, bool Sel = false> struct PeakStream {
+    // Gate (float, branching form): the common sample -- no plateau open and
+    // no candidate to judge -- costs one subtraction, one compare against a
+    // threshold and one select. The threshold holds the state the branches
+    // read: -inf (not rising), 0 (rising: a sample with d <= 0 is a candidate)
+    // or +inf (a plateau is open: every sample is judged). "d > thr" fails for
+    // every sample the branches would act on (and for NaN), so those take the
+    // full transitions below with rise and plateau read back from thr.
+    static constexpr bool Gate = !Sel && sizeof(T) == sizeof(float);
     T p1;          // d[k-1]
     bool rise;     // d[k-1] - d[k-2] > 1e-13
     bool plateau;  // a plateau is open: it started at candidate i0 and runs to j = k-1
@@ -66,10 +74,12 @@ template <class T, bool Sel = false> struct PeakStream {
     int i0;        // plateau: index of the candidate that opened it
     int n;         // peaks detected so far (the dropped first one included)
     int tprev;     // time index of the previous detected peak
+    T thr;         // Gate: -inf, 0 or +inf as above
 
     CHAOS_HD void init() {
-        k = 0; nc = 1; plateau = false; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false;
+        k = 0; nc = 1; plateau = false; i0 = 0; n = 0; tprev = 0; p1 = T(0); rise = false; thr = -kInfT();
     }
+    static CHAOS_HD T kInfT() { return T(__builtin_huge_valf()); }
 
     // Pushes d[k] = v; returns true and sets (val, t) when a peak was detected.
     // Outside a plateau, candidate k-1 (d[k-2], d[k-1] and d[k] known) is
@@ -87,6 +97,17 @@ template <class T, bool Sel = false> struct PeakStream {
     // 2.28 ms, equal at 100,000. Sweeps that fill the GPU (the paired kernels)
     // keep the branches, which issue fewer instructions.
     CHAOS_HD bool push(T v, T& val, int& t) {
+        if constexpr (Gate) {
+            const T d = v - p1;
+            if (__builtin_expect(d > thr, 1)) {
+                thr = d > T(1e-13f) ? T(0) : -kInfT();
+                p1 = v;
+                ++k;
+                return false;
+            }
+            rise = thr == T(0);
+            plateau = thr > T(0);
+        }
         const DiffTest c = diff_test(v, p1);
         if constexpr (Sel) {
             const bool open = !plateau && k > nc && rise && c.ge;
@@ -125,7 +146,39 @@ template <class T, bool Sel = false> struct PeakStream {
         rise = c.above;
         p1 = v;
         ++k;
+        if constexpr (Gate) thr = plateau ? kInfT() : (rise ? T(0) : -kInfT());
         return hit;
+    }
+
+    // Pushes the K samples s[0..K-1] (Gate form); on_peak(val, t) for every
+    // peak detected, in order. The gate runs over the whole block first: when
+    // no sample of it would leave the common path (the threshold of each
+    // sample follows from the previous one's difference), the block costs
+    // four operations a sample and one branch; otherwise every sample goes
+    // through push, exactly as one at a time.
+    template <int K, class OnPeak> CHAOS_HD void push_block(const T* s, OnPeak&& on_peak) {
+        static_assert(Gate, "push_block is the float detector's block form");
+        T th = thr, p = p1;
+        bool slow = false;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const T d = s[j] - p;
+            slow |= !(d > th);
+            th = d > T(1e-13f) ? T(0) : -kInfT();
+            p = s[j];
+        }
+        if (__builtin_expect(!slow, 1)) {
+            thr = th;
+            p1 = p;
+            k += K;
+            return;
+        }
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            T val;
+            int t;
+            if (push(s[j], val, t)) on_peak(val, t);
+        }
     }
 };
 

@@ -470,9 +470,10 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
 #define CHAOS_TUNE_LLE_F32_VARIANT 1
 /* CHAOS_TUNE_SWEEP_PAIRS: FP32 bifurcation / basins sweeps of the RK4 systems
    run two points per thread in packed FP32x2 lanes: 1 (default) for sweeps
-   of at least 4 x SMs x 1024 points, as hybrid pairs (packed transient,
-   recorded part lane by lane), 2 always fully packed, 0 never (one point per
-   thread), 3 always hybrid. Results are identical in every mode. */
+   of at least 4 x SMs x 1024 points -- 1-D bifurcations as hybrid pairs
+   (packed transient, recorded part lane by lane), basins maps fully packed --
+   2 always fully packed, 0 never (one point per thread), 3 always hybrid.
+   Results are identical in every mode. */
 #define CHAOS_TUNE_SWEEP_PAIRS 2
 /* CHAOS_TUNE_GRID_FMA: 0 (default) swept values start + n*scale with the
    multiply and the add rounded apart, as the reference's getValueByIdx is

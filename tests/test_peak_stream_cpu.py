@@ -140,3 +140,20 @@ def test_float_forms_match_oracle(checker, oracle):
         assert np.array_equal(counts, oc)
         assert _same(pk, opk, counts)
         assert _same(iv, oiv, counts)
+
+
+def test_float_forms_agree_on_hard_series(checker):
+    """The float detector's two forms -- branches behind the one-compare gate,
+    and selects -- on series built to exercise the gate's slow path: long
+    runs of equal samples, rises and drops just above and below the 1e-13
+    threshold (values near 1e-12, where such steps are representable in
+    float), NaN and infinities."""
+    rng = np.random.default_rng(7)
+    d = _plateau_series(rng, 400, 160, with_specials=True) * 4e-12
+    small = rng.random(d.shape) < 0.3
+    d[small] = rng.choice([0.0, 1e-12, 1.1e-12, 1.2e-12], size=int(small.sum()))
+    gated, sel = checker(d, 0.01, 160)[2:]
+    assert gated[0].sum() > 1000
+    assert np.array_equal(gated[0], sel[0])
+    assert _same(gated[1], sel[1], gated[0])
+    assert _same(gated[2], sel[2], gated[0])
