@@ -27,7 +27,6 @@ SOURCES = [
     ("kern_f32.cu", []),
     ("kern_ff.cu", ["--fmad=false"]),
     ("dbscan.cu", ["--fmad=false", "--extended-lambda"]),
-    ("basins_dbscan.cu", ["--fmad=false"]),
     ("capi.cu", []),
     ("batch.cu", []),
     ("batch_host.cu", []),

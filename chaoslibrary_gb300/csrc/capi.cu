@@ -19,6 +19,7 @@
 #include "../../include/chaos_gb300.h"
 #include "capi_internal.h"
 #include "dbscan.h"
+#include "order_keys.h"
 #include "launch.h"
 #include "systems.h"
 
@@ -900,19 +901,27 @@ int chaos_basins_dbscan(const chaos_exec* ex, int system, double tMax, int nPts,
     O.avgIntervals = (double*)c.alloc(n * sizeof(double));
     O.counts = (int*)c.alloc(n * sizeof(int));
     O.last = (double*)c.alloc(n * sizeof(double));
-    // the clustering reads the features as three columns; the row-major
-    // matrix is written only when the caller asks for it
+    // the integration kernels fold the features' minima and maxima into
+    // these keys; the clustering normalises the features on the fly and
+    // writes the row-major matrix only when the caller asks for it
+    O.mm = (unsigned long long*)c.alloc(6 * kKeyReplicas * sizeof(unsigned long long));
     double* F = features ? (double*)c.output(features, (size_t)n * 3 * sizeof(double)) : nullptr;
-    double* cols[3];
-    for (auto& col : cols) col = (double*)c.alloc(n * sizeof(double));
-    int* mask = (int*)c.alloc(n * sizeof(int));
-    double* minmax = (double*)c.alloc(6 * sizeof(double));
     int* dLabels = (int*)c.output(labels, n * sizeof(int));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = run_basins(c.ex.precision, P, O, c.stream);
-    if (e == cudaSuccess) e = launch_basin_feature_matrix(O, n, minmax, F, cols, mask, c.stream);
-    if (e != cudaSuccess) return c.finish(cuda_error(e, "basins feature kernels"));
-    rc = dbscan_device_soa(c, cols, n, 3, eps, minPts, mask, dLabels);
+    cudaError_t e = cudaMemsetAsync(O.mm, 0xff, 3 * kKeyReplicas * sizeof(unsigned long long), c.stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(O.mm + 3 * kKeyReplicas, 0, 3 * kKeyReplicas * sizeof(unsigned long long), c.stream);
+    if (e == cudaSuccess) e = run_basins(c.ex.precision, P, O, c.stream);
+    unsigned long long hm[6 * kKeyReplicas], keys[6];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hm, O.mm, sizeof hm, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "basins kernels"));
+    for (int k = 0; k < 6; ++k) {
+        keys[k] = hm[k * kKeyReplicas];
+        for (int r = 1; r < kKeyReplicas; ++r)
+            keys[k] = k < 3 ? std::min(keys[k], hm[k * kKeyReplicas + r]) : std::max(keys[k], hm[k * kKeyReplicas + r]);
+    }
+    rc = dbscan_basins_device(c, O, n, keys, eps, minPts, F, dLabels);
     if (!rc) rc = c.to_host(labels, dLabels, n * sizeof(int));
     if (!rc && features) rc = c.to_host(features, F, (size_t)n * 3 * sizeof(double));
     if (!rc && flags) rc = c.to_host(flags, O.flags, n * sizeof(int));

@@ -14,6 +14,14 @@ int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgInter
 int dbscan_device_soa(Call& c, const double* const* columns, long long n, int dims, double eps, int minPts,
                       const int* mask, int* labels);
 
+// DBSCAN with scikit-learn semantics on the normalised features of a basin
+// map, read from its per-point outputs: (amplitude, kept peak count, mean
+// interval) min-max scaled over the points with flag != 0, the bounds taken
+// from minmaxKeys (order keys: the three minima, then the three maxima).
+// features (may be null) receives the n x 3 normalised matrix.
+int dbscan_basins_device(Call& c, const BasinsOut& O, long long n, const unsigned long long* minmaxKeys, double eps,
+                         int minPts, double* features, int* labels);
+
 // DBSCAN with scikit-learn semantics on a row-major n x dims device matrix.
 int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,
                   int* labels);

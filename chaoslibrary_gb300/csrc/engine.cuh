@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "launch.h"
+#include "order_keys.h"
 #include "peaks.h"
 #include "systems.h"
 #include "ff.h"
@@ -416,6 +417,11 @@ __device__ __forceinline__ void basins_record(const SweepParams& P, const Basins
     O.avgIntervals[o] = ai;
     if (O.counts) O.counts[o] = flag == 1 ? kept : 0;
     if (O.last) O.last[o] = last;
+    if (O.mm) {  // the clustering's normalisation bounds
+        FeatureKeys fk;
+        fk.add(flag, flag == 1 ? kept : 0, ap, ai, last);
+        fk.flush(O.mm);
+    }
 }
 
 template <int S, class T, bool PRE1 = false, bool Sel = false>
@@ -1152,6 +1158,7 @@ __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const Ba
         if (!rec[0] && !rec[1]) break;
     }
     const long long oo[2] = {o0, o1};
+    FeatureKeys fk;
 #pragma unroll
     for (int l = 0; l < (two ? 2 : 1); ++l) {
         if (rec[l] && P.B > 0 && basins_fixed_lane<3>(x, xp, l)) flag[l] = -1;
@@ -1167,7 +1174,9 @@ __device__ __forceinline__ void basins_pair_point(const SweepParams& P, const Ba
         O.avgIntervals[oo[l]] = ai;
         if (O.counts) O.counts[oo[l]] = flag[l] == 1 ? kept : 0;
         if (O.last) O.last[oo[l]] = last;
+        fk.add(flag[l], flag[l] == 1 ? kept : 0, ap, ai, last);
     }
+    if (O.mm) fk.flush(O.mm);
 }
 
 // Two basins points per thread, hybrid: the transient (no tests, 80 % of the

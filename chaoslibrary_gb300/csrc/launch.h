@@ -73,6 +73,9 @@ struct BasinsOut {
     double* avgIntervals;
     int* counts;   // kept peaks (may be null)
     double* last;  // x[writableVar] at the last recorded sample (may be null)
+    // order-key minima / maxima of the clustering features of the points with
+    // flag != 0, kKeyReplicas replicas per key (order_keys.h); null: not kept
+    unsigned long long* mm = nullptr;
 };
 
 struct LleParams {
@@ -135,11 +138,6 @@ cudaError_t launch_trajectory_f32(int system, const double* x0, const double* a0
                                   double* out, long long n, cudaStream_t st);
 cudaError_t launch_trajectory_ff(int system, const double* x0, const double* a0, double h, int nSteps,
                                  double* out, long long n, cudaStream_t st);
-
-// Basin features in normalised form (basins_dbscan.cu): per point (amplitude,
-// peak count, mean interval), min-max scaled over the points with flag != 0.
-cudaError_t launch_basin_feature_matrix(const BasinsOut& O, long long n, double* minmax, double* features,
-                                        double* const* columns, int* mask, cudaStream_t st);
 
 // FP32 LLE kernel variant (kern_f32.cu): 0 = default, 2 = two points per
 // thread (packed FP32x2), 12 / 16 = one point per thread at that occupancy.
