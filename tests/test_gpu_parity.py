@@ -183,6 +183,49 @@ def test_dbscan_concentrated_vs_oracle(engine, oracle, d, min_pts, seed):
     assert np.array_equal(lab, ref)
 
 
+def test_dbscan_unsafe_cells_vs_oracle(engine, oracle):
+    """Groups of points far out (features ~1e5 against eps 0.05: their cell
+    coordinates clamp at 2^19), NaN features and a mask: the clamped and NaN
+    cells lose the one-cell shortcuts and are resolved by exact pair tests
+    (a node per core point in the union-find); labels identical to the
+    oracle's, which keeps 64-bit cell coordinates and no clamp."""
+    rng = np.random.default_rng(21)
+    d, eps = 3, 0.05
+    parts = [rng.normal(scale=0.03, size=(3000, d)) + 0.5,
+             np.full((1, d), 1e5) + rng.normal(scale=0.02, size=(400, d)),
+             np.full((1, d), -2e5) + rng.normal(scale=0.02, size=(300, d)),
+             np.array([[1e5, -1e5, 3e5]]) + rng.normal(scale=0.2, size=(200, d)),
+             rng.uniform(0, 1, size=(500, d))]
+    X = np.concatenate(parts)
+    X[rng.choice(len(X), 40, replace=False), rng.integers(0, d, 40)] = np.nan
+    X = X[rng.permutation(len(X))]
+    mask = (rng.random(len(X)) > 0.03).astype(np.int32)
+    for min_pts in (1, 5):
+        lab = engine.dbscan(X, eps, min_pts, mask=mask)
+        ref = oracle.dbscan(X, eps, min_pts, mask=mask)
+        assert np.array_equal(lab, ref), min_pts
+        assert (lab[np.isnan(X).any(axis=1) & (mask != 0)] == -1).all()
+
+
+def test_dbscan_compat_eps0_and_far_vs_oracle(engine, oracle):
+    """The reference clustering at eps = 0 (every cell unsafe: only equal
+    features connect) on data full of exact duplicates, and at eps = 0.05
+    with points far out (clamped cell coordinates), against the oracle's
+    brute-force breadth-first search."""
+    rng = np.random.default_rng(22)
+    n = 3000
+    ap = rng.integers(0, 40, n) * 0.1
+    ai = rng.integers(0, 40, n) * 0.1
+    flags = rng.choice([-1, 0, 1], size=n, p=[0.1, 0.1, 0.8]).astype(np.int32)
+    lab = engine.dbscan_compat(ap, ai, flags, 0.0)
+    assert np.array_equal(lab, oracle.dbscan_compat(ap, ai, flags, 0.0, method="bfs"))
+    ap2 = ap + rng.normal(scale=0.01, size=n)
+    ap2[:300] += 1e6
+    ai2 = ai + rng.normal(scale=0.01, size=n)
+    lab = engine.dbscan_compat(ap2, ai2, flags, 0.05)
+    assert np.array_equal(lab, oracle.dbscan_compat(ap2, ai2, flags, 0.05, method="bfs"))
+
+
 @pytest.mark.parametrize("n, spread, eps, seed", [(100000, 1.0, 0.005, 5), (400000, 3.0, 0.01, 6)])
 def test_dbscan_compat_random_vs_oracle(engine, oracle, n, spread, eps, seed):
     rng = np.random.default_rng(seed)
