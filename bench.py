@@ -534,6 +534,10 @@ def batch_arm(args, ws, rank, local):
                             "unit": "TFLOP/s", "frac": flops / mean_s / 1e12 / peak, "traffic": None,
                             "algorithmic": "71/63/79 flops per Lorenz/Rossler/Chen RK4 step",
                             "peak_source": "measured in this run: chaos_fma_probe"}
+        if lle_prec == C.FF32:
+            line["roofline"]["note"] = (
+                "the LLE half runs float-float (~7 FP32 operations per algorithmic flop), so the algorithmic "
+                "fraction is low by construction; other_lle_precision.roofline is the same batch with FP32 LLE jobs")
     # e2e: one-shot host-memory submission (descriptor upload, launch, results copied back)
     bh, _ = make(lle_prec, device=False)
     bh.run()
@@ -553,8 +557,12 @@ def batch_arm(args, ws, rank, local):
         torch.cuda.synchronize()
         ms2 = timed(b2, max(2, min(args.steps, 5)), flush, stream)
         b2.close()
+        s2 = statistics.mean(ms2) / 1e3
         line["other_lle_precision"] = {"lle_precision": "fp32" if other == C.FP32 else "ff32",
-                                       "value": total_steps / (statistics.mean(ms2) / 1e3), "unit": UNIT}
+                                       "value": total_steps / s2, "unit": UNIT, "ms_per_step": s2 * 1e3,
+                                       "roofline": {"bound": "fp32_fma", "achieved": flops / s2 / 1e12,
+                                                    "peak": peak, "unit": "TFLOP/s",
+                                                    "frac": flops / s2 / 1e12 / peak}}
         # the same jobs one at a time through the single-sweep entry points (device outputs)
         single = []
         for kind, system, kw in jobs:
