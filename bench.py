@@ -1243,7 +1243,10 @@ def main():
     ap.add_argument("--tmax", type=float, default=None, help="tMax override (profiling runs only)")
     args = ap.parse_args()
     if args.precision == "auto":  # the LLE arithmetic that matches FP64 to the FP64 map's own spread
-        args.precision = "ff32" if args.workload in ("lle", "batch") and args.impl == "engine" else "fp32"
+        if args.impl == "reference":
+            args.precision = "fp64"  # the reference's own code computes in FP64
+        else:
+            args.precision = "ff32" if args.workload in ("lle", "batch") else "fp32"
     for w in (LLE, BIF1D, BIF2D, BASINS, SPECTRUM):
         if args.npts:
             w["nPts"] = args.npts
