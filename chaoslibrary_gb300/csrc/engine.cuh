@@ -265,7 +265,7 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
             // blocks of kTransientBlock steps, one divergence branch a block:
             // a point's flags do not depend on the step at which it diverged
             // (the steps after it on an unbounded state report nothing). The
-            // select form (one-wave sweeps, one latency-bound orbit a warp)
+            // select form (small sweeps, one latency-bound orbit a warp)
             // keeps the one-step loop and its registers.
             constexpr int K = kTransientBlock;
             for (; s + K <= nS - 1; s += K) {

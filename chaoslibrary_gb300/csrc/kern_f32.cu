@@ -14,8 +14,8 @@ namespace {
 constexpr int kBlock = 128;     // default block
 constexpr int kMaxBlock = 256;  // largest block a tuned launch may use
 
-// Sel: the peak detector as selects (sweeps within one wave of resident
-// threads, where each warp waits on its own trajectory) or with branches.
+// Sel: the peak detector as selects (sweeps of at most 8 warps per SM, where
+// each warp waits on its own trajectory) or in the block form.
 template <int S, bool Sel>
 __global__ void __launch_bounds__(kMaxBlock) bif_kernel_f32(SweepParams P, BifOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -201,15 +201,18 @@ long long pair_threshold() {
     return threshold;
 }
 
-// Threads of one wave at 1024 resident threads per SM: below it a
-// one-point-per-thread sweep is latency-bound (every warp waits on its own
-// dependent chain).
-long long one_wave_threads() {
+// Sweeps of at most 8 warps per SM (SMs x 256 points) run the peak detector
+// as selects: there every warp waits on its own dependent chain, and the
+// selects overlap the detector with the next step; larger sweeps run the
+// block form. Measured on GB300 (1-D Lorenz, 20,000 steps): 1,000 points
+// 1.84 ms selects / 2.02 ms blocks, 5,000 1.94 / 2.00, 20,000 2.26 / 2.43,
+// 50,000 2.87 / 2.80; the reference's 300^2 Chameleon sweep 50.6 / 46.5 ms.
+long long select_form_threads() {
     static long long threads = [] {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        return (long long)std::max(sms, 1) * 1024;
+        return (long long)std::max(sms, 1) * 256;
     }();
     return threads;
 }
@@ -277,7 +280,7 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
         else launch_bif_hybrid<Chen>(P, O, l.block, st);
         return cudaGetLastError();
     }
-    const bool sel = P.nPoints <= one_wave_threads();
+    const bool sel = P.nPoints <= select_form_threads();
 #define CALL(S)                                                                           \
     (sel ? bif_kernel_f32<S, true><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O) \
          : bif_kernel_f32<S, false><<<grid_of(P.nPoints, l.block), l.block, 0, st>>>(P, O), \
@@ -311,7 +314,7 @@ cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStre
         return cudaGetLastError();
     }
     const unsigned g = grid_of(P.nPoints, l.block);
-    const bool sel = P.nPoints <= one_wave_threads();  // the detector as selects, as in the 1-D sweeps
+    const bool sel = P.nPoints <= select_form_threads();  // the detector as selects, as in the 1-D sweeps
 #define CALL(S)                                                                               \
     (P.preScaller == 1 ? (sel ? basins_kernel_f32<S, true, true><<<g, l.block, 0, st>>>(P, O)    \
                               : basins_kernel_f32<S, true, false><<<g, l.block, 0, st>>>(P, O))  \

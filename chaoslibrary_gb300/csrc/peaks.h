@@ -94,8 +94,9 @@ template <class T, bool Sel = false> struct PeakStream {
     // each run one latency-bound trajectory (small sweeps) then overlaps the
     // detector with the next step's arithmetic instead of waiting on its
     // branches: 1000 Lorenz points 2.50 -> 1.87 ms, 20,000 points 2.87 ->
-    // 2.28 ms, equal at 100,000. Sweeps that fill the GPU (the paired kernels)
-    // keep the branches, which issue fewer instructions.
+    // 2.28 ms against the branching form. Larger sweeps run the branching
+    // form behind its gate in blocks of samples (push_block), which issues
+    // fewer instructions.
     CHAOS_HD bool push(T v, T& val, int& t) {
         if constexpr (Gate) {
             const T d = v - p1;
