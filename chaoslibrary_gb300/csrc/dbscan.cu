@@ -1739,17 +1739,6 @@ int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgInter
     return cell_cluster(c, S, n, eps, 1, true, 0.0, nullptr, labels);
 }
 
-int dbscan_device_soa(Call& c, const double* const* columns, long long n, int dims, double eps, int minPts,
-                      const int* mask, int* labels) {
-    ColSrc S;
-    for (int d = 0; d < 3; ++d) S.f[d] = columns[d < dims ? d : dims - 1];
-    S.mask = mask;
-    S.flags = nullptr;
-    S.D = dims;
-    S.compat = false;
-    return cell_cluster(c, S, n, eps, minPts, false, 0.0, nullptr, labels);
-}
-
 int dbscan_device(Call& c, const double* features, long long n, int dims, double eps, int minPts, const int* mask,
                   int* labels) {
     RowSrc S;

@@ -10,10 +10,6 @@ namespace chaos {
 int dbscan_compat_device(Call& c, const double* avgPeaks, const double* avgIntervals, const int* flags, long long n,
                          double eps, int* labels);
 
-// The same on dims device columns of n values (one array per feature).
-int dbscan_device_soa(Call& c, const double* const* columns, long long n, int dims, double eps, int minPts,
-                      const int* mask, int* labels);
-
 // DBSCAN with scikit-learn semantics on the normalised features of a basin
 // map, read from its per-point outputs: (amplitude, kept peak count, mean
 // interval) min-max scaled over the points with flag != 0, the bounds taken
