@@ -245,7 +245,7 @@ def trajectory(system, x0, a, h, n_steps, precision=FP64):
 
 
 # grid modes (CHAOS_GRID_*) and the step-size axis marker (CHAOS_MUT_STEP)
-GRID_STATE, GRID_LOG0, GRID_LOG1, GRID_LOG_F32 = 1, 2, 4, 8
+GRID_STATE, GRID_LOG0, GRID_LOG1, GRID_LOG_F32, GRID_LEGACY_LOOP = 1, 2, 4, 8, 16
 MUT_STEP = -1
 
 TUNE_LLE_F32_VARIANT = 1
@@ -515,7 +515,8 @@ def bifurcation_sweep(system, dim, gridMode, tMax, nPts, h, initialConditions, r
                       precision=FP64, out=None, stream=None):
     """Bifurcation over parameters or initial conditions (GRID_STATE), linear
     or log-scale axes, or the step size (indicesOfMutVars[0] = MUT_STEP, dim 1)
-    (chaos_bifurcation_sweep). dim 1: counts, flags, first, peaks, intervals;
+    (chaos_bifurcation_sweep); GRID_LEGACY_LOOP runs the legacy library's
+    per-point loop in FP64. dim 1: counts, flags, first, peaks, intervals;
     dim 2: labels, counts."""
     A = _Args()
     ic = np.asarray(initialConditions, np.float64)

@@ -224,12 +224,15 @@ static int check_ff32_lle(const chaos_exec* ex, int system, const LleParams& L) 
 }
 
 // precision / plug-in dispatch of the sweep kernels
+// The legacy per-point loop runs in FP64, the legacy library's arithmetic.
 static cudaError_t run_bif(int prec, const SweepParams& P, const BifOut& O, cudaStream_t st) {
+    if (P.legacyLoop) prec = CHAOS_FP64;
     if (P.system == SYS_USER) return prec == CHAOS_FP32 ? cudaErrorNotSupported : launch_bif_user(P, O, st);
     return prec == CHAOS_FP32 ? launch_bif_f32(P, O, st) : launch_bif_f64(P, O, st);
 }
 static cudaError_t run_bif_list(int prec, const SweepParams& P, const BifOut& O, const int* list, int count,
                                 cudaStream_t st) {
+    if (P.legacyLoop) prec = CHAOS_FP64;
     return prec == CHAOS_FP32 ? launch_bif_list_f32(P, O, list, count, st) : launch_bif_list_f64(P, O, list, count, st);
 }
 static cudaError_t run_basins(int prec, const SweepParams& P, const BasinsOut& O, cudaStream_t st) {
@@ -258,7 +261,7 @@ void log_axis_values(double r0, double r1, int nPts, bool f32, std::vector<doubl
 
 // Checks a grid mode against the ranges: log-scale axes need positive ends and nPts >= 2.
 static int check_grid_mode(int gridMode, int dim, int nPts, const double* ranges) {
-    if (gridMode & ~(CHAOS_GRID_STATE | CHAOS_GRID_LOG0 | CHAOS_GRID_LOG1 | CHAOS_GRID_LOG_F32))
+    if (gridMode & ~(CHAOS_GRID_STATE | CHAOS_GRID_LOG0 | CHAOS_GRID_LOG1 | CHAOS_GRID_LOG_F32 | CHAOS_GRID_LEGACY_LOOP))
         return set_error(CHAOS_E_ARGS, "unknown grid mode bits 0x%x", gridMode);
     if ((gridMode & CHAOS_GRID_LOG1) && dim < 2) return set_error(CHAOS_E_ARGS, "CHAOS_GRID_LOG1 needs dim 2");
     for (int d = 0; d < dim; ++d) {
@@ -364,6 +367,10 @@ int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, doubl
     P.bPre = preScaller;
     P.tMax = tMax;
     P.transientTime = transientTime;
+    if (gridMode & CHAOS_GRID_LEGACY_LOOP) {
+        if (basins) return set_error(CHAOS_E_ARGS, "CHAOS_GRID_LEGACY_LOOP belongs to the bifurcation sweep");
+        P.legacyLoop = stepAxis ? 2 : 1;
+    }
     return CHAOS_OK;
 }
 
@@ -372,6 +379,8 @@ int fill_lle(LleParams& L, int system, double tMax, double NT, int nPts, double 
              const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues, int dim,
              int gridMode) {
     const int mutateState = gridMode & CHAOS_GRID_STATE;
+    if (gridMode & CHAOS_GRID_LEGACY_LOOP)
+        return set_error(CHAOS_E_ARGS, "CHAOS_GRID_LEGACY_LOOP belongs to the bifurcation sweep");
     int rc = check_system(system, amountOfInitialConditions, amountOfValues);
     if (rc) return rc;
     if (!initialConditions || !ranges || !indicesOfMutVars || !values) return set_error(CHAOS_E_ARGS, "null argument");
@@ -467,7 +476,7 @@ static int bif1d_run(const chaos_exec* ex, SweepParams P, int gridMode, const do
     if (!counts || !flags) return set_error(CHAOS_E_ARGS, "counts and flags are required");
     if (peakCapacity < 0 || ((peaks || intervals) && peakCapacity == 0))
         return set_error(CHAOS_E_ARGS, "peakCapacity must be > 0 when peaks or intervals are requested");
-    if ((rc = no_ff32(ex, "the bifurcation sweep"))) return rc;
+    if (!P.legacyLoop && (rc = no_ff32(ex, "the bifurcation sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     if ((rc = upload_log_axes(c, gridMode, P.dim, (int)P.grid.nPts, ranges, P.grid.table))) return c.finish(rc);
@@ -496,7 +505,7 @@ static int bif2d_run(const chaos_exec* ex, SweepParams P, int gridMode, const do
                      int* labels, int* counts) {
     int rc = CHAOS_OK;
     if (!labels) return set_error(CHAOS_E_ARGS, "labels is required");
-    if ((rc = no_ff32(ex, "the bifurcation sweep"))) return rc;
+    if (!P.legacyLoop && (rc = no_ff32(ex, "the bifurcation sweep"))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
     if ((rc = upload_log_axes(c, gridMode, P.dim, (int)P.grid.nPts, ranges, P.grid.table))) return c.finish(rc);

@@ -274,7 +274,8 @@ int chaos_compat_basinsOfAttraction_2(double tMax, int nPts, double h, int amoun
 
 // ---- the legacy library's analyses (namespace old_library, debri/hostLibrary.cuh) ----
 // Each runs the engine's sweep with the matching grid mode and writes the
-// legacy function's file format.
+// legacy function's file format. The bifurcation analyses run the legacy
+// per-point loop (CHAOS_GRID_LEGACY_LOOP, FP64).
 
 // Rows "value, peak" per kept peak, precision 12, no header: bifurcation1DIC
 // and bifurcation1DForH (debri/hostLibrary.cu:1447-1460, 1197-1210). The
@@ -378,9 +379,9 @@ int chaos_compat_bifurcation1DIC(double tMax, int nPts, double h, int amountOfIn
                                  int writableVar, double maxValue, double transientTime, const double* values,
                                  int amountOfValues, int preScaller, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
-        return legacy_bif1d(CHAOS_GRID_STATE, tMax, nPts, h, amountOfInitialConditions, initialConditions, ranges,
-                            indicesOfMutVars, writableVar, maxValue, transientTime, values, amountOfValues, preScaller,
-                            OUT_FILE_PATH);
+        return legacy_bif1d(CHAOS_GRID_STATE | CHAOS_GRID_LEGACY_LOOP, tMax, nPts, h, amountOfInitialConditions,
+                            initialConditions, ranges, indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                            amountOfValues, preScaller, OUT_FILE_PATH);
     });
 }
 
@@ -390,9 +391,9 @@ int chaos_compat_bifurcation1DForH(double tMax, int nPts, int amountOfInitialCon
                                    int preScaller, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
         const int mut[1] = {CHAOS_MUT_STEP};
-        return legacy_bif1d(CHAOS_GRID_LOG0 | CHAOS_GRID_LOG_F32, tMax, nPts, 0.0, amountOfInitialConditions,
-                            initialConditions, ranges, mut, writableVar, maxValue, transientTime, values, amountOfValues,
-                            preScaller, OUT_FILE_PATH);
+        return legacy_bif1d(CHAOS_GRID_LOG0 | CHAOS_GRID_LOG_F32 | CHAOS_GRID_LEGACY_LOOP, tMax, nPts, 0.0,
+                            amountOfInitialConditions, initialConditions, ranges, mut, writableVar, maxValue,
+                            transientTime, values, amountOfValues, preScaller, OUT_FILE_PATH);
     });
 }
 
@@ -406,10 +407,11 @@ int chaos_compat_bifurcation2DIC(double tMax, int nPts, double h, int amountOfIn
         const long long n = (long long)nPts * nPts;
         std::vector<int> labels(n);
         chaos_exec ex = active_exec();
-        int rc = chaos_bifurcation_sweep(&ex, active_system(), 2, CHAOS_GRID_STATE, tMax, nPts, h,
-                                         amountOfInitialConditions, initialConditions, ranges, indicesOfMutVars,
-                                         writableVar, maxValue, transientTime, values, amountOfValues, preScaller, eps, 0,
-                                         nullptr, nullptr, nullptr, nullptr, nullptr, labels.data());
+        int rc = chaos_bifurcation_sweep(&ex, active_system(), 2, CHAOS_GRID_STATE | CHAOS_GRID_LEGACY_LOOP, tMax,
+                                         nPts, h, amountOfInitialConditions, initialConditions, ranges,
+                                         indicesOfMutVars, writableVar, maxValue, transientTime, values,
+                                         amountOfValues, preScaller, eps, 0, nullptr, nullptr, nullptr, nullptr,
+                                         nullptr, labels.data());
         if (rc) return rc;
         std::ofstream o(OUT_FILE_PATH);
         if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);

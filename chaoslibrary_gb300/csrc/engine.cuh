@@ -300,6 +300,98 @@ __device__ __forceinline__ void bif_point(const SweepParams& P, const BifOut& O,
     }
 }
 
+// Bifurcation point of the legacy library's analyses (P.legacyLoop, FP64),
+// with the legacy per-point loop in place of the current library's.
+// P.legacyLoop 1, the grids over initial conditions or parameters
+// (calculateDiscreteModelICCUDA, debri/cudaLibrary.cu:1022-1116, over
+// loopCalculateDiscreteModel_int, :604-680, then peakFinderCUDA, :1345-1367):
+//  - the transient (one step a sample, no bound) ends the point with flag 0
+//    when state component 0 becomes NaN or infinite;
+//  - its fixed-point verdict does not stop the recorded part.
+// P.legacyLoop 2, the step-size sweep (calculateDiscreteModelCUDA_H,
+// :955-1000, over loopCalculateDiscreteModel, :472-527, then
+// peakFinderCUDA_H, :1396-1412):
+//  - the transient stops early at a NaN or infinite component 0, and its
+//    verdict is ignored.
+// Both recorded parts take sample x[wv] and then preScaller steps, and test
+// the sample for NaN, infinity and |(float)x[wv]| > maxValue (flag 0). The
+// change of state over the last sample, s = sum of squared differences,
+// marks a fixed point (flag -1, count -1):
+//  - loop 1: when sqrt(|s|) < 1e-9;
+//  - loop 2: when s == 0 or sqrt(s) < 1e-12 (the legacy keeps no peaks).
+// Peaks and intervals (units h * preScaller) are written as in bif_record.
+template <int S>
+__device__ __forceinline__ void bif_point_legacy(const SweepParams& P, const BifOut& O, long long p, long long o) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    double x[NX], a[NA], xp[NX];
+    load_point<S, double>(P, p, x, a);
+    double hp = P.h, hI = P.hInterval;
+    int nS = P.S, nB = P.B;
+    if (P.sweepStep) {
+        hp = grid_value(P.grid, p, 0);
+        nS = (int)__ddiv_rn(P.transientTime, hp);
+        nB = (int)__ddiv_rn(__ddiv_rn(P.tMax, hp), (double)P.bPre);
+        hI = __dmul_rn(hp, (double)P.bPre);
+    }
+    const StepCtx<double> c(hp);
+    const int wv = P.wv, pre = P.bPre;
+    auto nan_or_inf = [](double v) {
+        return ((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) > 0x7fefffffffffffffull;
+    };
+    int flag = 1;
+    for (int s = 0; s < nS; ++s) {
+        step<S>(x, a, c);
+        if (nan_or_inf(x[0])) {
+            if (P.legacyLoop == 1) flag = 0;
+            break;
+        }
+    }
+    PeakStream<double> ps;
+    ps.init();
+    double* pk = O.peaks ? O.peaks + o * (long long)O.cap : nullptr;
+    double* iv = O.intervals ? O.intervals + o * (long long)O.cap : nullptr;
+    auto on_peak = [&](double val, int t) {
+        if (ps.n >= 1) {
+            const int q = ps.n - 1;
+            if (q < O.cap) {
+                if (pk) pk[q] = val;
+                if (iv) iv[q] = __dmul_rn((double)(t - ps.tprev), hI);
+            }
+        }
+        ps.tprev = t;
+        ++ps.n;
+    };
+    double first = 0.0;
+    if (flag == 1) {
+        double v = pick<NX>(x, wv);
+        first = v;
+        for (int i = 0; i < nB; ++i) {
+#pragma unroll
+            for (int j = 0; j < NX; ++j) xp[j] = x[j];
+            double val;
+            int t;
+            if (ps.push(v, val, t)) on_peak(val, t);
+            for (int r = 0; r < pre; ++r) step<S>(x, a, c);
+            v = pick<NX>(x, wv);
+            if (basins_diverged(v, P)) { flag = 0; break; }
+        }
+        if (flag == 1 && nB > 0) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < NX; ++j) {
+                const double d = __dsub_rn(x[j], xp[j]);
+                s = __dadd_rn(s, __dmul_rn(d, d));
+            }
+            const bool fixed = P.legacyLoop == 1 ? __dsqrt_rn(fabs(s)) < 1e-9 : (s == 0.0 || __dsqrt_rn(s) < 1e-12);
+            if (fixed) flag = -1;
+        }
+    }
+    const int kept = ps.n > 1 ? ps.n - 1 : 0;
+    O.flags[o] = flag;
+    O.counts[o] = flag == 1 ? kept : (flag == -1 ? -1 : 0);
+    if (O.first) O.first[o] = flag == -1 ? first : 0.0;
+}
+
 // Sums over the kept peaks of a basins point: peak values and intervals.
 // FP64 path: the reference's per-peak FP64 sums (avgPeakFinderCUDA,
 // basinsCUDA.cu:818-864). FP32 path: no FP64 instruction per peak (the FP64

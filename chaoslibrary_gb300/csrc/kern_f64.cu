@@ -13,19 +13,22 @@ namespace chaos {
 namespace {
 constexpr int kBlock = 128;
 
-template <int S>
+// Legacy: the legacy library's per-point loop (P.legacyLoop != 0).
+template <int S, bool Legacy>
 __global__ void __launch_bounds__(kBlock) bif_kernel(SweepParams P, BifOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
-    bif_point<S, double>(P, O, P.pBegin + o, o);
+    if constexpr (Legacy) bif_point_legacy<S>(P, O, P.pBegin + o, o);
+    else bif_point<S, double>(P, O, P.pBegin + o, o);
 }
 
 // Bifurcation points list[0, count), result row k for list[k].
-template <int S>
+template <int S, bool Legacy>
 __global__ void __launch_bounds__(kBlock) bif_list_kernel(SweepParams P, BifOut O, const int* list, int count) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
-    bif_point<S, double>(P, O, list[k], k);
+    if constexpr (Legacy) bif_point_legacy<S>(P, O, list[k], k);
+    else bif_point<S, double>(P, O, list[k], k);
 }
 
 template <int S>
@@ -246,7 +249,12 @@ int launch_block_size() { return kBlock; }
 
 cudaError_t launch_bif_f64(const SweepParams& P, const BifOut& O, cudaStream_t st) {
     if (P.nPoints <= 0) return cudaSuccess;
-#define CALL(S) (bif_kernel<S><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O), note_launch())
+#define CALL(S)                                                             \
+    {                                                                       \
+        if (P.legacyLoop) bif_kernel<S, true><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O); \
+        else bif_kernel<S, false><<<grid_for(P.nPoints), kBlock, 0, st>>>(P, O); \
+        note_launch();                                                      \
+    }
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();
@@ -286,7 +294,12 @@ cudaError_t launch_spectrum_f64(const LleParams& L, double* out, cudaStream_t st
 
 cudaError_t launch_bif_list_f64(const SweepParams& P, const BifOut& O, const int* list, int count, cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
-#define CALL(S) (bif_list_kernel<S><<<grid_for(count), kBlock, 0, st>>>(P, O, list, count), note_launch())
+#define CALL(S)                                                                       \
+    {                                                                                 \
+        if (P.legacyLoop) bif_list_kernel<S, true><<<grid_for(count), kBlock, 0, st>>>(P, O, list, count); \
+        else bif_list_kernel<S, false><<<grid_for(count), kBlock, 0, st>>>(P, O, list, count); \
+        note_launch();                                                                \
+    }
     CHAOS_SYSTEM_SWITCH(P.system, CALL)
 #undef CALL
     return cudaGetLastError();

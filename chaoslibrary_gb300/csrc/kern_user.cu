@@ -23,7 +23,8 @@ inline unsigned grid_for(long long n) { return (unsigned)((n + kBlock - 1) / kBl
 __global__ void __launch_bounds__(kBlock) bif_kernel_user(SweepParams P, BifOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= P.nPoints) return;
-    bif_point<SYS_USER, double>(P, O, P.pBegin + o, o);
+    if (P.legacyLoop) bif_point_legacy<SYS_USER>(P, O, P.pBegin + o, o);
+    else bif_point<SYS_USER, double>(P, O, P.pBegin + o, o);
 }
 __global__ void __launch_bounds__(kBlock) basins_kernel_user(SweepParams P, BasinsOut O) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;

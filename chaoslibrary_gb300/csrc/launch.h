@@ -55,6 +55,9 @@ struct SweepParams {
     int sweepStep;
     int bPre;  // the caller's preScaller
     double tMax, transientTime;
+    // The legacy library's per-point loop (FP64 kernels only): 0 off, 1 the
+    // initial-condition / parameter grids, 2 the step-size sweep.
+    int legacyLoop;
 };
 
 // Per-point results of a bifurcation sweep (point-major rows of `cap`).

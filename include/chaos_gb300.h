@@ -72,6 +72,9 @@ extern "C" {
 #define CHAOS_GRID_LOG1 4  /* dimension 1 on a log scale (ranges[2..3]) */
 #define CHAOS_GRID_LOG_F32 8 /* log-scale values rounded as the legacy step-size sweep does,
                                 (double)powf(10, (float)x) (debri/cudaLibrary.cu:1001); else pow in FP64 */
+#define CHAOS_GRID_LEGACY_LOOP 16 /* chaos_bifurcation_sweep only: the legacy library's per-point loop
+                                     instead of the current library's, in FP64 whatever the precision (see
+                                     chaos_bifurcation_sweep) */
 /* indicesOfMutVars[0] == CHAOS_MUT_STEP: dimension 0 sweeps the integration step h itself
    (chaos_bifurcation_sweep, dim 1; the legacy bifurcation1DForH, debri/hostLibrary.cu:1005-1240). */
 #define CHAOS_MUT_STEP (-1)
@@ -135,14 +138,31 @@ int chaos_bifurcation2d(const chaos_exec* ex, int system, double tMax, int nPts,
  * Bifurcation sweep over a 1-D or 2-D grid with a grid mode (CHAOS_GRID_*):
  * parameters or initial conditions, linear or log-scale axes, or the step
  * size. The legacy library's bifurcation1DIC / bifurcation2DIC
- * (debri/hostLibrary.cu:1243-1486, 2819-3107) are gridMode CHAOS_GRID_STATE;
- * its step-size sweep bifurcation1DForH (debri/hostLibrary.cu:1005-1240) is
- * dim 1, indicesOfMutVars[0] = CHAOS_MUT_STEP, gridMode CHAOS_GRID_LOG0 |
- * CHAOS_GRID_LOG_F32 (h is then ignored: point k integrates with its own step
+ * (debri/hostLibrary.cu:1243-1486, 2819-3107) are gridMode CHAOS_GRID_STATE |
+ * CHAOS_GRID_LEGACY_LOOP; its step-size sweep bifurcation1DForH
+ * (debri/hostLibrary.cu:1005-1240) is dim 1, indicesOfMutVars[0] =
+ * CHAOS_MUT_STEP, gridMode CHAOS_GRID_LOG0 | CHAOS_GRID_LOG_F32 |
+ * CHAOS_GRID_LEGACY_LOOP (h is then ignored: point k integrates with its own step
  * h_k, (int)(transientTime / h_k) transient steps, (int)(tMax / h_k /
  * preScaller) samples, intervals in units h_k * preScaller). Loop, peak rule
  * and clustering are chaos_bifurcation1d's / chaos_bifurcation2d's, which are
  * this call with gridMode 0.
+ * CHAOS_GRID_LEGACY_LOOP runs the legacy library's per-point loop, as its
+ * analyses do, in FP64. Grids over initial conditions or parameters follow
+ * calculateDiscreteModelICCUDA (debri/cudaLibrary.cu:1022-1116, the loop
+ * :604-680):
+ *   - the transient tests only state component 0, and only for NaN or
+ *     infinity (flag 0);
+ *   - a transient that ends at a fixed point still runs the recorded part;
+ *   - every recorded sample is followed by preScaller steps;
+ *   - the fixed-point test is sqrt(|sum|) < 1e-9 in FP64 (flag -1, count -1).
+ * The step-size sweep follows calculateDiscreteModelCUDA_H (:955-1000, the
+ * loop :472-527):
+ *   - the transient's verdict is ignored (it only stops early at a NaN or
+ *     infinite component 0);
+ *   - a point whose last state change is exactly 0, or has a norm below
+ *     1e-12, keeps no peaks (flag -1).
+ * The peak rule and the per-point clustering are the same in both libraries.
  * dim 1: outputs as chaos_bifurcation1d (labels must be NULL).
  * dim 2: labels[nPts*nPts] and counts (may be NULL) as chaos_bifurcation2d;
  *        flags, firstSample, peaks and intervals must be NULL, peakCapacity 0.

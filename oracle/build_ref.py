@@ -35,8 +35,13 @@ BASINS_FUNCS = ["getValueByIdx", "calculateDiscreteModel", "calculateTransTimeCU
                 "CUDA_dbscan_search_clear_points_kernel", "CUDA_dbscan_search_fixed_points_kernel",
                 "CUDA_dbscan_kernel"]
 LLE_FUNCS = ["loopCalculateDiscreteModel", "calculateDiscreteModel", "calculateSystem", "linspace"]
-# the legacy library's helpers behind the engine's legacy analyses (debri/cudaLibrary.cu)
-LEGACY_FUNCS = ["getValueByIdx", "getValueByIdxLog", "peakFinder", "projectionOperator", "gramSchmidtProcess"]
+# the legacy library's functions behind the engine's legacy analyses (debri/cudaLibrary.cu): the
+# helpers, its hard-wired system and loops, and the per-thread kernels of its bifurcation and
+# basins analyses (in dependency order)
+LEGACY_FUNCS = ["getValueByIdx", "getValueByIdxLog", "peakFinder", "projectionOperator", "gramSchmidtProcess",
+                "calculateDiscreteModel", "loopCalculateDiscreteModel", "loopCalculateDiscreteModel_int",
+                "distance", "dbscan", "calculateDiscreteModelICCUDA", "calculateDiscreteModelCUDA_H",
+                "peakFinderCUDA", "peakFinderCUDA_H", "avgPeakFinderCUDA", "dbscanCUDA"]
 
 # plug-in systems: name -> (header text of a systems.cuh stand-in)
 PLUGINS = {
@@ -168,7 +173,7 @@ def build(systems: list[str] | None = None, verbose: bool = False) -> list[Path]
                   OUT / "ref_bif.inc")
         write_inc(REF / "Basins/src/basinsCUDA.cu", "basinsGPU", BASINS_FUNCS, None, OUT / "ref_basins.inc")
         write_inc(REF / "LLE/src/LLECUDA.cu", "LLE_constants", LLE_FUNCS, "sh_mem", OUT / "ref_lle.inc")
-        write_inc(REF / "debri/cudaLibrary.cu", "legacy", LEGACY_FUNCS, None, OUT / "ref_legacy.inc")
+        write_inc(REF / "debri/cudaLibrary.cu", "legacy", LEGACY_FUNCS, "s", OUT / "ref_legacy.inc")
     built = []
     if (OUT / "ref_legacy.inc").is_file():
         lib = OUT / "libref_legacy.so"

@@ -20,6 +20,10 @@
 //   * basins loop (preScaller, isnan/isinf, sqrt(abs))  Basins/src/basinsCUDA.cu:318-380
 //   * avgPeakFinderCUDA    Basins/src/basinsCUDA.cu:818-864
 //   * CUDA_dbscan + kernels Basins/src/basinsCUDA.cu:35-179, 866-923
+//   * the legacy library's bifurcation loops (grid mode kModeLegacy):
+//       calculateDiscreteModelICCUDA  debri/cudaLibrary.cu:1022-1116 (its loop,
+//       :604-680, is the basins loop above, token for token), and
+//       calculateDiscreteModelCUDA_H :955-1000 over loopCalculateDiscreteModel :472-527
 // Unlike the engine (which streams samples through a peak state machine and
 // never stores a trajectory), the oracle records every trajectory into an
 // array and scans it exactly as the reference does.
@@ -76,8 +80,9 @@ inline double log_value(long long n, int nPts, double start, double finish, bool
 }
 
 // Grid modes (the engine's CHAOS_GRID_* bits): initial conditions instead of
-// parameters, log-scale dimension 0 / 1, FP32 rounding of log values.
-constexpr int kModeState = 1, kModeLog0 = 2, kModeLog1 = 4, kModeLogF32 = 8;
+// parameters, log-scale dimension 0 / 1, FP32 rounding of log values, the
+// legacy library's per-point loop (bifurcation sweeps).
+constexpr int kModeState = 1, kModeLog0 = 2, kModeLog1 = 4, kModeLogF32 = 8, kModeLegacy = 16;
 
 // Value of dimension d at grid point idx of a bifurcation-type sweep.
 inline double sweep_value(long long idx, int nPts, const double* ranges, int d, int mode) {
@@ -135,6 +140,31 @@ int loop_basins(int sys, double* x, const double* a, const StepCtx<double>& c, i
     double t = 0;
     for (int j = 0; j < nx; ++j) t += (x[j] - xPrev[j]) * (x[j] - xPrev[j]);
     if (std::sqrt(std::fabs(t)) < 1e-9) return -1;
+    return 1;
+}
+
+// loopCalculateDiscreteModel of the legacy library (debri/cudaLibrary.cu:472-527),
+// the loop of its step-size sweep: x[wv] recorded before preScaller steps,
+// isnan/isinf and maxValue tests; a last state change of exactly 0, or of
+// norm below 1e-12, ends it as a fixed point. Returns 1 / 0 (diverged) / -1
+// (fixed point; the legacy returns false for both).
+int loop_legacy_bool(int sys, double* x, const double* a, const StepCtx<double>& c, int iters, int nx,
+                     int preScaller, int wv, double maxValue, double* data) {
+    double xPrev[kMaxX];
+    for (int j = 0; j < nx; ++j) xPrev[j] = x[j];
+    if (iters <= 0) return 1;  // the legacy reads an uninitialised xPrev here
+    for (int i = 0; i < iters; ++i) {
+        for (int j = 0; j < nx; ++j) xPrev[j] = x[j];
+        if (data) data[i] = x[wv];
+        for (int j = 0; j < preScaller; ++j) chaos::step_dyn(sys, x, a, c);
+        if (std::isnan(x[wv]) || std::isinf(x[wv])) return 0;
+        if (maxValue != 0)
+            if ((double)fabsf((float)x[wv]) > maxValue) return 0;
+    }
+    double t = 0;
+    for (int j = 0; j < nx; ++j) t += (x[j] - xPrev[j]) * (x[j] - xPrev[j]);
+    if (t == 0) return -1;
+    if (std::sqrt(t) < 1e-12) return -1;
     return 1;
 }
 
@@ -286,6 +316,7 @@ void orc_point_dbscan(const double* intervals, const int* counts, int nSeries, i
 // (dim 1): point k runs with its own h_k, (int)(transientTime / h_k)
 // transient steps, (int)(tMax / h_k / preScaller) samples, intervals in units
 // h_k * preScaller (the legacy step-size sweep, debri/hostLibrary.cu:1005-1240).
+// kModeLegacy: the legacy library's per-point loop instead of the current one.
 int orc_bifurcation_sweep(int sys, int dim, int gridMode, double tMax, int nPts, double h, const double* ic,
                           const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
                           const double* values, int preScaller, double eps, int cap, long long pBegin,
@@ -322,17 +353,30 @@ int orc_bifurcation_sweep(int sys, int dim, int gridMode, double tMax, int nPts,
             const int S = (int)(transientTime / hp);
             const StepCtx<double> c(hp);
             const double hh = hp * (double)preScaller;
+            int flag;
+            if (gridMode & kModeLegacy) {
+                // the legacy kernels: calculateDiscreteModelICCUDA (debri/cudaLibrary.cu:1022-1116) runs
+                // its transient with preScaller 1, writableVar 0 and no bound and stops the point only
+                // when it diverged; calculateDiscreteModelCUDA_H (:955-1000) ignores the transient's verdict
+                flag = 1;
+                if (stepAxis) loop_legacy_bool(sys, x, a, c, S, nx, 1, 0, 0.0, nullptr);
+                else if (loop_basins(sys, x, a, c, S, nx, 1, 0, 0.0, nullptr) == 0) flag = 0;
+                if (flag == 1 && B >= 1)
+                    flag = stepAxis ? loop_legacy_bool(sys, x, a, c, B, nx, preScaller, wv, maxValue, data.data())
+                                    : loop_basins(sys, x, a, c, B, nx, preScaller, wv, maxValue, data.data());
+            } else {
+                flag = loop_bif(sys, x, a, c, S, nx, wv, maxValue, nullptr);
+                if (B < 1) flag = flag == 1 ? 1 : 0;
+                else if (flag == 1) flag = loop_bif(sys, x, a, c, B, nx, wv, maxValue, data.data());
+                else flag = 0;
+            }
             if (B < 1) {  // no recorded sample: the transient decides alone
-                int flag = loop_bif(sys, x, a, c, S, nx, wv, maxValue, nullptr);
-                flags[o] = flag == 1 ? 1 : 0;
+                flags[o] = flag;
                 first[o] = 0.0;
                 counts[o] = 0;
                 if (labels) labels[o] = 0;
                 continue;
             }
-            int flag = loop_bif(sys, x, a, c, S, nx, wv, maxValue, nullptr);
-            if (flag == 1) flag = loop_bif(sys, x, a, c, B, nx, wv, maxValue, data.data());
-            else flag = 0;
             flags[o] = flag;
             first[o] = (flag == -1) ? data[0] : 0.0;
             int cnt;

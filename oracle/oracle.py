@@ -134,7 +134,7 @@ def bifurcation(system: int, dim: int, tMax, nPts, h, ic, ranges, mut, wv, maxVa
 
 
 # grid modes (the engine's CHAOS_GRID_* bits) and the step-size axis marker
-GRID_STATE, GRID_LOG0, GRID_LOG1, GRID_LOG_F32 = 1, 2, 4, 8
+GRID_STATE, GRID_LOG0, GRID_LOG1, GRID_LOG_F32, GRID_LEGACY_LOOP = 1, 2, 4, 8, 16
 MUT_STEP = -1
 
 
@@ -399,10 +399,12 @@ class RefLib:
 
 
 class LegacyLib:
-    """Host build of the reference's legacy helpers (debri/cudaLibrary.cu:
-    getValueByIdx, getValueByIdxLog, peakFinder, projectionOperator,
-    gramSchmidtProcess, extracted unchanged) with a host replay of the legacy
-    spectrum's block loop around them (oracle/ref_legacy_harness.cpp)."""
+    """Host build of the reference's legacy library functions
+    (debri/cudaLibrary.cu, extracted unchanged: the helpers, the hard-wired
+    system and its loops, the bifurcation / basins / step-sweep kernels) with
+    host replays around them (oracle/ref_legacy_harness.cpp): the spectrum's
+    block loop, and the legacy kernels of bifurcation1DIC / bifurcation2DIC,
+    basinsOfAttraction and bifurcation1DForH run one host thread per point."""
 
     def __init__(self):
         path = REF_DIR / "libref_legacy.so"
@@ -416,6 +418,15 @@ class LegacyLib:
         L.leg_gram_schmidt.argtypes = [_dp, _dp, C.c_int, _dp]
         L.leg_ls_replay.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
                                     C.c_double, _dp, _dp]
+        L.leg_ic_bifurcation.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, _dp,
+                                         C.c_int, _dp, C.c_int, _dp, _ip, C.c_int, C.c_double, C.c_double, _ip, _dp,
+                                         _dp, _ip]
+        L.leg_basins_v1.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, _dp, C.c_int, _dp,
+                                    C.c_int, _dp, _ip, C.c_int, C.c_double, _ip, _dp, _dp]
+        L.leg_step_sweep.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp,
+                                     C.c_int, C.c_double, _ip, _dp, C.c_int, C.POINTER(C.c_int)]
+        for f in (L.leg_ic_bifurcation, L.leg_basins_v1, L.leg_step_sweep):
+            f.restype = C.c_int
 
     def value_log(self, idx, nPts, start, finish, dim=0):
         return self.L.leg_value_log(idx, nPts, start, finish, dim)
@@ -428,6 +439,45 @@ class LegacyLib:
         pk, tm = np.zeros(d.size), np.zeros(d.size)
         c = self.L.leg_peak_finder(d, d.size, pk, tm, h)
         return c, pk[:max(c, 0)], tm[:max(c, 0)]
+
+    def ic_bifurcation(self, dim, nPts, tMax, h, transientTime, preScaller, ic, values, ranges, mut, wv,
+                       maxValue, eps=0.0):
+        """The legacy bifurcation1DIC (dim 1) / bifurcation2DIC (dim 2) kernels:
+        counts, peaks [n][B], intervals [n][B] (dim 2), labels (dim 2)."""
+        B = int(tMax / h / preScaller)
+        n = nPts ** dim
+        counts, labels = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        pk, iv = np.zeros(n * B), np.zeros(n * B)
+        ic, vals = _d(ic), _d(values)
+        rc = self.L.leg_ic_bifurcation(dim, nPts, tMax, h, transientTime, preScaller, ic, ic.size, vals, vals.size,
+                                       _d(ranges), _i(mut), wv, maxValue, eps, counts, pk, iv, labels)
+        if rc:
+            raise ValueError("bad legacy bifurcation arguments")
+        return dict(counts=counts, peaks=pk.reshape(n, B), intervals=iv.reshape(n, B),
+                    labels=labels if dim == 2 else None)
+
+    def basins_v1(self, nPts, tMax, h, transientTime, preScaller, ic, values, ranges, mut, wv, maxValue):
+        """The legacy basinsOfAttraction kernels: flags, avgPeaks, avgIntervals."""
+        n = nPts * nPts
+        flags, ap, ai = np.zeros(n, np.int32), np.zeros(n), np.zeros(n)
+        ic, vals = _d(ic), _d(values)
+        rc = self.L.leg_basins_v1(nPts, tMax, h, transientTime, preScaller, ic, ic.size, vals, vals.size,
+                                  _d(ranges), _i(mut), wv, maxValue, flags, ap, ai)
+        if rc:
+            raise ValueError("bad legacy basins arguments")
+        return dict(flags=flags, avgPeaks=ap, avgIntervals=ai)
+
+    def step_sweep(self, nPts, tMax, transientTime, preScaller, ic, values, ranges, wv, maxValue):
+        """The legacy bifurcation1DForH kernels: counts, peaks [n][block]."""
+        rows = int(tMax / min(ranges[0], ranges[1]) / preScaller) + 1
+        counts, pk = np.zeros(nPts, np.int32), np.zeros(nPts * rows)
+        ic, vals = _d(ic), _d(values)
+        blk = C.c_int(0)
+        rc = self.L.leg_step_sweep(nPts, tMax, transientTime, preScaller, ic, ic.size, vals, vals.size, _d(ranges),
+                                   wv, maxValue, counts, pk, rows, C.byref(blk))
+        if rc:
+            raise ValueError(f"legacy step sweep refused ({rc})")
+        return dict(counts=counts, peaks=pk[:nPts * blk.value].reshape(nPts, blk.value))
 
     def ls_replay(self, system, x0, a, h, trans, ntp, nblocks, eps, tmax, directions):
         n = len(x0)

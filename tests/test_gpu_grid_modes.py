@@ -137,6 +137,47 @@ def test_lle_sweep_log_axes_fp64_vs_oracle(engine, oracle, dim, mode):
     assert np.all(np.isfinite(g32))
 
 
+@pytest.mark.parametrize("rho, pre, maxValue", [(0.5, 1, 1e4), (0.5, 3, 1e4), (28.0, 3, 17.0), (28.0, 2, 1e4)])
+@pytest.mark.parametrize("dim", [1, 2])
+def test_bifurcation_legacy_loop_fp64_vs_oracle(engine, oracle, rho, pre, maxValue, dim):
+    """The legacy per-point loop (GRID_STATE | GRID_LEGACY_LOOP: the loop of
+    the legacy bifurcation1DIC / bifurcation2DIC, whose oracle restatement
+    the CPU tests pin to the legacy kernels) bit for bit against the oracle:
+    fixed points reported after the recorded part (rho 0.5), preScaller
+    sub-steps, the bound tested in the recorded part only (maxValue 17 at rho
+    28). Requested in FP32, the legacy loop still runs in FP64."""
+    vals = [10.0, rho, 8 / 3]
+    n, rng, mut = (48, [-20.0, 20.0], [2]) if dim == 1 else (16, [-20.0, 20.0, -20.0, 20.0], [0, 2])
+    gm = engine.GRID_STATE | engine.GRID_LEGACY_LOOP
+    kw = dict(tMax=10.0, nPts=n, h=0.01, initialConditions=IC, ranges=rng, indicesOfMutVars=mut, writableVar=0,
+              maxValue=maxValue, transientTime=40.0, values=vals, preScaller=pre)
+    o = oracle.bifurcation_sweep(0, dim, gm, 10.0, n, 0.01, IC, rng, mut, 0, maxValue, 40.0, vals, preScaller=pre,
+                                 eps=0.05, cap=400)
+    for prec in (engine.FP64, engine.FP32):
+        if dim == 1:
+            g = engine.bifurcation_sweep("lorenz", 1, gm, peakCapacity=400, precision=prec, **kw)
+            _assert_bif_equal(g, o, 400)
+        else:
+            g = engine.bifurcation_sweep("lorenz", 2, gm, eps=0.05, precision=prec, **kw)
+            assert np.array_equal(g["counts"], o["counts"])
+            assert np.array_equal(g["labels"], o["labels"])
+    if rho == 0.5:  # every orbit ends at the origin: reported as fixed points
+        assert (o["counts"] == -1).all()
+
+
+def test_step_sweep_legacy_loop_fp64_vs_oracle(engine, oracle):
+    """The legacy step-size sweep's loop (bifurcation1DForH) with preScaller
+    3, bit for bit against the oracle."""
+    gm = engine.GRID_LOG0 | engine.GRID_LOG_F32 | engine.GRID_LEGACY_LOOP
+    kw = dict(tMax=10.0, nPts=40, h=0.0, initialConditions=IC, ranges=[0.004, 0.02],
+              indicesOfMutVars=[engine.MUT_STEP], writableVar=0, maxValue=1e4, transientTime=5.0, values=LORENZ,
+              preScaller=3)
+    g = engine.bifurcation_sweep("lorenz", 1, gm, peakCapacity=500, **kw)
+    o = oracle.bifurcation_sweep(0, 1, gm, 10.0, 40, 0.0, IC, [0.004, 0.02], [-1], 0, 1e4, 5.0, LORENZ, preScaller=3,
+                                 cap=500)
+    _assert_bif_equal(g, o, 500)
+
+
 def test_spectrum_log_axis_fp64_vs_oracle(engine, oracle):
     kw = dict(tMax=10.0, NT=0.1, nPts=12, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0], ranges=[10.0, 100.0],
               indicesOfMutVars=[1], transientTime=2.0, values=LORENZ)
@@ -156,27 +197,29 @@ def test_legacy_csv_bytes(engine, oracle, tmp_path):
     L.set_precision(L.FP64)
     n = 20
     lin = [-8.0 + k * (16.0 / (n - 1)) for k in range(n)]
-    # bifurcation1DIC
+    LEG = oracle.GRID_LEGACY_LOOP  # the legacy analyses run the legacy per-point loop
+    # bifurcation1DIC (preScaller 2: a sample every second step)
     p = tmp_path / "bic.csv"
-    old.bifurcation1DIC(8.0, n, 0.01, 3, IC, [-8.0, 8.0], [2], 0, 1e4, 4.0, LORENZ, 3, 1, p)
-    o = oracle.bifurcation_sweep(0, 1, oracle.GRID_STATE, 8.0, n, 0.01, IC, [-8.0, 8.0], [2], 0, 1e4, 4.0, LORENZ)
+    old.bifurcation1DIC(8.0, n, 0.01, 3, IC, [-8.0, 8.0], [2], 0, 1e4, 4.0, LORENZ, 3, 2, p)
+    o = oracle.bifurcation_sweep(0, 1, oracle.GRID_STATE | LEG, 8.0, n, 0.01, IC, [-8.0, 8.0], [2], 0, 1e4, 4.0,
+                                 LORENZ, preScaller=2)
     expect = "".join("%.12g, %.12g\n" % (lin[k], o["peaks"][k, j]) for k in range(n)
                      for j in range(max(int(o["counts"][k]), 0)))
     assert p.read_text() == expect
     # bifurcation1DForH (log-scale step, FP32-rounded; rows labelled with the linear range)
     p = tmp_path / "bh.csv"
-    old.bifurcation1DForH(8.0, n, 3, IC, [0.005, 0.02], 0, 1e4, 4.0, LORENZ, 3, 1, p)
-    o = oracle.bifurcation_sweep(0, 1, oracle.GRID_LOG0 | oracle.GRID_LOG_F32, 8.0, n, 0.0, IC, [0.005, 0.02], [-1],
-                                 0, 1e4, 4.0, LORENZ)
+    old.bifurcation1DForH(8.0, n, 3, IC, [0.005, 0.02], 0, 1e4, 4.0, LORENZ, 3, 2, p)
+    o = oracle.bifurcation_sweep(0, 1, oracle.GRID_LOG0 | oracle.GRID_LOG_F32 | LEG, 8.0, n, 0.0, IC, [0.005, 0.02],
+                                 [-1], 0, 1e4, 4.0, LORENZ, preScaller=2)
     hl = [0.005 + k * ((0.02 - 0.005) / (n - 1)) for k in range(n)]
     expect = "".join("%.12g, %.12g\n" % (hl[k], o["peaks"][k, j]) for k in range(n)
                      for j in range(max(int(o["counts"][k]), 0)))
     assert p.read_text() == expect
     # bifurcation2DIC
     p = tmp_path / "b2.csv"
-    old.bifurcation2DIC(5.0, 9, 0.01, 3, IC, [-10.0, 10.0, -10.0, 10.0], [0, 1], 0, 1e4, 4.0, LORENZ, 3, 1, 0.05, p)
-    o = oracle.bifurcation_sweep(0, 2, oracle.GRID_STATE, 5.0, 9, 0.01, IC, [-10.0, 10.0, -10.0, 10.0], [0, 1], 0,
-                                 1e4, 4.0, LORENZ, eps=0.05)
+    old.bifurcation2DIC(5.0, 9, 0.01, 3, IC, [-10.0, 10.0, -10.0, 10.0], [0, 1], 0, 1e4, 4.0, LORENZ, 3, 2, 0.05, p)
+    o = oracle.bifurcation_sweep(0, 2, oracle.GRID_STATE | LEG, 5.0, 9, 0.01, IC, [-10.0, 10.0, -10.0, 10.0], [0, 1],
+                                 0, 1e4, 4.0, LORENZ, preScaller=2, eps=0.05)
     assert p.read_text() == "-10 10\n-10 10\n" + _csv_matrix(o["labels"], 9, str)
     # LLE1D / LLE1DIC / LLE2DIC
     kw = (10.0, 0.1)

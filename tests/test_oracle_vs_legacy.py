@@ -6,12 +6,16 @@ compiled for the host by oracle/build_ref.py. Runs where that build exists.
 Pinned bit for bit: the log-scale axis (getValueByIdxLog, raised to 10^x as
 the engine's CHAOS_GRID_LOG* tables are), the linear axis (getValueByIdx), the
 legacy peakFinder against the current library's (the engine follows the
-latter), and the spectrum's per-block classical Gram-Schmidt and
-renormalisation (projectionOperator, gramSchmidtProcess, the block loop of
-LSKernelCUDA replayed around them) against orc_lyapunov_spectrum with the same
-twin start and block count. Not pinned, by design: the legacy kernels'
-twin directions (cuRAND in LLEKernelCUDA; sinf of the chunk-relative thread
-index in LSKernelCUDA) and their hard-wired system."""
+latter), the spectrum's per-block classical Gram-Schmidt and renormalisation
+(projectionOperator, gramSchmidtProcess, the block loop of LSKernelCUDA
+replayed around them) against orc_lyapunov_spectrum with the same twin start
+and block count, and the legacy bifurcation1DIC / bifurcation2DIC,
+basinsOfAttraction and bifurcation1DForH kernels themselves (run one host
+thread per point; their hard-wired system is the sin3 plug-in's arithmetic)
+against the oracle's sweeps with the legacy loop (GRID_LEGACY_LOOP) and its
+basins features. Not pinned, by design: the legacy LLE kernels' twin
+directions (cuRAND in LLEKernelCUDA; sinf of the chunk-relative thread index
+in LSKernelCUDA)."""
 import math
 
 import numpy as np
@@ -72,3 +76,83 @@ def test_spectrum_block_loop_matches_legacy_gram_schmidt(leg, oracle, system, va
     blocks = int(tMax / h) // ntp + 2  # the LLE map's calcBlocks + 1
     legacy = leg.ls_replay(system, ic, values, h, trans, ntp, blocks, eps, tMax, np.eye(nx))
     assert np.array_equal(np.asarray(ours).ravel(), legacy)
+
+
+SIN3 = [0.5, 0.1, 1.4, 15.552, 2.0]  # the hard-wired legacy system's parameters; a[1] is the damping b
+
+
+def _sin3(b):
+    return [SIN3[0], b] + SIN3[2:]
+
+
+# b = 0.1 chaotic (maxValue 4 leaves most orbits unbounded), 0.5 every orbit ends at a fixed point,
+# 1.1 fixed points beside decaying orbits
+@pytest.mark.parametrize("b", [0.1, 0.5, 1.1])
+@pytest.mark.parametrize("pre", [1, 3])
+@pytest.mark.parametrize("dim", [1, 2])
+def test_ic_bifurcation_matches_legacy_kernels(leg, oracle, b, pre, dim):
+    """bifurcation1DIC / bifurcation2DIC: calculateDiscreteModelICCUDA,
+    peakFinderCUDA and dbscanCUDA against the oracle's sweep over initial
+    conditions with the legacy loop, on sin3: counts (with the legacy's -1 /
+    0), every kept peak, the intervals and the labels."""
+    n, rng, mut = (40, [-6.0, 6.0], [0]) if dim == 1 else (14, [-6.0, 6.0, -6.0, 6.0], [0, 1])
+    args = (30.0, n, 0.01)
+    L = leg.ic_bifurcation(dim, n, 30.0, 0.01, 50.0, pre, [0.0, 0.0, 0.0], _sin3(b), rng, mut, 0, 4.0, eps=0.05)
+    o = oracle.bifurcation_sweep(5, dim, oracle.GRID_STATE | oracle.GRID_LEGACY_LOOP, *args, [0.0, 0.0, 0.0], rng,
+                                 mut, 0, 4.0, 50.0, _sin3(b), preScaller=pre, eps=0.05)
+    assert np.array_equal(L["counts"], o["counts"])
+    for k, c in enumerate(L["counts"]):
+        assert np.array_equal(L["peaks"][k, :max(c, 0)], o["peaks"][k, :max(c, 0)]), k
+        if dim == 2:
+            assert np.array_equal(L["intervals"][k, :max(c, 0)], o["intervals"][k, :max(c, 0)]), k
+    if dim == 2:
+        assert np.array_equal(L["labels"], o["labels"])
+
+
+def test_legacy_loop_differs_from_current_loop(leg, oracle):
+    """Why the legacy analyses need their own loop: where every orbit ends at
+    a fixed point, the legacy kernels report it (-1) after the recorded part,
+    the current library's loop stops at the transient and reports 0; with
+    preScaller 3 the legacy samples every third step, the current loop every
+    step."""
+    rng, mut = [-6.0, 6.0, -6.0, 6.0], [0, 1]
+    L = leg.ic_bifurcation(2, 10, 30.0, 0.01, 50.0, 1, [0.0, 0.0, 0.0], _sin3(0.5), rng, mut, 0, 4.0, eps=0.05)
+    cur = oracle.bifurcation_sweep(5, 2, oracle.GRID_STATE, 30.0, 10, 0.01, [0.0, 0.0, 0.0], rng, mut, 0, 4.0, 50.0,
+                                   _sin3(0.5), eps=0.05)
+    assert (L["labels"] == -1).all() and (cur["labels"] == 0).all()
+    L = leg.ic_bifurcation(1, 40, 30.0, 0.01, 50.0, 3, [0.0, 0.0, 0.0], _sin3(0.2), [-6.0, 6.0], [0], 0, 1e8)
+    cur = oracle.bifurcation_sweep(5, 1, oracle.GRID_STATE, 30.0, 40, 0.01, [0.0, 0.0, 0.0], [-6.0, 6.0], [0], 0,
+                                   1e8, 50.0, _sin3(0.2), preScaller=3)
+    assert not np.array_equal(L["counts"], cur["counts"])
+
+
+@pytest.mark.parametrize("b", [0.1, 0.2, 0.5, 1.1])
+@pytest.mark.parametrize("pre", [1, 3])
+@pytest.mark.parametrize("maxValue", [1e8, 4.0])
+def test_basins_v1_matches_legacy_kernels(leg, oracle, b, pre, maxValue):
+    """basinsOfAttraction (the legacy basins map): calculateDiscreteModelICCUDA
+    and avgPeakFinderCUDA against the oracle's basins features (the current
+    library's basins loop, which the engine's basins map runs): flags, mean
+    peaks and mean intervals bit for bit."""
+    rng, mut = [-6.0, 6.0, -6.0, 6.0], [0, 1]
+    L = leg.basins_v1(14, 30.0, 0.01, 50.0, pre, [0.0, 0.0, 0.0], _sin3(b), rng, mut, 0, maxValue)
+    o = oracle.basins_features(5, 30.0, 14, 0.01, [0.0, 0.0, 0.0], rng, mut, 0, maxValue, 50.0, _sin3(b),
+                               preScaller=pre)
+    assert np.array_equal(L["flags"], o["flags"])
+    assert np.array_equal(L["avgPeaks"], o["avg_peaks"])
+    assert np.array_equal(L["avgIntervals"], o["avg_intervals"])
+
+
+@pytest.mark.parametrize("pre", [1, 2, 3])
+@pytest.mark.parametrize("rng", [[0.005, 0.02], [0.01, 0.05], [0.02, 0.004]])
+def test_step_sweep_matches_legacy_kernels(leg, oracle, pre, rng):
+    """bifurcation1DForH: calculateDiscreteModelCUDA_H and peakFinderCUDA_H
+    (the step on the powf-rounded log scale) against the oracle's step-size
+    sweep with the legacy loop: kept-peak counts and every kept peak."""
+    V = _sin3(0.2)
+    L = leg.step_sweep(24, 30.0, 20.0, pre, [0.3, 0.1, 0.0], V, rng, 0, 1e8)
+    o = oracle.bifurcation_sweep(5, 1, oracle.GRID_LOG0 | oracle.GRID_LOG_F32 | oracle.GRID_LEGACY_LOOP, 30.0, 24,
+                                 0.0, [0.3, 0.1, 0.0], rng, [oracle.MUT_STEP], 0, 1e8, 20.0, V, preScaller=pre)
+    assert np.array_equal(L["counts"], np.maximum(o["counts"], 0))
+    for k, c in enumerate(L["counts"]):
+        assert np.array_equal(L["peaks"][k, :c], o["peaks"][k, :c]), k
