@@ -66,6 +66,8 @@ _SIGS = {
     "chaos_compact_peaks": ([_P, _P, _P, _P, C.c_longlong, _I, _P, _P, _P, _P, C.c_longlong, _P], _I),
     "chaos_lle_from_states": ([_P, _I, C.c_longlong, _P, _D, _D, _D, _D, _P], _I),
     "chaos_lle_sweep": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
+    "chaos_lle_sweep_legacy": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _D, _P, _I, _P, _P], _I),
+    "chaos_legacy_lle_draws": ([_P, _I, C.c_longlong, _I, _P], _I),
     "chaos_lyapunov_spectrum": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
     "chaos_basins_features": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _P, _P, _P, _P], _I),
@@ -611,6 +613,39 @@ def lle_sweep(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, in
     _check(lib().chaos_lle_sweep(C.byref(ex), _sys(system), dim, mode, tMax, NT, nPts, h, eps,
                                  A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), transientTime, A.d(vals),
                                  vals.size, _out_ptr(out)))
+    return out
+
+
+def lle_sweep_legacy(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
+                     transientTime, values, maxValue=0.0, mutateState=False, draws=None, out=None, stream=None,
+                     gridMode=0):
+    """The legacy library's LLE analyses with its own kernels' scheme, FP64
+    (chaos_lle_sweep_legacy): LLE1D (a grid of parameters) or, with
+    mutateState, LLE1DIC / LLE2DIC. draws: raw twin draws [points, SIZE_X]
+    (None: the legacy's own, legacy_lle_draws)."""
+    A = _Args()
+    n = nPts ** dim
+    if out is None:
+        out = np.zeros(n)
+    ex = _exec(FP64, {"lle": out}, stream)
+    ic = np.asarray(initialConditions, np.float64)
+    vals = np.asarray(values, np.float64)
+    mode = gridMode | (GRID_STATE if mutateState else 0)
+    dr = None if draws is None else np.ascontiguousarray(draws, np.float64)
+    _check(lib().chaos_lle_sweep_legacy(C.byref(ex), _sys(system), dim, mode, tMax, NT, nPts, h, eps,
+                                        A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), maxValue,
+                                        transientTime, A.d(vals), vals.size, None if dr is None else A.d(dr),
+                                        _out_ptr(out)))
+    return out
+
+
+def legacy_lle_draws(kind, n, nx, stream=None):
+    """The legacy LLE kernels' raw twin draws [n, nx] drawn on the device
+    (chaos_legacy_lle_draws): kind 0 parameter grids (cuRAND), 1
+    initial-condition grids (sinf)."""
+    out = np.zeros((n, nx))
+    ex = _exec(FP64, {"draws": out}, stream)
+    _check(lib().chaos_legacy_lle_draws(C.byref(ex), kind, n, nx, _out_ptr(out)))
     return out
 
 

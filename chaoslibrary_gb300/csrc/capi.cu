@@ -240,6 +240,7 @@ static cudaError_t run_basins(int prec, const SweepParams& P, const BasinsOut& O
     return prec == CHAOS_FP32 ? launch_basins_f32(P, O, st) : launch_basins_f64(P, O, st);
 }
 static cudaError_t run_lle(int prec, const LleParams& L, double* out, cudaStream_t st) {
+    if (L.legacyLoop) prec = CHAOS_FP64;  // the legacy kernels' arithmetic
     if (L.system == SYS_USER) return prec != CHAOS_FP64 ? cudaErrorNotSupported : launch_lle_user(L, out, st);
     if (prec == CHAOS_FF32) return launch_lle_ff(L, out, st);
     return prec == CHAOS_FP32 ? launch_lle_f32(L, out, st) : launch_lle_f64(L, out, st);
@@ -699,6 +700,57 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
     cudaError_t e = run_lle(c.ex.precision, L, dOut, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "LLE kernel"));
     rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_lle_sweep_legacy(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
+                           int nPts, double h, double eps, const double* initialConditions,
+                           int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                           double maxValue, double transientTime, const double* values, int amountOfValues,
+                           const double* draws, double* lle) {
+    int rc = CHAOS_OK;
+    if (!lle) return set_error(CHAOS_E_ARGS, "null argument");
+    LleParams L;
+    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                       indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
+        return rc;
+    const double blocks = tMax / NT;
+    if (!(blocks >= 0) || blocks > 2.0e9) return set_error(CHAOS_E_ARGS, "tMax / NT must fit in int");
+    L.legacyLoop = 1;
+    L.legacyBlocks = (int)blocks;
+    L.maxValue = maxValue;
+    L.twin = 0;
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);
+    if (draws) {
+        const size_t bytes = (size_t)L.nPoints * amountOfInitialConditions * sizeof(double);
+        double* dDraws = (double*)c.alloc(bytes);
+        if (c.failed) return c.finish(CHAOS_E_NOMEM);
+        cudaError_t e = cudaMemcpyAsync(dDraws, draws, bytes, cudaMemcpyDefault, c.stream);
+        if (e != cudaSuccess) return c.finish(cuda_error(e, "twin draws upload"));
+        L.draws = dDraws;
+    }
+    double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = run_lle(CHAOS_FP64, L, dOut, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "legacy LLE kernel"));
+    rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
+    return c.finish(rc);
+}
+
+int chaos_legacy_lle_draws(const chaos_exec* ex, int kind, long long n, int nx, double* draws) {
+    if ((kind != 0 && kind != 1) || n < 0 || nx < 1 || nx > kMaxState || (n > 0 && !draws))
+        return set_error(CHAOS_E_ARGS, "bad twin-draw arguments");
+    if (n == 0) return CHAOS_OK;
+    Call c;
+    int rc = c.begin(ex);
+    if (rc) return rc;
+    double* d = (double*)c.output(draws, (size_t)n * nx * sizeof(double));
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = launch_legacy_draws(kind, n, nx, d, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "twin draws"));
+    rc = c.to_host(draws, d, (size_t)n * nx * sizeof(double));
     return c.finish(rc);
 }
 

@@ -309,17 +309,19 @@ static int legacy_bif1d(int gridMode, double tMax, int nPts, double h, int amoun
 // LLE1D / LLE1DIC: rows "value, lle" at precision 12, no header
 // (debri/hostLibrary.cu:3291-3300, 3508-3517); LLE2DIC: the matrix rule at the
 // default precision, no header (debri/hostLibrary.cu:3793-3805).
+// The legacy LLE kernels' scheme (chaos_lle_sweep_legacy, FP64). Their
+// writableVar argument reaches no loop (they run their loops on component 0).
 static int legacy_lle(int dim, int gridMode, double tMax, double NT, int nPts, double h, double eps,
                       const double* initialConditions, int amountOfInitialConditions, const double* ranges,
-                      const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
-                      const char* OUT_FILE_PATH) {
+                      const int* indicesOfMutVars, double maxValue, double transientTime, const double* values,
+                      int amountOfValues, const char* OUT_FILE_PATH) {
     if (nPts < 1) return chaos::set_error(CHAOS_E_ARGS, "nPts must be >= 1");
     const long long n = dim == 2 ? (long long)nPts * nPts : nPts;
     std::vector<double> lle(n);
     chaos_exec ex = lle_exec();
-    int rc = chaos_lle_sweep(&ex, active_system(), dim, gridMode, tMax, NT, nPts, h, eps, initialConditions,
-                             amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
-                             amountOfValues, lle.data());
+    int rc = chaos_lle_sweep_legacy(&ex, active_system(), dim, gridMode, tMax, NT, nPts, h, eps, initialConditions,
+                                    amountOfInitialConditions, ranges, indicesOfMutVars, maxValue, transientTime,
+                                    values, amountOfValues, nullptr, lle.data());
     if (rc) return rc;
     std::ofstream o(OUT_FILE_PATH);
     if (!o.is_open()) return chaos::set_error(CHAOS_E_IO, "cannot open %s", OUT_FILE_PATH);
@@ -429,9 +431,8 @@ int chaos_compat_LLE1D(double tMax, double NT, int nPts, double h, double eps, c
                        int amountOfValues, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
         (void)writableVar;
-        (void)maxValue;
         return legacy_lle(1, 0, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                          indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+                          indicesOfMutVars, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH);
     });
 }
 
@@ -441,9 +442,8 @@ int chaos_compat_LLE1DIC(double tMax, double NT, int nPts, double h, double eps,
                          int amountOfValues, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
         (void)writableVar;
-        (void)maxValue;
         return legacy_lle(1, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
-                          ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+                          ranges, indicesOfMutVars, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH);
     });
 }
 
@@ -453,9 +453,8 @@ int chaos_compat_LLE2DIC(double tMax, double NT, int nPts, double h, double eps,
                          int amountOfValues, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
         (void)writableVar;
-        (void)maxValue;
         return legacy_lle(2, CHAOS_GRID_STATE, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions,
-                          ranges, indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+                          ranges, indicesOfMutVars, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH);
     });
 }
 

@@ -7,6 +7,7 @@
 #include <climits>
 
 #include "engine.cuh"
+#include "legacy_lle.cuh"
 
 namespace chaos {
 
@@ -43,6 +44,20 @@ __global__ void __launch_bounds__(kBlock) lle_kernel(LleParams L, double* out) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= L.nPoints) return;
     out[o] = lle_point_full<S, double>(L, L.pBegin + o);
+}
+
+// The legacy library's LLE kernels' scheme (L.legacyLoop).
+template <int S>
+__global__ void __launch_bounds__(kBlock) lle_legacy_kernel(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    out[o] = lle_point_legacy<S>(L, L.pBegin + o);
+}
+
+__global__ void legacy_draws_kernel(int kind, long long n, int nx, double* out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * nx) return;
+    out[t] = legacy_twin_draw(kind, t / nx, (int)(t % nx));
 }
 
 // Benettin blocks from caller-supplied starting states (the reference's
@@ -270,9 +285,21 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
-#define CALL(S) (lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
+#define CALL(S)                                                               \
+    {                                                                         \
+        if (L.legacyLoop) lle_legacy_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
+        else lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
+        note_launch();                                                        \
+    }
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_legacy_draws(int kind, long long n, int nx, double* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    legacy_draws_kernel<<<grid_for(n * nx), kBlock, 0, st>>>(kind, n, nx, out);
+    note_launch();
     return cudaGetLastError();
 }
 

@@ -96,6 +96,12 @@ struct LleParams {
     int dim;          // 1: point p = index i of rangeA; 2: p = j*nPts + i (the LLE2D map)
     int mutateState;  // 0: the grid sets values[mut]; 1: it sets initial conditions ic[mut]
     const double* table[2];  // log-scale axes: device arrays of nPts values (null: linspace)
+    // The legacy library's LLE kernels' scheme (legacy_lle.cuh, FP64): legacyLoop
+    // 1, legacyBlocks = (int)(tMax / NT) blocks, the bound maxValue (0: none)
+    // and the raw twin draws of every point (null: the legacy's own).
+    int legacyLoop, legacyBlocks;
+    double maxValue;
+    const double* draws;
 };
 
 // precision-specific launchers (kern_f64.cu / kern_f32.cu)
@@ -104,6 +110,9 @@ cudaError_t launch_bif_f32(const SweepParams& P, const BifOut& O, cudaStream_t s
 cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
+// the legacy LLE kernels' raw twin draws of points [0, n) (kern_f64.cu): kind 0
+// parameter grids (cuRAND), 1 initial-condition grids (sinf); out[p*nx + k]
+cudaError_t launch_legacy_draws(int kind, long long n, int nx, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
 // float-float base trajectory, FP32 twin difference (kern_ff.cu; RK4 systems)
 cudaError_t launch_lle_ff(const LleParams& L, double* out, cudaStream_t st);

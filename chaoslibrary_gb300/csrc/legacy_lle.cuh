@@ -1,0 +1,102 @@
+// LLE of the legacy library's LLE analyses (FP64): the scheme of its kernels
+// LLEKernelCUDA (debri/cudaLibrary.cu:1897-2031, LLE1D: a grid of
+// parameters) and LLEKernelICCUDA (:2034-2139, LLE1DIC / LLE2DIC: a grid of
+// initial conditions), which differs from the LLE map's (LLE/src/LLECUDA.cu)
+// in its block count, its twin start and its renormalisation arithmetic.
+// Included by the FP64 translation units (built-in and user systems).
+#pragma once
+
+#include <curand_kernel.h>
+
+#include "engine.cuh"
+
+namespace chaos {
+
+// The raw twin-direction component k of point p (before normalisation), as
+// the legacy kernels draw it for a grid of one chunk (their thread index is
+// the point index):
+//  - parameter grids: the uniform of cuRAND's default generator seeded p + k
+//    (curand_init(p + k, 0, 0)), minus 0.5;
+//  - initial-condition grids: 0.5 * sinf(p * (k * p + 1) + 1), the integer
+//    expression in 32-bit wrap-around arithmetic.
+__device__ __forceinline__ double legacy_twin_draw(int stateGrid, long long p, int k) {
+    if (!stateGrid) {
+        curandState_t st;
+        curand_init((unsigned long long)p + (unsigned long long)k, 0ull, 0ull, &st);
+        return (double)curand_uniform(&st) - 0.5;
+    }
+    const unsigned i = (unsigned)p;
+    const int arg = (int)(i * ((unsigned)k * i + 1u) + 1u);
+    return 0.5 * (double)sinf((float)arg);
+}
+
+// loopCalculateDiscreteModel (:472-527) as the legacy LLE kernels call it:
+// n steps, preScaller 1, writableVar 0, no samples. It stops early when
+// x[0] becomes NaN or infinite, or |(float)x[0]| > maxValue (maxValue != 0);
+// its verdict is not used.
+template <int S>
+__device__ __forceinline__ void legacy_lle_run(double* x, const double* a, const StepCtx<double>& c, int n,
+                                               double maxValue) {
+    for (int s = 0; s < n; ++s) {
+        step<S>(x, a, c);
+        const double v = x[0];
+        if (((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) > 0x7fefffffffffffffull) return;
+        if (maxValue != 0.0 && (double)fabsf((float)v) > maxValue) return;
+    }
+}
+
+// LLE of point p (L.legacyLoop): the twin direction z (draws[p*NX + k], or
+// legacy_twin_draw) normalised in FP64; the transient of L.trans steps; the
+// twin y = x + eps z; then L.legacyBlocks = (int)(tMax / NT) blocks of
+// L.ntp steps of the orbit and of the twin, each adding log(d) for
+//  - parameter grids: d = sqrt(sum ((1/eps) (x - y))^2), y = x - (x - y) / d;
+//  - initial-condition grids: d = sqrt(sum (x - y)^2) / eps,
+//    y = x - (x - y) * (1/d) (1/d only when d != 0);
+// the sum divided by tMax.
+template <int S>
+__device__ __forceinline__ double lle_point_legacy(const LleParams& L, long long p) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    double x[NX], y[NX], z[NX], a[NA];
+    lle_load<NX, NA>(L, p, x, a);
+    double zp = 0.0;
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+        z[k] = L.draws ? L.draws[p * NX + k] : legacy_twin_draw(L.mutateState, p, k);
+        zp = zp + z[k] * z[k];
+    }
+    zp = sqrt(zp);
+#pragma unroll
+    for (int k = 0; k < NX; ++k) z[k] = z[k] / zp;
+    const StepCtx<double> c(L.h);
+    legacy_lle_run<S>(x, a, c, L.trans, L.maxValue);
+#pragma unroll
+    for (int k = 0; k < NX; ++k) y[k] = x[k] + z[k] * L.eps;
+    double result = 0.0;
+    for (int b = 0; b < L.legacyBlocks; ++b) {
+        legacy_lle_run<S>(x, a, c, L.ntp, L.maxValue);
+        legacy_lle_run<S>(y, a, c, L.ntp, L.maxValue);
+        double d = 0.0;
+        if (!L.mutateState) {
+#pragma unroll
+            for (int k = 0; k < NX; ++k) {
+                const double t = (1.0 / L.eps) * (x[k] - y[k]);
+                d = d + t * t;
+            }
+            d = sqrt(d);
+            result = result + log(d);
+#pragma unroll
+            for (int k = 0; k < NX; ++k) y[k] = x[k] - ((x[k] - y[k]) / d);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NX; ++k) d = d + (x[k] - y[k]) * (x[k] - y[k]);
+            d = sqrt(d) / L.eps;
+            result = result + log(d);
+            if (d != 0.0) d = 1.0 / d;
+#pragma unroll
+            for (int k = 0; k < NX; ++k) y[k] = x[k] - ((x[k] - y[k]) * d);
+        }
+    }
+    return result / L.tMax;
+}
+
+}  // namespace chaos

@@ -240,6 +240,39 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
                     int amountOfValues, double* lle);
 
 /*
+ * The legacy library's LLE analyses with its own kernels' scheme, in FP64
+ * whatever the precision: LLEKernelCUDA (debri/cudaLibrary.cu:1897-2031;
+ * LLE1D, gridMode without CHAOS_GRID_STATE) and LLEKernelICCUDA (:2034-2139;
+ * LLE1DIC / LLE2DIC, gridMode CHAOS_GRID_STATE). Grids and outputs as
+ * chaos_lle_sweep. Per point:
+ *   - the twin direction is the normalised raw draw z (see
+ *     chaos_legacy_lle_draws), or draws[p*SIZE_X + k] when draws is not NULL;
+ *   - transientTime / h steps of the orbit, then the twin y = x + eps*z;
+ *   - (int)(tMax / NT) blocks of NT / h steps of the orbit and of the twin;
+ *     every run of steps stops early where state component 0 becomes NaN or
+ *     infinite or |(float)x[0]| > maxValue (maxValue 0: no bound);
+ *   - each block adds log(d) with d = |x - y| / eps, computed and applied as
+ *     the kernel of the grid kind computes it;
+ *   - the sum is divided by tMax.
+ */
+int chaos_lle_sweep_legacy(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
+                           int nPts, double h, double eps, const double* initialConditions,
+                           int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                           double maxValue, double transientTime, const double* values, int amountOfValues,
+                           const double* draws, double* lle);
+
+/*
+ * The raw twin-direction draws of the legacy LLE kernels for points [0, n)
+ * of a one-chunk grid (the legacy thread index is the point index), nx
+ * components each: draws[p*nx + k].
+ *   kind 0 (parameter grids, LLEKernelCUDA): the uniform of cuRAND's default
+ *     generator seeded p + k (curand_init(p + k, 0, 0)), minus 0.5;
+ *   kind 1 (initial-condition grids, LLEKernelICCUDA): 0.5 * sinf(p * (k * p
+ *     + 1) + 1), the integer expression in 32-bit wrap-around arithmetic.
+ */
+int chaos_legacy_lle_draws(const chaos_exec* ex, int kind, long long n, int nx, double* draws);
+
+/*
  * Lyapunov spectrum over the same grids (the legacy library's LS1D / LS2D,
  * debri/hostLibrary.cu:3829-4111, kernel debri/cudaLibrary.cu:2141-2330):
  * one twin per state dimension started along the unit vectors, classical

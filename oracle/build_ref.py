@@ -41,7 +41,8 @@ LLE_FUNCS = ["loopCalculateDiscreteModel", "calculateDiscreteModel", "calculateS
 LEGACY_FUNCS = ["getValueByIdx", "getValueByIdxLog", "peakFinder", "projectionOperator", "gramSchmidtProcess",
                 "calculateDiscreteModel", "loopCalculateDiscreteModel", "loopCalculateDiscreteModel_int",
                 "distance", "dbscan", "calculateDiscreteModelICCUDA", "calculateDiscreteModelCUDA_H",
-                "peakFinderCUDA", "peakFinderCUDA_H", "avgPeakFinderCUDA", "dbscanCUDA"]
+                "peakFinderCUDA", "peakFinderCUDA_H", "avgPeakFinderCUDA", "dbscanCUDA", "LLEKernelCUDA",
+                "LLEKernelICCUDA"]
 
 # plug-in systems: name -> (header text of a systems.cuh stand-in)
 PLUGINS = {

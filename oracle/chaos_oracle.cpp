@@ -24,6 +24,8 @@
 //       calculateDiscreteModelICCUDA  debri/cudaLibrary.cu:1022-1116 (its loop,
 //       :604-680, is the basins loop above, token for token), and
 //       calculateDiscreteModelCUDA_H :955-1000 over loopCalculateDiscreteModel :472-527
+//   * the legacy library's LLE kernels: LLEKernelCUDA debri/cudaLibrary.cu:1897-2031,
+//       LLEKernelICCUDA :2034-2139 (orc_lle_sweep_legacy)
 // Unlike the engine (which streams samples through a peak state machine and
 // never stores a trajectory), the oracle records every trajectory into an
 // array and scans it exactly as the reference does.
@@ -504,6 +506,90 @@ int orc_lle_sweep(int sys, int dim, int gridMode, double tMax, double NT, int nP
             for (int k = 0; k < nx; ++k) q[k] = x[k] - ((x[k] - q[k]) / dist);
         }
         out[p - pBegin] = sum / tMax;
+    }
+    return 0;
+}
+
+// loopCalculateDiscreteModel (debri/cudaLibrary.cu:472-527) as the legacy
+// LLE kernels call it: n steps, preScaller 1, writableVar 0, no samples; it
+// stops early when x[0] is NaN or infinite or |(float)x[0]| > maxValue
+// (maxValue != 0), and its verdict is not used.
+static void legacy_lle_run(int sys, double* x, const double* a, const StepCtx<double>& c, int n, double maxValue) {
+    for (int s = 0; s < n; ++s) {
+        chaos::step_dyn(sys, x, a, c);
+        if (std::isnan(x[0]) || std::isinf(x[0])) return;
+        if (maxValue != 0)
+            if ((double)fabsf((float)x[0]) > maxValue) return;
+    }
+}
+
+// The legacy library's LLE analyses with its own kernels' scheme:
+// LLEKernelCUDA (debri/cudaLibrary.cu:1897-2031; parameter grids, LLE1D) and
+// LLEKernelICCUDA (:2034-2139; grids of initial conditions, kModeState, LLE1DIC
+// / LLE2DIC). draws[p*nx + k]: the raw twin draws of point p before
+// normalisation; null is allowed for the initial-condition grids, whose draw
+// is restated from the kernel: 0.5 * sinf(p * (k*p + 1) + 1) in 32-bit
+// wrap-around arithmetic, through the C library's sinf. The parameter grids'
+// draws come from cuRAND in the legacy kernel and must be given.
+// (int)(tMax / NT) blocks of (int)(NT / h) steps; out[p - pBegin].
+int orc_lle_sweep_legacy(int sys, int dim, int gridMode, double tMax, double NT, int nPts, double h, double eps,
+                         const double* ic, const double* ranges, const int* mut, double maxValue,
+                         double transientTime, const double* values, const double* draws, long long pBegin,
+                         long long pEnd, double* out, int nthreads) {
+    const int ntp = (int)(NT / h);
+    const int trans = (int)(transientTime / h);
+    const int blocks = (int)(tMax / NT);
+    const bool state = (gridMode & kModeState) != 0;
+    if (ntp < 0 || (dim != 1 && dim != 2) || (!state && !draws)) return 1;
+    const int nx = chaos::system_nx(sys), na = chaos::system_na(sys);
+    const long long total = dim == 2 ? (long long)nPts * nPts : nPts;
+    if (pEnd < 0 || pEnd > total) pEnd = total;
+    set_threads(nthreads);
+    const StepCtx<double> c(h);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long p = pBegin; p < pEnd; ++p) {
+        double x[kMaxX], y[kMaxX], z[kMaxX], a[32];
+        for (int k = 0; k < nx; ++k) x[k] = ic[k];
+        for (int k = 0; k < na; ++k) a[k] = values[k];
+        lle_grid_point(dim, gridMode, p, nPts, ranges, mut, x, a);
+        double zp = 0;
+        for (int k = 0; k < nx; ++k) {
+            if (draws) {
+                z[k] = draws[p * nx + k];
+            } else {
+                const uint32_t i = (uint32_t)p;
+                const int32_t arg = (int32_t)(i * ((uint32_t)k * i + 1u) + 1u);
+                z[k] = 0.5 * (double)sinf((float)arg);
+            }
+            zp += z[k] * z[k];
+        }
+        zp = std::sqrt(zp);
+        for (int k = 0; k < nx; ++k) z[k] = z[k] / zp;
+        legacy_lle_run(sys, x, a, c, trans, maxValue);
+        for (int k = 0; k < nx; ++k) y[k] = x[k] + z[k] * eps;
+        double result = 0;
+        for (int b = 0; b < blocks; ++b) {
+            legacy_lle_run(sys, x, a, c, ntp, maxValue);
+            legacy_lle_run(sys, y, a, c, ntp, maxValue);
+            double d = 0;
+            if (!state) {  // LLEKernelCUDA
+                for (int k = 0; k < nx; ++k) {
+                    double t2 = 1 / eps;
+                    t2 = t2 * (x[k] - y[k]);
+                    d += t2 * t2;
+                }
+                d = std::sqrt(d);
+                result += std::log(d);
+                for (int k = 0; k < nx; ++k) y[k] = x[k] - ((x[k] - y[k]) / d);
+            } else {  // LLEKernelICCUDA
+                for (int k = 0; k < nx; ++k) d += (x[k] - y[k]) * (x[k] - y[k]);
+                d = std::sqrt(d) / eps;
+                result += std::log(d);
+                if (d != 0) d = 1 / d;
+                for (int k = 0; k < nx; ++k) y[k] = x[k] - ((x[k] - y[k]) * d);
+            }
+        }
+        out[p - pBegin] = result / tMax;
     }
     return 0;
 }

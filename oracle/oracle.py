@@ -61,6 +61,9 @@ def lib() -> C.CDLL:
             getattr(L, name).argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
                                          C.c_double, _dp, _dp, _ip, C.c_double, _dp, C.c_longlong, C.c_longlong,
                                          _dp, C.c_int]
+        L.orc_lle_sweep_legacy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
+                                           C.c_double, _dp, _dp, _ip, C.c_double, C.c_double, _dp, C.c_void_p,
+                                           C.c_longlong, C.c_longlong, _dp, C.c_int]
         L.orc_basins_features.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
                                           C.c_double, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _ip,
                                           _dp, _dp, C.c_void_p, C.c_void_p, C.c_int]
@@ -195,6 +198,22 @@ def lle_sweep(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ranges, m
                              transientTime, _d(values), p_begin, p_end, out, nthreads)
     if rc:
         raise ValueError("bad LLE arguments")
+    return out
+
+
+def lle_sweep_legacy(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ranges, mut, maxValue, transientTime,
+                     values, draws=None, p_begin=0, p_end=-1, nthreads=0) -> np.ndarray:
+    """The legacy LLE kernels' scheme (orc_lle_sweep_legacy); draws: raw twin
+    draws [points, SIZE_X] (required for parameter grids)."""
+    total = nPts * nPts if dim == 2 else nPts
+    p_end = total if p_end < 0 else p_end
+    out = np.zeros(p_end - p_begin, np.float64)
+    dr = None if draws is None else _d(draws).ravel()
+    rc = lib().orc_lle_sweep_legacy(system, dim, grid_mode, tMax, NT, nPts, h, eps, _d(ic), _d(ranges), _i(mut),
+                                    maxValue, transientTime, _d(values), None if dr is None else dr.ctypes.data,
+                                    p_begin, p_end, out, nthreads)
+    if rc:
+        raise ValueError("bad legacy LLE arguments")
     return out
 
 
@@ -425,7 +444,9 @@ class LegacyLib:
                                     C.c_int, _dp, _ip, C.c_int, C.c_double, _ip, _dp, _dp]
         L.leg_step_sweep.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp,
                                      C.c_int, C.c_double, _ip, _dp, C.c_int, C.POINTER(C.c_int)]
-        for f in (L.leg_ic_bifurcation, L.leg_basins_v1, L.leg_step_sweep):
+        L.leg_lle.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                              _dp, C.c_int, _dp, C.c_int, _dp, _ip, C.c_double, C.c_void_p, _dp]
+        for f in (L.leg_ic_bifurcation, L.leg_basins_v1, L.leg_step_sweep, L.leg_lle):
             f.restype = C.c_int
 
     def value_log(self, idx, nPts, start, finish, dim=0):
@@ -478,6 +499,20 @@ class LegacyLib:
         if rc:
             raise ValueError(f"legacy step sweep refused ({rc})")
         return dict(counts=counts, peaks=pk[:nPts * blk.value].reshape(nPts, blk.value))
+
+    def lle(self, kind, dim, nPts, tMax, NT, h, eps, transientTime, ic, values, ranges, mut, maxValue,
+            uniforms=None):
+        """The legacy LLE1D (kind 0, LLEKernelCUDA; uniforms[seed]: its cuRAND
+        draws) or LLE1DIC / LLE2DIC (kind 1, LLEKernelICCUDA) kernel."""
+        n = nPts ** dim
+        out = np.zeros(n)
+        ic, vals = _d(ic), _d(values)
+        u = None if uniforms is None else np.ascontiguousarray(uniforms, np.float32)
+        rc = self.L.leg_lle(kind, dim, nPts, tMax, NT, h, eps, transientTime, ic, ic.size, vals, vals.size,
+                            _d(ranges), _i(mut), maxValue, None if u is None else u.ctypes.data, out)
+        if rc:
+            raise ValueError("bad legacy LLE arguments")
+        return out
 
     def ls_replay(self, system, x0, a, h, trans, ntp, nblocks, eps, tmax, directions):
         n = len(x0)

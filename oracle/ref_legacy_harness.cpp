@@ -11,15 +11,18 @@
 //   (:604-680), distance and dbscan (:1577-1666), and the kernels
 //   calculateDiscreteModelICCUDA (:1022-1116), calculateDiscreteModelCUDA_H
 //   (:955-1016), peakFinderCUDA (:1345-1367), peakFinderCUDA_H (:1396-1412),
-//   avgPeakFinderCUDA (:2334-2380) and dbscanCUDA (:1835-1863).
+//   avgPeakFinderCUDA (:2334-2380), dbscanCUDA (:1835-1863), LLEKernelCUDA
+//   (:1897-2031) and LLEKernelICCUDA (:2034-2139).
 // leg_ls_replay re-sequences the block loop of LSKernelCUDA (:2293-2327) on
 // the host around the verbatim Gram-Schmidt: the legacy kernel integrates a
 // system hard-wired into the legacy sources and starts its twins from sinf of
 // the chunk-relative thread index, so the replay takes the orbit step, the
 // twin start and the block count from its caller. leg_ic_bifurcation,
-// leg_basins_v1 and leg_step_sweep run the legacy kernels themselves, one
-// host "thread" per point (block size 1, one chunk of all points), in the
-// order the legacy host functions launch them.
+// leg_basins_v1, leg_step_sweep and leg_lle run the legacy kernels
+// themselves, one host "thread" per point (block size 1, one chunk of all
+// points), in the order the legacy host functions launch them. LLEKernelCUDA
+// draws its twin direction from cuRAND: here curand_init keeps the seed and
+// curand_uniform returns the caller's uniform for that seed.
 #include "cuda_runtime.h"
 
 #include <cmath>
@@ -28,6 +31,16 @@
 #include "../chaoslibrary_gb300/csrc/systems.h"
 
 thread_local dim3 threadIdx, blockIdx, blockDim;
+
+// the two cuRAND device calls of LLEKernelCUDA, fed from the caller's uniforms
+struct curandState_t {
+    unsigned long long seed;
+};
+thread_local const float* g_uniforms = nullptr;
+inline void curand_init(unsigned long long seed, unsigned long long, unsigned long long, curandState_t* s) {
+    s->seed = seed;
+}
+inline float curand_uniform(curandState_t* s) { return g_uniforms[s->seed]; }
 
 namespace legacy_src {
 namespace legacy {
@@ -212,6 +225,35 @@ int leg_step_sweep(int nPts, double tMax, double transientTime, int preScaller, 
         legacy_src::legacy::peakFinderCUDA_H(data.data(), blk, nPts, counts, out.data(), nullptr, 0);
     }
     for (size_t i = 0; i < (size_t)nPts * blk; ++i) peaks[i] = out[i];
+    return 0;
+}
+
+// The legacy LLE1D (kind 0: LLEKernelCUDA, debri/hostLibrary.cu:3111-3325) or
+// LLE1DIC / LLE2DIC (kind 1: LLEKernelICCUDA, :3328-3542, 3692-3825) kernel
+// over all n = nPts^dim points: (int)(tMax / NT) blocks, the transient of
+// (int)(transientTime / h) steps. uniforms[seed] (kind 0): the cuRAND uniform
+// of each seed the kernel draws (seeds 0 .. n + nIC - 2). out[n].
+int leg_lle(int kind, int dim, int nPts, double tMax, double NT, double h, double eps, double transientTime,
+            const double* ic, int nIC, const double* values, int nValues, const double* ranges, const int* mut,
+            double maxValue, const float* uniforms, double* out) {
+    const int blocks = tMax / NT;
+    const int S = transientTime / h;
+    const long long n = dim == 1 ? (long long)nPts : (long long)nPts * nPts;
+    if (3 * nIC + nValues > 4096 || n > 0x7fffffffLL || (kind == 0 && !uniforms)) return 1;
+    std::vector<double> rng(ranges, ranges + 2 * dim), x0(ic, ic + nIC), a(values, values + nValues);
+    std::vector<int> mv(mut, mut + dim);
+    g_uniforms = uniforms;
+    for (long long k = 0; k < n; ++k) {
+        as_thread(k);
+        if (kind == 0)
+            legacy_src::legacy::LLEKernelCUDA(nPts, (int)n, NT, tMax, blocks, 0, S, dim, rng.data(), h, eps, mv.data(),
+                                              x0.data(), nIC, a.data(), nValues, tMax / NT, 1, 0, maxValue, out);
+        else
+            legacy_src::legacy::LLEKernelICCUDA(nPts, (int)n, NT, tMax, blocks, 0, S, dim, rng.data(), h, eps,
+                                                mv.data(), x0.data(), nIC, a.data(), nValues, tMax / NT, 1, 0,
+                                                maxValue, out);
+    }
+    g_uniforms = nullptr;
     return 0;
 }
 

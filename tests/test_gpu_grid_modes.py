@@ -178,6 +178,44 @@ def test_step_sweep_legacy_loop_fp64_vs_oracle(engine, oracle):
     _assert_bif_equal(g, o, 500)
 
 
+@pytest.mark.parametrize("state, dim, maxValue", [(False, 1, 0.0), (False, 2, 18.0), (True, 1, 0.0), (True, 2, 18.0)])
+def test_lle_legacy_scheme_fp64_vs_oracle(engine, oracle, state, dim, maxValue):
+    """The legacy LLE kernels' scheme (chaos_lle_sweep_legacy: LLEKernelCUDA
+    on parameter grids, LLEKernelICCUDA on initial conditions; the oracle's
+    restatement is pinned to those kernels on the CPU) against the oracle fed
+    the twin draws the engine made: within 1e-12 (CUDA's log and glibc's may
+    differ in the last bit). The same draws passed in give the same map."""
+    n = 40 if dim == 1 else 9
+    if state:
+        rng, mut = ([-8.0, 8.0], [2]) if dim == 1 else ([-8.0, 8.0, -8.0, 8.0], [0, 2])
+    else:
+        rng, mut = ([20.0, 60.0], [1]) if dim == 1 else ([20.0, 60.0, 5.0, 15.0], [1, 0])
+    kw = dict(tMax=20.0, NT=0.2, nPts=n, h=0.01, eps=1e-7, initialConditions=[1.0, 1.0, 1.0], ranges=rng,
+              indicesOfMutVars=mut, transientTime=5.0, values=LORENZ, maxValue=maxValue, mutateState=state)
+    g = engine.lle_sweep_legacy("lorenz", dim, **kw)
+    draws = engine.legacy_lle_draws(int(state), n ** dim, 3)
+    o = oracle.lle_sweep_legacy(0, dim, oracle.GRID_STATE if state else 0, 20.0, 0.2, n, 0.01, 1e-7,
+                                [1.0, 1.0, 1.0], rng, mut, maxValue, 5.0, LORENZ, draws=draws)
+    assert np.allclose(g, o, rtol=1e-12, atol=1e-12), np.max(np.abs(g - o))
+    assert np.array_equal(engine.lle_sweep_legacy("lorenz", dim, draws=draws, **kw), g)
+
+
+def test_legacy_lle_draws(engine):
+    """The legacy kernels' twin draws: cuRAND seeded p + k (so neighbouring
+    points share draws, each a uniform in (0, 1] minus 0.5), and 0.5 sinf(p (k
+    p + 1) + 1) within CUDA's sinf error bound of the exact sine."""
+    d0 = engine.legacy_lle_draws(0, 200, 3)
+    assert np.array_equal(d0[1:, :2], d0[:-1, 1:])
+    assert (d0 > -0.5).all() and (d0 <= 0.5).all() and np.unique(d0).size == 202
+    d1 = engine.legacy_lle_draws(1, 200, 3)
+    p = np.arange(200, dtype=np.uint32)[:, None]
+    k = np.arange(3, dtype=np.uint32)[None, :]
+    arg = (p * (k * p + np.uint32(1)) + np.uint32(1)).astype(np.int32).astype(np.float32)
+    ref = 0.5 * np.sin(arg.astype(np.float64))
+    ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)  # of the halved value, in float
+    assert np.all(np.abs(d1 - ref) <= 3 * ulp)  # sinf's 2-ulp bound, plus the rounding of the float result
+
+
 def test_spectrum_log_axis_fp64_vs_oracle(engine, oracle):
     kw = dict(tMax=10.0, NT=0.1, nPts=12, h=0.01, eps=1e-8, initialConditions=[1.0, 1.0, 1.0], ranges=[10.0, 100.0],
               indicesOfMutVars=[1], transientTime=2.0, values=LORENZ)
@@ -228,7 +266,10 @@ def test_legacy_csv_bytes(engine, oracle, tmp_path):
         m = 12 if dim == 1 else 5
         p = tmp_path / f"{name}.csv"
         getattr(old, name)(*kw, m, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, rng, mut, 0, 0.0, 5.0, LORENZ, 3, p)
-        o = oracle.lle_sweep(0, dim, gm, 10.0, 0.1, m, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, mut, 5.0, LORENZ)
+        # the legacy LLE kernels' scheme, with the twin draws the engine made
+        draws = engine.legacy_lle_draws(gm, m ** dim, 3)
+        o = oracle.lle_sweep_legacy(0, dim, gm, 10.0, 0.1, m, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, mut, 0.0, 5.0,
+                                    LORENZ, draws=draws)
         got = p.read_text()
         if dim == 1:
             par = [rng[0] + k * ((rng[1] - rng[0]) / (m - 1)) for k in range(m)]

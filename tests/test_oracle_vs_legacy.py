@@ -13,9 +13,11 @@ and block count, and the legacy bifurcation1DIC / bifurcation2DIC,
 basinsOfAttraction and bifurcation1DForH kernels themselves (run one host
 thread per point; their hard-wired system is the sin3 plug-in's arithmetic)
 against the oracle's sweeps with the legacy loop (GRID_LEGACY_LOOP) and its
-basins features. Not pinned, by design: the legacy LLE kernels' twin
-directions (cuRAND in LLEKernelCUDA; sinf of the chunk-relative thread index
-in LSKernelCUDA)."""
+basins features, and the legacy LLE kernels (LLEKernelCUDA with its cuRAND
+uniforms supplied, LLEKernelICCUDA with its sinf twin) against
+orc_lle_sweep_legacy. Not pinned: the legacy spectrum's twin directions
+(sinf of the chunk-relative thread index in LSKernelCUDA); the spectrum runs
+from the unit vectors."""
 import math
 
 import numpy as np
@@ -156,3 +158,32 @@ def test_step_sweep_matches_legacy_kernels(leg, oracle, pre, rng):
     assert np.array_equal(L["counts"], np.maximum(o["counts"], 0))
     for k, c in enumerate(L["counts"]):
         assert np.array_equal(L["peaks"][k, :c], o["peaks"][k, :c]), k
+
+
+@pytest.mark.parametrize("maxValue", [0.0, 3.0])
+def test_lle1d_matches_legacy_kernel(leg, oracle, maxValue):
+    """LLE1D: LLEKernelCUDA, its cuRAND uniforms supplied (seed p + k for
+    component k of point p, so neighbouring points share draws), against
+    orc_lle_sweep_legacy given the same raw draws u[p + k] - 0.5, over the sin3
+    damping b; maxValue 3 stops runs of steps early."""
+    n = 30
+    u = np.random.default_rng(5).random(n + 2).astype(np.float32)
+    V = _sin3(0.2)
+    L = leg.lle(0, 1, n, 50.0, 0.5, 0.01, 1e-6, 20.0, [0.3, 0.1, 0.0], V, [0.1, 0.4], [1], maxValue, uniforms=u)
+    draws = np.array([[float(u[p + k]) - 0.5 for k in range(3)] for p in range(n)])
+    o = oracle.lle_sweep_legacy(5, 1, 0, 50.0, 0.5, n, 0.01, 1e-6, [0.3, 0.1, 0.0], [0.1, 0.4], [1], maxValue, 20.0,
+                                V, draws=draws)
+    assert np.array_equal(L, o)
+
+
+@pytest.mark.parametrize("dim", [1, 2])
+@pytest.mark.parametrize("maxValue", [0.0, 3.0])
+def test_lle_ic_matches_legacy_kernel(leg, oracle, dim, maxValue):
+    """LLE1DIC / LLE2DIC: LLEKernelICCUDA (twin 0.5 sinf(p (k p + 1) + 1),
+    normalised) against orc_lle_sweep_legacy over initial conditions."""
+    n, rng, mut = (30, [-3.0, 3.0], [0]) if dim == 1 else (8, [-3.0, 3.0, -3.0, 3.0], [0, 2])
+    V = _sin3(0.2)
+    L = leg.lle(1, dim, n, 50.0, 0.5, 0.01, 1e-6, 20.0, [0.3, 0.1, 0.0], V, rng, mut, maxValue)
+    o = oracle.lle_sweep_legacy(5, dim, oracle.GRID_STATE, 50.0, 0.5, n, 0.01, 1e-6, [0.3, 0.1, 0.0], rng, mut,
+                                maxValue, 20.0, V)
+    assert np.array_equal(L, o)
