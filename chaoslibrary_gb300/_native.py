@@ -68,6 +68,8 @@ _SIGS = {
     "chaos_lle_sweep": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle_sweep_legacy": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _D, _P, _I, _P, _P], _I),
     "chaos_legacy_lle_draws": ([_P, _I, C.c_longlong, _I, _P], _I),
+    "chaos_lyapunov_spectrum_legacy": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _D, _P, _I, _P, _P],
+                                       _I),
     "chaos_lyapunov_spectrum": ([_P, _I, _I, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _P], _I),
     "chaos_lle2d_checked": ([_P, _I, _D, _D, _I, _D, _D, _P, _I, _P, _P, _D, _P, _I, _D, _D, _P, _P, _P], _I),
     "chaos_basins_features": ([_P, _I, _D, _I, _D, _I, _P, _P, _P, _I, _D, _D, _P, _I, _I, _P, _P, _P, _P], _I),
@@ -639,11 +641,33 @@ def lle_sweep_legacy(system, dim, tMax, NT, nPts, h, eps, initialConditions, ran
     return out
 
 
+def lyapunov_spectrum_legacy(system, dim, tMax, NT, nPts, h, eps, initialConditions, ranges, indicesOfMutVars,
+                             transientTime, values, maxValue=0.0, mutateState=False, draws=None, out=None,
+                             stream=None, gridMode=0):
+    """The legacy library's LS1D / LS2D with its own kernel's scheme, FP64
+    (chaos_lyapunov_spectrum_legacy): [points, SIZE_X]. draws: raw twin
+    draws [points, SIZE_X, SIZE_X] (None: the legacy's own)."""
+    A = _Args()
+    ic = np.asarray(initialConditions, np.float64)
+    n = nPts ** dim
+    if out is None:
+        out = np.zeros((n, ic.size))
+    ex = _exec(FP64, {"spectrum": out}, stream)
+    vals = np.asarray(values, np.float64)
+    mode = gridMode | (GRID_STATE if mutateState else 0)
+    dr = None if draws is None else np.ascontiguousarray(draws, np.float64)
+    _check(lib().chaos_lyapunov_spectrum_legacy(C.byref(ex), _sys(system), dim, mode, tMax, NT, nPts, h, eps,
+                                                A.d(ic), ic.size, A.d(ranges), A.i(indicesOfMutVars), maxValue,
+                                                transientTime, A.d(vals), vals.size,
+                                                None if dr is None else A.d(dr), _out_ptr(out)))
+    return out
+
+
 def legacy_lle_draws(kind, n, nx, stream=None):
-    """The legacy LLE kernels' raw twin draws [n, nx] drawn on the device
-    (chaos_legacy_lle_draws): kind 0 parameter grids (cuRAND), 1
-    initial-condition grids (sinf)."""
-    out = np.zeros((n, nx))
+    """The legacy kernels' raw twin draws drawn on the device
+    (chaos_legacy_lle_draws): kind 0 parameter-grid LLE (cuRAND) and 1
+    initial-condition LLE (sinf), [n, nx]; kind 2 the spectrum, [n, nx, nx]."""
+    out = np.zeros((n, nx, nx) if kind == 2 else (n, nx))
     ex = _exec(FP64, {"draws": out}, stream)
     _check(lib().chaos_legacy_lle_draws(C.byref(ex), kind, n, nx, _out_ptr(out)))
     return out

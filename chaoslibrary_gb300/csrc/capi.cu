@@ -677,6 +677,47 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     return c.finish(rc);
 }
 
+// The legacy LLE kernels' scheme (legacy_lle.cuh), FP64: the LLE (spectrum
+// false, out[p]) or the spectrum (out[p*SIZE_X + j]). draws: the raw twin
+// draws (SIZE_X per point, SIZE_X^2 for the spectrum), host or device memory, or null.
+static int run_legacy_scheme(const chaos_exec* ex, bool spectrum, int system, int dim, int gridMode, double tMax,
+                             double NT, int nPts, double h, double eps, const double* initialConditions,
+                             int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                             double maxValue, double transientTime, const double* values, int amountOfValues,
+                             const double* draws, double* out) {
+    int rc = CHAOS_OK;
+    if (!out) return set_error(CHAOS_E_ARGS, "null argument");
+    LleParams L;
+    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
+                       indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
+        return rc;
+    const double blocks = tMax / NT;
+    if (!(blocks >= 0) || blocks > 2.0e9) return set_error(CHAOS_E_ARGS, "tMax / NT must fit in int");
+    L.legacyLoop = 1;
+    L.legacyBlocks = (int)blocks;
+    L.maxValue = maxValue;
+    L.twin = 0;
+    const int nx = amountOfInitialConditions;
+    Call c;
+    if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);
+    if (draws) {
+        const size_t bytes = (size_t)L.nPoints * nx * (spectrum ? nx : 1) * sizeof(double);
+        double* dDraws = (double*)c.alloc(bytes);
+        if (c.failed) return c.finish(CHAOS_E_NOMEM);
+        cudaError_t e = cudaMemcpyAsync(dDraws, draws, bytes, cudaMemcpyDefault, c.stream);
+        if (e != cudaSuccess) return c.finish(cuda_error(e, "twin draws upload"));
+        L.draws = dDraws;
+    }
+    const size_t outBytes = (size_t)L.nPoints * (spectrum ? nx : 1) * sizeof(double);
+    double* dOut = (double*)c.output(out, outBytes);
+    if (c.failed) return c.finish(CHAOS_E_NOMEM);
+    cudaError_t e = spectrum ? launch_spectrum_f64(L, dOut, c.stream) : run_lle(CHAOS_FP64, L, dOut, c.stream);
+    if (e != cudaSuccess) return c.finish(cuda_error(e, "legacy LLE kernel"));
+    rc = c.to_host(out, dOut, outBytes);
+    return c.finish(rc);
+}
+
 int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT, int nPts,
                     double h, double eps, const double* initialConditions, int amountOfInitialConditions,
                     const double* ranges, const int* indicesOfMutVars, double transientTime, const double* values,
@@ -708,49 +749,35 @@ int chaos_lle_sweep_legacy(const chaos_exec* ex, int system, int dim, int gridMo
                            int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
                            double maxValue, double transientTime, const double* values, int amountOfValues,
                            const double* draws, double* lle) {
-    int rc = CHAOS_OK;
-    if (!lle) return set_error(CHAOS_E_ARGS, "null argument");
-    LleParams L;
-    if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                       indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
-        return rc;
-    const double blocks = tMax / NT;
-    if (!(blocks >= 0) || blocks > 2.0e9) return set_error(CHAOS_E_ARGS, "tMax / NT must fit in int");
-    L.legacyLoop = 1;
-    L.legacyBlocks = (int)blocks;
-    L.maxValue = maxValue;
-    L.twin = 0;
-    Call c;
-    if ((rc = c.begin(ex))) return rc;
-    if ((rc = upload_log_axes(c, gridMode, dim, nPts, ranges, L.table))) return c.finish(rc);
-    if (draws) {
-        const size_t bytes = (size_t)L.nPoints * amountOfInitialConditions * sizeof(double);
-        double* dDraws = (double*)c.alloc(bytes);
-        if (c.failed) return c.finish(CHAOS_E_NOMEM);
-        cudaError_t e = cudaMemcpyAsync(dDraws, draws, bytes, cudaMemcpyDefault, c.stream);
-        if (e != cudaSuccess) return c.finish(cuda_error(e, "twin draws upload"));
-        L.draws = dDraws;
-    }
-    double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
-    if (c.failed) return c.finish(CHAOS_E_NOMEM);
-    cudaError_t e = run_lle(CHAOS_FP64, L, dOut, c.stream);
-    if (e != cudaSuccess) return c.finish(cuda_error(e, "legacy LLE kernel"));
-    rc = c.to_host(lle, dOut, L.nPoints * sizeof(double));
-    return c.finish(rc);
+    return run_legacy_scheme(ex, false, system, dim, gridMode, tMax, NT, nPts, h, eps, initialConditions,
+                             amountOfInitialConditions, ranges, indicesOfMutVars, maxValue, transientTime, values,
+                             amountOfValues, draws, lle);
+}
+
+int chaos_lyapunov_spectrum_legacy(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
+                                   int nPts, double h, double eps, const double* initialConditions,
+                                   int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                                   double maxValue, double transientTime, const double* values, int amountOfValues,
+                                   const double* draws, double* spectrum) {
+    if (system == SYS_USER) return set_error(CHAOS_E_UNSUPPORTED, "the spectrum runs on the built-in systems");
+    return run_legacy_scheme(ex, true, system, dim, gridMode, tMax, NT, nPts, h, eps, initialConditions,
+                             amountOfInitialConditions, ranges, indicesOfMutVars, maxValue, transientTime, values,
+                             amountOfValues, draws, spectrum);
 }
 
 int chaos_legacy_lle_draws(const chaos_exec* ex, int kind, long long n, int nx, double* draws) {
-    if ((kind != 0 && kind != 1) || n < 0 || nx < 1 || nx > kMaxState || (n > 0 && !draws))
+    if (kind < 0 || kind > 2 || n < 0 || nx < 1 || nx > kMaxState || (n > 0 && !draws))
         return set_error(CHAOS_E_ARGS, "bad twin-draw arguments");
     if (n == 0) return CHAOS_OK;
+    const size_t bytes = (size_t)n * nx * (kind == 2 ? nx : 1) * sizeof(double);
     Call c;
     int rc = c.begin(ex);
     if (rc) return rc;
-    double* d = (double*)c.output(draws, (size_t)n * nx * sizeof(double));
+    double* d = (double*)c.output(draws, bytes);
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e = launch_legacy_draws(kind, n, nx, d, c.stream);
     if (e != cudaSuccess) return c.finish(cuda_error(e, "twin draws"));
-    rc = c.to_host(draws, d, (size_t)n * nx * sizeof(double));
+    rc = c.to_host(draws, d, bytes);
     return c.finish(rc);
 }
 

@@ -338,19 +338,19 @@ static int legacy_lle(int dim, int gridMode, double tMax, double NT, int nPts, d
 // (debri/hostLibrary.cu:3927-3936). LS2D: one file per exponent,
 // OUT_FILE_PATH + "<k+1>.csv", the range header then the matrix rule
 // (debri/hostLibrary.cu:4030-4040, 4078-4094).
+// The legacy spectrum kernel's scheme (chaos_lyapunov_spectrum_legacy, FP64).
 static int legacy_ls(int dim, double tMax, double NT, int nPts, double h, double eps,
                      const double* initialConditions, int amountOfInitialConditions, const double* ranges,
-                     const int* indicesOfMutVars, double transientTime, const double* values, int amountOfValues,
-                     const char* OUT_FILE_PATH) {
+                     const int* indicesOfMutVars, double maxValue, double transientTime, const double* values,
+                     int amountOfValues, const char* OUT_FILE_PATH) {
     if (nPts < 1 || amountOfInitialConditions < 1) return chaos::set_error(CHAOS_E_ARGS, "bad sweep arguments");
     const long long n = dim == 2 ? (long long)nPts * nPts : nPts;
     const int nx = amountOfInitialConditions;
     std::vector<double> sp((size_t)n * nx);
     chaos_exec ex = lle_exec();
-    if (ex.precision == CHAOS_FF32) ex.precision = CHAOS_FP64;  // the spectrum has no float-float kernel
-    int rc = chaos_lyapunov_spectrum(&ex, active_system(), dim, 0, tMax, NT, nPts, h, eps, initialConditions,
-                                     amountOfInitialConditions, ranges, indicesOfMutVars, transientTime, values,
-                                     amountOfValues, sp.data());
+    int rc = chaos_lyapunov_spectrum_legacy(&ex, active_system(), dim, 0, tMax, NT, nPts, h, eps, initialConditions,
+                                            amountOfInitialConditions, ranges, indicesOfMutVars, maxValue,
+                                            transientTime, values, amountOfValues, nullptr, sp.data());
     if (rc) return rc;
     if (dim == 1) {
         std::ofstream o(OUT_FILE_PATH);
@@ -464,9 +464,8 @@ int chaos_compat_LS1D(double tMax, double NT, int nPts, double h, double eps, co
                       int amountOfValues, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
         (void)writableVar;
-        (void)maxValue;
         return legacy_ls(1, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                         indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+                         indicesOfMutVars, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH);
     });
 }
 
@@ -476,9 +475,8 @@ int chaos_compat_LS2D(double tMax, double NT, int nPts, double h, double eps, co
                       int amountOfValues, const char* OUT_FILE_PATH) {
     return guarded([&]() -> int {
         (void)writableVar;
-        (void)maxValue;
         return legacy_ls(2, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
-                         indicesOfMutVars, transientTime, values, amountOfValues, OUT_FILE_PATH);
+                         indicesOfMutVars, maxValue, transientTime, values, amountOfValues, OUT_FILE_PATH);
     });
 }
 

@@ -54,10 +54,14 @@ __global__ void __launch_bounds__(kBlock) lle_legacy_kernel(LleParams L, double*
     out[o] = lle_point_legacy<S>(L, L.pBegin + o);
 }
 
+// kind 0 / 1: out[p*nx + k] = legacy_twin_draw; kind 2: out[(p*nx + j)*nx + i] = legacy_spectrum_draw
 __global__ void legacy_draws_kernel(int kind, long long n, int nx, double* out) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n * nx) return;
-    out[t] = legacy_twin_draw(kind, t / nx, (int)(t % nx));
+    const long long per = kind == 2 ? (long long)nx * nx : nx;
+    if (t >= n * per) return;
+    const long long p = t / per;
+    const int r = (int)(t % per);
+    out[t] = kind == 2 ? legacy_spectrum_draw(p, r % nx, r / nx) : legacy_twin_draw(kind, p, r);
 }
 
 // Benettin blocks from caller-supplied starting states (the reference's
@@ -86,6 +90,14 @@ __global__ void __launch_bounds__(kBlock) spectrum_kernel(LleParams L, double* o
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= L.nPoints) return;
     spectrum_point_full<S>(L, L.pBegin + o, out);
+}
+
+// The legacy library's spectrum kernel's scheme (L.legacyLoop).
+template <int S>
+__global__ void __launch_bounds__(kBlock) spectrum_legacy_kernel(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    spectrum_point_legacy<S>(L, L.pBegin + o, out);
 }
 
 // FP64 LLE of the points list[0, *count): out[k] (scatter = 0) or out[list[k]]
@@ -298,7 +310,7 @@ cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
 
 cudaError_t launch_legacy_draws(int kind, long long n, int nx, double* out, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    legacy_draws_kernel<<<grid_for(n * nx), kBlock, 0, st>>>(kind, n, nx, out);
+    legacy_draws_kernel<<<grid_for(n * (kind == 2 ? (long long)nx * nx : nx)), kBlock, 0, st>>>(kind, n, nx, out);
     note_launch();
     return cudaGetLastError();
 }
@@ -313,7 +325,12 @@ cudaError_t launch_lle_states_f64(const LleParams& L, const double* states, doub
 
 cudaError_t launch_spectrum_f64(const LleParams& L, double* out, cudaStream_t st) {
     if (L.nPoints <= 0) return cudaSuccess;
-#define CALL(S) (spectrum_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out), note_launch())
+#define CALL(S)                                                                    \
+    {                                                                              \
+        if (L.legacyLoop) spectrum_legacy_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
+        else spectrum_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
+        note_launch();                                                             \
+    }
     CHAOS_SYSTEM_SWITCH(L.system, CALL)
 #undef CALL
     return cudaGetLastError();

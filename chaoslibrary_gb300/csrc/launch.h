@@ -111,7 +111,8 @@ cudaError_t launch_basins_f64(const SweepParams& P, const BasinsOut& O, cudaStre
 cudaError_t launch_basins_f32(const SweepParams& P, const BasinsOut& O, cudaStream_t st);
 cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st);
 // the legacy LLE kernels' raw twin draws of points [0, n) (kern_f64.cu): kind 0
-// parameter grids (cuRAND), 1 initial-condition grids (sinf); out[p*nx + k]
+// parameter grids (cuRAND), 1 initial-condition grids (sinf), out[p*nx + k];
+// kind 2 the spectrum's, out[(p*nx + j)*nx + i] for component i of twin j
 cudaError_t launch_legacy_draws(int kind, long long n, int nx, double* out, cudaStream_t st);
 cudaError_t launch_lle_f32(const LleParams& L, double* out, cudaStream_t st);
 // float-float base trajectory, FP32 twin difference (kern_ff.cu; RK4 systems)

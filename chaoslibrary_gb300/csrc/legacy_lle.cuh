@@ -1,9 +1,10 @@
-// LLE of the legacy library's LLE analyses (FP64): the scheme of its kernels
-// LLEKernelCUDA (debri/cudaLibrary.cu:1897-2031, LLE1D: a grid of
-// parameters) and LLEKernelICCUDA (:2034-2139, LLE1DIC / LLE2DIC: a grid of
-// initial conditions), which differs from the LLE map's (LLE/src/LLECUDA.cu)
-// in its block count, its twin start and its renormalisation arithmetic.
-// Included by the FP64 translation units (built-in and user systems).
+// LLE and Lyapunov spectrum of the legacy library's analyses (FP64): the
+// scheme of its kernels LLEKernelCUDA (debri/cudaLibrary.cu:1897-2031, LLE1D:
+// a grid of parameters), LLEKernelICCUDA (:2034-2139, LLE1DIC / LLE2DIC: a
+// grid of initial conditions) and LSKernelCUDA (:2189-2330, LS1D / LS2D),
+// which differs from the LLE map's (LLE/src/LLECUDA.cu) in its block count,
+// its twin start and its renormalisation arithmetic. Included by the FP64
+// translation units (built-in and user systems).
 #pragma once
 
 #include <curand_kernel.h>
@@ -97,6 +98,104 @@ __device__ __forceinline__ double lle_point_legacy(const LleParams& L, long long
         }
     }
     return result / L.tMax;
+}
+
+// The raw draw of component i of twin j of point p of the legacy spectrum
+// (LSKernelCUDA, :2250): sinf of 0.2171828 (i+1)(j+1) + p + (0.2171828 +
+// i j p), the argument in FP64 rounded to float, times 0.5.
+__device__ __forceinline__ double legacy_spectrum_draw(long long p, int i, int j) {
+    const int idx = (int)p;
+    const double arg = 0.2171828 * (i + 1) * (j + 1) + idx + (0.2171828 + i * j * idx);
+    return (double)sinf((float)arg) * 0.5;
+}
+
+// Classical Gram-Schmidt of the rows of v as gramSchmidtProcess
+// (:2141-2187) computes it: w_j = v_j minus, for m < j, <v_j, w_m> / <w_m,
+// w_m> w_m (0 for a zero w_m); then u_j = w_j / |w_j| (0 where |w_j| = 0)
+// and nrm[j] = |w_j|.
+template <int N>
+__device__ __forceinline__ void legacy_gram_schmidt(const double (&v)[N][N], double (&u)[N][N], double (&nrm)[N]) {
+    double w[N][N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) w[j][i] = v[j][i];
+#pragma unroll
+        for (int m = 0; m < j; ++m) {
+            double num = 0.0, den = 0.0;
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                num = num + v[j][i] * w[m][i];
+                den = den + w[m][i] * w[m][i];
+            }
+            const double frac = den == 0.0 ? 0.0 : num / den;
+#pragma unroll
+            for (int i = 0; i < N; ++i) w[j][i] = w[j][i] - frac * w[m][i];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        double n2 = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) n2 = n2 + w[j][i] * w[j][i];
+        nrm[j] = sqrt(n2);
+#pragma unroll
+        for (int i = 0; i < N; ++i) u[j][i] = nrm[j] == 0.0 ? 0.0 : w[j][i] / nrm[j];
+    }
+}
+
+// Lyapunov spectrum of point p (L.legacyLoop), LSKernelCUDA's scheme: twin
+// directions from the normalised raw draws (draws[(p*N + j)*N + i], or
+// legacy_spectrum_draw), the transient, the directions orthonormalised and
+// the twins started at x + eps u_j; then L.legacyBlocks blocks of L.ntp steps
+// of the orbit and of every twin (each run stopping early as
+// legacy_lle_run), the differences y_j - x through Gram-Schmidt, exponent j
+// adding log(|w_j| / eps) and twin j restarting at x + eps u_j; the sums
+// divided by tMax. out[p*N + j].
+template <int S>
+__device__ __forceinline__ void spectrum_point_legacy(const LleParams& L, long long p, double* out) {
+    constexpr int N = Traits<S>::NX, NA = Traits<S>::NA;
+    double x[N], y[N][N], z[N][N], a[NA], sum[N], nrm[N];
+    lle_load<N, NA>(L, p, x, a);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        double zp = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            z[j][i] = L.draws ? L.draws[(p * N + j) * N + i] : legacy_spectrum_draw(p, i, j);
+            zp = zp + z[j][i] * z[j][i];
+        }
+        zp = sqrt(zp);
+#pragma unroll
+        for (int i = 0; i < N; ++i) z[j][i] = z[j][i] / zp;
+    }
+    const StepCtx<double> c(L.h);
+    legacy_lle_run<S>(x, a, c, L.trans, L.maxValue);
+    legacy_gram_schmidt<N>(z, y, nrm);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        sum[j] = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) y[j][i] = y[j][i] * L.eps + x[i];
+    }
+    for (int b = 0; b < L.legacyBlocks; ++b) {
+        legacy_lle_run<S>(x, a, c, L.ntp, L.maxValue);
+#pragma unroll
+        for (int j = 0; j < N; ++j) legacy_lle_run<S>(y[j], a, c, L.ntp, L.maxValue);
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+#pragma unroll
+            for (int i = 0; i < N; ++i) y[j][i] = y[j][i] - x[i];
+        legacy_gram_schmidt<N>(y, z, nrm);
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            sum[j] = sum[j] + log(nrm[j] / L.eps);
+#pragma unroll
+            for (int i = 0; i < N; ++i) y[j][i] = x[i] + z[j][i] * L.eps;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) out[p * N + j] = sum[j] / L.tMax;
 }
 
 }  // namespace chaos

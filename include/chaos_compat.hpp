@@ -52,9 +52,9 @@ int basinsOfAttraction_2(const double tMax, const int nPts, const double h, cons
 // The legacy library's analyses (debri/hostLibrary.cuh:30-400, namespace
 // old_library) with their signatures and file formats, on the engine's sweeps:
 // the *IC variants sweep initial conditions (CHAOS_GRID_STATE), the step-size
-// sweep runs the step on the legacy log scale, the LLE analyses run the
-// legacy LLE kernels' scheme in FP64 (chaos_lle_sweep_legacy), the LS
-// analyses the Gram-Schmidt spectrum. The bifurcation analyses run the legacy
+// sweep runs the step on the legacy log scale, the LLE and LS analyses run the
+// legacy kernels' schemes in FP64 (chaos_lle_sweep_legacy,
+// chaos_lyapunov_spectrum_legacy). The bifurcation analyses run the legacy
 // per-point loop in FP64 (CHAOS_GRID_LEGACY_LOOP);
 // the peak rule and the per-point clustering are the same in both libraries;
 // basinsOfAttraction is the current library's basins map (its loop is the

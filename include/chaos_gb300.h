@@ -262,13 +262,36 @@ int chaos_lle_sweep_legacy(const chaos_exec* ex, int system, int dim, int gridMo
                            const double* draws, double* lle);
 
 /*
+ * The legacy library's LS1D / LS2D with its own kernel's scheme, in FP64
+ * (LSKernelCUDA, debri/cudaLibrary.cu:2189-2330; built-in systems). Grids and
+ * spectrum[p*SIZE_X + j] as chaos_lyapunov_spectrum. Per point:
+ *   - twin j starts along row j of the raw draws (chaos_legacy_lle_draws kind
+ *     2, or draws[(p*SIZE_X + j)*SIZE_X + i]), each row normalised, after the
+ *     transient the rows orthonormalised by classical Gram-Schmidt, twin j at
+ *     x + eps*u_j;
+ *   - (int)(tMax / NT) blocks of NT / h steps of the orbit and of every twin,
+ *     each run stopping early as in chaos_lle_sweep_legacy;
+ *   - the differences through Gram-Schmidt, exponent j adding
+ *     log(|w_j| / eps), twin j restarting at x + eps*w_j/|w_j|;
+ *   - the sums divided by tMax.
+ */
+int chaos_lyapunov_spectrum_legacy(const chaos_exec* ex, int system, int dim, int gridMode, double tMax, double NT,
+                                   int nPts, double h, double eps, const double* initialConditions,
+                                   int amountOfInitialConditions, const double* ranges, const int* indicesOfMutVars,
+                                   double maxValue, double transientTime, const double* values, int amountOfValues,
+                                   const double* draws, double* spectrum);
+
+/*
  * The raw twin-direction draws of the legacy LLE kernels for points [0, n)
  * of a one-chunk grid (the legacy thread index is the point index), nx
  * components each: draws[p*nx + k].
  *   kind 0 (parameter grids, LLEKernelCUDA): the uniform of cuRAND's default
  *     generator seeded p + k (curand_init(p + k, 0, 0)), minus 0.5;
  *   kind 1 (initial-condition grids, LLEKernelICCUDA): 0.5 * sinf(p * (k * p
- *     + 1) + 1), the integer expression in 32-bit wrap-around arithmetic.
+ *     + 1) + 1), the integer expression in 32-bit wrap-around arithmetic;
+ *   kind 2 (the spectrum, LSKernelCUDA): nx rows of nx, draws[(p*nx + j)*nx +
+ *     i] = 0.5 * sinf(0.2171828 (i+1)(j+1) + p + (0.2171828 + i j p)), the
+ *     argument in FP64 rounded to float.
  */
 int chaos_legacy_lle_draws(const chaos_exec* ex, int kind, long long n, int nx, double* draws);
 

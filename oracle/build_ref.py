@@ -42,7 +42,7 @@ LEGACY_FUNCS = ["getValueByIdx", "getValueByIdxLog", "peakFinder", "projectionOp
                 "calculateDiscreteModel", "loopCalculateDiscreteModel", "loopCalculateDiscreteModel_int",
                 "distance", "dbscan", "calculateDiscreteModelICCUDA", "calculateDiscreteModelCUDA_H",
                 "peakFinderCUDA", "peakFinderCUDA_H", "avgPeakFinderCUDA", "dbscanCUDA", "LLEKernelCUDA",
-                "LLEKernelICCUDA"]
+                "LLEKernelICCUDA", "LSKernelCUDA"]
 
 # plug-in systems: name -> (header text of a systems.cuh stand-in)
 PLUGINS = {

@@ -25,7 +25,8 @@
 //       :604-680, is the basins loop above, token for token), and
 //       calculateDiscreteModelCUDA_H :955-1000 over loopCalculateDiscreteModel :472-527
 //   * the legacy library's LLE kernels: LLEKernelCUDA debri/cudaLibrary.cu:1897-2031,
-//       LLEKernelICCUDA :2034-2139 (orc_lle_sweep_legacy)
+//       LLEKernelICCUDA :2034-2139 (orc_lle_sweep_legacy), and its spectrum
+//       kernel LSKernelCUDA :2189-2330 (orc_lyapunov_spectrum_legacy)
 // Unlike the engine (which streams samples through a peak state machine and
 // never stores a trajectory), the oracle records every trajectory into an
 // array and scans it exactly as the reference does.
@@ -650,6 +651,97 @@ int orc_lyapunov_spectrum(int sys, int dim, int gridMode, double tMax, double NT
                 const double nrm = std::sqrt(n2);
                 sum[j] += std::log(nrm / eps);
                 for (int i = 0; i < nx; ++i) y[j][i] = x[i] + (nrm == 0.0 ? 0.0 : g[j][i] / nrm) * eps;
+            }
+        }
+        for (int j = 0; j < nx; ++j) out[(p - pBegin) * nx + j] = sum[j] / tMax;
+    }
+    return 0;
+}
+
+// Classical Gram-Schmidt of the rows of v (n x n), as gramSchmidtProcess
+// (debri/cudaLibrary.cu:2141-2187): w_j = v_j minus its projections
+// <v_j, w_m>/<w_m, w_m> w_m on the earlier w_m, u_j = w_j/|w_j| (0 for a zero
+// w_j), nrm[j] = |w_j|.
+static void gram_schmidt(const double (*v)[kMaxX], double (*u)[kMaxX], double* nrm, int n) {
+    double w[kMaxX][kMaxX];
+    for (int j = 0; j < n; ++j) {
+        for (int i = 0; i < n; ++i) w[j][i] = v[j][i];
+        for (int m = 0; m < j; ++m) {
+            double num = 0.0, den = 0.0;
+            for (int i = 0; i < n; ++i) {
+                num += v[j][i] * w[m][i];
+                den += w[m][i] * w[m][i];
+            }
+            const double frac = den == 0.0 ? 0.0 : num / den;
+            for (int i = 0; i < n; ++i) w[j][i] -= frac * w[m][i];
+        }
+    }
+    for (int j = 0; j < n; ++j) {
+        double n2 = 0.0;
+        for (int i = 0; i < n; ++i) n2 += w[j][i] * w[j][i];
+        nrm[j] = std::sqrt(n2);
+        for (int i = 0; i < n; ++i) u[j][i] = nrm[j] == 0.0 ? 0.0 : w[j][i] / nrm[j];
+    }
+}
+
+// The legacy library's LS1D / LS2D with its own kernel's scheme
+// (LSKernelCUDA, debri/cudaLibrary.cu:2189-2330): twin j along row j of the
+// raw draws (draws[(p*nx + j)*nx + i]; null: restated from the kernel, 0.5 *
+// sinf((float)(0.2171828 (i+1)(j+1) + p + (0.2171828 + i j p))) through the
+// C library's sinf), each row normalised; after the transient the rows
+// orthonormalised and twin j started at x + eps u_j; (int)(tMax / NT) blocks
+// of (int)(NT / h) steps (runs stopping early as legacy_lle_run), the
+// differences through Gram-Schmidt, exponent j adding log(|w_j| / eps) and
+// twin j restarting at x + eps u_j; sums / tMax. out[(p - pBegin)*nx + j].
+int orc_lyapunov_spectrum_legacy(int sys, int dim, int gridMode, double tMax, double NT, int nPts, double h,
+                                 double eps, const double* ic, const double* ranges, const int* mut, double maxValue,
+                                 double transientTime, const double* values, const double* draws, long long pBegin,
+                                 long long pEnd, double* out, int nthreads) {
+    const int ntp = (int)(NT / h);
+    const int trans = (int)(transientTime / h);
+    const int blocks = (int)(tMax / NT);
+    if (ntp < 0 || (dim != 1 && dim != 2)) return 1;
+    const int nx = chaos::system_nx(sys), na = chaos::system_na(sys);
+    const long long total = dim == 2 ? (long long)nPts * nPts : nPts;
+    if (pEnd < 0 || pEnd > total) pEnd = total;
+    set_threads(nthreads);
+    const StepCtx<double> c(h);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long p = pBegin; p < pEnd; ++p) {
+        double x[kMaxX], y[kMaxX][kMaxX], z[kMaxX][kMaxX], a[32], sum[kMaxX], nrm[kMaxX];
+        for (int k = 0; k < nx; ++k) x[k] = ic[k];
+        for (int k = 0; k < na; ++k) a[k] = values[k];
+        lle_grid_point(dim, gridMode, p, nPts, ranges, mut, x, a);
+        const int idx = (int)p;
+        for (int j = 0; j < nx; ++j) {
+            double zp = 0;
+            for (int i = 0; i < nx; ++i) {
+                if (draws) {
+                    z[j][i] = draws[(p * nx + j) * nx + i];
+                } else {
+                    const double arg = 0.2171828 * (i + 1) * (j + 1) + idx + (0.2171828 + i * j * idx);
+                    z[j][i] = (double)sinf((float)arg) * 0.5;
+                }
+                zp += z[j][i] * z[j][i];
+            }
+            zp = std::sqrt(zp);
+            for (int i = 0; i < nx; ++i) z[j][i] = z[j][i] / zp;
+        }
+        legacy_lle_run(sys, x, a, c, trans, maxValue);
+        gram_schmidt(z, y, nrm, nx);
+        for (int j = 0; j < nx; ++j) {
+            sum[j] = 0.0;
+            for (int i = 0; i < nx; ++i) y[j][i] = y[j][i] * eps + x[i];
+        }
+        for (int b = 0; b < blocks; ++b) {
+            legacy_lle_run(sys, x, a, c, ntp, maxValue);
+            for (int j = 0; j < nx; ++j) legacy_lle_run(sys, y[j], a, c, ntp, maxValue);
+            for (int j = 0; j < nx; ++j)
+                for (int i = 0; i < nx; ++i) y[j][i] = y[j][i] - x[i];
+            gram_schmidt(y, z, nrm, nx);
+            for (int j = 0; j < nx; ++j) {
+                sum[j] += std::log(nrm[j] / eps);
+                for (int i = 0; i < nx; ++i) y[j][i] = x[i] + z[j][i] * eps;
             }
         }
         for (int j = 0; j < nx; ++j) out[(p - pBegin) * nx + j] = sum[j] / tMax;

@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
         L.orc_lle_sweep_legacy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
                                            C.c_double, _dp, _dp, _ip, C.c_double, C.c_double, _dp, C.c_void_p,
                                            C.c_longlong, C.c_longlong, _dp, C.c_int]
+        L.orc_lyapunov_spectrum_legacy.argtypes = L.orc_lle_sweep_legacy.argtypes
         L.orc_basins_features.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _ip, C.c_int,
                                           C.c_double, C.c_double, _dp, C.c_int, C.c_longlong, C.c_longlong, _ip,
                                           _dp, _dp, C.c_void_p, C.c_void_p, C.c_int]
@@ -215,6 +216,23 @@ def lle_sweep_legacy(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ra
     if rc:
         raise ValueError("bad legacy LLE arguments")
     return out
+
+
+def lyapunov_spectrum_legacy(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ranges, mut, maxValue,
+                             transientTime, values, draws=None, p_begin=0, p_end=-1, nthreads=0) -> np.ndarray:
+    """The legacy spectrum kernel's scheme (orc_lyapunov_spectrum_legacy):
+    [points, SIZE_X]; draws: raw twin draws [points, SIZE_X, SIZE_X]."""
+    total = nPts * nPts if dim == 2 else nPts
+    p_end = total if p_end < 0 else p_end
+    nx = len(ic)
+    out = np.zeros((p_end - p_begin) * nx, np.float64)
+    dr = None if draws is None else _d(draws).ravel()
+    rc = lib().orc_lyapunov_spectrum_legacy(system, dim, grid_mode, tMax, NT, nPts, h, eps, _d(ic), _d(ranges),
+                                            _i(mut), maxValue, transientTime, _d(values),
+                                            None if dr is None else dr.ctypes.data, p_begin, p_end, out, nthreads)
+    if rc:
+        raise ValueError("bad legacy spectrum arguments")
+    return out.reshape(p_end - p_begin, nx)
 
 
 def lyapunov_spectrum(system: int, dim, grid_mode, tMax, NT, nPts, h, eps, ic, ranges, mut, transientTime,
@@ -446,7 +464,9 @@ class LegacyLib:
                                      C.c_int, C.c_double, _ip, _dp, C.c_int, C.POINTER(C.c_int)]
         L.leg_lle.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                               _dp, C.c_int, _dp, C.c_int, _dp, _ip, C.c_double, C.c_void_p, _dp]
-        for f in (L.leg_ic_bifurcation, L.leg_basins_v1, L.leg_step_sweep, L.leg_lle):
+        L.leg_ls.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, _dp,
+                             C.c_int, _dp, C.c_int, _dp, _ip, C.c_double, _dp]
+        for f in (L.leg_ic_bifurcation, L.leg_basins_v1, L.leg_step_sweep, L.leg_lle, L.leg_ls):
             f.restype = C.c_int
 
     def value_log(self, idx, nPts, start, finish, dim=0):
@@ -513,6 +533,17 @@ class LegacyLib:
         if rc:
             raise ValueError("bad legacy LLE arguments")
         return out
+
+    def ls(self, dim, nPts, tMax, NT, h, eps, transientTime, ic, values, ranges, mut, maxValue):
+        """The legacy LS1D / LS2D kernel LSKernelCUDA: [points, SIZE_X]."""
+        n = nPts ** dim
+        ic, vals = _d(ic), _d(values)
+        out = np.zeros(n * ic.size)
+        rc = self.L.leg_ls(dim, nPts, tMax, NT, h, eps, transientTime, ic, ic.size, vals, vals.size, _d(ranges),
+                           _i(mut), maxValue, out)
+        if rc:
+            raise ValueError("bad legacy spectrum arguments")
+        return out.reshape(n, ic.size)
 
     def ls_replay(self, system, x0, a, h, trans, ntp, nblocks, eps, tmax, directions):
         n = len(x0)

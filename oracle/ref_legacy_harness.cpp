@@ -12,13 +12,13 @@
 //   calculateDiscreteModelICCUDA (:1022-1116), calculateDiscreteModelCUDA_H
 //   (:955-1016), peakFinderCUDA (:1345-1367), peakFinderCUDA_H (:1396-1412),
 //   avgPeakFinderCUDA (:2334-2380), dbscanCUDA (:1835-1863), LLEKernelCUDA
-//   (:1897-2031) and LLEKernelICCUDA (:2034-2139).
+//   (:1897-2031), LLEKernelICCUDA (:2034-2139) and LSKernelCUDA (:2189-2330).
 // leg_ls_replay re-sequences the block loop of LSKernelCUDA (:2293-2327) on
 // the host around the verbatim Gram-Schmidt: the legacy kernel integrates a
 // system hard-wired into the legacy sources and starts its twins from sinf of
 // the chunk-relative thread index, so the replay takes the orbit step, the
 // twin start and the block count from its caller. leg_ic_bifurcation,
-// leg_basins_v1, leg_step_sweep and leg_lle run the legacy kernels
+// leg_basins_v1, leg_step_sweep, leg_lle and leg_ls run the legacy kernels
 // themselves, one host "thread" per point (block size 1, one chunk of all
 // points), in the order the legacy host functions launch them. LLEKernelCUDA
 // draws its twin direction from cuRAND: here curand_init keeps the seed and
@@ -254,6 +254,26 @@ int leg_lle(int kind, int dim, int nPts, double tMax, double NT, double h, doubl
                                                 maxValue, out);
     }
     g_uniforms = nullptr;
+    return 0;
+}
+
+// The legacy LS1D / LS2D kernel (LSKernelCUDA, debri/hostLibrary.cu:3829-4111)
+// over all n = nPts^dim points of a parameter grid: (int)(tMax / NT) blocks,
+// the transient of (int)(transientTime / h) steps. out[n][nIC].
+int leg_ls(int dim, int nPts, double tMax, double NT, double h, double eps, double transientTime, const double* ic,
+           int nIC, const double* values, int nValues, const double* ranges, const int* mut, double maxValue,
+           double* out) {
+    const int blocks = tMax / NT;
+    const int S = transientTime / h;
+    const long long n = dim == 1 ? (long long)nPts : (long long)nPts * nPts;
+    if (3 * nIC + 2 * nIC * nIC + nValues > 4096 || n > 0x7fffffffLL) return 1;
+    std::vector<double> rng(ranges, ranges + 2 * dim), x0(ic, ic + nIC), a(values, values + nValues);
+    std::vector<int> mv(mut, mut + dim);
+    for (long long k = 0; k < n; ++k) {
+        as_thread(k);
+        legacy_src::legacy::LSKernelCUDA(nPts, (int)n, NT, tMax, blocks, 0, S, dim, rng.data(), h, eps, mv.data(),
+                                         x0.data(), nIC, a.data(), nValues, tMax / NT, 1, 0, maxValue, out);
+    }
     return 0;
 }
 

@@ -200,6 +200,22 @@ def test_lle_legacy_scheme_fp64_vs_oracle(engine, oracle, state, dim, maxValue):
     assert np.array_equal(engine.lle_sweep_legacy("lorenz", dim, draws=draws, **kw), g)
 
 
+@pytest.mark.parametrize("dim, maxValue", [(1, 0.0), (2, 18.0)])
+def test_spectrum_legacy_scheme_fp64_vs_oracle(engine, oracle, dim, maxValue):
+    """The legacy spectrum kernel's scheme (chaos_lyapunov_spectrum_legacy;
+    the oracle's restatement is pinned to LSKernelCUDA on the CPU) against the
+    oracle fed the engine's twin draws: every exponent within 1e-12."""
+    n, rng, mut = (24, [20.0, 60.0], [1]) if dim == 1 else (6, [20.0, 60.0, 5.0, 15.0], [1, 0])
+    kw = dict(tMax=20.0, NT=0.2, nPts=n, h=0.01, eps=1e-7, initialConditions=[1.0, 1.0, 1.0], ranges=rng,
+              indicesOfMutVars=mut, transientTime=5.0, values=LORENZ, maxValue=maxValue)
+    g = engine.lyapunov_spectrum_legacy("lorenz", dim, **kw)
+    draws = engine.legacy_lle_draws(2, n ** dim, 3)
+    o = oracle.lyapunov_spectrum_legacy(0, dim, 0, 20.0, 0.2, n, 0.01, 1e-7, [1.0, 1.0, 1.0], rng, mut, maxValue,
+                                        5.0, LORENZ, draws=draws)
+    assert np.allclose(g, o, rtol=1e-12, atol=1e-12), np.max(np.abs(g - o))
+    assert np.array_equal(engine.lyapunov_spectrum_legacy("lorenz", dim, draws=draws, **kw), g)
+
+
 def test_legacy_lle_draws(engine):
     """The legacy kernels' twin draws: cuRAND seeded p + k (so neighbouring
     points share draws, each a uniform in (0, 1] minus 0.5), and 0.5 sinf(p (k
@@ -214,6 +230,14 @@ def test_legacy_lle_draws(engine):
     ref = 0.5 * np.sin(arg.astype(np.float64))
     ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)  # of the halved value, in float
     assert np.all(np.abs(d1 - ref) <= 3 * ulp)  # sinf's 2-ulp bound, plus the rounding of the float result
+    d2 = engine.legacy_lle_draws(2, 50, 3)  # the spectrum's rows: [p, twin j, component i]
+    p = np.arange(50)[:, None, None]
+    j = np.arange(3)[None, :, None]
+    i = np.arange(3)[None, None, :]
+    arg = ((0.2171828 * (i + 1) * (j + 1) + p) + (0.2171828 + i * j * p)).astype(np.float32)
+    ref = np.sin(arg.astype(np.float64)) * 0.5
+    ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    assert np.all(np.abs(d2 - ref) <= 3 * ulp)
 
 
 def test_spectrum_log_axis_fp64_vs_oracle(engine, oracle):
@@ -280,19 +304,21 @@ def test_legacy_csv_bytes(engine, oracle, tmp_path):
         else:
             cells = [float(c) for c in got.replace("\n", "").split(", ")]
             assert np.allclose(cells, o, rtol=1e-5, atol=1e-6) and got.count("\n") == m - 1
-    # LS1D / LS2D
+    # LS1D / LS2D (the legacy spectrum kernel's scheme, with the engine's twin draws)
     rng = [20.0, 60.0]
     p = tmp_path / "ls1.csv"
     old.LS1D(10.0, 0.1, 6, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, rng, [1], 0, 0.0, 5.0, LORENZ, 3, p)
-    o = oracle.lyapunov_spectrum(0, 1, 0, 10.0, 0.1, 6, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, [1], 5.0, LORENZ)
+    o = oracle.lyapunov_spectrum_legacy(0, 1, 0, 10.0, 0.1, 6, 0.01, 1e-8, [1.0, 1.0, 1.0], rng, [1], 0.0, 5.0,
+                                        LORENZ, draws=engine.legacy_lle_draws(2, 6, 3))
     rows = [ln.split(", ") for ln in p.read_text().splitlines()]
     assert [r[0] for r in rows] == [_g(6)(20.0 + k * 8.0) for k in range(6)]
     assert np.allclose(np.array([[float(x) for x in r[1:]] for r in rows]), o, rtol=1e-5, atol=1e-6)
     base = tmp_path / "ls2_"
     old.LS2D(10.0, 0.1, 4, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, [20.0, 60.0, 5.0, 15.0], [1, 0], 0, 0.0, 5.0, LORENZ, 3,
              base)
-    o = oracle.lyapunov_spectrum(0, 2, 0, 10.0, 0.1, 4, 0.01, 1e-8, [1.0, 1.0, 1.0], [20.0, 60.0, 5.0, 15.0],
-                                 [1, 0], 5.0, LORENZ)
+    o = oracle.lyapunov_spectrum_legacy(0, 2, 0, 10.0, 0.1, 4, 0.01, 1e-8, [1.0, 1.0, 1.0],
+                                        [20.0, 60.0, 5.0, 15.0], [1, 0], 0.0, 5.0, LORENZ,
+                                        draws=engine.legacy_lle_draws(2, 16, 3))
     for j in range(3):
         t = (tmp_path / f"ls2_{j + 1}.csv").read_text()
         assert t.startswith("20 60\n5 15\n")

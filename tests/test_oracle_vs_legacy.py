@@ -15,9 +15,8 @@ thread per point; their hard-wired system is the sin3 plug-in's arithmetic)
 against the oracle's sweeps with the legacy loop (GRID_LEGACY_LOOP) and its
 basins features, and the legacy LLE kernels (LLEKernelCUDA with its cuRAND
 uniforms supplied, LLEKernelICCUDA with its sinf twin) against
-orc_lle_sweep_legacy. Not pinned: the legacy spectrum's twin directions
-(sinf of the chunk-relative thread index in LSKernelCUDA); the spectrum runs
-from the unit vectors."""
+orc_lle_sweep_legacy, and the legacy spectrum kernel LSKernelCUDA against
+orc_lyapunov_spectrum_legacy."""
 import math
 
 import numpy as np
@@ -186,4 +185,18 @@ def test_lle_ic_matches_legacy_kernel(leg, oracle, dim, maxValue):
     L = leg.lle(1, dim, n, 50.0, 0.5, 0.01, 1e-6, 20.0, [0.3, 0.1, 0.0], V, rng, mut, maxValue)
     o = oracle.lle_sweep_legacy(5, dim, oracle.GRID_STATE, 50.0, 0.5, n, 0.01, 1e-6, [0.3, 0.1, 0.0], rng, mut,
                                 maxValue, 20.0, V)
+    assert np.array_equal(L, o)
+
+
+@pytest.mark.parametrize("dim", [1, 2])
+@pytest.mark.parametrize("maxValue", [0.0, 3.0])
+def test_ls_matches_legacy_kernel(leg, oracle, dim, maxValue):
+    """LS1D / LS2D: LSKernelCUDA (twins from its sinf draws, orthonormalised
+    after the transient, classical Gram-Schmidt every block) against
+    orc_lyapunov_spectrum_legacy, every exponent bit for bit."""
+    n, rng, mut = (20, [0.1, 0.4], [1]) if dim == 1 else (6, [0.1, 0.4, 0.3, 0.7], [1, 0])
+    V = _sin3(0.2)
+    L = leg.ls(dim, n, 50.0, 0.5, 0.01, 1e-6, 20.0, [0.3, 0.1, 0.0], V, rng, mut, maxValue)
+    o = oracle.lyapunov_spectrum_legacy(5, dim, 0, 50.0, 0.5, n, 0.01, 1e-6, [0.3, 0.1, 0.0], rng, mut, maxValue,
+                                        20.0, V)
     assert np.array_equal(L, o)
