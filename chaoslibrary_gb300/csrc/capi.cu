@@ -42,7 +42,13 @@ int env_flag(const char* name) {
     return s && atoi(s) == 1 ? 1 : 0;
 }
 std::atomic<int> g_grid_fma{env_flag("CHAOS_GRID_FMA")};  // CHAOS_TUNE_GRID_FMA
-std::atomic<int> g_lle_twin{env_flag("CHAOS_LLE_TWIN")};  // CHAOS_TUNE_LLE_TWIN
+// an environment value in [0, hi], else 0
+int env_level(const char* name, int hi) {
+    const char* s = getenv(name);
+    const int v = s ? atoi(s) : 0;
+    return v >= 0 && v <= hi ? v : 0;
+}
+std::atomic<int> g_lle_twin{env_level("CHAOS_LLE_TWIN", 2)};  // CHAOS_TUNE_LLE_TWIN
 std::atomic<int> g_bif2d_cap{0};                          // CHAOS_TUNE_BIF2D_CAP
 }  // namespace
 
@@ -219,7 +225,7 @@ static int check_ff32_lle(const chaos_exec* ex, int system, const LleParams& L) 
     if (!ex || ex->precision != CHAOS_FF32) return CHAOS_OK;
     if (system == SYS_USER || !system_has_difference_form(system))
         return set_error(CHAOS_E_UNSUPPORTED, "CHAOS_FF32 LLE needs an RK4 system (0-2); use CHAOS_FP64");
-    if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+    if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin starts (CHAOS_TUNE_LLE_TWIN 1, 2) are FP64 only");
     return CHAOS_OK;
 }
 
@@ -665,7 +671,7 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_fp32_lle(system)))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
-        return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+        return set_error(CHAOS_E_UNSUPPORTED, "the reference twin starts (CHAOS_TUNE_LLE_TWIN 1, 2) are FP64 only");
     if ((rc = check_ff32_lle(ex, system, L))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
@@ -731,7 +737,7 @@ int chaos_lle_sweep(const chaos_exec* ex, int system, int dim, int gridMode, dou
     if (ex && ex->precision == CHAOS_FP32 && (system == SYS_USER || !system_has_fp32_lle(system)))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon; use CHAOS_FP64");
     if (ex && ex->precision == CHAOS_FP32 && L.twin != 0)
-        return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+        return set_error(CHAOS_E_UNSUPPORTED, "the reference twin starts (CHAOS_TUNE_LLE_TWIN 1, 2) are FP64 only");
     if ((rc = check_ff32_lle(ex, system, L))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
@@ -865,7 +871,7 @@ int chaos_lle2d_checked(const chaos_exec* ex, int system, double tMax, double NT
         return rc;
     if (system == SYS_USER || !system_has_fp32_lle(system))
         return set_error(CHAOS_E_UNSUPPORTED, "FP32 LLE needs a quadratic RK4 system (0-2) or Chameleon");
-    if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin start (CHAOS_TUNE_LLE_TWIN 1) is FP64 only");
+    if (L.twin != 0) return set_error(CHAOS_E_UNSUPPORTED, "the reference twin starts (CHAOS_TUNE_LLE_TWIN 1, 2) are FP64 only");
     if (L.nPoints > 0x7fffffffLL) return set_error(CHAOS_E_ARGS, "nPts^2 must be < 2^31");
     Call c;
     if ((rc = c.begin(ex))) return rc;
@@ -1119,7 +1125,8 @@ int chaos_set_tuning(int knob, int value) {
         return CHAOS_OK;
     }
     if (knob == CHAOS_TUNE_GRID_FMA || knob == CHAOS_TUNE_LLE_TWIN) {
-        if (value != 0 && value != 1) return set_error(CHAOS_E_ARGS, "knob %d takes 0 or 1", knob);
+        const int hi = knob == CHAOS_TUNE_LLE_TWIN ? 2 : 1;
+        if (value < 0 || value > hi) return set_error(CHAOS_E_ARGS, "knob %d takes 0 to %d", knob, hi);
         (knob == CHAOS_TUNE_GRID_FMA ? g_grid_fma : g_lle_twin).store(value);
         return CHAOS_OK;
     }

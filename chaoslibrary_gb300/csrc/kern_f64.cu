@@ -54,6 +54,14 @@ __global__ void __launch_bounds__(kBlock) lle_legacy_kernel(LleParams L, double*
     out[o] = lle_point_legacy<S>(L, L.pBegin + o);
 }
 
+// The LLE map with the reference's cuRAND twin start (L.twin == 2).
+template <int S>
+__global__ void __launch_bounds__(kBlock) lle_reftwin_kernel(LleParams L, double* out) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= L.nPoints) return;
+    out[o] = lle_point_reftwin<S>(L, L.pBegin + o);
+}
+
 // kind 0 / 1: out[p*nx + k] = legacy_twin_draw; kind 2: out[(p*nx + j)*nx + i] = legacy_spectrum_draw
 __global__ void legacy_draws_kernel(int kind, long long n, int nx, double* out) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -300,6 +308,7 @@ cudaError_t launch_lle_f64(const LleParams& L, double* out, cudaStream_t st) {
 #define CALL(S)                                                               \
     {                                                                         \
         if (L.legacyLoop) lle_legacy_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
+        else if (L.twin == 2) lle_reftwin_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
         else lle_kernel<S><<<grid_for(L.nPoints), kBlock, 0, st>>>(L, out); \
         note_launch();                                                        \
     }

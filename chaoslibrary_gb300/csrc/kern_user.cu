@@ -35,7 +35,9 @@ __global__ void __launch_bounds__(kBlock) basins_kernel_user(SweepParams P, Basi
 __global__ void __launch_bounds__(kBlock) lle_kernel_user(LleParams L, double* out) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= L.nPoints) return;
-    out[o] = L.legacyLoop ? lle_point_legacy<SYS_USER>(L, L.pBegin + o) : lle_point_full<SYS_USER, double>(L, L.pBegin + o);
+    out[o] = L.legacyLoop  ? lle_point_legacy<SYS_USER>(L, L.pBegin + o)
+             : L.twin == 2 ? lle_point_reftwin<SYS_USER>(L, L.pBegin + o)
+                           : lle_point_full<SYS_USER, double>(L, L.pBegin + o);
 }
 __global__ void __launch_bounds__(kBlock) trajectory_kernel_user(const double* x0, const double* a0, double h,
                                                                  int nSteps, double* out, long long n) {

@@ -3,8 +3,9 @@
 // a grid of parameters), LLEKernelICCUDA (:2034-2139, LLE1DIC / LLE2DIC: a
 // grid of initial conditions) and LSKernelCUDA (:2189-2330, LS1D / LS2D),
 // which differs from the LLE map's (LLE/src/LLECUDA.cu) in its block count,
-// its twin start and its renormalisation arithmetic. Included by the FP64
-// translation units (built-in and user systems).
+// its twin start and its renormalisation arithmetic; and the LLE map's own
+// cuRAND twin start. Included by the FP64 translation units (built-in and
+// user systems).
 #pragma once
 
 #include <curand_kernel.h>
@@ -196,6 +197,44 @@ __device__ __forceinline__ void spectrum_point_legacy(const LleParams& L, long l
     }
 #pragma unroll
     for (int j = 0; j < N; ++j) out[p * N + j] = sum[j] / L.tMax;
+}
+
+// The LLE map's twin start as the reference draws it (LLE/src/LLECUDA.cu:87-101):
+// cuRAND's default generator seeded with the point index (the first swept
+// parameter fastest), 2*NX uniforms in turn. The first NX give the norm
+// factor n = sum of (u - 0.5)^2 by float FMAs, then n * rsqrtf(n) in float;
+// the next NX the direction z_k = (u - 0.5) / n (float division) and the twin
+// q_k = fmaf(z_k, (float)eps, (float)x_k), every step in FP32 as there.
+template <int NX>
+__device__ __forceinline__ void reference_twin_start(long long p, double eps, const double* x, double* q) {
+    curandState_t st;
+    curand_init((unsigned long long)p, 0ull, 0ull, &st);
+    float nf = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+        const float z = curand_uniform(&st) - 0.5f;
+        nf = __fmaf_rn(z, z, nf);
+    }
+    nf = __fmul_rn(rsqrtf(nf), nf);
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+        const float z = __fdiv_rn(curand_uniform(&st) - 0.5f, nf);
+        q[k] = (double)__fmaf_rn(z, (float)eps, (float)x[k]);
+    }
+}
+
+// LLE point of the LLE map with that twin start (L.twin == 2): the
+// transient, reference_twin_start, then the Benettin blocks of
+// lle_point_full.
+template <int S>
+__device__ __forceinline__ double lle_point_reftwin(const LleParams& L, long long p) {
+    constexpr int NX = Traits<S>::NX, NA = Traits<S>::NA;
+    double x[NX], q[NX], a[NA];
+    lle_load<NX, NA>(L, p, x, a);
+    const StepCtx<double> c(L.h);
+    for (int s = 0; s < L.trans; ++s) step<S>(x, a, c);
+    reference_twin_start<NX>(p, L.eps, x, q);
+    return lle_benettin_full<S, double>(L, x, q, a);
 }
 
 }  // namespace chaos

@@ -560,9 +560,11 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
    Initial value from the environment: CHAOS_GRID_FMA=1. */
 #define CHAOS_TUNE_GRID_FMA 3
 /* CHAOS_TUNE_LLE_TWIN: 0 (default) the twin trajectory starts at x + eps*e_x;
-   1 the reference's start (LLECUDA.cu:97-101): every state component rounded
-   to float and eps added along e_x by a float FMA (the reference draws the
-   direction with cuRAND). FP64 only. Initial value: CHAOS_LLE_TWIN=1. */
+   1 the reference's start (LLECUDA.cu:97-101) along e_x: every state
+   component rounded to float and eps added by a float FMA; 2 the reference's
+   start itself (LLECUDA.cu:87-101): the direction drawn by cuRAND's device
+   API seeded with the point index, normalised and applied in FP32 as there.
+   FP64 only. Initial value: CHAOS_LLE_TWIN=1 or 2. */
 #define CHAOS_TUNE_LLE_TWIN 4
 /* CHAOS_TUNE_BIF2D_CAP: peak rows per point of the 2-D bifurcation's
    clustering scratch. 0 (default): B/2 (the most a point can keep) when the

@@ -10,7 +10,8 @@ getValueByIdx into one FMA (nvcc's default), so the engine reproduces its
 default (the source as written, as the host build of the reference computes)
 differs exactly on the grid points where that contraction changes the value.
 The reference's LLE starts its twin from the float-rounded state;
-CHAOS_TUNE_LLE_TWIN = 1 reproduces that start up to its cuRAND direction."""
+CHAOS_TUNE_LLE_TWIN = 1 reproduces that start up to its cuRAND direction, and
+CHAOS_TUNE_LLE_TWIN = 2 draws that direction as the reference does."""
 import subprocess
 from fractions import Fraction
 from pathlib import Path
@@ -88,7 +89,7 @@ def test_lle_reference_twin_start_agrees_with_reference_gpu_build(engine, tmp_pa
     engine.set_system("rossler")
     engine.set_precision("fp64")
     within = {}
-    for twin in (0, 1):
+    for twin in (0, 1, 2):
         engine.set_tuning(engine.TUNE_LLE_TWIN, twin)
         try:
             engine.LLE2D(tmax, 0.1, n, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, [0.1, 0.4, 2.0, 10.0], [0, 2], 0, 0.0, 50.0,
@@ -101,6 +102,8 @@ def test_lle_reference_twin_start_agrees_with_reference_gpu_build(engine, tmp_pa
     # measured on GB300: twin 1 -> 82.6 % of all points and 97.4 % of the regular ones within 1e-3
     assert within[1][0] >= 0.80 and within[1][1] >= 0.95
     assert within[1][0] > within[0][0]
+    # twin 2 draws the reference's own cuRAND start: only the per-block log differs (FP32 __logf there)
+    assert within[2][0] >= 0.999 and within[2][1] >= 0.999, within[2]
 
 
 REF_STATES = ROOT / "oracle" / "_ref" / "ref_gpu_lle_states"
@@ -140,6 +143,15 @@ def test_lle_on_reference_twin_starts_matches_reference_gpu_build(engine, tmp_pa
     ok = fin & np.isfinite(lff)
     reg = ok & (ref < 0.005)
     assert np.mean(np.abs(lff - ref)[reg] <= 1e-3) >= 0.999
+    # CHAOS_TUNE_LLE_TWIN 2 draws the reference's own cuRAND start: the engine's map from its own start
+    # equals its map from the reference's starting states, point for point (point ia, ib at ib * n + ia)
+    engine.set_tuning(engine.TUNE_LLE_TWIN, 2)
+    try:
+        own = engine.lle2d("rossler", tmax, 0.1, n, 0.01, 1e-8, [1.0, 1.0, 1.0], [0.1, 0.4, 2.0, 10.0], [0, 2],
+                           50.0, [0.2, 0.2, 5.7])
+    finally:
+        engine.set_tuning(engine.TUNE_LLE_TWIN, 0)
+    assert np.array_equal(own, l64.reshape(n, n).T.ravel(), equal_nan=True)
     # the transient: 5,000 FP64 steps from (1, 1, 1) with the reference's parameters
     rows = np.random.default_rng(5).choice(n * n, 256, replace=False)
     t = engine.trajectory("rossler", np.tile([1.0, 1.0, 1.0], (256, 1)), semi[rows, 3:6], 0.01, 5000,
