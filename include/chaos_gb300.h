@@ -226,8 +226,9 @@ int chaos_lle_from_states(const chaos_exec* ex, int system, long long n, const d
 /*
  * LLE over a 1-D or 2-D grid of parameters (gridMode 0) or of initial
  * conditions (gridMode CHAOS_GRID_STATE), linear or log-scale axes
- * (CHAOS_GRID_LOG0 / LOG1 / LOG_F32): the legacy library's LLE1D, LLE1DIC,
- * LLE2D and LLE2DIC analyses (debri/hostLibrary.cu:3111-3828) with the
+ * (CHAOS_GRID_LOG0 / LOG1 / LOG_F32): the grids of the legacy library's
+ * LLE1D, LLE1DIC, LLE2D and LLE2DIC analyses (debri/hostLibrary.cu:3111-3828;
+ * their own kernels' scheme is chaos_lle_sweep_legacy) with the
  * Benettin scheme of chaos_lle2d (twin at x + eps*e_x, calcBlocks + 1 blocks,
  * sum / tMax). dim 1: ranges[0..1] and indicesOfMutVars[0], lle[i] for
  * i < nPts; dim 2: ranges[0..3], indicesOfMutVars[0..1], lle[j*nPts + i] as
@@ -297,7 +298,8 @@ int chaos_legacy_lle_draws(const chaos_exec* ex, int kind, long long n, int nx, 
 
 /*
  * Lyapunov spectrum over the same grids (the legacy library's LS1D / LS2D,
- * debri/hostLibrary.cu:3829-4111, kernel debri/cudaLibrary.cu:2141-2330):
+ * debri/hostLibrary.cu:3829-4111, kernel debri/cudaLibrary.cu:2141-2330; its
+ * own kernel's twin start and block count are chaos_lyapunov_spectrum_legacy):
  * one twin per state dimension started along the unit vectors, classical
  * Gram-Schmidt of the twin differences after every block of NT, exponent j =
  * sum of log(|b_j| / eps) / tMax over calcBlocks + 1 blocks (the LLE map's
