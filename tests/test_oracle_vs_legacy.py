@@ -200,3 +200,58 @@ def test_ls_matches_legacy_kernel(leg, oracle, dim, maxValue):
     o = oracle.lyapunov_spectrum_legacy(5, dim, 0, 50.0, 0.5, n, 0.01, 1e-6, [0.3, 0.1, 0.0], rng, mut, maxValue,
                                         20.0, V)
     assert np.array_equal(L, o)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_legacy_kernels_random_configurations(leg, oracle, seed):
+    """Random configurations of the legacy system (damping, preScaller 1-4,
+    bound, recorded component, ranges, horizons): every legacy kernel above
+    against its oracle restatement, bit for bit."""
+    rng = np.random.default_rng(100 + seed)
+    b = float(rng.uniform(0.05, 1.2))
+    V = _sin3(b)
+    pre = int(rng.integers(1, 5))
+    mx = float(rng.choice([0.0, 2.5, 4.0, 1e8]))
+    wv = int(rng.integers(0, 3))
+    lo = float(rng.uniform(-6.0, -1.0))
+    hi = float(rng.uniform(1.0, 6.0))
+    tmax, trans = float(rng.choice([10.0, 20.0, 30.0])), float(rng.choice([5.0, 20.0, 50.0]))
+    ic = [float(v) for v in rng.uniform(-1.0, 1.0, 3)]
+    # bifurcation over initial conditions, 1-D and 2-D
+    for dim in (1, 2):
+        n, rg, mut = (24, [lo, hi], [int(rng.integers(0, 3))]) if dim == 1 else (8, [lo, hi, lo, hi], [0, 2])
+        L = leg.ic_bifurcation(dim, n, tmax, 0.01, trans, pre, ic, V, rg, mut, wv, mx, eps=0.05)
+        o = oracle.bifurcation_sweep(5, dim, oracle.GRID_STATE | oracle.GRID_LEGACY_LOOP, tmax, n, 0.01, ic, rg, mut,
+                                     wv, mx, trans, V, preScaller=pre, eps=0.05)
+        assert np.array_equal(L["counts"], o["counts"])
+        for k, c in enumerate(L["counts"]):
+            assert np.array_equal(L["peaks"][k, :max(c, 0)], o["peaks"][k, :max(c, 0)])
+        if dim == 2:
+            assert np.array_equal(L["labels"], o["labels"])
+    # the basins map
+    L = leg.basins_v1(8, tmax, 0.01, trans, pre, ic, V, [lo, hi, lo, hi], [0, 1], wv, mx)
+    o = oracle.basins_features(5, tmax, 8, 0.01, ic, [lo, hi, lo, hi], [0, 1], wv, mx, trans, V, preScaller=pre)
+    assert np.array_equal(L["flags"], o["flags"])
+    assert np.array_equal(L["avgPeaks"], o["avg_peaks"]) and np.array_equal(L["avgIntervals"], o["avg_intervals"])
+    # the step-size sweep (a range whose rounded steps stay within the legacy's blocks)
+    hr = [0.008, 0.02] if seed % 2 else [0.02, 0.008]
+    L = leg.step_sweep(16, tmax, trans, pre, ic, V, hr, wv, mx)
+    o = oracle.bifurcation_sweep(5, 1, oracle.GRID_LOG0 | oracle.GRID_LOG_F32 | oracle.GRID_LEGACY_LOOP, tmax, 16,
+                                 0.0, ic, hr, [oracle.MUT_STEP], wv, mx, trans, V, preScaller=pre)
+    assert np.array_equal(L["counts"], np.maximum(o["counts"], 0))
+    for k, c in enumerate(L["counts"]):
+        assert np.array_equal(L["peaks"][k, :c], o["peaks"][k, :c])
+    # the LLE kernels and the spectrum (NT 0.2, the bound on component 0)
+    mxl = float(rng.choice([0.0, 3.0]))
+    u = rng.random(30).astype(np.float32)
+    L = leg.lle(0, 1, 12, tmax, 0.2, 0.01, 1e-6, trans, ic, V, [0.1, 0.6], [1], mxl, uniforms=u)
+    draws = np.array([[float(u[p + k]) - 0.5 for k in range(3)] for p in range(12)])
+    o = oracle.lle_sweep_legacy(5, 1, 0, tmax, 0.2, 12, 0.01, 1e-6, ic, [0.1, 0.6], [1], mxl, trans, V, draws=draws)
+    assert np.array_equal(L, o)
+    L = leg.lle(1, 2, 5, tmax, 0.2, 0.01, 1e-6, trans, ic, V, [lo, hi, lo, hi], [0, 1], mxl)
+    o = oracle.lle_sweep_legacy(5, 2, oracle.GRID_STATE, tmax, 0.2, 5, 0.01, 1e-6, ic, [lo, hi, lo, hi], [0, 1], mxl,
+                                trans, V)
+    assert np.array_equal(L, o)
+    L = leg.ls(1, 6, tmax, 0.2, 0.01, 1e-6, trans, ic, V, [0.1, 0.6], [1], mxl)
+    o = oracle.lyapunov_spectrum_legacy(5, 1, 0, tmax, 0.2, 6, 0.01, 1e-6, ic, [0.1, 0.6], [1], mxl, trans, V)
+    assert np.array_equal(L, o)
