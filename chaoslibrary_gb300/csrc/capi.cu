@@ -302,6 +302,33 @@ static int upload_log_axes(Call& c, int gridMode, int dim, int nPts, const doubl
     return CHAOS_OK;
 }
 
+// With CHAOS_TUNE_GRID_FMA, the linear axes of an LLE grid take start + i*step
+// fused into one FMA. The reference's host linspace (LLE/src/LLECUDA.cu:195-200)
+// computes them that way where its host compiler contracts the expression
+// (aarch64 by default). They are uploaded as value tables, like the log-scale
+// axes, so the kernels are unchanged.
+static int upload_fused_axes(Call& c, int gridMode, int dim, int nPts, const double* ranges, const double** table) {
+    if (!g_grid_fma.load(std::memory_order_relaxed) || nPts < 2) return CHAOS_OK;
+    for (int d = 0; d < dim; ++d) {
+        if (gridMode & (d ? CHAOS_GRID_LOG1 : CHAOS_GRID_LOG0)) continue;
+        std::vector<double> v;
+        try {
+            v.resize(nPts);
+        } catch (const std::bad_alloc&) {
+            return set_error(CHAOS_E_NOMEM, "host allocation of a grid axis failed");
+        }
+        const double step = (ranges[2 * d + 1] - ranges[2 * d]) / (double)(nPts - 1);
+        for (int i = 0; i < nPts; ++i) v[i] = std::fma((double)i, step, ranges[2 * d]);
+        double* dv = (double*)c.alloc(v.size() * sizeof(double));
+        if (c.failed) return CHAOS_E_NOMEM;
+        cudaError_t e = cudaMemcpyAsync(dv, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        // (a copy from pageable memory has read v when it returns)
+        if (e != cudaSuccess) return cuda_error(e, "grid table upload");
+        table[d] = dv;
+    }
+    return CHAOS_OK;
+}
+
 int fill_sweep(SweepParams& P, int system, int dim, double tMax, int nPts, double h, int nIC, const double* ic,
                const double* ranges, const int* mut, int wv, double maxValue, double transientTime,
                const double* values, int nValues, int preScaller, bool basins, int gridMode) {
@@ -675,6 +702,7 @@ int chaos_lle2d(const chaos_exec* ex, int system, double tMax, double NT, int nP
     if ((rc = check_ff32_lle(ex, system, L))) return rc;
     Call c;
     if ((rc = c.begin(ex))) return rc;
+    if ((rc = upload_fused_axes(c, 0, 2, nPts, ranges, L.table))) return c.finish(rc);
     double* dOut = (double*)c.output(lle, L.nPoints * sizeof(double));
     if (c.failed) return c.finish(CHAOS_E_NOMEM);
     cudaError_t e = run_lle(c.ex.precision, L, dOut, c.stream);

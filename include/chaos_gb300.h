@@ -559,6 +559,9 @@ int chaos_trajectory(const chaos_exec* ex, int system, long long nTraj, const do
    what the reference's own GPU build computes (nvcc contracts the expression
    by default): with 1, FP64 bifurcation and basins sweeps reproduce that
    build's output bit for bit (for plug-ins free of contractible products).
+   With 1 the LLE map (chaos_lle2d) also takes its swept values as one FMA,
+   as the reference's host linspace (LLECUDA.cu:195-200) computes them where
+   its host compiler contracts the expression (aarch64 by default).
    Initial value from the environment: CHAOS_GRID_FMA=1. */
 #define CHAOS_TUNE_GRID_FMA 3
 /* CHAOS_TUNE_LLE_TWIN: 0 (default) the twin trajectory starts at x + eps*e_x;

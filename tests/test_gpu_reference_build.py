@@ -109,6 +109,46 @@ def test_lle_reference_twin_start_agrees_with_reference_gpu_build(engine, tmp_pa
     assert within[2][0] > within[1][0] and within[2][1] >= 0.995, within
 
 
+def test_lle_twin_start_and_fused_linspace_reproduce_reference_gpu_build(engine, tmp_path):
+    """With the reference's own twin start (CHAOS_TUNE_LLE_TWIN 2) and its
+    host linspace as this machine's host compiler builds it (contracted into
+    an FMA on aarch64: CHAOS_TUNE_GRID_FMA 1), the engine's FP64 map agrees
+    with the reference's own GPU build within 1e-3 on >= 99.9 % of the points
+    (only the per-block log differs: FP32 __logf there), and its map equals
+    the map from the reference's dumped starting states bit for bit."""
+    import platform
+
+    _need(REF_LLE)
+    _need(REF_STATES)
+    if platform.machine() not in ("aarch64", "arm64"):
+        pytest.skip("the reference's host linspace is contracted by the aarch64 host compiler only")
+    n, tmax = 128, 500.0
+    ref_csv, eng_csv = tmp_path / "ref.csv", tmp_path / "eng.csv"
+    subprocess.run([str(REF_LLE), str(ref_csv), str(n), str(tmax)], check=True, capture_output=True, timeout=600)
+    semi, ref_states = _ref_states(tmp_path, n, tmax)
+    engine.set_system("rossler")
+    engine.set_precision("fp64")
+    engine.set_tuning(engine.TUNE_LLE_TWIN, 2)
+    engine.set_tuning(engine.TUNE_GRID_FMA, 1)
+    try:
+        engine.LLE2D(tmax, 0.1, n, 0.01, 1e-8, [1.0, 1.0, 1.0], 3, [0.1, 0.4, 2.0, 10.0], [0, 2], 0, 0.0, 50.0,
+                     [0.2, 0.2, 5.7], 3, str(eng_csv))
+        own = engine.lle2d("rossler", tmax, 0.1, n, 0.01, 1e-8, [1.0, 1.0, 1.0], [0.1, 0.4, 2.0, 10.0], [0, 2],
+                           50.0, [0.2, 0.2, 5.7])
+    finally:
+        engine.set_tuning(engine.TUNE_LLE_TWIN, 0)
+        engine.set_tuning(engine.TUNE_GRID_FMA, 0)
+
+    def values(path):
+        rows = Path(path).read_text().splitlines()
+        return np.array([float(v) for v in ", ".join(rows[2:]).split(", ") if v.strip()])
+
+    d = np.abs(values(eng_csv) - values(ref_csv))
+    assert np.mean(d <= 1e-3) >= 0.999, np.mean(d <= 1e-3)
+    l64 = engine.lle_from_states("rossler", semi, tmax, 0.1, 0.01, 1e-8, precision=engine.FP64)
+    assert np.array_equal(own.reshape(n, n).T.ravel(), l64, equal_nan=True)
+
+
 REF_STATES = ROOT / "oracle" / "_ref" / "ref_gpu_lle_states"
 
 
