@@ -725,10 +725,8 @@ static int run_legacy_scheme(const chaos_exec* ex, bool spectrum, int system, in
     if ((rc = fill_lle(L, system, tMax, NT, nPts, h, eps, initialConditions, amountOfInitialConditions, ranges,
                        indicesOfMutVars, transientTime, values, amountOfValues, dim, gridMode)))
         return rc;
-    const double blocks = tMax / NT;
-    if (!(blocks >= 0) || blocks > 2.0e9) return set_error(CHAOS_E_ARGS, "tMax / NT must fit in int");
     L.legacyLoop = 1;
-    L.legacyBlocks = (int)blocks;
+    L.legacyBlocks = (int)(tMax / NT);  // <= tMax / h, which fill_lle bounds
     L.maxValue = maxValue;
     L.twin = 0;
     const int nx = amountOfInitialConditions;

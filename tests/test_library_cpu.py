@@ -152,6 +152,38 @@ def test_grid_mode_argument_errors(native):
     with pytest.raises(native.ChaosError, match="dim 2"):
         native.lle_sweep("lorenz", 1, 5.0, 0.1, 8, 0.01, 1e-8, [0.1, 0.1, 0.1], [1.0, 10.0], [1], 1.0,
                          [10.0, 28.0, 8 / 3], gridMode=native.GRID_LOG1)
+    # the legacy per-point loop belongs to the bifurcation sweep; the LLE sweeps have their own legacy scheme
+    with pytest.raises(native.ChaosError, match="bifurcation sweep"):
+        native.lle_sweep("lorenz", 1, 5.0, 0.1, 8, 0.01, 1e-8, [0.1, 0.1, 0.1], [1.0, 10.0], [1], 1.0,
+                         [10.0, 28.0, 8 / 3], gridMode=native.GRID_LEGACY_LOOP)
+    with pytest.raises(native.ChaosError, match="bifurcation sweep"):
+        native.lle_sweep_legacy("lorenz", 1, 5.0, 0.1, 8, 0.01, 1e-8, [0.1, 0.1, 0.1], [1.0, 10.0], [1], 1.0,
+                                [10.0, 28.0, 8 / 3], gridMode=native.GRID_LEGACY_LOOP)
+
+
+def test_legacy_scheme_argument_errors(native):
+    """The legacy LLE / spectrum schemes and their twin draws validate on the
+    host; the twin-start knob takes 0, 1 or 2."""
+    with pytest.raises(native.ChaosError, match="twin-draw"):
+        native.legacy_lle_draws(3, 10, 3)
+    with pytest.raises(native.ChaosError, match="twin-draw"):
+        native.legacy_lle_draws(0, 10, 13)
+    with pytest.raises(native.ChaosError, match="built-in systems"):  # 15: CHAOS_SYS_USER
+        native.lyapunov_spectrum_legacy(15, 1, 5.0, 0.1, 8, 0.01, 1e-8, [0.1, 0.1, 0.1], [1.0, 10.0], [1], 1.0,
+                                        [10.0, 28.0, 8 / 3])
+    with pytest.raises(native.ChaosError, match="NT / h"):
+        native.lle_sweep_legacy("lorenz", 1, 5.0, 0.001, 8, 0.01, 1e-8, [0.1, 0.1, 0.1], [1.0, 10.0], [1], 1.0,
+                                [10.0, 28.0, 8 / 3])
+    knob = native.TUNE_LLE_TWIN
+    try:
+        native.set_tuning(knob, 2)
+        assert native.get_tuning(knob) == 2
+        with pytest.raises(native.ChaosError, match="0 to 2"):
+            native.set_tuning(knob, 3)
+        with pytest.raises(native.ChaosError, match="0 to 1"):
+            native.set_tuning(native.TUNE_GRID_FMA, 2)
+    finally:
+        native.set_tuning(knob, 0)
 
 
 def test_compact_peaks_argument_errors(native):
