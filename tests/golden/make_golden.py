@@ -1,10 +1,12 @@
 """Generates the golden fixtures in this folder from the reference's own code.
 
 Run here, where the reference sources are present:
-    python oracle/build_ref.py && python tests/golden/make_golden.py
+    python oracle/build_ref.py && python tests/golden/make_golden.py [legacy]
 Every fixture is produced by the host build of the reference's functions
 (oracle/_ref/libref_<system>.so, see oracle/build_ref.py), except
-dbscan_sklearn.npz, which records scikit-learn's DBSCAN labels. The fixtures
+dbscan_sklearn.npz, which records scikit-learn's DBSCAN labels. The legacy_*
+fixtures come from the legacy library's own kernels run on the host
+(oracle/_ref/libref_legacy.so); "legacy" writes only those. The fixtures
 are small .npz files; the tests compare both the oracle and the GPU engine
 against them.
 """
@@ -161,5 +163,59 @@ def main() -> None:
     print("fixtures written to", HERE)
 
 
+# the legacy library's hard-wired system (the sin3 plug-in's arithmetic) in two regimes: damping 0.4
+# under a bound of 2.5 (fixed points beside oscillations), damping 0.15 under 4 (mostly unbounded)
+LEGACY_IC = [0.2, -0.1, 0.0]
+LEGACY_REGIMES = {"fixed": (0.4, 2.5), "bound": (0.15, 4.0)}
+
+
+def legacy_values(b: float) -> list:
+    return [0.5, b, 1.4, 15.552, 2.0]
+
+
+def legacy_fixtures() -> None:
+    """The legacy kernels of bifurcation1DIC / bifurcation2DIC, basinsOfAttraction
+    and bifurcation1DForH in both regimes, and of LLE1D (with recorded cuRAND
+    uniforms), LLE1DIC and LS1D."""
+    leg = O.LegacyLib()
+    ic = LEGACY_IC
+    for regime, (b, mx) in LEGACY_REGIMES.items():
+        V = legacy_values(b)
+        for dim, n, rng, mut in ((1, 48, [-6.0, 6.0], [0]), (2, 12, [-6.0, 6.0, -6.0, 6.0], [0, 1])):
+            kw = dict(tMax=40.0, nPts=n, h=0.01, transientTime=30.0, preScaller=2, ic=ic, values=V, ranges=rng,
+                      mut=mut, wv=0, maxValue=mx, eps=0.05)
+            r = leg.ic_bifurcation(dim, n, 40.0, 0.01, 30.0, 2, ic, V, rng, mut, 0, mx, eps=0.05)
+            c = r["counts"]
+            m = max(int(c.max()), 1)
+            np.savez_compressed(HERE / f"legacy_ic_bif{dim}d_{regime}.npz", counts=c, peaks=r["peaks"][:, :m],
+                                intervals=r["intervals"][:, :m],
+                                labels=r["labels"] if dim == 2 else np.zeros(0, np.int32), dim=dim,
+                                **{k: np.asarray(v) for k, v in kw.items()})
+        kw = dict(tMax=40.0, nPts=12, h=0.01, transientTime=30.0, preScaller=3, ic=ic, values=V,
+                  ranges=[-6.0, 6.0, -6.0, 6.0], mut=[0, 1], wv=1, maxValue=mx)
+        r = leg.basins_v1(12, 40.0, 0.01, 30.0, 3, ic, V, kw["ranges"], [0, 1], 1, mx)
+        np.savez_compressed(HERE / f"legacy_basins_{regime}.npz", flags=r["flags"], avg_peaks=r["avgPeaks"],
+                            avg_intervals=r["avgIntervals"], **{k: np.asarray(v) for k, v in kw.items()})
+        kw = dict(tMax=40.0, nPts=24, transientTime=10.0, preScaller=2, ic=ic, values=V, ranges=[0.005, 0.02],
+                  wv=0, maxValue=mx)
+        r = leg.step_sweep(24, 40.0, 10.0, 2, ic, V, [0.005, 0.02], 0, mx)
+        m = max(int(r["counts"].max()), 1)
+        np.savez_compressed(HERE / f"legacy_step_sweep_{regime}.npz", counts=r["counts"], peaks=r["peaks"][:, :m],
+                            **{k: np.asarray(v) for k, v in kw.items()})
+    V = legacy_values(0.2)
+    u = np.random.default_rng(321).random(40).astype(np.float32)
+    lle1d = leg.lle(0, 1, 32, 30.0, 0.5, 0.01, 1e-6, 10.0, ic, V, [0.1, 0.6], [1], 0.0, uniforms=u)
+    lle1dic = leg.lle(1, 1, 32, 30.0, 0.5, 0.01, 1e-6, 10.0, ic, V, [-3.0, 3.0], [0], 3.0)
+    ls1d = leg.ls(1, 12, 30.0, 0.5, 0.01, 1e-6, 10.0, ic, V, [0.1, 0.6], [1], 0.0)
+    np.savez_compressed(HERE / "legacy_lle.npz", uniforms=u, lle1d=lle1d, lle1dic=lle1dic, ls1d=ls1d,
+                        tMax=30.0, NT=0.5, h=0.01, eps=1e-6, transientTime=10.0, ic=np.asarray(ic),
+                        values=np.asarray(V))
+    print("legacy fixtures written to", HERE)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["legacy"]:
+        legacy_fixtures()
+    else:
+        main()
+        legacy_fixtures()

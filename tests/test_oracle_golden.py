@@ -93,3 +93,57 @@ def test_basin_features_dbscan_matches_sklearn(oracle):
     ref = sk.DBSCAN(eps=0.05, min_samples=8).fit(F[m]).labels_
     assert np.array_equal(lab[m], ref)
     assert np.all(lab[~m] == -2)
+
+
+# the legacy library's kernels (tests/golden/make_golden.py legacy_fixtures); its hard-wired system is sin3's arithmetic
+@pytest.mark.parametrize("regime", ["fixed", "bound"])
+@pytest.mark.parametrize("dim", [1, 2])
+def test_legacy_ic_bifurcation_golden(oracle, regime, dim):
+    g = golden(f"legacy_ic_bif{dim}d_{regime}")
+    o = oracle.bifurcation_sweep(5, dim, oracle.GRID_STATE | oracle.GRID_LEGACY_LOOP, float(g["tMax"]),
+                                 int(g["nPts"]), float(g["h"]), g["ic"], g["ranges"], g["mut"], int(g["wv"]),
+                                 float(g["maxValue"]), float(g["transientTime"]), g["values"],
+                                 preScaller=int(g["preScaller"]), eps=float(g["eps"]))
+    assert np.array_equal(o["counts"], g["counts"])
+    for k, c in enumerate(g["counts"]):
+        assert np.array_equal(o["peaks"][k, :max(c, 0)], g["peaks"][k, :max(c, 0)])
+        if dim == 2:
+            assert np.array_equal(o["intervals"][k, :max(c, 0)], g["intervals"][k, :max(c, 0)])
+    if dim == 2:
+        assert np.array_equal(o["labels"], g["labels"])
+
+
+@pytest.mark.parametrize("regime", ["fixed", "bound"])
+def test_legacy_basins_golden(oracle, regime):
+    g = golden(f"legacy_basins_{regime}")
+    o = oracle.basins_features(5, float(g["tMax"]), int(g["nPts"]), float(g["h"]), g["ic"], g["ranges"], g["mut"],
+                               int(g["wv"]), float(g["maxValue"]), float(g["transientTime"]), g["values"],
+                               preScaller=int(g["preScaller"]))
+    assert np.array_equal(o["flags"], g["flags"])
+    assert np.array_equal(o["avg_peaks"], g["avg_peaks"]) and np.array_equal(o["avg_intervals"], g["avg_intervals"])
+
+
+@pytest.mark.parametrize("regime", ["fixed", "bound"])
+def test_legacy_step_sweep_golden(oracle, regime):
+    g = golden(f"legacy_step_sweep_{regime}")
+    o = oracle.bifurcation_sweep(5, 1, oracle.GRID_LOG0 | oracle.GRID_LOG_F32 | oracle.GRID_LEGACY_LOOP,
+                                 float(g["tMax"]), int(g["nPts"]), 0.0, g["ic"], g["ranges"], [oracle.MUT_STEP],
+                                 int(g["wv"]), float(g["maxValue"]), float(g["transientTime"]), g["values"],
+                                 preScaller=int(g["preScaller"]))
+    assert np.array_equal(np.maximum(o["counts"], 0), g["counts"])
+    for k, c in enumerate(g["counts"]):
+        assert np.array_equal(o["peaks"][k, :c], g["peaks"][k, :c])
+
+
+def test_legacy_lle_golden(oracle):
+    g = golden("legacy_lle")
+    a = (float(g["tMax"]), float(g["NT"]))
+    rest = (float(g["h"]), float(g["eps"]), g["ic"])
+    u = g["uniforms"]
+    draws = np.array([[float(u[p + k]) - 0.5 for k in range(3)] for p in range(32)])
+    assert np.array_equal(oracle.lle_sweep_legacy(5, 1, 0, *a, 32, *rest, [0.1, 0.6], [1], 0.0,
+                                                  float(g["transientTime"]), g["values"], draws=draws), g["lle1d"])
+    assert np.array_equal(oracle.lle_sweep_legacy(5, 1, oracle.GRID_STATE, *a, 32, *rest, [-3.0, 3.0], [0], 3.0,
+                                                  float(g["transientTime"]), g["values"]), g["lle1dic"])
+    assert np.array_equal(oracle.lyapunov_spectrum_legacy(5, 1, 0, *a, 12, *rest, [0.1, 0.6], [1], 0.0,
+                                                          float(g["transientTime"]), g["values"]), g["ls1d"])
