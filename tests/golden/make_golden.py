@@ -48,7 +48,7 @@ def crafted_series(rng) -> np.ndarray:
     return np.array(rows)
 
 
-def main() -> None:
+def main(out: Path = HERE) -> None:
     rng = np.random.default_rng(12345)
     lor = O.RefLib("lorenz")
     cham = O.RefLib("chameleon")
@@ -61,7 +61,7 @@ def main() -> None:
             c, p, t = lor.peak_finder(row, 0.01)
             counts.append(c)
             pk[s, :c], iv[s, :c] = p, t
-        np.savez_compressed(HERE / f"{name}.npz", data=data, h=0.01, counts=np.array(counts, np.int32),
+        np.savez_compressed(out / f"{name}.npz", data=data, h=0.01, counts=np.array(counts, np.int32),
                             peaks=pk, intervals=iv)
 
     # per-point dbscan of the 2-D bifurcation (Bifurcation_constants::dbscan)
@@ -70,15 +70,15 @@ def main() -> None:
     iv[::7] = np.round(iv[::7], 1)
     counts = rng.integers(-1, P + 1, size=60).astype(np.int32)
     counts[:4] = [-1, 0, 1, 2]
-    out = []
+    labels = []
     for k in range(60):
         c = int(counts[k])
         if c <= 0:
-            out.append(-1 if c == -1 else 0)
+            labels.append(-1 if c == -1 else 0)
         else:
-            out.append(lor.point_dbscan(np.zeros(P), iv[k], c, 2 * P + 2, 0.05))
-    np.savez_compressed(HERE / "point_dbscan.npz", intervals=iv, counts=counts, eps=0.05,
-                        labels=np.array(out, np.int32))
+            labels.append(lor.point_dbscan(np.zeros(P), iv[k], c, 2 * P + 2, 0.05))
+    np.savez_compressed(out / "point_dbscan.npz", intervals=iv, counts=counts, eps=0.05,
+                        labels=np.array(labels, np.int32))
 
     # 1-D / 2-D bifurcation sweeps through the reference kernels
     sweeps = {
@@ -108,7 +108,7 @@ def main() -> None:
             if c[k] == -1:
                 first[k] = r["data"][k, 0]
         extra = dict(labels=r["labels"]) if dim == 2 else {}
-        np.savez_compressed(HERE / f"{name}.npz", dim=dim, eps=eps, counts=c, peaks=pk, intervals=iv, first=first,
+        np.savez_compressed(out / f"{name}.npz", dim=dim, eps=eps, counts=c, peaks=pk, intervals=iv, first=first,
                             **{k: np.asarray(v) for k, v in kw.items()}, **extra)
 
     # basins: features and the reference's global clustering
@@ -123,7 +123,7 @@ def main() -> None:
     for name, (R, kw, eps) in bas.items():
         r = R.basins(**kw)
         labels = R.basins_dbscan(r["avg_peaks"], r["avg_intervals"], r["flags"], eps)
-        np.savez_compressed(HERE / f"{name}.npz", eps=eps, flags=r["flags"], avg_peaks=r["avg_peaks"],
+        np.savez_compressed(out / f"{name}.npz", eps=eps, flags=r["flags"], avg_peaks=r["avg_peaks"],
                             avg_intervals=r["avg_intervals"], labels=labels,
                             **{k: np.asarray(v) for k, v in kw.items()})
 
@@ -140,7 +140,7 @@ def main() -> None:
     ap[zero], ai[zero] = 999.0, 999.0
     ap[:20] = np.round(ap[:20], 1)  # exact duplicates
     labels = lor.basins_dbscan(ap, ai, flags, 0.05)
-    np.savez_compressed(HERE / "dbscan_compat.npz", avg_peaks=ap, avg_intervals=ai, flags=flags, eps=0.05,
+    np.savez_compressed(out / "dbscan_compat.npz", avg_peaks=ap, avg_intervals=ai, flags=flags, eps=0.05,
                         labels=labels)
 
     # LLE through the reference's calculateSystem (deterministic twin offset)
@@ -148,7 +148,7 @@ def main() -> None:
     kw = dict(tMax=50.0, NT=0.1, nPts=8, h=0.01, eps=1e-8, ic=[1.0, 1.0, 1.0], ranges=[0.1, 0.4, 2.0, 10.0],
               mut=[0, 2], transientTime=10.0, values=[0.2, 0.2, 5.7])
     lle = rl.lle(**kw)
-    np.savez_compressed(HERE / "lle_rossler.npz", lle=lle, **{k: np.asarray(v) for k, v in kw.items()})
+    np.savez_compressed(out / "lle_rossler.npz", lle=lle, **{k: np.asarray(v) for k, v in kw.items()})
 
     # textbook DBSCAN labels from scikit-learn
     from sklearn.cluster import DBSCAN
@@ -158,9 +158,9 @@ def main() -> None:
     X = np.concatenate([X, rng.uniform(0, 1, size=(200, 3))])
     X = np.round(X, 4)
     sk = DBSCAN(eps=0.05, min_samples=8).fit(X).labels_.astype(np.int32)
-    np.savez_compressed(HERE / "dbscan_sklearn.npz", X=X, eps=0.05, min_pts=8, labels=sk,
+    np.savez_compressed(out / "dbscan_sklearn.npz", X=X, eps=0.05, min_pts=8, labels=sk,
                         sklearn_version=sklearn.__version__)
-    print("fixtures written to", HERE)
+    print("fixtures written to", out)
 
 
 # the legacy library's hard-wired system (the sin3 plug-in's arithmetic) in two regimes: damping 0.4
@@ -173,7 +173,7 @@ def legacy_values(b: float) -> list:
     return [0.5, b, 1.4, 15.552, 2.0]
 
 
-def legacy_fixtures() -> None:
+def legacy_fixtures(out: Path = HERE) -> None:
     """The legacy kernels of bifurcation1DIC / bifurcation2DIC, basinsOfAttraction
     and bifurcation1DForH in both regimes, and of LLE1D (with recorded cuRAND
     uniforms), LLE1DIC and LS1D."""
@@ -187,30 +187,30 @@ def legacy_fixtures() -> None:
             r = leg.ic_bifurcation(dim, n, 40.0, 0.01, 30.0, 2, ic, V, rng, mut, 0, mx, eps=0.05)
             c = r["counts"]
             m = max(int(c.max()), 1)
-            np.savez_compressed(HERE / f"legacy_ic_bif{dim}d_{regime}.npz", counts=c, peaks=r["peaks"][:, :m],
+            np.savez_compressed(out / f"legacy_ic_bif{dim}d_{regime}.npz", counts=c, peaks=r["peaks"][:, :m],
                                 intervals=r["intervals"][:, :m],
                                 labels=r["labels"] if dim == 2 else np.zeros(0, np.int32), dim=dim,
                                 **{k: np.asarray(v) for k, v in kw.items()})
         kw = dict(tMax=40.0, nPts=12, h=0.01, transientTime=30.0, preScaller=3, ic=ic, values=V,
                   ranges=[-6.0, 6.0, -6.0, 6.0], mut=[0, 1], wv=1, maxValue=mx)
         r = leg.basins_v1(12, 40.0, 0.01, 30.0, 3, ic, V, kw["ranges"], [0, 1], 1, mx)
-        np.savez_compressed(HERE / f"legacy_basins_{regime}.npz", flags=r["flags"], avg_peaks=r["avgPeaks"],
+        np.savez_compressed(out / f"legacy_basins_{regime}.npz", flags=r["flags"], avg_peaks=r["avgPeaks"],
                             avg_intervals=r["avgIntervals"], **{k: np.asarray(v) for k, v in kw.items()})
         kw = dict(tMax=40.0, nPts=24, transientTime=10.0, preScaller=2, ic=ic, values=V, ranges=[0.005, 0.02],
                   wv=0, maxValue=mx)
         r = leg.step_sweep(24, 40.0, 10.0, 2, ic, V, [0.005, 0.02], 0, mx)
         m = max(int(r["counts"].max()), 1)
-        np.savez_compressed(HERE / f"legacy_step_sweep_{regime}.npz", counts=r["counts"], peaks=r["peaks"][:, :m],
+        np.savez_compressed(out / f"legacy_step_sweep_{regime}.npz", counts=r["counts"], peaks=r["peaks"][:, :m],
                             **{k: np.asarray(v) for k, v in kw.items()})
     V = legacy_values(0.2)
     u = np.random.default_rng(321).random(40).astype(np.float32)
     lle1d = leg.lle(0, 1, 32, 30.0, 0.5, 0.01, 1e-6, 10.0, ic, V, [0.1, 0.6], [1], 0.0, uniforms=u)
     lle1dic = leg.lle(1, 1, 32, 30.0, 0.5, 0.01, 1e-6, 10.0, ic, V, [-3.0, 3.0], [0], 3.0)
     ls1d = leg.ls(1, 12, 30.0, 0.5, 0.01, 1e-6, 10.0, ic, V, [0.1, 0.6], [1], 0.0)
-    np.savez_compressed(HERE / "legacy_lle.npz", uniforms=u, lle1d=lle1d, lle1dic=lle1dic, ls1d=ls1d,
+    np.savez_compressed(out / "legacy_lle.npz", uniforms=u, lle1d=lle1d, lle1dic=lle1dic, ls1d=ls1d,
                         tMax=30.0, NT=0.5, h=0.01, eps=1e-6, transientTime=10.0, ic=np.asarray(ic),
                         values=np.asarray(V))
-    print("legacy fixtures written to", HERE)
+    print("legacy fixtures written to", out)
 
 
 if __name__ == "__main__":
